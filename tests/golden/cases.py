@@ -1,0 +1,495 @@
+"""The reference's golden-image test cases, written once against a backend.
+
+Each case re-enacts one block of the reference's own tests (file:line given)
+through a small backend interface, so the same case renders on the oracle
+(CPU) and on the CUDA library (GPU).  The goldens themselves are the PNGs the
+reference's tests write (straight alpha); make_fixtures.py stores them in
+goldens.npz.
+
+Backend interface (all images premultiplied RGBX):
+  new_image(w, h) -> img        fill(img, color4f)
+  fill_path(img, cmds, color4f, opacity, blend, mat9, winding)
+  stroke_path(img, cmds, color4f, opacity, blend, mat9, width, cap, join, miter, dashes)
+  draw(a, b, tx, ty, blend)     blur(img, radius, oob_rgbx)     pixels(img) -> (h,w,4) uint8
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from pixie_gb300 import f32 as F
+from pixie_gb300.paths import Path, parse_path
+
+NORMAL, MASK, OVERWRITE, EXCLUDE_MASK, EXCLUSION = 0, 16, 17, 19, 11
+BUTT, ROUND_CAP, SQUARE = 0, 1, 2
+MITER, ROUND_JOIN, BEVEL = 0, 1, 2
+DEFAULT_MITER = 4.0  # paths.nim:46
+
+
+def rgba(r, g, b, a):
+    """ColorRGBA as a paint: chroma's Color = c / 255 in float32."""
+    return [F.div(float(r), 255.0), F.div(float(g), 255.0), F.div(float(b), 255.0),
+            F.div(float(a), 255.0)]
+
+
+def color(r, g, b, a):
+    return [F.f32(r), F.f32(g), F.f32(b), F.f32(a)]
+
+
+def translate(x, y):
+    return [1, 0, 0, 0, 1, 0, F.f32(x), F.f32(y), 1]
+
+
+def scale(x, y):
+    return [F.f32(x), 0, 0, 0, F.f32(y), 0, 0, 0, 1]
+
+
+WHITE = rgba(255, 255, 255, 255)
+PINK = rgba(0xFC, 0x42, 0x7B, 0xFF)  # parseHtmlColor("#FC427B")
+HEART = """
+    M 10,30
+    A 20,20 0,0,1 50,30
+    A 20,20 0,0,1 90,30
+    Q 90,60 50,90
+    Q 10,60 10,30 z
+  """
+
+
+def _fill(B, w, h, path, col, bg=None, **kw):
+    img = B.new_image(w, h)
+    if bg is not None:
+        B.fill(img, bg)
+    B.fill_path(img, parse_path(path).array() if isinstance(path, str) else path.array(), col, **kw)
+    return img
+
+
+def _stroke(B, img, path, col, **kw):
+    cmds = parse_path(path).array() if isinstance(path, str) else path.array()
+    B.stroke_path(img, cmds, col, **kw)
+    return img
+
+
+CASES = {}
+
+
+def case(name, src):
+    def deco(fn):
+        CASES[name] = (fn, src)
+        return fn
+    return deco
+
+
+# ---- tests/test_paths.nim -------------------------------------------------
+@case("paths/pathStroke1", "tests/test_paths.nim:51-57")
+def _c(B):
+    return _stroke(B, B.new_image(100, 100), "M 10 10 L 90 90", rgba(255, 0, 0, 255), width=10)
+
+
+@case("paths/pathStroke2", "tests/test_paths.nim:59-65")
+def _c(B):
+    return _stroke(B, B.new_image(100, 100), "M 10 10 L 50 60 90 90", rgba(255, 0, 0, 255), width=10)
+
+
+@case("paths/pathStroke3", "tests/test_paths.nim:67-74")
+def _c(B):
+    return _stroke(B, B.new_image(100, 100), "M 15 10 L 30 90 60 30 90 90",
+                   rgba(255, 255, 0, 255), width=10)
+
+
+@case("paths/pathBlackRectangle", "tests/test_paths.nim:76-82")
+def _c(B):
+    return _fill(B, 100, 100, "M 10 10 H 90 V 90 H 10 L 10 10", rgba(0, 0, 0, 255))
+
+
+@case("paths/pathBlackRectangleZ", "tests/test_paths.nim:84-90")
+def _c(B):
+    return _fill(B, 100, 100, "M 10 10 H 90 V 90 H 10 Z", rgba(0, 0, 0, 255))
+
+
+@case("paths/pathYellowRectangle", "tests/test_paths.nim:92-98")
+def _c(B):
+    return _fill(B, 100, 100, "M 10 10 H 90 V 90 H 10 L 10 10", rgba(255, 255, 0, 255))
+
+
+@case("paths/pathRedRectangle", "tests/test_paths.nim:100-110")
+def _c(B):
+    p = Path()
+    p.move_to(10, 10)
+    p.line_to(10, 90)
+    p.line_to(90, 90)
+    p.line_to(90, 10)
+    p.line_to(10, 10)
+    return _fill(B, 100, 100, p, rgba(255, 0, 0, 255))
+
+
+@case("paths/pathBottomArc", "tests/test_paths.nim:112-118")
+def _c(B):
+    return _fill(B, 100, 100, "M30 60 A 20 20 0 0 0 90 60 L 30 60", PINK)
+
+
+@case("paths/pathHeart", "tests/test_paths.nim:120-133")
+def _c(B):
+    return _fill(B, 100, 100, HEART, PINK)
+
+
+@case("paths/pathRotatedArc", "tests/test_paths.nim:135-141")
+def _c(B):
+    return _fill(B, 100, 100, "M 20 50 A 20 10 45 1 1 80 50 L 20 50", PINK)
+
+
+@case("paths/pathInvertedCornerArc", "tests/test_paths.nim:143-149")
+def _c(B):
+    return _fill(B, 100, 100, "M 0 50 A 50 50 0 0 0 50 0 L 50 50 L 0 50", PINK)
+
+
+@case("paths/pathCornerArc", "tests/test_paths.nim:151-157")
+def _c(B):
+    return _fill(B, 100, 100, "M 0 50 A 50 50 0 0 1 50 0 L 50 50 L 0 50", PINK)
+
+
+@case("paths/pixelScale", "tests/test_paths.nim:175-185")
+def _c(B):
+    img = B.new_image(200, 200)
+    B.fill(img, WHITE)
+    p = parse_path("M1 0.5C1 0.776142 0.776142 1 0.5 1C0.223858 1 0 0.776142 0 0.5C0 0.223858 "
+                   "0.223858 0 0.5 0C0.776142 0 1 0.223858 1 0.5Z").array()
+    B.fill_path(img, p, rgba(255, 0, 0, 255), mat=scale(200, 200))
+    B.stroke_path(img, p, rgba(0, 255, 0, 255), mat=scale(200, 200), width=0.01)
+    return img
+
+
+def _box(B, path, cap, join):
+    img = B.new_image(60, 60)
+    B.fill(img, WHITE)
+    return _stroke(B, img, path, rgba(0, 0, 0, 255), mat=translate(10, 10), width=10, cap=cap,
+                   join=join)
+
+
+@case("paths/boxRound", "tests/test_paths.nim:187-197")
+def _c(B):
+    return _box(B, "M 3 3 L 20 3 L 20 20 L 3 20 Z", ROUND_CAP, ROUND_JOIN)
+
+
+@case("paths/boxBevel", "tests/test_paths.nim:199-209")
+def _c(B):
+    return _box(B, "M 3 3 L 20 3 L 20 20 L 3 20 Z", ROUND_CAP, BEVEL)
+
+
+@case("paths/boxMiter", "tests/test_paths.nim:211-221")
+def _c(B):
+    return _box(B, "M 3 3 L 20 3 L 20 20 L 3 20 Z", ROUND_CAP, MITER)
+
+
+@case("paths/ButtCap", "tests/test_paths.nim:223-233")
+def _c(B):
+    return _box(B, "M 3 3 L 20 3 L 20 20 L 3 20", BUTT, BEVEL)
+
+
+@case("paths/RoundCap", "tests/test_paths.nim:235-245")
+def _c(B):
+    return _box(B, "M 3 3 L 20 3 L 20 20 L 3 20", ROUND_CAP, BEVEL)
+
+
+@case("paths/SquareCap", "tests/test_paths.nim:247-257")
+def _c(B):
+    return _box(B, "M 3 3 L 20 3 L 20 20 L 3 20", SQUARE, BEVEL)
+
+
+@case("paths/dashes", "tests/test_paths.nim:259-296")
+def _c(B):
+    img = B.new_image(60, 120)
+    B.fill(img, WHITE)
+    for ty, dashes in ((5, ()), (25, (2, 2)), (45, (4, 4)), (65, (2, 4, 6, 2)), (85, (1,)),
+                       (105, (1, 2, 3, 4, 5, 6, 7, 8, 9))):
+        _stroke(B, img, "M 0 0 L 50 0", rgba(0, 0, 0, 255), mat=translate(5, ty), width=10,
+                cap=BUTT, join=BEVEL, dashes=[F.f32(d) for d in dashes])
+    return img
+
+
+def _miter(B, angle, limit):
+    img = B.new_image(60, 60)
+    B.fill(img, WHITE)
+    p = Path()
+    p.move_to(-20, 0)
+    p.line_to(0, 0)
+    # th = angle.float32.degToRad() + PI/2 is float64 (degToRad narrows to float32)
+    th = F.f32(F.f32(angle) * math.pi / 180) + math.pi / 2
+    p.line_to(math.sin(th) * 20, math.cos(th) * 20)
+    return _stroke(B, img, p, rgba(0, 0, 0, 255), mat=translate(30, 30), width=8, cap=BUTT,
+                   join=MITER, miter=F.f32(limit))
+
+
+for _a, _l in ((10, 2), (145, 2), (155, 2), (165, 2), (165, 10), (145, 3.32), (145, 3.33)):
+    CASES[f"paths/miterLimit_{_a}deg_{_l:0.2f}num"] = (
+        (lambda a, l: (lambda B: _miter(B, a, l)))(_a, _l), "tests/test_paths.nim:298-320")
+
+
+@case("paths/selfclosing", "tests/test_paths.nim:322-330")
+def _c(B):
+    return _fill(B, 60, 60, "M0 0 L0 0 L60 0 L60 60 L0 60", rgba(127, 127, 127, 255), bg=WHITE)
+
+
+def _two_rects(B, first, second, blend, stroke=False):
+    img = B.new_image(100, 100)
+    B.fill_path(img, parse_path(first).array(), color(1, 0, 0, 1))
+    if stroke:
+        B.stroke_path(img, parse_path(second).array(), color(0, 1, 0, 1), blend=blend, width=10)
+    else:
+        B.fill_path(img, parse_path(second).array(), color(0, 1, 0, 1), blend=blend)
+    return img
+
+
+@case("paths/rectExcludeMask", "tests/test_paths.nim:376-390")
+def _c(B):
+    return _two_rects(B, "M 10 10 H 60 V 60 H 10 z", "M 30 30 H 80 V 80 H 30 z", EXCLUDE_MASK)
+
+
+@case("paths/rectExcludeMaskAA", "tests/test_paths.nim:392-406")
+def _c(B):
+    return _two_rects(B, "M 10.1 10.1 H 60.1 V 60.1 H 10.1 z", "M 30.1 30.1 H 80.1 V 80.1 H 30.1 z",
+                      EXCLUDE_MASK)
+
+
+@case("paths/rectMask", "tests/test_paths.nim:408-422")
+def _c(B):
+    return _two_rects(B, "M 10 10 H 60 V 60 H 10 z", "M 30 30 H 80 V 80 H 30 z", MASK)
+
+
+@case("paths/rectMaskAA", "tests/test_paths.nim:424-438")
+def _c(B):
+    return _two_rects(B, "M 10.1 10.1 H 60.1 V 60.1 H 10.1 z", "M 30.1 30.1 H 80.1 V 80.1 H 30.1 z",
+                      MASK)
+
+
+@case("paths/rectMaskStroke", "tests/test_paths.nim:440-455")
+def _c(B):
+    return _two_rects(B, "M 10 10 H 60 V 60 H 10 z", "M 30 30 H 50 V 50 H 30 z", MASK, stroke=True)
+
+
+CTX_STROKE = dict(width=1.0, cap=BUTT, join=MITER, miter=10.0)  # contexts.nim:53-66
+
+
+@case("paths/arc", "tests/test_paths.nim:457-482")
+def _c(B):
+    img = B.new_image(256, 256)
+    B.fill(img, WHITE)
+    for i in range(4):
+        for j in range(3):
+            p = Path()
+            x = F.add(25.0, F.mul(F.f32(j), 50.0))
+            y = F.add(25.0, F.mul(F.f32(i), 50.0))
+            end = math.pi + (math.pi * F.f32(j)) / 2  # float64, narrowed by arc()
+            p.arc(x, y, 20.0, 0.0, end, i % 2 == 1)
+            if i > 1:
+                B.fill_path(img, p.array(), color(0, 0, 0, 1))
+            else:
+                B.stroke_path(img, p.array(), color(0, 0, 0, 1), **CTX_STROKE)
+    return img
+
+
+@case("paths/arcTo1", "tests/test_paths.nim:484-501")
+def _c(B):
+    img = B.new_image(256, 256)
+    B.fill(img, WHITE)
+    p = Path()
+    p.move_to(230, 20)
+    p.arc_to(90, 130, 20, 20, 50)
+    p.line_to(20, 20)
+    B.stroke_path(img, p.array(), color(0, 0, 0, 1), **CTX_STROKE)
+    return img
+
+
+@case("paths/arcTo2", "tests/test_paths.nim:503-536")
+def _c(B):
+    img = B.new_image(256, 256)
+    B.fill(img, WHITE)
+    p = Path()
+    p.move_to(200, 20)
+    p.line_to(200, 130)
+    p.line_to(50, 20)
+    B.stroke_path(img, p.array(), rgba(128, 128, 128, 255), **CTX_STROKE)
+    p = Path()
+    p.move_to(200, 20)
+    p.arc_to(200, 130, 50, 20, 40)
+    B.stroke_path(img, p.array(), rgba(0, 0, 0, 255), width=5.0, cap=BUTT, join=MITER, miter=10.0)
+    p = Path()
+    p.arc(200, 20, 5, 0, 2 * math.pi)
+    B.fill_path(img, p.array(), rgba(0, 0, 255, 255))
+    p = Path()
+    p.arc(200, 130, 5, 0, 2 * math.pi)
+    p.arc(50, 20, 5, 0, 2 * math.pi)
+    B.fill_path(img, p.array(), rgba(255, 0, 0, 255))
+    return img
+
+
+@case("paths/arcTo3", "tests/test_paths.nim:538-551")
+def _c(B):
+    img = B.new_image(256, 256)
+    B.fill(img, WHITE)
+    p = Path()
+    p.move_to(180, 90)
+    p.arc_to(180, 130, 110, 130, 130)
+    p.line_to(110, 130)
+    B.stroke_path(img, p.array(), color(0, 0, 0, 1), **CTX_STROKE)
+    return img
+
+
+@case("paths/opacityFill", "tests/test_paths.nim:582-593")
+def _c(B):
+    p = Path()
+    p.circle(50, 50, 30)
+    img = B.new_image(100, 100)
+    B.fill_path(img, p.array(), color(1, 0, 1, 1), opacity=0.5)
+    return img
+
+
+@case("paths/opacityStroke", "tests/test_paths.nim:595-606")
+def _c(B):
+    p = Path()
+    p.circle(50, 50, 30)
+    img = B.new_image(100, 100)
+    B.stroke_path(img, p.array(), color(1, 0, 1, 1), opacity=0.5, width=10)
+    return img
+
+
+@case("paths/pathStroke1Big", "tests/test_paths.nim:608-614")
+def _c(B):
+    return _stroke(B, B.new_image(100, 100), "M0 0 L200 200", rgba(255, 0, 0, 255), width=10)
+
+
+@case("paths/path1pxCover", "tests/test_paths.nim:616-622")
+def _c(B):
+    return _fill(B, 100, 100, "M99 99 L999 99 L999 100 L99 100 Z", rgba(255, 0, 0, 255))
+
+
+@case("paths/path0pxCover", "tests/test_paths.nim:624-630")
+def _c(B):
+    return _fill(B, 100, 100, "M100 100 L999 100 L999 101 L100 101 Z", rgba(255, 0, 0, 255))
+
+
+for _i in range(3, 9):
+    def _mk(i):
+        def fn(B):
+            p = Path()
+            p.polygon(50, 50, 30, i)
+            img = B.new_image(100, 100)
+            B.fill_path(img, p.array(), color(1, 1, 1, 1))
+            return img
+        return fn
+    CASES[f"paths/polygon{_i}"] = (_mk(_i), "tests/test_paths.nim:650-657")
+
+
+@case("paths/pathSwish", "tests/test_paths.nim:701-710")
+def _c(B):
+    return _fill(B, 100, 100, "M 40 40 L 40 80 L 80 80 L 80 40 C 80 -20 40 100 40 40",
+                 rgba(0, 0, 0, 255), bg=WHITE)
+
+
+# ---- tests/test_paints.nim ------------------------------------------------
+@case("paths/paintSolid", "tests/test_paints.nim:11-17")
+def _c(B):
+    return _fill(B, 100, 100, HEART, rgba(255, 0, 0, 255))
+
+
+# ---- tests/test_images.nim / test_images_draw.nim ------------------------
+def _blur20(B, oob):
+    img = B.new_image(100, 100)
+    B.fill(img, rgba(0, 0, 0, 255))
+    p = Path()
+    p.rect(25, 25, 50, 50)
+    B.fill_path(img, p.array(), rgba(255, 255, 255, 255))
+    B.blur(img, 20.0, oob)
+    return img
+
+
+@case("images/imageblur20", "tests/test_images.nim:126-132")
+def _c(B):
+    return _blur20(B, (0, 0, 0, 0))
+
+
+@case("images/imageblur20oob", "tests/test_images.nim:134-140")
+def _c(B):
+    return _blur20(B, (0, 0, 0, 255))
+
+
+@case("images/fillOptimization", "tests/test_images_draw.nim:266-281")
+def _c(B):
+    path = "M 0 0 L 20 0 L 20 20 L 0 20 z"
+    img = B.new_image(20, 20)
+    stroke = B.new_image(20, 20)
+    B.fill_path(img, parse_path(path).array(), color(1.0, 0.5, 0.25, 1.0))
+    B.stroke_path(stroke, parse_path(path).array(), color(1, 1, 1, 1), width=4)
+    B.draw(img, stroke, 0, 0, NORMAL)
+    return img
+
+
+@case("images/fillOptimization2", "tests/test_images_draw.nim:284-309")
+def _c(B):
+    a = B.new_image(100, 100)
+    B.fill(a, color(1, 1, 1, 1))
+    draws = [((-50, -50), color(1, 0, 0, 1)), ((50, -50), color(0, 1, 0, 1)),
+             ((50, 50), color(0, 0, 1, 1)), ((-50, 50), color(1, 1, 0, 1)),
+             ((-100, 0), color(1, 0, 1, 1)), ((0, -100), color(0, 1, 1, 1)),
+             ((100, 0), color(0.5, 0.5, 0.5, 1)), ((0, 100), color(0.75, 0.75, 0, 1))]
+    for (tx, ty), col in draws:
+        b = B.new_image(100, 100)
+        p = Path()
+        p.rect(0, 0, 100, 100)
+        B.stroke_path(b, p.array(), col, width=20)
+        B.draw(a, b, tx, ty, NORMAL)
+    return a
+
+
+def _mask_rect(B):
+    p = Path()
+    p.rect(10, 10, 80, 80)
+    mask = B.new_image(100, 100)
+    B.fill_path(mask, p.array(), color(1, 1, 1, 1))
+    return mask
+
+
+for _i, (_tx, _ty) in enumerate([(0, 0), (50, -50), (50, 50), (-50, 50), (-50, -50)]):
+    def _mk(tx, ty):
+        def fn(B):
+            mask = _mask_rect(B)
+            a = B.new_image(100, 100)
+            B.fill(a, color(0, 0, 1, 1))
+            B.draw(a, mask, tx, ty, MASK)
+            return a
+        return fn
+    CASES[f"images/maskClearsOnDraw{_i}"] = (_mk(_tx, _ty), "tests/test_images_draw.nim:311-331")
+
+
+# ---- tests/test_contexts.nim ----------------------------------------------
+@case("contexts/blendmode_1", "tests/test_contexts.nim:526-540")
+def _c(B):
+    img = B.new_image(300, 150)
+    B.fill(img, rgba(255, 255, 255, 255))
+    p = Path()
+    p.rect(10, 10, 100, 100)
+    B.fill_path(img, p.array(), color(0, 0, 1, 1), blend=EXCLUSION)
+    return img
+
+
+# Known-answer asserts (not images) --------------------------------------
+MASK_OUT_OF_BOUNDS = [(100, 100), (100, -100), (-100, 100), (-100, -100), (0, 1000), (0, -1000),
+                      (1000, 0), (-1000, 0), (1000, 1000), (1000, -1000), (-1000, 1000),
+                      (-1000, -1000)]  # tests/test_images_draw.nim:333-360
+
+
+def mask_out_of_bounds_transparent(B) -> bool:
+    mask = _mask_rect(B)
+    a = B.new_image(100, 100)
+    for tx, ty in MASK_OUT_OF_BOUNDS:
+        B.fill(a, color(0, 0, 1, 1))
+        B.draw(a, mask, tx, ty, MASK)
+        if B.pixels(a)[..., 3].any():
+            return False
+    return True
+
+
+def fill_optimization_pixel(B):
+    """tests/test_images_draw.nim:282: image[10, 10] == rgbx(255, 128, 64, 255)"""
+    img = CASES["images/fillOptimization"][0](B)
+    return tuple(int(v) for v in B.pixels(img)[10, 10])

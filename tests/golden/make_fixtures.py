@@ -1,0 +1,33 @@
+"""Regenerates tests/golden/goldens.npz from the reference's golden PNGs.
+
+Run once in a checkout that has the pixie reference next to it:
+    python tests/golden/make_fixtures.py /path/to/pixie
+Each entry is the straight-alpha RGBA uint8 pixel array of one master PNG that
+the reference's own tests write (tests/paths, tests/images, tests/contexts),
+keyed like "paths/pathHeart".  Only the masters used by tests/golden/cases.py
+are stored.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+sys.path.insert(0, HERE)
+
+from png import read_png  # noqa: E402
+from cases import CASES  # noqa: E402
+
+
+def main(ref_root: str) -> None:
+    out = {}
+    for name in sorted(CASES):
+        path = os.path.join(ref_root, "tests", name + ".png")
+        out[name.replace("/", "__")] = read_png(path)
+    np.savez_compressed(os.path.join(HERE, "goldens.npz"), **out)
+    print(f"wrote {len(out)} goldens")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
