@@ -1,0 +1,490 @@
+#!/usr/bin/env python3
+"""Benchmark of pixie's raster hot path on GB300 (one JSON line on stdout).
+
+Workload (the composite-and-blur configuration): per step
+  * draw() of a 2048x2048 premultiplied RGBX image onto another under each of
+    the 16 blend modes and the 4 mask modes (20 destination/source pairs, so
+    a step's working set, 640 MB, is far larger than the 129 MB L2);
+  * gaussian blur of a 4096x4096 image at radius 1, 4, 16 and 64;
+  * shadow (offset (8, 8), spread 4, blur 12) of a 1024x1024 mask of 64 discs.
+Metric unit: Gpix/s = pixels processed (20 x 2048^2 + 4 x 4096^2 + 1024^2)
+per step / step time.  Inputs are seeded synthetic data with the shapes and
+value distributions of the configuration.
+
+  --impl pxg        (default) the CUDA library through its C ABI
+  --impl reference  the reference's CPU path (the C++ restatement in oracle/,
+                    pixie itself is Nim and cannot be built here) on all host
+                    cores, on a bounded sample of the same workload
+Also reported: the plain per-call fillPath (512x512, 64 random cubics) and
+the batched 4096-glyph fill, in "extra".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "paths/s & Gpix/s on 1 GB300, batched vs plain GPU, bit-exact; p50/p99 job latency"
+DRAW_W = 2048
+BLUR_W = 4096
+RADII = (1, 4, 16, 64)
+SHADOW_W = 1024
+N_MODES = 20
+STEP_PIXELS = N_MODES * DRAW_W * DRAW_W + len(RADII) * BLUR_W * BLUR_W + SHADOW_W * SHADOW_W
+WORKLOAD = {"workload": "composite+blur: draw 2048^2 x 20 modes, blur 4096^2 r in {1,4,16,64}, "
+                        "shadow 1024^2 (offset 8,8 spread 4 blur 12)",
+            "draw_images": "20 dst + 20 src 2048x2048 RGBX", "blur_image": "4096x4096 RGBX x 4",
+            "l2": "inputs larger than L2: 640 MB of draw images cycled per step"}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# -- clocks -------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi samples every 100 ms while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        time.sleep(0.15)
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# -- distributed helpers ----------------------------------------------------------------
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, v):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# -- GPU arm ------------------------------------------------------------------------------
+def run_gpu(args, ws, rank, local):
+    import torch
+
+    import pixie_gb300 as px
+    from pixie_gb300 import workloads as wl
+
+    torch.cuda.set_device(local)
+    px.lib().pxg_init(local)
+    stream = torch.cuda.Stream()
+    px.set_stream(stream.cuda_stream)
+
+    seed = 1 + rank
+    a_host = [wl.premultiplied_image(seed * 10 + i, DRAW_W, DRAW_W) for i in range(2)]
+    b_host = [wl.premultiplied_image(seed * 10 + 5 + i, DRAW_W, DRAW_W) for i in range(2)]
+    blur_host = wl.premultiplied_image(seed * 10 + 9, BLUR_W, BLUR_W)
+    A = [px.Image.from_numpy(a_host[i % 2]) for i in range(N_MODES)]
+    B = [px.Image.from_numpy(b_host[i % 2]) for i in range(N_MODES)]
+    BL = [px.Image.from_numpy(blur_host) for _ in RADII]
+    M = px.Image(SHADOW_W, SHADOW_W)
+    M.fill_path(wl.disc_mask_path(seed), [1, 1, 1, 1])
+    SH = px.Image(SHADOW_W, SHADOW_W)
+    black = [0, 0, 0, 1]
+    px.set_blocking(False)
+
+    ops = ([("draw", k) for k in range(N_MODES)] + [("blur", r) for r in RADII] + [("shadow", 0)])
+
+    def run_op(op):
+        kind, p = op
+        if kind == "draw":
+            A[p].draw(B[p], (0, 0), p)
+        elif kind == "blur":
+            BL[RADII.index(p)].blur(p)
+        else:
+            M.shadow_into(SH, (8, 8), 4, 12, black)
+
+    # warm-up
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            for op in ops:
+                run_op(op)
+    stream.synchronize()
+
+    # timed region: K steps, events around every op on the library's stream
+    n_ops = len(ops)
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(n_ops + 1)] for _ in range(args.steps)]
+    l0 = px.launch_count()
+    barrier(ws)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for s in range(args.steps):
+            for i, op in enumerate(ops):
+                evs[s][i].record(stream)
+                run_op(op)
+            evs[s][n_ops].record(stream)
+        t1.record(stream)
+        stream.synchronize()
+        torch.cuda.synchronize()
+        barrier(ws)
+    launches = (px.launch_count() - l0) // args.steps
+    total_ms = max_over_ranks(ws, t0.elapsed_time(t1))
+    ms_step = total_ms / args.steps
+    op_ms = np.zeros(n_ops)
+    for s in range(args.steps):
+        for i in range(n_ops):
+            op_ms[i] += evs[s][i].elapsed_time(evs[s][i + 1])
+    op_ms /= args.steps
+
+    # roofline of the dominant operation
+    dom = int(np.argmax(op_ms))
+    kind, p = ops[dom]
+    if kind == "draw":
+        bpp = 8 if p == 17 else 12
+        algo = bpp * DRAW_W * DRAW_W
+        unit_desc = f"draw mode {p}: {bpp} B/px x 2048^2 px"
+    elif kind == "blur":
+        algo = 8 * BLUR_W * BLUR_W
+        unit_desc = f"blur r={p}: 8 B/px x 4096^2 px (X and Y pass, read once + write once)"
+    else:
+        algo = 5 * SHADOW_W * SHADOW_W
+        unit_desc = "shadow: 5 B/px x 1024^2 px"
+    peak, peak_src = peaks()
+    achieved = algo / (op_ms[dom] * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": f"{kind}:{p}", "unit_bytes": algo, "unit": "GB/s",
+            "achieved": round(achieved, 1), "peak": peak, "peak_source": peak_src,
+            "frac": round(achieved / peak, 4), "traffic": TRAFFIC.get(f"{kind}:{p}"),
+            "per_launch": unit_desc}
+    draw_ms = op_ms[:N_MODES]
+    draw_gbs = [(8 if m == 17 else 12) * DRAW_W * DRAW_W / (t * 1e-3) / 1e9 for m, t in enumerate(draw_ms)]
+    blur_ms = {r: round(float(op_ms[N_MODES + i]), 4) for i, r in enumerate(RADII)}
+
+    # end to end through the C ABI with host buffers (pinned), copies timed
+    e2e = run_e2e(px, A, B, BL, M, SH, a_host, b_host, blur_host, run_op, ops, args, ws)
+
+    extra = {"per_op_ms": {f"{k}:{p}": round(float(t), 4) for (k, p), t in zip(ops, op_ms)},
+             "draw_gbs_min_median_max": [round(min(draw_gbs), 1), round(statistics.median(draw_gbs), 1),
+                                         round(max(draw_gbs), 1)],
+             "blur_ms": blur_ms}
+    if rank == 0 and not args.no_fill:
+        extra.update(run_fill_extras(px, wl, args))
+    return ms_step, launches, roof, e2e, extra, clk.summary()
+
+
+def run_e2e(px, A, B, BL, M, SH, a_host, b_host, blur_host, run_op, ops, args, ws):
+    import torch
+    pinned_a = [torch.from_numpy(a).pin_memory().numpy() for a in a_host]
+    pinned_b = [torch.from_numpy(b).pin_memory().numpy() for b in b_host]
+    pinned_blur = torch.from_numpy(blur_host).pin_memory().numpy()
+    out_draw = torch.empty((DRAW_W, DRAW_W, 4), dtype=torch.uint8).pin_memory().numpy()
+    out_blur = torch.empty((BLUR_W, BLUR_W, 4), dtype=torch.uint8).pin_memory().numpy()
+    out_sh = torch.empty((SHADOW_W, SHADOW_W, 4), dtype=torch.uint8).pin_memory().numpy()
+    mask_host = M.to_numpy()
+    pinned_mask = torch.from_numpy(mask_host).pin_memory().numpy()
+    steps = max(1, min(args.steps, args.e2e_steps))
+    h2d = d2h = 0
+    barrier(ws)
+    px.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        h2d = d2h = 0
+        for k in range(N_MODES):  # inputs host -> device
+            A[k].upload(pinned_a[k % 2])
+            B[k].upload(pinned_b[k % 2])
+            h2d += 2 * DRAW_W * DRAW_W * 4
+        for im in BL:
+            im.upload(pinned_blur)
+            h2d += BLUR_W * BLUR_W * 4
+        M.upload(pinned_mask)
+        h2d += SHADOW_W * SHADOW_W * 4
+        for op in ops:
+            run_op(op)
+        for k in range(N_MODES):  # results device -> host
+            px.lib().pxg_image_download(A[k]._h, px._ptr(out_draw), out_draw.nbytes)
+            d2h += out_draw.nbytes
+        for im in BL:
+            px.lib().pxg_image_download(im._h, px._ptr(out_blur), out_blur.nbytes)
+            d2h += out_blur.nbytes
+        px.lib().pxg_image_download(SH._h, px._ptr(out_sh), out_sh.nbytes)
+        d2h += out_sh.nbytes
+    px.synchronize()
+    dt = time.perf_counter() - t0
+    dt = max_over_ranks(ws, dt)
+    return {"value": round(STEP_PIXELS * steps * int(os.environ.get("WORLD_SIZE", "1")) / dt / 1e9, 3),
+            "unit": "Gpix/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "steps": steps, "ms_per_step": round(dt / steps * 1e3, 3)}
+
+
+def run_fill_extras(px, wl, args):
+    """Plain per-call fillPath and the batched glyph fill (paths/s)."""
+    out = {}
+    img = px.Image(512, 512)
+    paths = [wl.plain_path(s) for s in range(1, 41)]
+    px.set_blocking(True)
+    for c in paths[:5]:
+        img.fill_path(c, wl.PLAIN_COLOR)
+    t = time.perf_counter()
+    gpu_ms = 0.0
+    n = 0
+    for rep in range(5):
+        for c in paths:
+            img.fill_path(c, wl.PLAIN_COLOR)
+            gpu_ms += px.last_gpu_ms()
+            n += 1
+    dt = time.perf_counter() - t
+    out["plain_fill_512_64cubics"] = {"paths_per_s": round(n / dt, 1),
+                                      "gpu_ms_per_path": round(gpu_ms / n, 4),
+                                      "note": "one blocking C-ABI call per path, host pre-pass included"}
+    glyphs, _ = wl.glyph_batch(7, n=args.glyphs)
+    imgs = [px.Image(w, h) for (_, w, h, _) in glyphs]
+    cmds = [g[0] for g in glyphs]
+    cols = [[1, 1, 1, 1]] * len(glyphs)
+    winds = [g[3] for g in glyphs]
+    px.fill_paths_batch(imgs, cmds, cols, winding_rules=winds)
+    t = time.perf_counter()
+    reps = 3
+    for _ in range(reps):
+        px.fill_paths_batch(imgs, cmds, cols, winding_rules=winds)
+    dt_b = (time.perf_counter() - t) / reps
+    t = time.perf_counter()
+    for im, c, w in zip(imgs, cmds, winds):
+        im.fill_path(c, [1, 1, 1, 1], None, w)
+    dt_p = time.perf_counter() - t
+    out["glyph_batch"] = {"glyphs": len(glyphs), "batched_paths_per_s": round(len(glyphs) / dt_b, 1),
+                          "plain_paths_per_s": round(len(glyphs) / dt_p, 1),
+                          "batched_over_plain": round(dt_p / dt_b, 2)}
+    px.set_blocking(False)
+    return out
+
+
+# Per-launch DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) from
+# the ncu captures summarised in profiles/; None until captured.
+TRAFFIC = {}
+
+
+# -- CPU baseline / reference arm ----------------------------------------------------------
+def cpu_sample_rates(seed=1):
+    """Single-thread oracle throughput per operation on a bounded sample.
+    Returns (estimated seconds for one full step, description)."""
+    from oracle import pxo
+    from pixie_gb300 import workloads as wl
+    S = 1024
+    a = wl.premultiplied_image(seed * 10, S, S)
+    b = wl.premultiplied_image(seed * 10 + 5, S, S)
+    est = 0.0
+    for mode in range(N_MODES):
+        x = a.copy()
+        t = time.perf_counter()
+        pxo.draw(x, b, 0, 0, mode)
+        dt = time.perf_counter() - t
+        est += dt * (DRAW_W * DRAW_W) / (S * S)
+    bl = wl.premultiplied_image(seed * 10 + 9, 1024, 384)
+    for r in RADII:
+        x = bl.copy()
+        t = time.perf_counter()
+        pxo.blur(x, r)
+        dt = time.perf_counter() - t
+        est += dt * (BLUR_W * BLUR_W) / x[..., 0].size
+    mask = pxo.new_image(SHADOW_W, SHADOW_W)
+    pxo.fill_path(mask, wl.disc_mask_path(seed), [1, 1, 1, 1])
+    t = time.perf_counter()
+    pxo.shadow(mask, 8, 8, 4, 12, [0, 0, 0, 1])
+    est += time.perf_counter() - t
+    return est, ("oracle (C++ restatement of pixie's scalar path), 1 thread: draw 20 modes on "
+                 "1024^2, blur r in {1,4,16,64} on 1024x384, shadow on 1024^2; scaled per pixel "
+                 "to the full step")
+
+
+def _ref_worker(seed):
+    sys.path.insert(0, ROOT)
+    est, _ = cpu_sample_rates(seed)
+    return est
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return None
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        for _ in range(args.warmup):
+            pool.map(_ref_worker, range(1, cores + 1))
+        t = time.perf_counter()
+        est_total = 0.0
+        for _ in range(args.steps):
+            ests = pool.map(_ref_worker, range(1, cores + 1))
+            est_total += statistics.mean(ests)
+        wall = time.perf_counter() - t
+    per_step_single = est_total / args.steps
+    value = STEP_PIXELS * cores / per_step_single / 1e9  # cores run independent steps
+    return {"value": value, "cores": cores, "wall_s": wall,
+            "ms_per_step": per_step_single * 1e3 / cores}
+
+
+def run_case(case: str):
+    """One small, self-contained invocation of a single operation (used for
+    ncu captures of one kernel on a small case)."""
+    import pixie_gb300 as px
+    from pixie_gb300 import workloads as wl
+    px.lib().pxg_init(0)
+    if case == "fill512":  # the plain fill: 512x512, 64 random cubics
+        img = px.Image(512, 512)
+        for s in (1, 2, 3):
+            img.fill_path(wl.plain_path(s), wl.PLAIN_COLOR)
+    elif case == "blur64":  # blur radius 64 of a 4096x4096 image
+        img = px.Image.from_numpy(wl.premultiplied_image(9, 4096, 4096))
+        for _ in range(2):
+            img.blur(64)
+    elif case == "draw":  # NormalBlend draw of 4096x4096 onto 4096x4096 (inputs > L2)
+        a = px.Image.from_numpy(wl.premultiplied_image(1, 4096, 4096))
+        b = px.Image.from_numpy(wl.premultiplied_image(2, 4096, 4096))
+        for _ in range(2):
+            a.draw(b, (0, 0), 0)
+    elif case == "glyphs":  # batched fill of 512 glyph masks
+        glyphs, _ = wl.glyph_batch(7, n=512)
+        imgs = [px.Image(w, h) for (_, w, h, _) in glyphs]
+        for _ in range(2):
+            px.fill_paths_batch(imgs, [g[0] for g in glyphs], [[1, 1, 1, 1]] * len(glyphs),
+                                winding_rules=[g[3] for g in glyphs])
+    else:
+        raise SystemExit(f"unknown case {case}")
+    px.synchronize()
+    print(json.dumps({"case": case, "launches": px.launch_count()}))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="pxg", choices=["pxg", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--glyphs", type=int, default=4096)
+    ap.add_argument("--no-fill", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--case", default=None,
+                    help="run one small operation for profiling: fill512 | blur64 | draw | glyphs")
+    args = ap.parse_args()
+    if args.case:
+        run_case(args.case)
+        return
+    ws, rank, local = dist_setup()
+
+    if args.impl == "reference":
+        r = run_reference(args, ws, rank)
+        if rank == 0:
+            line = {"metric": METRIC, "value": round(r["value"], 4), "unit": "Gpix/s",
+                    "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+                    "ms_per_step": round(r["ms_per_step"], 3), "higher_is_better": True,
+                    "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+                    "config": WORKLOAD, "impl": "reference",
+                    "cpu_baseline": {"value": round(r["value"], 4), "unit": "Gpix/s",
+                                     "cores": r["cores"], "kind": "port",
+                                     "sample": "per core: draw 20 modes on 1024^2, blur r in "
+                                               "{1,4,16,64} on 1024x384, shadow 1024^2, scaled "
+                                               "per pixel; pixie (Nim) cannot be built here, so "
+                                               "this is the oracle's C++ restatement"},
+                    "e2e": {"value": round(r["value"], 4), "unit": "Gpix/s",
+                            "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            print(json.dumps(line), flush=True)
+        return
+
+    ms_step, launches, roof, e2e, extra, clocks = run_gpu(args, ws, rank, local)
+    if rank != 0:
+        return
+    value = STEP_PIXELS * ws / (ms_step * 1e-3) / 1e9
+    cpu = None
+    if not args.no_cpu_baseline:
+        est, sample = cpu_sample_rates(1)
+        cpu = {"value": round(STEP_PIXELS / est / 1e9, 5), "unit": "Gpix/s", "cores": 1,
+               "kind": "port", "sample": sample}
+    line = {"metric": METRIC, "value": round(value, 3), "unit": "Gpix/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+            "data": "synthetic (seeded splitmix64; shapes/distributions of the configuration)",
+            "config": WORKLOAD, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": int(launches), "clocks": clocks, "extra": extra}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,297 @@
+"""pixie's raster hot path on a GB300, behind pixie's own API shape.
+
+``Image`` mirrors pixie's Image (src/pixie/common.nim:34-37) with its pixels
+resident in GPU memory; its methods are the reference's fillPath,
+strokePath, draw, blur, shadow and fill (src/pixie/paths.nim:2093-2175,
+src/pixie/images.nim:55-776), executed by the CUDA library libpxg.so through
+the C ABI declared in include/pxg.h.  There is no CPU fallback: constructing
+an Image fails loudly if the library or the GPU is unavailable.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+import os
+
+import numpy as np
+
+from .paths import Path, PixieError, as_commands, parse_path  # noqa: F401
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libpxg.so")
+
+
+class BlendMode(enum.IntEnum):  # common.nim:6-29
+    NormalBlend = 0
+    DarkenBlend = 1
+    MultiplyBlend = 2
+    ColorBurnBlend = 3
+    LightenBlend = 4
+    ScreenBlend = 5
+    ColorDodgeBlend = 6
+    OverlayBlend = 7
+    SoftLightBlend = 8
+    HardLightBlend = 9
+    DifferenceBlend = 10
+    ExclusionBlend = 11
+    HueBlend = 12
+    SaturationBlend = 13
+    ColorBlend = 14
+    LuminosityBlend = 15
+    MaskBlend = 16
+    OverwriteBlend = 17
+    SubtractMaskBlend = 18
+    ExcludeMaskBlend = 19
+
+
+class WindingRule(enum.IntEnum):  # paths.nim:5-8
+    NonZero = 0
+    EvenOdd = 1
+
+
+class LineCap(enum.IntEnum):  # paths.nim:10-12
+    ButtCap = 0
+    RoundCap = 1
+    SquareCap = 2
+
+
+class LineJoin(enum.IntEnum):  # paths.nim:14-16
+    MiterJoin = 0
+    RoundJoin = 1
+    BevelJoin = 2
+
+
+DEFAULT_MITER_LIMIT = 4.0  # paths.nim:46
+
+_lib = None
+
+
+def lib():
+    """The loaded libpxg.so (raises if it is missing: no CPU fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise PixieError(f"libpxg.so is not built ({LIB_PATH}); run python -m pixie_gb300.build")
+        L = C.CDLL(LIB_PATH)
+        P, I64, F, I = C.c_void_p, C.c_int64, C.c_float, C.c_int
+        L.pxg_take_error.restype = C.c_char_p
+        L.pxg_init.argtypes = [I]
+        L.pxg_set_stream.argtypes = [P]
+        L.pxg_new_image.restype = P
+        L.pxg_new_image.argtypes = [I64, I64]
+        L.pxg_image_wrap.restype = P
+        L.pxg_image_wrap.argtypes = [P, I64, I64]
+        L.pxg_image_free.argtypes = [P]
+        L.pxg_image_free.restype = None
+        L.pxg_image_width.argtypes = [P]
+        L.pxg_image_width.restype = I64
+        L.pxg_image_height.argtypes = [P]
+        L.pxg_image_height.restype = I64
+        L.pxg_image_device_ptr.argtypes = [P]
+        L.pxg_image_device_ptr.restype = P
+        L.pxg_image_upload.argtypes = [P, P, I64]
+        L.pxg_image_download.argtypes = [P, P, I64]
+        L.pxg_image_fill.argtypes = [P, P]
+        L.pxg_image_fill_path.argtypes = [P, P, I64, P, F, I, P, I]
+        L.pxg_image_stroke_path.argtypes = [P, P, I64, P, F, I, P, F, I, I, F, P, I64]
+        L.pxg_image_draw.argtypes = [P, P, I64, I64, I]
+        L.pxg_image_blur.argtypes = [P, F, P]
+        L.pxg_image_spread.argtypes = [P, F]
+        L.pxg_image_shadow.argtypes = [P, F, F, F, F, P]
+        L.pxg_image_shadow.restype = P
+        L.pxg_image_shadow_into.argtypes = [P, P, F, F, F, F, P]
+        L.pxg_set_blocking.argtypes = [I]
+        L.pxg_launch_count.restype = I64
+        L.pxg_blend_pixels.argtypes = [I, P, P, P, I64]
+        L.pxg_fill_paths_batch.argtypes = [P, I64, P, P, P, P, P, P, P, P]
+        L.pxg_last_gpu_ms.restype = F
+        _lib = L
+    return _lib
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise PixieError(lib().pxg_take_error().decode())
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _color(c) -> np.ndarray:
+    return np.ascontiguousarray(c, dtype=np.float32).reshape(4)
+
+
+def _mat(m):
+    if m is None:
+        return None
+    return np.ascontiguousarray(m, dtype=np.float32).reshape(9)
+
+
+def rgba(r, g, b, a=255):
+    """ColorRGBA as a paint colour: chroma's Color is c / 255 in float32."""
+    return [np.float32(v) / np.float32(255) for v in (r, g, b, a)]
+
+
+def translate(x, y):
+    return np.array([1, 0, 0, 0, 1, 0, x, y, 1], dtype=np.float32)
+
+
+def scale(x, y):
+    return np.array([x, 0, 0, 0, y, 0, 0, 0, 1], dtype=np.float32)
+
+
+class Paint:
+    """A solid paint (paints.nim:12-26): colour, opacity and blend mode."""
+
+    def __init__(self, color=(0, 0, 0, 1), opacity=1.0, blend_mode=BlendMode.NormalBlend):
+        self.color = color
+        self.opacity = opacity
+        self.blend_mode = blend_mode
+
+
+def _paint(p):
+    if isinstance(p, Paint):
+        return _color(p.color), float(p.opacity), int(p.blend_mode)
+    return _color(p), 1.0, int(BlendMode.NormalBlend)
+
+
+class Image:
+    """A premultiplied RGBX image resident in GPU memory."""
+
+    def __init__(self, width: int, height: int, _handle=None):
+        if _handle is None:
+            _handle = lib().pxg_new_image(int(width), int(height))
+            if not _handle:
+                raise PixieError(lib().pxg_take_error().decode())
+        self._h = _handle
+        self.width = int(lib().pxg_image_width(self._h))
+        self.height = int(lib().pxg_image_height(self._h))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.pxg_image_free(h)
+            self._h = None
+
+    @classmethod
+    def from_numpy(cls, arr: np.ndarray) -> "Image":
+        arr = np.ascontiguousarray(arr, dtype=np.uint8)
+        img = cls(arr.shape[1], arr.shape[0])
+        _check(lib().pxg_image_upload(img._h, _ptr(arr), arr.nbytes))
+        return img
+
+    @classmethod
+    def wrap(cls, device_ptr: int, width: int, height: int) -> "Image":
+        h = lib().pxg_image_wrap(C.c_void_p(device_ptr), int(width), int(height))
+        if not h:
+            raise PixieError(lib().pxg_take_error().decode())
+        return cls(width, height, _handle=h)
+
+    @property
+    def device_ptr(self) -> int:
+        return int(lib().pxg_image_device_ptr(self._h))
+
+    def to_numpy(self) -> np.ndarray:
+        out = np.empty((self.height, self.width, 4), dtype=np.uint8)
+        _check(lib().pxg_image_download(self._h, _ptr(out), out.nbytes))
+        return out
+
+    def upload(self, arr: np.ndarray):
+        arr = np.ascontiguousarray(arr, dtype=np.uint8)
+        _check(lib().pxg_image_upload(self._h, _ptr(arr), arr.nbytes))
+
+    # -- pixie's Image procs -------------------------------------------------
+    def fill(self, color):
+        _check(lib().pxg_image_fill(self._h, _ptr(_color(color))))
+
+    def fill_path(self, path, paint, transform=None, winding_rule=WindingRule.NonZero):
+        cmds = as_commands(path)
+        col, op, blend = _paint(paint)
+        m = _mat(transform)
+        _check(lib().pxg_image_fill_path(self._h, _ptr(cmds), cmds.size, _ptr(col), op, blend,
+                                         None if m is None else _ptr(m), int(winding_rule)))
+
+    def stroke_path(self, path, paint, transform=None, stroke_width=1.0,
+                    line_cap=LineCap.ButtCap, line_join=LineJoin.MiterJoin,
+                    miter_limit=DEFAULT_MITER_LIMIT, dashes=()):
+        cmds = as_commands(path)
+        col, op, blend = _paint(paint)
+        m = _mat(transform)
+        d = np.ascontiguousarray(list(dashes) if len(dashes) else [0.0], dtype=np.float32)
+        _check(lib().pxg_image_stroke_path(self._h, _ptr(cmds), cmds.size, _ptr(col), op, blend,
+                                           None if m is None else _ptr(m), float(stroke_width),
+                                           int(line_cap), int(line_join), float(miter_limit),
+                                           _ptr(d), len(dashes)))
+
+    def draw(self, b: "Image", translate_xy=(0, 0), blend_mode=BlendMode.NormalBlend):
+        tx, ty = translate_xy
+        if tx != int(tx) or ty != int(ty):
+            raise PixieError("only integer translations take draw's blendRect path")
+        _check(lib().pxg_image_draw(self._h, b._h, int(tx), int(ty), int(blend_mode)))
+
+    def blur(self, radius: float, out_of_bounds=(0, 0, 0, 0)):
+        _check(lib().pxg_image_blur(self._h, float(radius), _ptr(_color(out_of_bounds))))
+
+    def spread(self, spread: float):
+        _check(lib().pxg_image_spread(self._h, float(spread)))
+
+    def shadow(self, offset, spread: float, blur: float, color) -> "Image":
+        h = lib().pxg_image_shadow(self._h, float(offset[0]), float(offset[1]), float(spread),
+                                   float(blur), _ptr(_color(color)))
+        if not h:
+            raise PixieError(lib().pxg_take_error().decode())
+        return Image(0, 0, _handle=h)
+
+    def shadow_into(self, out: "Image", offset, spread: float, blur: float, color):
+        _check(lib().pxg_image_shadow_into(self._h, out._h, float(offset[0]), float(offset[1]),
+                                           float(spread), float(blur), _ptr(_color(color))))
+
+
+def blend_pixels(mode: int, backdrop_dev: int, source_dev: int, out_dev: int, n: int):
+    """blender(mode) over n device pixels (for testing the blend modes)."""
+    _check(lib().pxg_blend_pixels(int(mode), C.c_void_p(backdrop_dev), C.c_void_p(source_dev),
+                                  C.c_void_p(out_dev), int(n)))
+
+
+def fill_paths_batch(images, paths, colors, opacities=None, blend_modes=None, transforms=None,
+                     winding_rules=None) -> np.ndarray:
+    """Many independent fillPath calls (one per image) in one launch."""
+    n = len(images)
+    cmds = [as_commands(p) for p in paths]
+    offs = np.zeros(n + 1, np.int64)
+    offs[1:] = np.cumsum([c.size for c in cmds])
+    allc = np.concatenate(cmds).astype(np.float32) if n else np.zeros(1, np.float32)
+    cols = np.ascontiguousarray(colors, np.float32).reshape(n, 4)
+    ops = np.ascontiguousarray(np.ones(n) if opacities is None else opacities, np.float32)
+    bl = np.ascontiguousarray(np.zeros(n) if blend_modes is None else blend_modes, np.int32)
+    wr = np.ascontiguousarray(np.zeros(n) if winding_rules is None else winding_rules, np.int32)
+    tr = None if transforms is None else np.ascontiguousarray(transforms, np.float32).reshape(n, 9)
+    handles = (C.c_void_p * n)(*[im._h for im in images])
+    status = np.zeros(n, np.int32)
+    _check(lib().pxg_fill_paths_batch(handles, n, _ptr(allc), _ptr(offs), _ptr(cols), _ptr(ops),
+                                      _ptr(bl), None if tr is None else _ptr(tr), _ptr(wr),
+                                      _ptr(status)))
+    return status
+
+
+def last_gpu_ms() -> float:
+    return float(lib().pxg_last_gpu_ms())
+
+
+def set_blocking(blocking: bool):
+    """True (default): calls wait for their GPU work; False: image operations
+    only enqueue their kernels (see pxg_set_blocking in include/pxg.h)."""
+    _check(lib().pxg_set_blocking(1 if blocking else 0))
+
+
+def synchronize():
+    _check(lib().pxg_synchronize())
+
+
+def set_stream(cuda_stream: int):
+    _check(lib().pxg_set_stream(C.c_void_p(cuda_stream)))
+
+
+def launch_count() -> int:
+    return int(lib().pxg_launch_count())

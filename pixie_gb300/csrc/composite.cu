@@ -1,0 +1,191 @@
+// draw() with an integer translation (src/pixie/images.nim:468-529 blendRect),
+// image fill (images.nim:55-57) and the coverage-free per-pixel blends.
+//
+// HBM-bound: a draw reads both images and writes the destination (12 B/px;
+// Overwrite reads only the source, 8 B/px).  Each thread moves 16-byte
+// vectors (4 pixels) when both row layouts allow it; the blend is a
+// compile-time template per mode so the inner loop carries no dispatch.
+#include <atomic>
+
+#include "pxg_device.cuh"
+
+namespace pxg {
+
+static std::atomic<unsigned long long> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+unsigned long long launch_count() { return g_launches.load(); }
+
+template <int MODE>
+__device__ __forceinline__ uint32_t draw_px(const uint8_t* tbl, uint32_t a, uint32_t b) {
+  if (MODE == kNormal) return blendNormal(a, b);
+  if (MODE == kOverwrite) return b;
+  if (MODE == kMask) return blendMaskPx(a, b);
+  return blend_px(MODE, tbl, a, b);
+}
+
+// Overlap rectangle: w x h pixels, a at (ax, ay), b at (bx, by).
+// vec: rows of both images and both x offsets are multiples of 4 pixels.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_draw(uint32_t* __restrict__ a, const uint32_t* __restrict__ b,
+                                              long long Wa, long long Wb, long long ax, long long ay,
+                                              long long bx, long long by, long long w, long long h,
+                                              const uint8_t* tbl, int vec) {
+  if (vec) {
+    // 4 independent 16-byte quads per thread per iteration, all loads issued
+    // before any blend, so each SM keeps enough bytes in flight to saturate HBM.
+    const long long qpr = w >> 2;  // quads per row
+    const long long nq = qpr * h;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long q0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; q0 < nq; q0 += 4 * stride) {
+      uint4* pa[4];
+      uint4 va[4], vb[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        long long q = q0 + u * stride;
+        pa[u] = nullptr;
+        if (q < nq) {
+          long long r = q / qpr, c = (q - r * qpr) << 2;
+          pa[u] = reinterpret_cast<uint4*>(a + (ay + r) * Wa + ax + c);
+          vb[u] = __ldcs(reinterpret_cast<const uint4*>(b + (by + r) * Wb + bx + c));
+          if (MODE != kOverwrite) va[u] = __ldcs(pa[u]);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        if (!pa[u]) continue;
+        uint4 o;
+        if (MODE == kOverwrite) {
+          o = vb[u];
+        } else {
+          o.x = draw_px<MODE>(tbl, va[u].x, vb[u].x);
+          o.y = draw_px<MODE>(tbl, va[u].y, vb[u].y);
+          o.z = draw_px<MODE>(tbl, va[u].z, vb[u].z);
+          o.w = draw_px<MODE>(tbl, va[u].w, vb[u].w);
+        }
+        __stcs(pa[u], o);
+      }
+    }
+    // leftover columns (w % 4)
+    const long long rem = w & 3;
+    if (rem) {
+      for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < rem * h;
+           i += (long long)gridDim.x * blockDim.x) {
+        long long r = i / rem, c = (w - rem) + (i - r * rem);
+        uint32_t* pa = a + (ay + r) * Wa + ax + c;
+        *pa = draw_px<MODE>(tbl, *pa, b[(by + r) * Wb + bx + c]);
+      }
+    }
+    return;
+  }
+  const long long n = w * h;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    long long r = i / w, c = i - r * w;
+    uint32_t* pa = a + (ay + r) * Wa + ax + c;
+    *pa = draw_px<MODE>(tbl, *pa, b[(by + r) * Wb + bx + c]);
+  }
+}
+
+// MaskBlend zeroes the destination outside the overlap (images.nim:473-520).
+__global__ void __launch_bounds__(256) k_clear_outside(uint32_t* a, long long Wa, long long Ha,
+                                                       long long x0, long long y0, long long x1,
+                                                       long long y1) {
+  const long long n = Wa * Ha;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    long long y = i / Wa, x = i - y * Wa;
+    if (y < y0 || y >= y1 || x < x0 || x >= x1) a[i] = 0u;
+  }
+}
+
+// fillUnsafe over the whole image (internal.nim:55-66)
+__global__ void __launch_bounds__(256) k_fill(uint32_t* a, long long n, uint32_t c) {
+  const long long nq = n >> 2;
+  uint4 v = make_uint4(c, c, c, c);
+  uint4* a4 = reinterpret_cast<uint4*>(a);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nq;
+       i += (long long)gridDim.x * blockDim.x)
+    a4[i] = v;
+  for (long long i = (nq << 2) + (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    a[i] = c;
+}
+
+// blend_px over pixel arrays, for unit-testing the blend modes themselves
+__global__ void k_blend_pixels(int mode, const uint8_t* tbl, const uint32_t* bd, const uint32_t* src,
+                               uint32_t* out, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    out[i] = blend_px(mode, tbl, bd[i], src[i]);
+}
+
+typedef void (*DrawKernel)(uint32_t*, const uint32_t*, long long, long long, long long, long long,
+                           long long, long long, long long, long long, const uint8_t*, int);
+
+template <int M>
+struct DrawTable {
+  static void fill(DrawKernel* t) {
+    t[M] = k_draw<M>;
+    DrawTable<M + 1>::fill(t);
+  }
+};
+template <>
+struct DrawTable<kNumBlends> {
+  static void fill(DrawKernel*) {}
+};
+
+DrawKernel draw_kernel(int mode) {
+  static DrawKernel table[kNumBlends] = {nullptr};
+  if (!table[0]) DrawTable<0>::fill(table);
+  return table[mode];
+}
+
+void launch_draw(uint32_t* a, const uint32_t* b, long long Wa, long long Ha, long long Wb,
+                 long long Hb, long long px, long long py, int mode, const uint8_t* tbl, int nsm,
+                 cudaStream_t st) {
+  // blendRect  images.nim:468-529
+  if (px >= Wa || px + Wb <= 0 || py >= Ha || py + Hb <= 0) {
+    if (mode == kMask) {
+      k_fill<<<nsm * 4, 256, 0, st>>>(a, Wa * Ha, 0u);
+      note_launch();
+    }
+    return;
+  }
+  long long xStart = px < 0 ? -px : 0, yStart = py < 0 ? -py : 0;
+  long long xEnd = Wb < Wa - px ? Wb : Wa - px, yEnd = Hb < Ha - py ? Hb : Ha - py;
+  long long w = xEnd - xStart, h = yEnd - yStart;
+  long long ax = xStart + px, ay = yStart + py;
+  int vec = (Wa % 4 == 0) && (Wb % 4 == 0) && (ax % 4 == 0) && (xStart % 4 == 0);
+  long long work = vec ? ((w / 4) * h + 3) / 4 : w * h;
+  long long blocks = (work + 255) / 256;
+  long long cap = (long long)nsm * 8;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  if (mode == kMask) {
+    k_clear_outside<<<nsm * 4, 256, 0, st>>>(a, Wa, Ha, ax, ay, ax + w, ay + h);
+    note_launch();
+  }
+  if (w > 0 && h > 0) {
+    draw_kernel(mode)<<<(unsigned)blocks, 256, 0, st>>>(a, b, Wa, Wb, ax, ay, xStart, yStart, w, h,
+                                                        tbl, vec);
+    note_launch();
+  }
+}
+
+void launch_fill(uint32_t* a, long long n, uint32_t c, int nsm, cudaStream_t st) {
+  long long blocks = (n / 4 + 255) / 256;
+  long long cap = (long long)nsm * 8;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  k_fill<<<(unsigned)blocks, 256, 0, st>>>(a, n, c); note_launch();
+}
+
+void launch_blend_pixels(int mode, const uint8_t* tbl, const uint32_t* bd, const uint32_t* src,
+                         uint32_t* out, long long n, cudaStream_t st) {
+  long long blocks = (n + 255) / 256;
+  if (blocks > 4096) blocks = 4096;
+  if (blocks < 1) blocks = 1;
+  k_blend_pixels<<<(unsigned)blocks, 256, 0, st>>>(mode, tbl, bd, src, out, n); note_launch();
+}
+
+}  // namespace pxg

@@ -1,0 +1,40 @@
+// Host-side geometry of the fill/stroke entry points: what pixie computes on
+// the CPU before its scan converter runs, and what stays on the host here.
+//   - the command walk of commandsToShapes (src/pixie/paths.nim:654-1057):
+//     arc-free subpaths become GPU primitives (lines, quadratics, cubics,
+//     flattened on the device); subpaths with arcs are flattened here
+//     (cosf/sinf/acosf per step) and uploaded as lines;
+//   - strokeShapes (paths.nim:1922-2082): stroke outlines are built here and
+//     uploaded as lines;
+//   - gaussianKernel (internal.nim:17-34) weights and chroma colour
+//     conversion of the paint.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "raster.cuh"
+
+namespace pxg {
+
+struct GeomError {
+  std::string msg;
+};
+
+// Builds the primitives of fillPath (closeSubpaths = true).  Throws GeomError.
+void build_fill_prims(const float* cmds, int64_t n, float pixelScale, std::vector<Prim>& out);
+// Builds the outline primitives of strokePath.  Throws GeomError.
+void build_stroke_prims(const float* cmds, int64_t n, float pixelScale, float strokeWidth,
+                        int lineCap, int lineJoin, float miterLimit, const float* dashes,
+                        int64_t nDashes, std::vector<Prim>& out);
+// Validates the command stream (kinds, parameter counts, finiteness).
+void validate_commands(const float* cmds, int64_t n);
+
+float pixel_scale(const float* mat9);
+bool is_identity(const float* mat9);
+float error_margin_sq(float pixelScale);
+uint32_t color_to_rgbx(const float* color4);  // straight float colour -> premultiplied RGBX
+std::vector<uint16_t> gaussian_kernel(int64_t radius);
+void straight_alpha_table(uint8_t* out256x256);
+
+}  // namespace pxg

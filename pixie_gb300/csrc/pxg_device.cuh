@@ -1,0 +1,296 @@
+// Device-side scalar semantics shared by every kernel: pixie's premultiplied
+// RGBX pixel, its integer blend modes (src/pixie/blends.nim), its colour
+// multiplies (src/pixie/common.nim:67-90) and Nim's float->int conversions.
+// Compiled with -fmad=false so float32 expressions keep the reference's
+// operation order and rounding.
+#pragma once
+#include <cstdint>
+
+namespace pxg {
+
+enum Blend {
+  kNormal = 0, kDarken, kMultiply, kColorBurn, kLighten, kScreen, kColorDodge, kOverlay,
+  kSoftLight, kHardLight, kDifference, kExclusion, kHue, kSaturation, kColor, kLuminosity,
+  kMask, kOverwrite, kSubtractMask, kExcludeMask, kNumBlends
+};
+
+struct Px {
+  uint32_t r, g, b, a;
+};
+__device__ __forceinline__ Px unpack(uint32_t v) {
+  return Px{v & 255u, (v >> 8) & 255u, (v >> 16) & 255u, v >> 24};
+}
+__device__ __forceinline__ uint32_t pack(uint32_t r, uint32_t g, uint32_t b, uint32_t a) {
+  return (r & 255u) | ((g & 255u) << 8) | ((b & 255u) << 16) | ((a & 255u) << 24);
+}
+
+// Nim float32 -> int conversions as the reference's x86-64 builds perform them
+// (cvttss2si: NaN and out-of-range give INT_MIN).
+__device__ __forceinline__ long long nim_int(float f) {
+  if (!(f >= -9223372036854775808.0f && f < 9223372036854775808.0f)) return (long long)(-9223372036854775807LL - 1);
+  return (long long)f;
+}
+__device__ __forceinline__ int nim_i32(float f) {
+  if (!(f >= -2147483648.0f && f < 2147483648.0f)) return (int)0x80000000u;
+  return (int)f;
+}
+__device__ __forceinline__ uint32_t nim_u32(float f) { return (uint32_t)(unsigned long long)nim_int(f); }
+__device__ __forceinline__ float nmin(float x, float y) { return x <= y ? x : y; }
+__device__ __forceinline__ float nmax(float x, float y) { return y <= x ? x : y; }
+
+// `*`(ColorRGBX, uint8)  common.nim:79-90
+__device__ __forceinline__ uint32_t mul_c(uint32_t c, uint32_t k) {
+  if (k == 0) return 0u;
+  if (k == 255) return c;
+  Px p = unpack(c);
+  return pack((p.r * k + 127) / 255, (p.g * k + 127) / 255, (p.b * k + 127) / 255,
+              (p.a * k + 127) / 255);
+}
+// `*`(ColorRGBX, float32)  common.nim:67-77
+__device__ __forceinline__ uint32_t mul_f(uint32_t c, float opacity) {
+  if (opacity == 0.0f) return 0u;
+  uint32_t x = nim_u32(roundf(opacity * 255.0f));
+  Px p = unpack(c);
+  return pack((p.r * x + 127) / 255, (p.g * x + 127) / 255, (p.b * x + 127) / 255,
+              (p.a * x + 127) / 255);
+}
+
+__device__ __forceinline__ uint32_t blendAlpha(uint32_t b, uint32_t s) {  // blends.nim:41-43
+  return (s + ((b * (255 - s)) / 255)) & 255u;
+}
+__device__ __forceinline__ uint32_t screen1(uint32_t b, uint32_t s) {  // :45-46
+  return (uint32_t)((int)(b + s) - (int)((b * s) / 255)) & 255u;
+}
+__device__ __forceinline__ uint32_t hardLight1(uint32_t bc, uint32_t ba, uint32_t sc, uint32_t sa) {
+  if (sc * 2 <= sa) return ((2 * sc * bc + sc * (255 - ba) + bc * (255 - sa)) / 255) & 255u;
+  return screen1(bc, sc);
+}
+
+__device__ __forceinline__ uint32_t blendNormal(uint32_t bv, uint32_t sv) {  // :60-70
+  uint32_t sa = sv >> 24, ba = bv >> 24;
+  if (ba == 0 || sa == 255) return sv;
+  if (sa == 0) return bv;
+  Px b = unpack(bv), s = unpack(sv);
+  uint32_t k = 255 - sa;
+  return pack(s.r + (b.r * k) / 255, s.g + (b.g * k) / 255, s.b + (b.b * k) / 255,
+              blendAlpha(ba, sa));
+}
+__device__ __forceinline__ uint32_t blendMaskPx(uint32_t bv, uint32_t sv) {  // :227-232
+  uint32_t k = sv >> 24;
+  Px b = unpack(bv);
+  return pack((b.r * k) / 255, (b.g * k) / 255, (b.b * k) / 255, (b.a * k) / 255);
+}
+
+// The straight-alpha table (internal.nim:68-74), uploaded once per device:
+// tbl[a*256 + c] = min(round(c * (255/a)), 255) evaluated in float64.
+struct BlendTables {
+  const uint8_t* straight;
+};
+
+__device__ __forceinline__ uint32_t alphaFix8(Px bd, Px src, Px mixed) {  // :18-39 -> straight RGBA
+  uint32_t sa = src.a, ba = bd.a;
+  uint32_t t0 = sa * (255 - ba), t1 = sa * ba, t2 = (255 - sa) * ba;
+  uint32_t r = t0 * src.r + t1 * mixed.r + t2 * bd.r;
+  uint32_t g = t0 * src.g + t1 * mixed.g + t2 * bd.g;
+  uint32_t b = t0 * src.b + t1 * mixed.b + t2 * bd.b;
+  uint32_t a = sa + ba * (255 - sa) / 255;
+  if (a == 0) return 0u;
+  return pack(r / a / 255, g / a / 255, b / a / 255, a);
+}
+__device__ __forceinline__ uint32_t premul8(uint32_t sv) {  // internal.nim:86-96
+  Px s = unpack(sv);
+  if (s.a == 255) return sv;
+  return pack((s.r * s.a + 127) / 255, (s.g * s.a + 127) / 255, (s.b * s.a + 127) / 255, s.a);
+}
+__device__ __forceinline__ Px straight8(const uint8_t* tbl, uint32_t v) {
+  Px p = unpack(v);
+  const uint8_t* row = tbl + p.a * 256;
+  return Px{row[p.r], row[p.g], row[p.b], p.a};
+}
+__device__ __forceinline__ uint32_t unit_to_u8(float c) {
+  float v = roundf(c * 255.0f);
+  if (!(v > 0.0f)) return 0u;
+  if (v > 255.0f) return 255u;
+  return (uint32_t)v;
+}
+
+// chroma float modes (UNPINNED, W3C Compositing Level 1; same operation order
+// as the oracle).
+struct F3 {
+  float r, g, b;
+};
+__device__ __forceinline__ float lum3(F3 c) { return 0.3f * c.r + 0.59f * c.g + 0.11f * c.b; }
+__device__ __forceinline__ F3 clipColor(F3 c) {
+  float l = lum3(c);
+  float n = fminf(c.r, fminf(c.g, c.b));
+  float x = fmaxf(c.r, fmaxf(c.g, c.b));
+  if (n < 0.0f) {
+    float d = l - n;
+    c.r = l + ((c.r - l) * l) / d;
+    c.g = l + ((c.g - l) * l) / d;
+    c.b = l + ((c.b - l) * l) / d;
+  }
+  if (x > 1.0f) {
+    float d = x - l;
+    float k = 1.0f - l;
+    c.r = l + ((c.r - l) * k) / d;
+    c.g = l + ((c.g - l) * k) / d;
+    c.b = l + ((c.b - l) * k) / d;
+  }
+  return c;
+}
+__device__ __forceinline__ F3 setLum(F3 c, float l) {
+  float d = l - lum3(c);
+  return clipColor(F3{c.r + d, c.g + d, c.b + d});
+}
+__device__ __forceinline__ float sat3(F3 c) {
+  return fmaxf(c.r, fmaxf(c.g, c.b)) - fminf(c.r, fminf(c.g, c.b));
+}
+__device__ __forceinline__ F3 setSat(F3 c, float s) {
+  float v[3] = {c.r, c.g, c.b};
+  int imax = 0, imin = 0;
+#pragma unroll
+  for (int i = 1; i < 3; i++) {
+    if (v[i] > v[imax]) imax = i;
+    if (v[i] < v[imin]) imin = i;
+  }
+  if (imax == imin) return F3{0.0f, 0.0f, 0.0f};
+  int imid = 3 - imax - imin;
+  float cmax = v[imax], cmin = v[imin], cmid = v[imid];
+  float out[3];
+  if (cmax > cmin) {
+    out[imid] = ((cmid - cmin) * s) / (cmax - cmin);
+    out[imax] = s;
+  } else {
+    out[imid] = 0.0f;
+    out[imax] = 0.0f;
+  }
+  out[imin] = 0.0f;
+  return F3{out[0], out[1], out[2]};
+}
+__device__ __forceinline__ float softLight1(float cb, float cs) {
+  if (cs <= 0.5f) return cb - ((1.0f - 2.0f * cs) * cb) * (1.0f - cb);
+  float d = cb <= 0.25f ? ((16.0f * cb - 12.0f) * cb + 4.0f) * cb : sqrtf(cb);
+  return cb + (2.0f * cs - 1.0f) * (d - cb);
+}
+static __device__ __noinline__ uint32_t blendFloat(const uint8_t* tbl, uint32_t bp, uint32_t sp, int mode) {
+  Px b8 = straight8(tbl, bp), s8 = straight8(tbl, sp);
+  F3 cb{b8.r / 255.0f, b8.g / 255.0f, b8.b / 255.0f};
+  F3 cs{s8.r / 255.0f, s8.g / 255.0f, s8.b / 255.0f};
+  float ab = b8.a / 255.0f, as = s8.a / 255.0f;
+  F3 m;
+  switch (mode) {
+    case kSoftLight:
+      m = F3{softLight1(cb.r, cs.r), softLight1(cb.g, cs.g), softLight1(cb.b, cs.b)};
+      break;
+    case kHue: m = setLum(setSat(cs, sat3(cb)), lum3(cb)); break;
+    case kSaturation: m = setLum(setSat(cb, sat3(cs)), lum3(cb)); break;
+    case kColor: m = setLum(cs, lum3(cb)); break;
+    default: m = setLum(cb, lum3(cs)); break;
+  }
+  float ao = as + ab * (1.0f - as);
+  if (!(ao > 0.0f)) return 0u;
+  float k = (1.0f - as) * ab;
+  float csr = (1.0f - ab) * cs.r + ab * m.r;
+  float csg = (1.0f - ab) * cs.g + ab * m.g;
+  float csb = (1.0f - ab) * cs.b + ab * m.b;
+  float orr = (as * csr + k * cb.r) / ao;
+  float og = (as * csg + k * cb.g) / ao;
+  float ob = (as * csb + k * cb.b) / ao;
+  return premul8(pack(unit_to_u8(orr), unit_to_u8(og), unit_to_u8(ob), unit_to_u8(ao)));
+}
+
+__device__ __forceinline__ uint32_t colorBurn1(uint32_t b, uint32_t s) {  // :115-121
+  if (b == 255) return 255;
+  if (s == 0) return 0;
+  uint32_t v = (255 * (255 - b)) / s;
+  return (255 - (v < 255 ? v : 255)) & 255u;
+}
+__device__ __forceinline__ uint32_t colorDodge1(uint32_t b, uint32_t s) {  // :162-168
+  if (b == 0) return 0;
+  if (s == 255) return 255;
+  uint32_t v = (255 * b) / (255 - s);
+  return v < 255 ? v : 255;
+}
+
+// blender(mode)(backdrop, source)  blends.nim:275-299
+__device__ __forceinline__ uint32_t blend_px(int mode, const uint8_t* tbl, uint32_t bv, uint32_t sv) {
+  switch (mode) {
+    case kNormal: return blendNormal(bv, sv);
+    case kMask: return blendMaskPx(bv, sv);
+    case kOverwrite: return sv;
+    default: break;
+  }
+  Px b = unpack(bv), s = unpack(sv);
+  switch (mode) {
+    case kDarken: {  // :72-84
+      auto f = [](uint32_t bc, uint32_t ba, uint32_t sc, uint32_t sa) {
+        uint32_t x = bc + ((255 - ba) * sc) / 255, y = sc + ((255 - sa) * bc) / 255;
+        return (x < y ? x : y) & 255u;
+      };
+      return pack(f(b.r, b.a, s.r, s.a), f(b.g, b.a, s.g, s.a), f(b.b, b.a, s.b, s.a), blendAlpha(b.a, s.a));
+    }
+    case kMultiply: {  // :86-100
+      auto f = [](uint32_t bc, uint32_t ba, uint32_t sc, uint32_t sa) {
+        return (((255 - ba) * sc + (255 - sa) * bc + bc * sc) / 255) & 255u;
+      };
+      return pack(f(b.r, b.a, s.r, s.a), f(b.g, b.a, s.g, s.a), f(b.b, b.a, s.b, s.a), blendAlpha(b.a, s.a));
+    }
+    case kLighten: {  // :128-140
+      auto f = [](uint32_t bc, uint32_t ba, uint32_t sc, uint32_t sa) {
+        uint32_t x = bc + ((255 - ba) * sc) / 255, y = sc + ((255 - sa) * bc) / 255;
+        return (x > y ? x : y) & 255u;
+      };
+      return pack(f(b.r, b.a, s.r, s.a), f(b.g, b.a, s.g, s.a), f(b.b, b.a, s.b, s.a), blendAlpha(b.a, s.a));
+    }
+    case kScreen:  // :142-146
+      return pack(screen1(b.r, s.r), screen1(b.g, s.g), screen1(b.b, s.b), blendAlpha(b.a, s.a));
+    case kOverlay:  // :175-179
+      return pack(hardLight1(s.r, s.a, b.r, b.a), hardLight1(s.g, s.a, b.g, b.a),
+                  hardLight1(s.b, s.a, b.b, b.a), blendAlpha(b.a, s.a));
+    case kHardLight:  // :184-188
+      return pack(hardLight1(b.r, b.a, s.r, s.a), hardLight1(b.g, b.a, s.g, s.a),
+                  hardLight1(b.b, b.a, s.b, s.a), blendAlpha(b.a, s.a));
+    case kDifference: {  // :190-204; (bc + sc) wraps as uint8
+      auto f = [](uint32_t bc, uint32_t ba, uint32_t sc, uint32_t sa) {
+        uint32_t m1 = bc * sa, m2 = sc * ba;
+        int mn = (int)((m1 < m2 ? m1 : m2) / 255);
+        return (uint32_t)((int)((bc + sc) & 255u) - 2 * mn) & 255u;
+      };
+      return pack(f(b.r, b.a, s.r, s.a), f(b.g, b.a, s.g, s.a), f(b.b, b.a, s.b, s.a), blendAlpha(b.a, s.a));
+    }
+    case kExclusion: {  // :206-213
+      auto f = [](uint32_t bc, uint32_t sc) {
+        int v = (int)(bc + sc) - (int)((2 * bc * sc) / 255);
+        return (uint32_t)(v > 0 ? v : 0) & 255u;
+      };
+      return pack(f(b.r, s.r), f(b.g, s.g), f(b.b, s.b), blendAlpha(b.a, s.a));
+    }
+    case kColorBurn:
+    case kColorDodge: {  // :111-126, :158-173
+      Px bd = straight8(tbl, bv), sr = straight8(tbl, sv), m;
+      if (mode == kColorBurn) {
+        m = Px{colorBurn1(bd.r, sr.r), colorBurn1(bd.g, sr.g), colorBurn1(bd.b, sr.b), 0};
+      } else {
+        m = Px{colorDodge1(bd.r, sr.r), colorDodge1(bd.g, sr.g), colorDodge1(bd.b, sr.b), 0};
+      }
+      return premul8(alphaFix8(bd, sr, m));
+    }
+    case kSoftLight:
+    case kHue:
+    case kSaturation:
+    case kColor:
+    case kLuminosity: return blendFloat(tbl, bv, sv, mode);
+    case kSubtractMask: {  // :234-239
+      uint32_t a = (b.a * (255 - s.a)) / 255;
+      return pack((b.r * a) / 255, (b.g * a) / 255, (b.b * a) / 255, a);
+    }
+    case kExcludeMask: {  // :241-246
+      uint32_t a = (b.a > s.a ? b.a : s.a) - (b.a < s.a ? b.a : s.a);
+      return pack((s.r * a) / 255, (s.g * a) / 255, (s.b * a) / 255, a);
+    }
+  }
+  return bv;
+}
+
+}  // namespace pxg

@@ -1,0 +1,991 @@
+// GPU fill pipeline: pixie's commandsToShapes (cubic/quadratic flattening),
+// shapesToSegments, computeBounds/snapToPixels, partitionSegments and the
+// fillShapes row loop (src/pixie/paths.nim:654-1912), restated for sm_103a.
+//
+// k_setup   one CTA per fill job: flatten primitives, emit pixie's segments
+//           (quantised, oriented, horizontals dropped) in the reference's
+//           order, reduce the bounds, derive the partition geometry, each
+//           segment's band range and each band's count and AA flag.
+// k_rows    one warp per image row: a ballot scan over the segments collects
+//           the row's band entries in segment order (clipped to the band as
+//           partitionSegments does), then the reference's per-row decision
+//           (the non-AA two-edge fill, the trapezoid fast path, or 5-sample
+//           coverage with the nonzero/even-odd walk) and the fused
+//           coverage -> paint -> blend write of the row.
+// Float math is compiled with -fmad=false: every expression keeps the
+// reference's float32 operation order.
+#include <cfloat>
+#include <climits>
+
+#include "pxg_device.cuh"
+#include "raster.cuh"
+
+namespace pxg {
+
+static __device__ constexpr float kEps = (float)(0.0001 * 3.141592653589793);  // paths.nim:44
+static constexpr long long kIterCap = 1LL << 24;
+
+struct V2 {
+  float x, y;
+};
+__device__ __forceinline__ V2 operator+(V2 a, V2 b) { return V2{a.x + b.x, a.y + b.y}; }
+__device__ __forceinline__ V2 operator-(V2 a, V2 b) { return V2{a.x - b.x, a.y - b.y}; }
+__device__ __forceinline__ V2 operator*(V2 a, float s) { return V2{a.x * s, a.y * s}; }
+__device__ __forceinline__ V2 operator/(V2 a, float s) { return V2{a.x / s, a.y / s}; }
+__device__ __forceinline__ float lengthSq(V2 v) { return v.x * v.x + v.y * v.y; }
+__device__ __forceinline__ float length(V2 v) { return sqrtf(lengthSq(v)); }
+
+// ---------------------------------------------------------------------------
+// Flattening  paths.nim:677-762
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ V2 cubicAt(V2 a, V2 c1, V2 c2, V2 to, float t) {
+  float t2 = t * t, t3 = t2 * t;
+  return a * (((-t3 + 3 * t2) - 3 * t) + 1) + c1 * ((3 * t3 - 6 * t2) + 3 * t) +
+         c2 * (-3 * t3 + 3 * t2) + to * (t3);
+}
+__device__ __forceinline__ V2 cubicDeriv(V2 a, V2 c1, V2 c2, V2 to, float t) {
+  float t2 = t * t;
+  return a * ((-3 * t2 + 6 * t) - 3) + c1 * ((9 * t2 - 12 * t) + 3) + c2 * (-9 * t2 + 6 * t) +
+         to * (3 * t2);
+}
+__device__ __forceinline__ V2 quadAt(V2 a, V2 c, V2 to, float t) {
+  float t2 = t * t;
+  return a * ((t2 - 2 * t) + 1) + c * (-2 * t2 + 2 * t) + to * t2;
+}
+
+// Calls emit(prev, next) for every segment addSegment would add (zero-length
+// segments are dropped as in paths.nim:669-675).  Returns a JobStatus.
+template <class Emit>
+__device__ int flatten_prim(const Prim& p, float ems, Emit&& emit) {
+  V2 at{p.x[0], p.y[0]};
+  if (p.kind == kPrimLine) {
+    V2 to{p.x[1], p.y[1]};
+    if (at.x - to.x != 0.0f || at.y - to.y != 0.0f) emit(at, to);
+    return kOk;
+  }
+  float t = 0, step = 1;
+  V2 prev = at;
+  long long iters = 0;
+  if (p.kind == kPrimCubic) {
+    V2 c1{p.x[1], p.y[1]}, c2{p.x[2], p.y[2]}, to{p.x[3], p.y[3]};
+    V2 next = cubicAt(at, c1, c2, to, t + step);
+    V2 halfway = cubicAt(at, c1, c2, to, t + step / 2);
+    while (true) {
+      if (step <= FLT_EPSILON) return kErrCubic;
+      if (++iters > kIterCap) return kErrIterLimit;
+      V2 midpoint = (prev + next) / 2;
+      V2 lineTangent = midpoint - prev;
+      V2 curveTangent = cubicDeriv(at, c1, c2, to, t + step / 2);
+      V2 scaled = (curveTangent / length(curveTangent)) * length(lineTangent);
+      float error = lengthSq(midpoint - halfway);
+      float errorTangent = lengthSq(lineTangent - scaled);
+      if (error + errorTangent > ems) {
+        next = halfway;
+        halfway = cubicAt(at, c1, c2, to, t + step / 4);
+        step /= 2;
+      } else {
+        if (prev.x - next.x != 0.0f || prev.y - next.y != 0.0f) emit(prev, next);
+        t += step;
+        if (t == 1) break;
+        prev = next;
+        step = nmin(step * 2, 1 - t);
+        next = cubicAt(at, c1, c2, to, t + step);
+        halfway = cubicAt(at, c1, c2, to, t + step / 2);
+      }
+    }
+    return kOk;
+  }
+  // quadratic
+  V2 c{p.x[1], p.y[1]}, to{p.x[2], p.y[2]};
+  V2 next = quadAt(at, c, to, t + step);
+  V2 halfway = quadAt(at, c, to, t + step / 2);
+  bool halfStepping = false;
+  while (true) {
+    if (step <= FLT_EPSILON) return kErrQuad;
+    if (++iters > kIterCap) return kErrIterLimit;
+    V2 midpoint = (prev + next) / 2;
+    float error = lengthSq(midpoint - halfway);
+    if (error > ems) {
+      next = halfway;
+      halfway = quadAt(at, c, to, t + step / 4);
+      halfStepping = true;
+      step /= 2;
+    } else {
+      if (prev.x - next.x != 0.0f || prev.y - next.y != 0.0f) emit(prev, next);
+      t += step;
+      if (t == 1) break;
+      prev = next;
+      step = halfStepping ? nmin(step, 1 - t) : nmin(step * 2, 1 - t);
+      next = quadAt(at, c, to, t + step);
+      halfway = quadAt(at, c, to, t + step / 2);
+    }
+  }
+  return kOk;
+}
+
+// transform + shapesToSegments for one emitted pair (paths.nim:1059-1096).
+// vmath quantize(v, 1/256) = sign(v) * floor(|v| / n) * n.
+__device__ __forceinline__ float quantize256(float v) {
+  const float n = 1.0f / 256;
+  float sgn = v >= 0 ? 1.0f : -1.0f;
+  return sgn * (floorf(fabsf(v) / n) * n);
+}
+__device__ __forceinline__ bool make_seg(const PathJob& J, V2 a, V2 b, float4& s, int& w) {
+  if (!J.identity) {
+    const float* m = J.mat;
+    a = V2{m[0] * a.x + m[3] * a.y + m[6], m[1] * a.x + m[4] * a.y + m[7]};
+    b = V2{m[0] * b.x + m[3] * b.y + m[6], m[1] * b.x + m[4] * b.y + m[7]};
+  }
+  a.y = quantize256(a.y);
+  b.y = quantize256(b.y);
+  if (a.y == b.y) return false;
+  w = 1;
+  if (a.y > b.y) {
+    V2 t = a;
+    a = b;
+    b = t;
+    w = -1;
+  }
+  s = make_float4(a.x, a.y, b.x, b.y);
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Partitions  paths.nim:1127-1262
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool hasFractional(float v) { return v - truncf(v) != 0; }
+__device__ __forceinline__ bool segRequiresAA(float4 s) {  // :1149-1160
+  return s.x != s.z || hasFractional(s.x) || hasFractional(s.y) || hasFractional(s.w);
+}
+// bumpy intersects(Segment, Line): the parametric form of internal.nim:36-48
+// without the range check on the line parameter; the point is on the segment.
+__device__ __forceinline__ bool intersectSegLine(V2 sa, V2 sb, V2 l0, V2 l1, V2& at) {
+  V2 s1 = sb - sa, s2 = l1 - l0;
+  float den = (-s2.x * s1.y + s1.x * s2.y);
+  float t = (s2.x * (sa.y - l0.y) - s2.y * (sa.x - l0.x)) / den;
+  if (t >= 0 && t <= 1) {
+    at = sa + s1 * t;
+    return true;
+  }
+  return false;
+}
+__device__ __forceinline__ bool intersectsInside(V2 aa, V2 ab, V2 ba, V2 bb) {  // internal.nim:36-48
+  V2 s1 = ab - aa, s2 = bb - ba;
+  float den = (-s2.x * s1.y + s1.x * s2.y);
+  float s = (-s1.y * (aa.x - ba.x) + s1.x * (aa.y - ba.y)) / den;
+  float t = (s2.x * (aa.y - ba.y) - s2.y * (aa.x - ba.x)) / den;
+  return s > 0 && s < 1 && t > 0 && t < 1;
+}
+__device__ __forceinline__ Entry make_entry(float4 s, int w, float top, float bottom) {
+  Entry e;
+  e.w = w;
+  e.pad = 0;
+  e.m = 0;
+  e.b = 0;
+  float d = s.x - s.z;  // initPartitionEntry :1127-1135
+  if (d == 0) {
+    e.b = s.x;
+  } else {
+    e.m = (s.y - s.w) / d;
+    e.b = s.y - e.m * s.x;
+  }
+  V2 a{s.x, s.y}, b{s.z, s.w};
+  if (a.y <= top && b.y >= bottom) {  // clip :1236-1248
+    V2 at{0, 0};
+    intersectSegLine(a, b, V2{0, top}, V2{1000, top}, at);
+    a = at;
+    intersectSegLine(a, b, V2{0, bottom}, V2{1000, bottom}, at);
+    b = at;
+  }
+  e.ax = a.x;
+  e.ay = a.y;
+  e.bx = b.x;
+  e.by = b.y;
+  return e;
+}
+
+__device__ __forceinline__ long long warp_sum_ll(long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+// Block-wide exclusive scan of one value per thread (blockDim.x <= 1024).
+__device__ long long block_excl_scan(long long v, long long* s_warp, long long& total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  long long x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  __syncthreads();
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    long long t = lane < nw ? s_warp[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      long long y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    if (lane < nw) s_warp[lane] = t;
+  }
+  __syncthreads();
+  total = s_warp[nw - 1];
+  long long before = warp > 0 ? s_warp[warp - 1] : 0;
+  __syncthreads();
+  return before + x - v;
+}
+
+// ---------------------------------------------------------------------------
+// k_setup: flatten -> segments -> bounds -> partitions (one CTA per job)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_setup(PathJob* jobs, Arena A, int maxBands) {
+  extern __shared__ int dsm[];
+  int* bandc = dsm;             // per band: entry count
+  int* bandf = dsm + maxBands;  // per band: flags
+  __shared__ long long s_warp[32];
+  __shared__ long long s_err;
+  __shared__ int s_status;
+  __shared__ long long s_segbase, s_bandbase, s_nseg;
+  __shared__ float s_red[4][32];
+  __shared__ long long s_hdr[6];
+
+  PathJob& J = jobs[blockIdx.x];
+  const int tid = threadIdx.x, T = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) {
+    s_err = LLONG_MAX;
+    s_status = kOk;
+  }
+  __syncthreads();
+
+  const Prim* P = A.prims + J.prim_off;
+  const int np = J.nprims;
+  const int chunk = (np + T - 1) / T;
+  const int p0 = min(np, tid * chunk), p1 = min(np, p0 + chunk);
+
+  // Phase A: count the segments each thread's primitives emit
+  long long cnt = 0;
+  for (int p = p0; p < p1; p++) {
+    int st = flatten_prim(P[p], J.ems, [&](V2 a, V2 b) {
+      float4 s;
+      int w;
+      if (make_seg(J, a, b, s, w)) cnt++;
+    });
+    if (st != kOk) {  // the reference raises at the first failing primitive
+      atomicMin(&s_err, ((long long)p << 8) | st);
+      break;
+    }
+  }
+  long long total;
+  long long excl = block_excl_scan(cnt, s_warp, total);
+  if (tid == 0) {
+    if (s_err != LLONG_MAX) {
+      s_status = (int)(s_err & 255);
+    } else {
+      unsigned long long base = atomicAdd(&A.counters[kCtrSegs], (unsigned long long)total);
+      s_segbase = (long long)base;
+      s_nseg = total;
+      if ((long long)base + total > A.seg_cap) s_status = kErrArenaFull;
+    }
+  }
+  __syncthreads();
+  if (s_status != kOk) {
+    if (tid == 0) J.status = s_status;
+    return;
+  }
+
+  // Phase B: emit the segments in order and reduce the bounds (:1098-1117)
+  float xmin = INFINITY, xmax = -INFINITY, ymin = INFINITY, ymax = -INFINITY;
+  {
+    long long o = s_segbase + excl;
+    for (int p = p0; p < p1; p++) {
+      flatten_prim(P[p], J.ems, [&](V2 a, V2 b) {
+        float4 s;
+        int w;
+        if (make_seg(J, a, b, s, w)) {
+          A.segs[o] = s;
+          A.segw[o] = w;
+          o++;
+          xmin = nmin(xmin, nmin(s.x, s.z));
+          xmax = nmax(xmax, nmax(s.x, s.z));
+          ymin = nmin(ymin, s.y);
+          ymax = nmax(ymax, s.w);
+        }
+      });
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    xmin = nmin(xmin, __shfl_xor_sync(0xffffffffu, xmin, o));
+    xmax = nmax(xmax, __shfl_xor_sync(0xffffffffu, xmax, o));
+    ymin = nmin(ymin, __shfl_xor_sync(0xffffffffu, ymin, o));
+    ymax = nmax(ymax, __shfl_xor_sync(0xffffffffu, ymax, o));
+  }
+  if (lane == 0) {
+    s_red[0][warp] = xmin;
+    s_red[1][warp] = xmax;
+    s_red[2][warp] = ymin;
+    s_red[3][warp] = ymax;
+  }
+  __syncthreads();
+
+  // Phase C: bounds -> pixel window, partition geometry (:1602-1619, :1172-1192)
+  const long long W = J.W, H = J.H;
+  if (tid == 0) {
+    const int nw = (T + 31) >> 5;
+    float x0 = INFINITY, x1 = -INFINITY, y0 = INFINITY, y1 = -INFINITY;
+    for (int i = 0; i < nw; i++) {
+      x0 = nmin(x0, s_red[0][i]);
+      x1 = nmax(x1, s_red[1][i]);
+      y0 = nmin(y0, s_red[2][i]);
+      y1 = nmax(y1, s_red[3][i]);
+    }
+    float bx = 0, by = 0, bw = 0, bh = 0;
+    if (!(isnan(x0) || isnan(x1) || isnan(y0) || isnan(y1))) {
+      bx = x0;
+      by = y0;
+      bw = x1 - x0;
+      bh = y1 - y0;
+    }
+    float sx = floorf(bx), sw = ceilf(bx + bw) - sx;  // snapToPixels common.nim:92-101
+    float sy = floorf(by), sh = ceilf(by + bh) - sy;
+    long long startX = max(0LL, nim_int(sx)), startY = max(0LL, nim_int(sy));
+    long long pathWidth = startX < W ? min(nim_int(sw), W - startX) : 0LL;
+    long long pathHeight = min(H, nim_int(sy + sh));
+    int status = kOk;
+    if (pathWidth == 0) status = kNothing;
+    else if (pathWidth < 0) status = kErrIntOverflow;
+    long long height = pathHeight - startY;
+    long long nseg = s_nseg;
+    uint32_t maxP = (uint32_t)max(1LL, height / 4);
+    uint32_t numP = min(maxP, (uint32_t)max(1LL, nseg / 2));
+    uint32_t ph = (uint32_t)height / numP;
+    if (status == kOk && numP > (uint32_t)maxBands) status = kErrArenaFull;
+    s_status = status;
+    s_hdr[0] = startX;
+    s_hdr[1] = startY;
+    s_hdr[2] = pathWidth;
+    s_hdr[3] = pathHeight;
+    s_hdr[4] = numP;
+    s_hdr[5] = ph;
+    J.seg_off = s_segbase;
+    J.nseg = (int)nseg;
+    J.startX = startX;
+    J.startY = startY;
+    J.pathWidth = pathWidth;
+    J.pathHeight = pathHeight;
+    J.nb = (int)numP;
+    J.ph = ph;
+  }
+  __syncthreads();
+  if (s_status != kOk) {
+    if (tid == 0) J.status = s_status;
+    return;
+  }
+  const long long startY = s_hdr[1], pathHeight = s_hdr[3];
+  const uint32_t numP = (uint32_t)s_hdr[4], ph = (uint32_t)s_hdr[5];
+  const long long height = pathHeight - startY;
+  const long long nseg = s_nseg, segbase = s_segbase;
+  const float fStartY = (float)(uint32_t)startY;
+
+  auto bandRange = [&](float4 s, uint32_t& a, uint32_t& b) {  // partitionRange :1201-1213
+    if (numP == 1) {
+      a = b = 0;
+      return;
+    }
+    a = nim_u32(nmax(0.0f, s.y - fStartY)) / ph;
+    b = nim_u32(nmax(0.0f, s.w - fStartY)) / ph;
+    a = min(a, numP - 1);
+    b = min(b, numP - 1);
+  };
+  (void)height;
+
+  // Phase D: each segment's band range (partitionRange :1201-1213), each
+  // band's entry count and anti-aliasing flag (:1215-1234)
+  for (uint32_t k = tid; k < numP; k += T) {
+    bandc[k] = 0;
+    bandf[k] = 0;
+  }
+  __syncthreads();
+  for (long long i = tid; i < nseg; i += T) {
+    float4 s = A.segs[segbase + i];
+    uint32_t a, b;
+    bandRange(s, a, b);
+    A.segband[segbase + i] = make_uint2(a, b);
+    bool aa = segRequiresAA(s);
+    for (uint32_t k = a; k <= b; k++) {
+      atomicAdd(&bandc[k], 1);
+      if (aa) atomicOr(&bandf[k], kBandAA);
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    unsigned long long base = atomicAdd(&A.counters[kCtrBands], (unsigned long long)numP);
+    s_bandbase = (long long)base;
+    if ((long long)base + numP > A.band_cap) s_status = kErrArenaFull;
+  }
+  __syncthreads();
+  if (s_status != kOk) {
+    if (tid == 0) J.status = s_status;
+    return;
+  }
+  for (uint32_t k = tid; k < numP; k += T) {
+    Band bd;
+    bd.count = bandc[k];
+    bd.flags = bandf[k];
+    A.bands[s_bandbase + k] = bd;
+  }
+  if (tid == 0) {
+    J.band_off = s_bandbase;
+    J.status = kOk;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_rows: the per-row loop of fillShapes (:1631-1908), one warp per row
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool shouldFill(int rule, long long count) {  // :1288-1296
+  return rule == 0 ? count != 0 : (count % 2 != 0);
+}
+// FILL: a fillHits span (:1540-1591)
+__device__ __forceinline__ uint32_t op_fill(int mode, const uint8_t* tbl, uint32_t b, uint32_t c) {
+  switch (mode) {
+    case kOverwrite: return c;
+    case kNormal: return (c >> 24) == 255 ? c : blendNormal(b, c);
+    case kMask: return (c >> 24) != 255 ? blendMaskPx(b, c) : b;
+    default: return blend_px(mode, tbl, b, c);
+  }
+}
+// COV: fillCoverage with coverage k (:1442-1526)
+__device__ __forceinline__ uint32_t op_cov(int mode, const uint8_t* tbl, uint32_t b, uint32_t c, uint32_t k) {
+  if (mode == kMask) return k != 255 ? blendMaskPx(b, mul_c(c, k)) : b;
+  if (k == 0) return b;
+  if (mode == kOverwrite) return mul_c(c, k);
+  if (mode == kNormal) return blendNormal(b, mul_c(c, k));
+  return blend_px(mode, tbl, b, mul_c(c, k));
+}
+
+template <int MAXH, int XT>
+struct RowScratch {
+  static constexpr int SPCAP = 5 * (MAXH / 2 + 2);
+  Entry ent[MAXH];  // the band's entries overlapping the row, in segment order
+  int idx[MAXH];
+  int a0[MAXH], a1[MAXH], a2[MAXH], a3[MAXH], a4[MAXH], a5[MAXH];
+  int2 sp[SPCAP];
+  int acc[XT + 1];
+  int nsp, flag;
+};
+
+// Stable rank of element i among n keys (ties keep the original order).
+__device__ __forceinline__ int stable_rank_i(const int* keys, int n, int i) {
+  int ki = keys[i], r = 0;
+  for (int j = 0; j < n; j++) {
+    int kj = keys[j];
+    r += (kj < ki) || (kj == ki && j < i);
+  }
+  return r;
+}
+__device__ __forceinline__ int stable_rank_f(const float* keys, int n, int i) {
+  float ki = keys[i];
+  int r = 0;
+  for (int j = 0; j < n; j++) {
+    float kj = keys[j];
+    r += (kj < ki) || (kj == ki && j < i);
+  }
+  return r;
+}
+
+// Linear-index clear of [y*W + a, y*W + b) (clearUnsafe :1433-1440 with
+// startY == toY).  Pixels before row y are recorded for the cross-row pass.
+__device__ void clear_span_linear(const PathJob& J, const Arena& A, int job, uint32_t* row,
+                                  long long y, long long a, long long b, int lane) {
+  if (a == J.W) return;
+  if (b <= a) return;
+  for (long long x = max(a, 0LL) + lane; x < b; x += 32) row[x] = 0u;
+  if (a < 0 && lane == 0) {
+    long long lo = y * J.W + a, hi = y * J.W + min(b, 0LL);
+    if (lo < 0) lo = 0;
+    if (hi > lo) {
+      unsigned long long slot = atomicAdd(&A.counters[kCtrXClears], 1ull);
+      if ((long long)slot < A.xclear_cap) {
+        A.xclears[3 * slot] = job;
+        A.xclears[3 * slot + 1] = lo;
+        A.xclears[3 * slot + 2] = hi;
+      }
+    }
+  }
+}
+
+template <int MAXH, int XT>
+__device__ void process_row(const PathJob& J, const Arena& A, const uint8_t* tbl, int job,
+                            long long y, RowScratch<MAXH, XT>& S, int lane) {
+  const long long W = J.W;
+  uint32_t* row = reinterpret_cast<uint32_t*>(J.img) + y * W;
+  const int mode = J.mode;
+  const uint32_t rgbx = J.rgbx;
+  const bool maskMode = mode == kMask;
+  const unsigned lt = (1u << lane) - 1;
+
+  long long k = (y - J.startY) / (long long)J.ph;
+  if (k >= J.nb) k = J.nb - 1;
+  const Band bd = A.bands[J.band_off + k];
+  const float scanTop = (float)y, scanBottom = (float)(y + 1);
+  // the band's top and bottom (:1178-1190)
+  const float top = (float)(J.startY + k * (long long)J.ph);
+  const float bottom = (float)(k == J.nb - 1 ? J.pathHeight : J.startY + (k + 1) * (long long)J.ph);
+  const float4* SG = A.segs + J.seg_off;
+  const int* SW = A.segw + J.seg_off;
+  const uint2* SB = A.segband + J.seg_off;
+  const uint32_t kk = (uint32_t)k;
+  const int nseg = J.nseg;
+  Entry* E = S.ent;
+
+  // a band of exactly two entries: are they two non-intersecting segments
+  // spanning the band (:1250-1262)?
+  bool two = false;
+  if (bd.count == 2) {
+    int got = 0;
+    for (int c0 = 0; c0 < nseg && got < 2; c0 += 32) {
+      int i = c0 + lane;
+      bool in = false;
+      if (i < nseg) {
+        uint2 r = SB[i];
+        in = r.x <= kk && kk <= r.y;
+      }
+      unsigned m = __ballot_sync(0xffffffffu, in);
+      int pos = got + __popc(m & lt);
+      if (in && pos < 2) E[pos] = make_entry(SG[i], SW[i], top, bottom);
+      got += __popc(m);
+    }
+    __syncwarp();
+    Entry e0 = E[0], e1 = E[1];
+    if (!intersectsInside(V2{e0.ax, e0.ay}, V2{e0.bx, e0.by}, V2{e1.ax, e1.ay}, V2{e1.bx, e1.by}) &&
+        e0.ay <= top && e0.by >= bottom && e1.ay <= top && e1.by >= bottom) {
+      two = true;
+      if ((e0.ax + e0.bx) * 0.5f > (e1.ax + e1.bx) * 0.5f) {
+        __syncwarp();
+        if (lane == 0) {
+          E[0] = e1;
+          E[1] = e0;
+        }
+      }
+    }
+    __syncwarp();
+  }
+
+  // (i) non-AA band with two spanning vertical edges (:1644-1668)
+  if (two && !(bd.flags & kBandAA)) {
+    long long minX = min(max(nim_int(E[0].ax), 0LL), W);
+    long long maxX = min(max(nim_int(E[1].ax), 0LL), W);
+    for (long long x = lane; x < W; x += 32) {
+      if (x >= minX && x < maxX) row[x] = op_fill(mode, tbl, row[x], rgbx);
+      else if (maskMode) row[x] = 0u;
+    }
+    return;
+  }
+
+  // entries overlapping the scanline [y, y+1) in band order (:1677-1693)
+  int n = 0;
+  bool allSpan = true;
+  if (two) {
+    n = 2;
+  } else {
+    for (int c0 = 0; c0 < nseg; c0 += 32) {
+      int i = c0 + lane;
+      bool pred = false, ns = false;
+      Entry e;
+      if (i < nseg) {
+        uint2 r = SB[i];
+        if (r.x <= kk && kk <= r.y) {
+          e = make_entry(SG[i], SW[i], top, bottom);
+          pred = !(e.by <= scanTop || e.ay >= scanBottom);
+          ns = e.ay > scanTop || e.by < scanBottom;
+        }
+      }
+      unsigned m = __ballot_sync(0xffffffffu, pred);
+      if (__any_sync(0xffffffffu, pred && ns)) allSpan = false;
+      int pos = n + __popc(m & lt);
+      if (pred && pos < MAXH) E[pos] = e;
+      n += __popc(m);
+    }
+  }
+  for (int i = lane; i < min(n, MAXH); i += 32) S.idx[i] = i;
+  if (n > MAXH) {  // too many crossings for this kernel: hand the row to the wide kernel
+    if (lane == 0) {
+      unsigned long long slot = atomicAdd(&A.counters[kCtrOvfRows], 1ull);
+      if ((long long)slot < A.ovf_cap) A.ovf_rows[slot] = ((long long)job << 32) | y;
+    }
+    return;
+  }
+  __syncwarp();
+
+  // (ii) trapezoid fast path (:1695-1872)
+  if (allSpan && (n % 2) == 0) {
+    float* t0 = reinterpret_cast<float*>(S.a0);
+    float* t1 = reinterpret_cast<float*>(S.a1);
+    float* key = reinterpret_cast<float*>(S.a2);
+    bool anyNaN = false;
+    for (int i = lane; i < n; i += 32) {
+      Entry e = E[S.idx[i]];
+      float xa = e.m == 0 ? e.b : (scanTop - e.b) / e.m;   // solveX :1137-1141
+      float xb = e.m == 0 ? e.b : (scanBottom - e.b) / e.m;
+      t0[i] = xa;
+      t1[i] = xb;
+      key[i] = (xa + xb) * 0.5f;
+      anyNaN |= isnan(key[i]);
+    }
+    anyNaN = __any_sync(0xffffffffu, anyNaN);
+    __syncwarp();
+    // stable insertion sort by midpoint (:1710-1719)
+    if (anyNaN) {
+      if (lane == 0) {
+        for (int i = 1; i < n; i++) {
+          int j = i - 1, kk = i;
+          while (j >= 0 && key[j] > key[kk]) {
+            float tk = key[j]; key[j] = key[j + 1]; key[j + 1] = tk;
+            float ta = t0[j]; t0[j] = t0[j + 1]; t0[j + 1] = ta;
+            float tb = t1[j]; t1[j] = t1[j + 1]; t1[j + 1] = tb;
+            int ti = S.idx[j]; S.idx[j] = S.idx[j + 1]; S.idx[j + 1] = ti;
+            j--;
+            kk--;
+          }
+        }
+      }
+    } else {
+      float* t0s = reinterpret_cast<float*>(S.a3);
+      float* t1s = reinterpret_cast<float*>(S.a4);
+      for (int i = lane; i < n; i += 32) {
+        int r = stable_rank_f(key, n, i);
+        S.a5[r] = S.idx[i];
+        t0s[r] = t0[i];
+        t1s[r] = t1[i];
+      }
+      __syncwarp();
+      for (int i = lane; i < n; i += 32) {
+        S.idx[i] = S.a5[i];
+        t0[i] = t0s[i];
+        t1[i] = t1s[i];
+      }
+    }
+    __syncwarp();
+    // partial coverage of neighbours must not overlap (:1721-1731)
+    bool overlap = false;
+    for (int i = lane; i < n - 1; i += 32) {
+      float leftMaxX = nmax(t0[i], t1[i]);
+      float rightMinX = nmin(t0[i + 1], t1[i + 1]);
+      if (nim_int(ceilf(leftMaxX)) > nim_int(rightMinX)) overlap = true;
+    }
+    overlap = __any_sync(0xffffffffu, overlap);
+    bool simple = false;
+    if (!overlap) {  // pairs must be simple fills (:1733-1750)
+      int ok = 1;
+      if (lane == 0) {
+        long long wc = 0;
+        for (int i = 0; i < n; i += 2) {
+          wc += E[S.idx[i]].w;
+          if (!shouldFill(J.winding, wc)) { ok = 0; break; }
+          wc += E[S.idx[i + 1]].w;
+          if (shouldFill(J.winding, wc)) { ok = 0; break; }
+        }
+      }
+      simple = __shfl_sync(0xffffffffu, ok, 0) != 0;
+    }
+    if (simple) {
+      long long filledTo = 0;
+      for (int i = 0; i < n; i += 2) {
+        const Entry L = E[S.idx[i]], R = E[S.idx[i + 1]];
+        const float tl0 = t0[i], tl1 = t1[i], tr0 = t0[i + 1], tr1 = t1[i + 1];
+        const float leftMaxX = nmax(tl0, tl1), rightMinX = nmin(tr0, tr1);
+        const long long leftCoverEnd = nim_int(ceilf(leftMaxX));
+        const long long rightCoverBegin = nim_int(truncf(rightMinX));
+        {  // left sliver (:1752-1788)
+          const bool inv = tl0 < tl1;
+          const float sliverStart = nmin(tl0, tl1), rectStart = leftMaxX;
+          const long long xs = nim_int(sliverStart), xe = nim_int(ceilf(rectStart));
+          for (long long x = max(xs, 0LL) + lane; x < min(xe, W); x += 32) {
+            float prevPen = x == xs ? sliverStart : (float)x;
+            float pen = (float)(x + 1);
+            float rightRectArea = 0;
+            if (pen > rectStart) {
+              rightRectArea = pen - rectStart;
+              pen = rectStart;
+            }
+            float prevPenY = x == xs ? (inv ? (float)y : (float)(y + 1)) : L.m * (float)x + L.b;
+            float penY = L.m * pen + L.b;
+            float run = pen - prevPen;
+            float tri = 0.5f * run * fabsf(penY - prevPenY);
+            float rect = inv ? (prevPenY - (float)y) * run : ((float)(y + 1) - prevPenY) * run;
+            float area = tri + rect + rightRectArea;
+            row[x] = blend_px(mode, tbl, row[x], mul_f(rgbx, area));
+          }
+        }
+        {  // right sliver (:1790-1828)
+          const bool inv = tr0 > tr1;
+          const float rectEnd = rightMinX, sliverEnd = nmax(tr0, tr1);
+          const long long xs = nim_int(rectEnd), xe = nim_int(ceilf(sliverEnd));
+          for (long long x = max(xs, 0LL) + lane; x < min(xe, W); x += 32) {
+            float prevPen = x == xs ? rectEnd : (float)x;
+            float pen = (float)(x + 1);
+            float ap = fabsf(prevPen);
+            float leftRectArea = ap - floorf(ap);  // vmath fractional: fractional part of |v|
+            if (pen > sliverEnd) pen = sliverEnd;
+            float prevPenY = x == xs ? (inv ? (float)(y + 1) : (float)y) : R.m * (float)x + R.b;
+            float penY = R.m * pen + R.b;
+            float run = pen - prevPen;
+            float tri = 0.5f * run * fabsf(penY - prevPenY);
+            float rect = inv ? (penY - (float)y) * run : ((float)(y + 1) - penY) * run;
+            float area = leftRectArea + tri + rect;
+            row[x] = blend_px(mode, tbl, row[x], mul_f(rgbx, area));
+          }
+        }
+        {  // the fully covered middle (:1830-1835)
+          long long fb = min(max(leftCoverEnd, 0LL), W), fe = min(max(rightCoverBegin, 0LL), W);
+          for (long long x = fb + lane; x < fe; x += 32) row[x] = op_fill(mode, tbl, row[x], rgbx);
+        }
+        if (maskMode) {  // :1837-1845
+          long long clearTo = nim_int(nmin(tl0, tl1));
+          clear_span_linear(J, A, job, row, y, min(filledTo, W), min(clearTo, W), lane);
+        }
+        filledTo = nim_int(ceilf(nmax(tr0, tr1)));
+      }
+      if (maskMode) clear_span_linear(J, A, job, row, y, min(filledTo, W), W, lane);
+      return;
+    }
+  }
+
+  // (iii) computeCoverage (:1350-1431) + fillCoverage / fillHits
+  const bool aa = (bd.flags & kBandAA) != 0;
+  const int quality = aa ? 5 : 1;
+  const int sc = 255 / quality;
+  const float offset = 1.0f / (float)quality;
+  const float initialOffset = offset / 2 + kEps;
+  float yLine = (float)y + initialOffset - offset;
+  if (lane == 0) S.nsp = 0;
+  __syncwarp();
+  for (int m = 0; m < quality; m++) {
+    yLine += offset;
+    int nh = 0;
+    for (int c0 = 0; c0 < n; c0 += 32) {
+      int i = c0 + lane;
+      bool hit = false;
+      int fx = 0, w = 0;
+      if (i < n) {
+        Entry e = E[S.idx[i]];
+        if (e.ay <= yLine && e.by >= yLine) {
+          hit = true;
+          float x = e.m == 0 ? e.b : (yLine - e.b) / e.m;
+          fx = nim_i32(nmin(x, (float)W) * 256.0f);
+          w = e.w;
+        }
+      }
+      unsigned msk = __ballot_sync(0xffffffffu, hit);
+      if (hit) {
+        int pos = nh + __popc(msk & lt);
+        S.a0[pos] = fx;
+        S.a1[pos] = w;
+      }
+      nh += __popc(msk);
+    }
+    __syncwarp();
+    for (int i = lane; i < nh; i += 32) {  // stable sort (:1277-1286)
+      int r = stable_rank_i(S.a0, nh, i);
+      S.a2[r] = S.a0[i];
+      S.a3[r] = S.a1[i];
+    }
+    __syncwarp();
+    if (lane == 0) {  // walk (:1298-1334)
+      int i = 0, ns = S.nsp;
+      long long count = 0;
+      int prevAt = 0;
+      while (i < nh) {
+        int at = S.a2[i], winding = S.a3[i];
+        if (at > 0) {
+          if (shouldFill(J.winding, count)) {
+            if (i < nh - 1) {
+              int nextAt = S.a2[i + 1], nextW = S.a3[i + 1];
+              if (nextAt == at && winding + nextW == 0) {
+                i += 2;
+                continue;
+              }
+              if (J.winding == 0 && count + winding != 0) {
+                count += winding;
+                i++;
+                continue;
+              }
+            }
+            if (ns < RowScratch<MAXH, XT>::SPCAP) S.sp[ns] = make_int2(prevAt, at);
+            ns++;
+          }
+          prevAt = at;
+        }
+        count += winding;
+        i++;
+      }
+      S.nsp = ns;
+    }
+    __syncwarp();
+  }
+  const int nsp = min(S.nsp, RowScratch<MAXH, XT>::SPCAP);
+
+  if (aa) {
+    // coverage row over [startX, startX + pathWidth) in tiles of XT pixels
+    const long long cx0 = J.startX, cx1 = J.startX + J.pathWidth;
+    if (maskMode) {
+      for (long long x = lane; x < W; x += 32)
+        if (x < cx0 || x >= cx1) row[x] = 0u;
+    }
+    for (long long tx0 = cx0; tx0 < cx1; tx0 += XT) {
+      const long long tx1 = min(tx0 + (long long)XT, cx1);
+      const int L = (int)(tx1 - tx0);
+      for (int i = lane; i <= L; i += 32) S.acc[i] = 0;
+      __syncwarp();
+      for (int j = lane; j < nsp; j += 32) {
+        int prevAt = S.sp[j].x, at = S.sp[j].y;
+        long long pi = prevAt / 256, ai = at / 256;
+        long long fillStart = pi;
+        bool crossed = ai != pi;
+        int leftCover = crossed ? (prevAt / 256) * 256 + 256 - prevAt : at - prevAt;
+        if (leftCover != 0) {
+          fillStart++;
+          int v = ((leftCover * sc) / 256) & 255;
+          if (pi >= tx0 && pi < tx1) {
+            atomicAdd(&S.acc[pi - tx0], v);
+            atomicAdd(&S.acc[pi - tx0 + 1], -v);
+          }
+        }
+        if (crossed) {
+          int rightCover = at - (at / 256) * 256;
+          if (rightCover > 0) {
+            int v = ((rightCover * sc) / 256) & 255;
+            if (ai >= tx0 && ai < tx1) {
+              atomicAdd(&S.acc[ai - tx0], v);
+              atomicAdd(&S.acc[ai - tx0 + 1], -v);
+            }
+          }
+        }
+        long long fe = ai;
+        long long lo = max(fillStart, tx0), hi = min(fe, tx1);
+        if (hi > lo) {
+          atomicAdd(&S.acc[lo - tx0], sc);
+          atomicAdd(&S.acc[hi - tx0], -sc);
+        }
+      }
+      __syncwarp();
+      // prefix sum of the difference array; coverage = sum mod 256
+      const int C = (L + 31) / 32;
+      int base = lane * C, s = 0;
+      for (int i = base; i < min(base + C, L); i++) s += S.acc[i];
+      int incl = s;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+      }
+      int run = incl - s;
+      __syncwarp();
+      for (int i = base; i < min(base + C, L); i++) {
+        run += S.acc[i];
+        S.acc[i] = run;
+      }
+      __syncwarp();
+      for (int i = lane; i < L; i += 32) {
+        uint32_t cov = (uint32_t)S.acc[i] & 255u;
+        long long x = tx0 + i;
+        row[x] = op_cov(mode, tbl, row[x], rgbx, cov);
+      }
+      __syncwarp();
+    }
+  } else {
+    // fillHits with the single sample's spans (:1540-1591); spans are sorted
+    // and disjoint, so a pixel is inside at most one.
+    const long long startX = J.startX;
+    for (long long x = lane; x < W; x += 32) {
+      bool inside = false;
+      for (int j = 0; j < nsp && !inside; j++) {
+        long long fs = S.sp[j].x / 256, fe = S.sp[j].y / 256;
+        if (fe - fs > 0 && x >= fs && x < fe) inside = true;
+      }
+      if (maskMode) {
+        row[x] = (x >= startX && inside) ? op_fill(mode, tbl, row[x], rgbx) : 0u;
+      } else if (inside) {
+        row[x] = op_fill(mode, tbl, row[x], rgbx);
+      }
+    }
+  }
+}
+
+constexpr int kFastMaxH = 256, kFastXT = 1024, kFastWarps = 4;
+constexpr int kWideMaxH = 2048, kWideXT = 1024;
+
+__global__ void __launch_bounds__(kFastWarps * 32) k_rows(PathJob* jobs, int njobs, Arena A,
+                                                          const uint8_t* tbl, long long totalRows) {
+  extern __shared__ __align__(16) unsigned char rsm[];
+  using Scratch = RowScratch<kFastMaxH, kFastXT>;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  Scratch& S = reinterpret_cast<Scratch*>(rsm)[warp];
+  for (long long item = (long long)blockIdx.x * kFastWarps + warp; item < totalRows;
+       item += (long long)gridDim.x * kFastWarps) {
+    int lo = 0, hi = njobs - 1;  // job with row_off <= item
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (jobs[mid].row_off <= item) lo = mid;
+      else hi = mid - 1;
+    }
+    const PathJob& J = jobs[lo];
+    const long long y = item - J.row_off;
+    if (J.status != kOk || y >= J.H) continue;
+    if (y < J.startY || y >= J.pathHeight) {
+      if (J.mode == kMask) {  // :1910-1912
+        uint32_t* row = reinterpret_cast<uint32_t*>(J.img) + y * J.W;
+        for (long long x = lane; x < J.W; x += 32) row[x] = 0u;
+      }
+      continue;
+    }
+    process_row<kFastMaxH, kFastXT>(J, A, tbl, lo, y, S, lane);
+  }
+}
+
+// Rows whose crossings exceed the fast kernel's capacity: one warp per CTA
+// with room for kWideMaxH crossings.
+__global__ void __launch_bounds__(32) k_rows_wide(PathJob* jobs, Arena A, const uint8_t* tbl) {
+  extern __shared__ __align__(16) unsigned char rsm[];
+  using Scratch = RowScratch<kWideMaxH, kWideXT>;
+  Scratch& S = *reinterpret_cast<Scratch*>(rsm);
+  const int lane = threadIdx.x & 31;
+  long long n = (long long)min((unsigned long long)A.ovf_cap, A.counters[kCtrOvfRows]);
+  for (long long i = blockIdx.x; i < n; i += gridDim.x) {
+    long long v = A.ovf_rows[i];
+    int job = (int)(v >> 32);
+    long long y = v & 0xffffffffLL;
+    PathJob& J = jobs[job];
+    // a row whose band exceeds the wide kernel too reports an error
+    long long k = (y - J.startY) / (long long)J.ph;
+    if (k >= J.nb) k = J.nb - 1;
+    const Band bd = A.bands[J.band_off + k];
+    if (bd.count > kWideMaxH) {
+      if (lane == 0) J.status = kErrRowTooComplex;
+      continue;
+    }
+    process_row<kWideMaxH, kWideXT>(J, A, tbl, job, y, S, lane);
+  }
+}
+
+// Clears that the reference's linear-index clearUnsafe applies to earlier
+// rows (a trapezoid fill extending left of the image in MaskBlend); they
+// run after every row has been drawn, as they did in the row-ordered loop.
+__global__ void k_xclears(PathJob* jobs, Arena A) {
+  long long n = (long long)min((unsigned long long)A.xclear_cap, A.counters[kCtrXClears]);
+  for (long long i = blockIdx.x; i < n; i += gridDim.x) {
+    const PathJob& J = jobs[A.xclears[3 * i]];
+    uint32_t* px = reinterpret_cast<uint32_t*>(J.img);
+    for (long long p = A.xclears[3 * i + 1] + threadIdx.x; p < A.xclears[3 * i + 2]; p += blockDim.x)
+      px[p] = 0u;
+  }
+}
+
+size_t rows_smem_fast() { return sizeof(RowScratch<kFastMaxH, kFastXT>) * kFastWarps; }
+size_t rows_smem_wide() { return sizeof(RowScratch<kWideMaxH, kWideXT>); }
+int rows_warps_fast() { return kFastWarps; }
+
+}  // namespace pxg
