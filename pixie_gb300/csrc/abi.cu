@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -58,18 +59,20 @@ using namespace pxg;
 
 namespace {
 
-thread_local std::string t_err;
+// Per-thread error text in fixed buffers: setting an error allocates nothing.
+thread_local char t_err[1024];
 thread_local bool t_has_err = false;
-thread_local std::string t_taken;
+thread_local char t_taken[1024];
 
 struct ApiError {
   std::string msg;
 };
 
-void set_err(const std::string& m) {
-  t_err = m;
+void set_err(const char* m) {
+  snprintf(t_err, sizeof t_err, "%s", m);
   t_has_err = true;
 }
+void set_err(const std::string& m) { set_err(m.c_str()); }
 
 #define CU(x)                                                                               \
   do {                                                                                      \
@@ -391,15 +394,20 @@ void run_single(pxg_image* img, std::vector<Prim>& prims, uint32_t rgbx, int ble
 
 }  // namespace
 
+namespace pxg {
+// Records an error for pxg_take_error() without allocating.
+void record_error(const char* msg) { set_err(msg); }
+}  // namespace pxg
+
 extern "C" {
 
 int pxg_check_error(void) { return t_has_err ? 1 : 0; }
 
 const char* pxg_take_error(void) {
-  t_taken = t_has_err ? t_err : std::string();
-  t_err.clear();
+  snprintf(t_taken, sizeof t_taken, "%s", t_has_err ? t_err : "");
+  t_err[0] = 0;
   t_has_err = false;
-  return t_taken.c_str();
+  return t_taken;
 }
 
 int pxg_init(int device) {
@@ -662,9 +670,9 @@ pxg_image* pxg_image_shadow(const pxg_image* im, float ox, float oy, float sprea
   guarded([&] {
     check_image(im);
     pxg_image* res = pxg_new_image(im->width, im->height);
-    if (!res) throw ApiError{t_err};
+    if (!res) throw ApiError{std::string(t_err)};
     if (pxg_image_shadow_into(im, res, ox, oy, spread, blur, color) != 0) {
-      std::string m = t_err;
+      std::string m(t_err);
       pxg_image_free(res);
       throw ApiError{m};
     }

@@ -392,7 +392,10 @@ size_t blur_y_smem(int r) { return (size_t)(kTY + 2 * r) * kTX * 4 + (size_t)(2 
 // integer tiles, then the direct kernels.
 void launch_blur(uint32_t* img, uint32_t* tmp, long long W, long long H, int r,
                  const uint16_t* kern, uint32_t oob, int nsm, size_t maxSmem, cudaStream_t st) {
-  if (blockblur_smem(r) <= maxSmem && (H + 31) / 32 <= 65535 && (W + 31) / 32 <= 65535) {
+  // radius >= 8: register-blocked tiles; smaller radii stay on the one-output
+  // float32 tiles, where the blocked kernel's 8-tap granularity and halo cost
+  // more than they save.
+  if (r >= 8 && blockblur_smem(r) <= maxSmem && (H + 31) / 32 <= 65535 && (W + 31) / 32 <= 65535) {
     dim3 gx((unsigned)((W + kBT - 1) / kBT), (unsigned)((H + 31) / 32));
     k_blurb<true><<<gx, kBWarps * 32, blockblur_smem(r), st>>>(img, tmp, W, H, r, kern, oob); note_launch();
     dim3 gy((unsigned)((H + kBT - 1) / kBT), (unsigned)((W + 31) / 32));

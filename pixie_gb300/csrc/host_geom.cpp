@@ -579,10 +579,11 @@ uint32_t color_to_rgbx(const float* c) {
 }
 
 // gaussianKernel  internal.nim:17-34 (the `1 / sqrt(2*PI*s^2) * exp(..)`
-// term meets the float64 PI and is float64; `total` is float64).
-std::vector<uint16_t> gaussian_kernel(int64_t radius) {
-  size_t n = (size_t)(radius * 2 + 1);
-  std::vector<float> f(n);
+// term meets the float64 PI and is float64; `total` is float64).  Writes
+// 2*radius+1 weights into `out`, using `floats` (same length) as work space;
+// allocates nothing.
+void gaussian_kernel_into(int64_t radius, float* f, uint16_t* out) {
+  const size_t n = (size_t)(radius * 2 + 1);
   double total = 0.0;
   for (int64_t step = -radius; step <= radius; step++) {
     float s = (float)radius / 2.2f;
@@ -591,12 +592,17 @@ std::vector<uint16_t> gaussian_kernel(int64_t radius) {
     f[(size_t)(step + radius)] = (float)a;
     total += a;
   }
-  std::vector<uint16_t> out(n);
   for (size_t i = 0; i < n; i++) {
     float v = (float)((double)f[i] / total);
     float r = roundf(v * 255 * 256);
     out[i] = (uint16_t)(uint32_t)(int32_t)r;
   }
+}
+
+std::vector<uint16_t> gaussian_kernel(int64_t radius) {
+  std::vector<float> f((size_t)(radius * 2 + 1));
+  std::vector<uint16_t> out(f.size());
+  gaussian_kernel_into(radius, f.data(), out.data());
   return out;
 }
 

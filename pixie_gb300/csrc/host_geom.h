@@ -35,6 +35,7 @@ bool is_identity(const float* mat9);
 float error_margin_sq(float pixelScale);
 uint32_t color_to_rgbx(const float* color4);  // straight float colour -> premultiplied RGBX
 std::vector<uint16_t> gaussian_kernel(int64_t radius);
+void gaussian_kernel_into(int64_t radius, float* work, uint16_t* out);  // no allocation
 void straight_alpha_table(uint8_t* out256x256);
 
 }  // namespace pxg
