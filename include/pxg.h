@@ -121,6 +121,21 @@ int pxg_fill_paths_batch(pxg_image* const* images, int64_t n_jobs, const float* 
                          const int32_t* blend_modes, const float* transforms,
                          const int32_t* winding_rules, int32_t* status);
 
+/* Blur without allocating: the same result as pxg_image_blur, for callers
+ * that cannot call cudaMalloc (programs whose device memory is owned by their
+ * own pool allocator, or latency-critical paths where an allocation's
+ * blocking and device-wide synchronisation are not acceptable).  It works in
+ * place on the caller's image (`rgbx`, 4 * width * height bytes, 16-byte
+ * aligned) on the caller's stream and takes its work space from a fixed
+ * 8 MiB + 16 KiB array in the library's device image, so images are limited
+ * to 2097152 pixels and radii to 2048 (larger ones are rejected).  Every call
+ * shares that array: calls whose GPU work overlaps race.  The first call on a
+ * device sets the array up (cudaGetSymbolAddress) and should come before any
+ * stream capture.  It returns once the work is enqueued.  No counterpart in
+ * the reference, which has no device memory. */
+int pxg_image_blur_noalloc(void* rgbx, int64_t width, int64_t height, float radius,
+                           const float out_of_bounds[4], void* cuda_stream);
+
 /* Time of the last blocking call's GPU work in milliseconds (CUDA events on
  * the library's stream); for measurement only. */
 float pxg_last_gpu_ms(void);
