@@ -313,26 +313,188 @@ def run_fill_extras(px, wl, args):
     out["plain_fill_512_64cubics"] = {"paths_per_s": round(n / dt, 1),
                                       "gpu_ms_per_path": round(gpu_ms / n, 4),
                                       "note": "one blocking C-ABI call per path, host pre-pass included"}
-    glyphs, _ = wl.glyph_batch(7, n=args.glyphs)
-    imgs = [px.Image(w, h) for (_, w, h, _) in glyphs]
-    cmds = [g[0] for g in glyphs]
-    cols = [[1, 1, 1, 1]] * len(glyphs)
-    winds = [g[3] for g in glyphs]
-    px.fill_paths_batch(imgs, cmds, cols, winding_rules=winds)
-    t = time.perf_counter()
-    reps = 3
-    for _ in range(reps):
-        px.fill_paths_batch(imgs, cmds, cols, winding_rules=winds)
-    dt_b = (time.perf_counter() - t) / reps
-    t = time.perf_counter()
-    for im, c, w in zip(imgs, cmds, winds):
-        im.fill_path(c, [1, 1, 1, 1], None, w)
-    dt_p = time.perf_counter() - t
-    out["glyph_batch"] = {"glyphs": len(glyphs), "batched_paths_per_s": round(len(glyphs) / dt_b, 1),
-                          "plain_paths_per_s": round(len(glyphs) / dt_p, 1),
-                          "batched_over_plain": round(dt_p / dt_b, 2)}
+    out["glyph_batch"] = run_glyphs(px, wl, args.glyphs)
+    out["dense_scene_1024_2000"] = run_scene(px, wl)
+    if args.serve_jobs > 0:
+        out["serving"] = run_serving(px, wl, args.serve_jobs, args.serve_pool)
     px.set_blocking(False)
     return out
+
+
+def record_scene(px, items):
+    sc = px.Scene()
+    failed = 0
+    for it in items:
+        paint = px.Paint(it["color"], 1.0, it["blend"])
+        try:
+            if it["kind"] == "fill":
+                sc.fill_path(it["cmds"], paint, None, it["winding"])
+            else:
+                sc.stroke_path(it["cmds"], paint, None, it["width"], it["cap"], it["join"], it["miter"])
+        except px.PixieError:
+            failed += 1
+    return sc, failed
+
+
+def run_serving(px, wl, n_jobs, pool, rates=(100, 300, 1000, 3000, 10000, 20000), seed=11):
+    """Open-loop serving sweep: Poisson arrivals at each rate, n_jobs jobs per
+    rate drawn from a pool of recorded jobs (canvas side log-U[256, 4096],
+    10..5000 dense-scene paths, blur r in 2..32 on 20% of jobs), admitted
+    against a 40 GB budget.  Latency = arrival -> canvas copied back to the
+    host.  Every served canvas is compared with the same job rendered alone."""
+    t = time.perf_counter()
+    jobs = [wl.serving_job(seed * 100 + k) for k in range(pool)]
+    scenes = [record_scene(px, j["items"])[0] for j in jobs]
+    prep_s = time.perf_counter() - t
+    alone = []
+    for j, sc in zip(jobs, scenes):
+        img = px.Image(j["side"], j["side"])
+        img.draw_scene(sc)
+        if j["blur"]:
+            img.blur(j["blur"])
+        alone.append(img.to_numpy())
+    res = {"pool_jobs": pool, "jobs_per_rate": n_jobs, "budget_gb": 40,
+           "pool_sides": [j["side"] for j in jobs], "pool_paths": [len(s) for s in scenes],
+           "pool_blur": [j["blur"] for j in jobs], "prep_s": round(prep_s, 1), "rates": []}
+    all_exact = True
+    for ri, rate in enumerate(rates):
+        sv = px.Server(40 << 30, 512, 16384)
+        arr = wl.poisson_arrivals(seed + ri, float(rate), n_jobs)
+        which = {}
+        lat = []
+        exact = True
+        i = 0
+        done = 0
+        t0 = time.perf_counter()
+        while done < n_jobs:
+            now = time.perf_counter() - t0
+            while i < n_jobs and arr[i] <= now:
+                k = i % pool
+                jid = sv.submit(scenes[k], jobs[k]["side"], jobs[k]["side"], jobs[k]["blur"])
+                which[jid] = (k, arr[i])
+                i += 1
+            if sv.pending() > 0:
+                sv.step()
+            elif i < n_jobs:
+                time.sleep(max(0.0, min(arr[i] - (time.perf_counter() - t0), 0.002)))
+            for jid in sv.poll():
+                outimg, _ = sv.take(jid)
+                k, a = which.pop(jid)
+                lat.append(time.perf_counter() - t0 - a)
+                exact = exact and outimg is not None and np.array_equal(outimg, alone[k])
+                done += 1
+        wall = time.perf_counter() - t0
+        st = sv.stats()
+        lat_ms = np.sort(np.asarray(lat)) * 1e3
+        res["rates"].append({"rate_jobs_per_s": rate, "jobs": n_jobs,
+                             "jobs_per_s": round(n_jobs / wall, 2),
+                             "p50_ms": round(float(np.percentile(lat_ms, 50)), 2),
+                             "p99_ms": round(float(np.percentile(lat_ms, 99)), 2),
+                             "steps": st["steps"], "peak_admitted": st["peak_admitted"],
+                             "peak_gb": round(st["peak_bytes"] / 2**30, 2),
+                             "bitexact_vs_alone": bool(exact)})
+        all_exact = all_exact and exact
+        del sv
+    res["all_bitexact_vs_alone"] = all_exact
+    return res
+
+
+def run_glyphs(px, wl, n, seed=7, page_side=4096, reps=5):
+    """The glyph batch: n glyph outlines, each into its own 8-bit mask, then
+    composited in order onto a page with NormalBlend.  Batched: one mask
+    batch (recorded once; one graph launch renders it) + one ordered
+    composite.  Plain: one blocking fillPath per glyph into its own image,
+    then one draw per glyph."""
+    glyphs, pos = wl.glyph_batch(seed, n=n, page=page_side)
+    page = px.Image(page_side, page_side)
+    t = time.perf_counter()
+    m = px.Masks()
+    for cmds, w, h, wind in glyphs:
+        m.add_path(cmds, w, h, None, wind)
+    rec_s = time.perf_counter() - t
+    m.render()  # first render of the class: the autotuner times its candidates
+    page.draw_masks(m, pos)
+    px.synchronize()
+    render_ms, wall, comp_ms = [], [], []
+    for _ in range(reps):
+        page.fill([0, 0, 0, 0])
+        px.synchronize()
+        t = time.perf_counter()
+        m.render()
+        render_ms.append(px.last_gpu_ms())
+        page.draw_masks(m, pos)
+        px.synchronize()
+        wall.append(time.perf_counter() - t)
+    # composite alone, timed on the library's stream
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        page.draw_masks(m, pos)
+        px.synchronize()
+        comp_ms.append((time.perf_counter() - t0) * 1e3)
+    imgs = [px.Image(w, h) for (_, w, h, _) in glyphs]
+    for im, (c, _, _, wd) in zip(imgs[:64], glyphs[:64]):
+        im.fill_path(c, [1, 1, 1, 1], None, wd)
+    page.fill([0, 0, 0, 0])
+    px.synchronize()
+    t = time.perf_counter()
+    for im, (c, _, _, wd), (x, y) in zip(imgs, glyphs, pos):
+        im.fill_path(c, [1, 1, 1, 1], None, wd)
+        page.draw(im, (int(x), int(y)))
+    px.synchronize()
+    dt_plain = time.perf_counter() - t
+    b = sorted(wall)[len(wall) // 2]
+    return {"glyphs": n, "page": f"{page_side}x{page_side}",
+            "batched_paths_per_s": round(n / b, 1),
+            "batched_incl_recording_paths_per_s": round(n / (b + rec_s), 1),
+            "plain_paths_per_s": round(n / dt_plain, 1),
+            "batched_over_plain": round(dt_plain / b, 2),
+            "batched_incl_recording_over_plain": round(dt_plain / (b + rec_s), 2),
+            "render_gpu_ms": round(sorted(render_ms)[len(render_ms) // 2], 3),
+            "composite_call_ms": round(sorted(comp_ms)[len(comp_ms) // 2], 3),
+            "record_ms_host": round(rec_s * 1e3, 1),
+            "autotune": px.autotune_report().strip().splitlines(),
+            "note": "batched = one graph launch rendering all masks + one ordered composite; "
+                    "plain = blocking fillPath + draw per glyph"}
+
+
+def run_scene(px, wl, seed=7, n_paths=2000, size=1024, reps=3):
+    """The dense scene: 2000 mixed paths recorded (host geometry), then painted
+    in order onto a 1024x1024 canvas by one draw_scene call."""
+    items = wl.dense_scene(seed, n_paths=n_paths, size=float(size))
+    t = time.perf_counter()
+    sc = px.Scene()
+    failed = 0
+    for it in items:
+        paint = px.Paint(it["color"], 1.0, it["blend"])
+        try:
+            if it["kind"] == "fill":
+                sc.fill_path(it["cmds"], paint, None, it["winding"])
+            else:
+                sc.stroke_path(it["cmds"], paint, None, it["width"], it["cap"], it["join"], it["miter"])
+        except px.PixieError:
+            failed += 1  # arcs the reference's arc stepping cannot discretise
+    rec_s = time.perf_counter() - t
+    canvas = px.Image(size, size)
+    canvas.draw_scene(sc)
+    stats = px.last_fill_stats()
+    gpu_ms = []
+    wall = []
+    for _ in range(reps):
+        canvas.fill([0, 0, 0, 0])
+        t = time.perf_counter()
+        canvas.draw_scene(sc)
+        wall.append(time.perf_counter() - t)
+        gpu_ms.append(px.last_gpu_ms())
+    g = sorted(gpu_ms)[len(gpu_ms) // 2]
+    w = sorted(wall)[len(wall) // 2]
+    painted = len(sc)
+    return {"paths_recorded": painted, "paths_raising_in_reference": failed,
+            "segments": stats["segments"], "primitives": stats["primitives"],
+            "gpu_ms_per_scene": round(g, 3), "paths_per_s_gpu": round(painted / (g / 1e3), 1),
+            "edges_per_s_gpu": round(stats["segments"] / (g / 1e3), 1),
+            "draw_call_ms": round(w * 1e3, 3), "record_ms_host": round(rec_s * 1e3, 1),
+            "note": "gpu_ms covers the primitive upload, setup and scene launches of draw_scene; "
+                    "record_ms is the host command walk and stroke outlining of all paths"}
 
 
 # Per-launch DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) from
@@ -439,6 +601,8 @@ def main():
     ap.add_argument("--impl", default="pxg", choices=["pxg", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--glyphs", type=int, default=4096)
+    ap.add_argument("--serve-jobs", type=int, default=40, help="jobs per arrival rate (0: skip serving)")
+    ap.add_argument("--serve-pool", type=int, default=12, help="distinct recorded jobs the arrivals draw from")
     ap.add_argument("--no-fill", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--case", default=None,

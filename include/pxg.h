@@ -121,6 +121,107 @@ int pxg_fill_paths_batch(pxg_image* const* images, int64_t n_jobs, const float* 
                          const int32_t* blend_modes, const float* transforms,
                          const int32_t* winding_rules, int32_t* status);
 
+/* Scenes: a recorded sequence of fillPath/strokePath calls painted onto one
+ * image in order -- what a caller of the reference does when it draws many
+ * paths onto one image (src/pixie/paths.nim:2093-2175 called in a loop, as
+ * svg.nim:557-600 and contexts.nim:384-400 do).  pxg_scene_fill_path and
+ * pxg_scene_stroke_path take the arguments of pxg_image_fill_path and
+ * pxg_image_stroke_path, check them and build the path's geometry at once
+ * (geometry errors are returned by the recording call, and that path is not
+ * recorded); paths whose paint draws nothing are skipped, as fillPath skips
+ * them.  pxg_image_draw_scene paints every recorded path in order with one
+ * setup launch and one row launch (MaskBlend paths, whose clears reach rows
+ * outside the path, are drawn alone between the runs around them).  If a
+ * path fails while drawing (e.g. "Unable to discretize cubic"), the paths
+ * before it are drawn, it and the later paths are not, and the error is
+ * returned -- the state the reference leaves when that call raises. */
+typedef struct pxg_scene pxg_scene;
+pxg_scene* pxg_scene_new(void);
+void pxg_scene_free(pxg_scene* scene);
+int pxg_scene_clear(pxg_scene* scene);
+int64_t pxg_scene_len(const pxg_scene* scene);
+int pxg_scene_fill_path(pxg_scene* scene, const float* commands, int64_t n_commands,
+                        const float color[4], float opacity, int blend_mode,
+                        const float transform[9], int winding_rule);
+int pxg_scene_stroke_path(pxg_scene* scene, const float* commands, int64_t n_commands,
+                          const float color[4], float opacity, int blend_mode,
+                          const float transform[9], float stroke_width, int line_cap,
+                          int line_join, float miter_limit, const float* dashes, int64_t n_dashes);
+int pxg_image_draw_scene(pxg_image* image, const pxg_scene* scene);
+
+/* Mask batches: many paths, each filled with color(1, 1, 1, 1) onto a
+ * transparent image of its own size, kept as the 8-bit alpha of that image
+ * (every channel of such an image equals its alpha).  This is the first half
+ * of rendering glyphs in the reference: fillPath of each glyph's path into
+ * its own image (src/pixie/paths.nim:2093-2113; fonts.nim:566-596 fills
+ * glyph paths).  pxg_masks_add_path builds the primitives on the host;
+ * pxg_masks_render renders every mask of the batch in one setup launch and
+ * one persistent row launch (a device work queue of row items), captured
+ * once in a CUDA graph and replayed while the batch's shape is unchanged;
+ * pxg_masks_download copies mask i (width * height bytes) to the host.
+ * pxg_image_draw_masks is the second half: draw(page, mask_i,
+ * translate(xy[2i], xy[2i+1]), blend_mode) for i = 0..n-1 in order
+ * (images.nim:636-678, blendRect :468-529) in one launch; MaskBlend, whose
+ * draw clears the whole page outside each mask, is rejected.  No
+ * counterpart in the reference's bindings. */
+typedef struct pxg_masks pxg_masks;
+pxg_masks* pxg_masks_new(void);
+void pxg_masks_free(pxg_masks* masks);
+int64_t pxg_masks_len(const pxg_masks* masks);
+int pxg_masks_add_path(pxg_masks* masks, const float* commands, int64_t n_commands, int64_t width,
+                       int64_t height, const float transform[9], int winding_rule);
+int pxg_masks_render(pxg_masks* masks);
+/* Renders with a given row-kernel configuration instead of the tuned one
+ * (variant 0: 256-crossing scratch, 1: 32-crossing scratch; rows per work
+ * item 1..64); for tests and tuning. */
+int pxg_masks_render_config(pxg_masks* masks, int variant, int rows_per_item);
+int pxg_masks_download(const pxg_masks* masks, int64_t index, void* out, int64_t nbytes);
+const void* pxg_masks_device_ptr(const pxg_masks* masks, int64_t index);
+int pxg_image_draw_masks(pxg_image* page, const pxg_masks* masks, const int64_t* xy, int blend_mode);
+
+/* Serving: render jobs admitted against a device-memory budget and advanced
+ * together by continuous batching.  A job paints a recorded scene onto a
+ * fresh transparent width x height canvas (the reference's newImage + the
+ * scene's fillPath/strokePath calls), then blurs it when blur_radius rounds
+ * to a radius > 0 (images.nim:304-365, transparent out-of-bounds colour).
+ * pxg_server_submit queues a job (the scene must stay alive and unchanged
+ * until the job's result is taken) and returns its id (0 on error).
+ * pxg_server_step admits queued jobs in arrival order while their canvases
+ * (and blur work space) fit the budget, then advances every admitted job by
+ * up to paths_per_job of its paths -- at most paths_per_step in all -- in
+ * one setup launch and one scene launch; jobs whose paths are all painted
+ * are blurred and finish, freeing their memory for the next admissions.
+ * pxg_server_poll returns finished job ids; pxg_server_take copies a
+ * finished job's canvas to the host (out may be NULL), reports its submit,
+ * admit and finish times (seconds, steady clock) and releases it; a job
+ * whose path raised returns that error from pxg_server_take.
+ * pxg_server_stats: steps, bytes in use, peak bytes, peak admitted jobs,
+ * queued jobs, admitted jobs.  No counterpart in the reference. */
+typedef struct pxg_server pxg_server;
+pxg_server* pxg_server_new(int64_t budget_bytes, int64_t paths_per_job, int64_t paths_per_step);
+void pxg_server_free(pxg_server* server);
+int64_t pxg_server_submit(pxg_server* server, const pxg_scene* scene, int64_t width, int64_t height,
+                          float blur_radius);
+int pxg_server_step(pxg_server* server);
+int64_t pxg_server_pending(const pxg_server* server);
+int64_t pxg_server_poll(pxg_server* server, int64_t* ids, int64_t capacity);
+int pxg_server_take(pxg_server* server, int64_t id, void* out_rgbx, int64_t nbytes, double times[3]);
+int pxg_server_stats(const pxg_server* server, int64_t out[6]);
+
+/* Autotuner: for each operation and shape class, the fastest of a few launch
+ * configurations (row-kernel scratch size and rows per work item for mask
+ * batches; the page tile of the mask composite), timed once the first time
+ * the class is seen.  Every configuration writes the same bytes.  On by
+ * default; pxg_autotune_report writes one line per tuned class into buf and
+ * returns the report's length.  No counterpart in the reference. */
+int pxg_autotune(int enable);
+int64_t pxg_autotune_report(char* buf, int64_t capacity);
+
+/* Counts of the last fill launch (fillPath, strokePath, batch or scene):
+ * out[0] paths, out[1] primitives uploaded, out[2] segments after
+ * flattening, out[3] band entries.  No counterpart in the reference. */
+int pxg_last_fill_stats(int64_t out[4]);
+
 /* Blur without allocating: the same result as pxg_image_blur, for callers
  * that cannot call cudaMalloc (programs whose device memory is owned by their
  * own pool allocator, or latency-critical paths where an allocation's

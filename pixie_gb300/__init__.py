@@ -105,6 +105,44 @@ def lib():
         L.pxg_blend_pixels.argtypes = [I, P, P, P, I64]
         L.pxg_fill_paths_batch.argtypes = [P, I64, P, P, P, P, P, P, P, P]
         L.pxg_last_gpu_ms.restype = F
+        L.pxg_scene_new.restype = P
+        L.pxg_scene_free.argtypes = [P]
+        L.pxg_scene_free.restype = None
+        L.pxg_scene_clear.argtypes = [P]
+        L.pxg_scene_len.argtypes = [P]
+        L.pxg_scene_len.restype = I64
+        L.pxg_scene_fill_path.argtypes = [P, P, I64, P, F, I, P, I]
+        L.pxg_scene_stroke_path.argtypes = [P, P, I64, P, F, I, P, F, I, I, F, P, I64]
+        L.pxg_image_draw_scene.argtypes = [P, P]
+        L.pxg_last_fill_stats.argtypes = [P]
+        L.pxg_masks_new.restype = P
+        L.pxg_masks_free.argtypes = [P]
+        L.pxg_masks_free.restype = None
+        L.pxg_masks_len.argtypes = [P]
+        L.pxg_masks_len.restype = I64
+        L.pxg_masks_add_path.argtypes = [P, P, I64, I64, I64, P, I]
+        L.pxg_masks_render.argtypes = [P]
+        L.pxg_masks_render_config.argtypes = [P, I, I]
+        L.pxg_masks_download.argtypes = [P, I64, P, I64]
+        L.pxg_masks_device_ptr.argtypes = [P, I64]
+        L.pxg_masks_device_ptr.restype = P
+        L.pxg_image_draw_masks.argtypes = [P, P, P, I]
+        L.pxg_server_new.restype = P
+        L.pxg_server_new.argtypes = [I64, I64, I64]
+        L.pxg_server_free.argtypes = [P]
+        L.pxg_server_free.restype = None
+        L.pxg_server_submit.argtypes = [P, P, I64, I64, F]
+        L.pxg_server_submit.restype = I64
+        L.pxg_server_step.argtypes = [P]
+        L.pxg_server_pending.argtypes = [P]
+        L.pxg_server_pending.restype = I64
+        L.pxg_server_poll.argtypes = [P, P, I64]
+        L.pxg_server_poll.restype = I64
+        L.pxg_server_take.argtypes = [P, I64, P, I64, P]
+        L.pxg_server_stats.argtypes = [P, P]
+        L.pxg_autotune.argtypes = [I]
+        L.pxg_autotune_report.argtypes = [P, I64]
+        L.pxg_autotune_report.restype = I64
         _lib = L
     return _lib
 
@@ -248,6 +286,173 @@ class Image:
                                            float(spread), float(blur), _ptr(_color(color))))
 
 
+    def draw_masks(self, masks: "Masks", positions, blend_mode=BlendMode.NormalBlend):
+        draw_masks(self, masks, positions, blend_mode)
+
+    def draw_scene(self, scene: "Scene"):
+        """Paints the scene's recorded paths in order (one setup and one row
+        launch for the whole sequence)."""
+        _check(lib().pxg_image_draw_scene(self._h, scene._h))
+
+
+class Scene:
+    """A recorded sequence of fill_path/stroke_path calls, painted in order
+    onto an image by Image.draw_scene.  Each call takes the arguments of the
+    Image method of the same name."""
+
+    def __init__(self):
+        self._h = lib().pxg_scene_new()
+        if not self._h:
+            raise PixieError(lib().pxg_take_error().decode())
+
+    def __del__(self):
+        h, self._h = getattr(self, "_h", None), None
+        if h and _lib is not None:
+            _lib.pxg_scene_free(h)
+
+    def __len__(self):
+        return int(lib().pxg_scene_len(self._h))
+
+    def clear(self):
+        _check(lib().pxg_scene_clear(self._h))
+
+    def fill_path(self, path, paint, transform=None, winding_rule=WindingRule.NonZero):
+        cmds = as_commands(path)
+        col, op, blend = _paint(paint)
+        m = _mat(transform)
+        _check(lib().pxg_scene_fill_path(self._h, _ptr(cmds), cmds.size, _ptr(col), op, blend,
+                                         None if m is None else _ptr(m), int(winding_rule)))
+
+    def stroke_path(self, path, paint, transform=None, stroke_width=1.0,
+                    line_cap=LineCap.ButtCap, line_join=LineJoin.MiterJoin,
+                    miter_limit=DEFAULT_MITER_LIMIT, dashes=()):
+        cmds = as_commands(path)
+        col, op, blend = _paint(paint)
+        m = _mat(transform)
+        d = np.ascontiguousarray(list(dashes) if len(dashes) else [0.0], dtype=np.float32)
+        _check(lib().pxg_scene_stroke_path(self._h, _ptr(cmds), cmds.size, _ptr(col), op, blend,
+                                           None if m is None else _ptr(m), float(stroke_width),
+                                           int(line_cap), int(line_join), float(miter_limit),
+                                           _ptr(d), len(dashes)))
+
+
+class Masks:
+    """A batch of 8-bit masks: add_path(path, width, height) fills the path
+    with color(1, 1, 1, 1) on a transparent width x height image and keeps its
+    alpha; render() renders the whole batch on the GPU (one graph launch);
+    Image.draw_masks composites them in order."""
+
+    def __init__(self):
+        self._h = lib().pxg_masks_new()
+        if not self._h:
+            raise PixieError(lib().pxg_take_error().decode())
+        self._sizes = []
+
+    def __del__(self):
+        h, self._h = getattr(self, "_h", None), None
+        if h and _lib is not None:
+            _lib.pxg_masks_free(h)
+
+    def __len__(self):
+        return int(lib().pxg_masks_len(self._h))
+
+    def add_path(self, path, width: int, height: int, transform=None,
+                 winding_rule=WindingRule.NonZero):
+        cmds = as_commands(path)
+        m = _mat(transform)
+        _check(lib().pxg_masks_add_path(self._h, _ptr(cmds), cmds.size, int(width), int(height),
+                                        None if m is None else _ptr(m), int(winding_rule)))
+        self._sizes.append((int(width), int(height)))
+
+    def render(self):
+        _check(lib().pxg_masks_render(self._h))
+
+    def render_config(self, variant: int, rows_per_item: int):
+        """Renders with a fixed row-kernel configuration (tests, tuning)."""
+        _check(lib().pxg_masks_render_config(self._h, int(variant), int(rows_per_item)))
+
+    def mask(self, i: int) -> np.ndarray:
+        w, h = self._sizes[i]
+        out = np.empty((h, w), np.uint8)
+        _check(lib().pxg_masks_download(self._h, int(i), _ptr(out), out.nbytes))
+        return out
+
+
+def draw_masks(page: "Image", masks: Masks, positions, blend_mode=BlendMode.NormalBlend):
+    """draw(page, mask_i, translate(x_i, y_i), blend_mode) for every mask in order."""
+    xy = np.ascontiguousarray(positions, np.int64).reshape(-1, 2)
+    if len(xy) != len(masks):
+        raise PixieError("one position per mask is required")
+    _check(lib().pxg_image_draw_masks(page._h, masks._h, _ptr(xy), int(blend_mode)))
+
+
+class Server:
+    """Continuous-batching render server (see pxg_server_* in include/pxg.h).
+    submit(scene, width, height, blur) -> job id; step() advances admitted
+    jobs; poll() -> finished ids; take(id) -> (canvas RGBX array or None,
+    (submit, admit, done) times)."""
+
+    def __init__(self, budget_bytes=40 << 30, paths_per_job=512, paths_per_step=16384):
+        self._h = lib().pxg_server_new(int(budget_bytes), int(paths_per_job), int(paths_per_step))
+        if not self._h:
+            raise PixieError(lib().pxg_take_error().decode())
+        self._scenes = {}
+        self._sizes = {}
+
+    def __del__(self):
+        h, self._h = getattr(self, "_h", None), None
+        if h and _lib is not None:
+            _lib.pxg_server_free(h)
+
+    def submit(self, scene: "Scene", width: int, height: int, blur: float = 0.0) -> int:
+        jid = int(lib().pxg_server_submit(self._h, scene._h, int(width), int(height), float(blur)))
+        if jid == 0:
+            raise PixieError(lib().pxg_take_error().decode())
+        self._scenes[jid] = scene  # kept alive until taken
+        self._sizes[jid] = (int(width), int(height))
+        return jid
+
+    def step(self):
+        _check(lib().pxg_server_step(self._h))
+
+    def pending(self) -> int:
+        return int(lib().pxg_server_pending(self._h))
+
+    def poll(self, cap: int = 4096):
+        ids = np.zeros(cap, np.int64)
+        n = int(lib().pxg_server_poll(self._h, _ptr(ids), cap))
+        return [int(v) for v in ids[:n]]
+
+    def take(self, jid: int, download: bool = True):
+        w, h = self._sizes[jid]
+        out = np.empty((h, w, 4), np.uint8) if download else None
+        times = np.zeros(3, np.float64)
+        try:
+            _check(lib().pxg_server_take(self._h, int(jid), None if out is None else _ptr(out),
+                                         0 if out is None else out.nbytes, _ptr(times)))
+        finally:
+            self._scenes.pop(jid, None)
+            self._sizes.pop(jid, None)
+        return out, tuple(float(t) for t in times)
+
+    def stats(self) -> dict:
+        v = np.zeros(6, np.int64)
+        _check(lib().pxg_server_stats(self._h, _ptr(v)))
+        return dict(zip(["steps", "bytes_used", "peak_bytes", "peak_admitted", "queued", "admitted"],
+                        [int(x) for x in v]))
+
+
+def autotune(enable: bool):
+    _check(lib().pxg_autotune(1 if enable else 0))
+
+
+def autotune_report() -> str:
+    n = int(lib().pxg_autotune_report(None, 0))
+    buf = C.create_string_buffer(n + 1)
+    lib().pxg_autotune_report(buf, n + 1)
+    return buf.value.decode()
+
+
 def blend_pixels(mode: int, backdrop_dev: int, source_dev: int, out_dev: int, n: int):
     """blender(mode) over n device pixels (for testing the blend modes)."""
     _check(lib().pxg_blend_pixels(int(mode), C.c_void_p(backdrop_dev), C.c_void_p(source_dev),
@@ -277,6 +482,13 @@ def fill_paths_batch(images, paths, colors, opacities=None, blend_modes=None, tr
 
 def last_gpu_ms() -> float:
     return float(lib().pxg_last_gpu_ms())
+
+
+def last_fill_stats() -> dict:
+    """Counts of the last fill launch: paths, primitives, segments, band entries."""
+    v = np.zeros(4, np.int64)
+    _check(lib().pxg_last_fill_stats(_ptr(v)))
+    return {"paths": int(v[0]), "primitives": int(v[1]), "segments": int(v[2]), "band_entries": int(v[3])}
 
 
 def set_blocking(blocking: bool):

@@ -4,7 +4,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
+#include <deque>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -23,11 +25,88 @@ struct pxg_image {
   int owned;
 };
 
+struct GraphCacheHolder;
+
+// A batch of 8-bit masks: each the alpha of fillPath(color(1, 1, 1, 1)) on a
+// transparent image of its own size.  Primitives are built at add time; the
+// masks live in one device buffer.
+struct pxg_masks {
+  std::vector<pxg::Prim> prims;
+  std::vector<pxg::PathJob> jobs;
+  std::vector<long long> offs;  // byte offset of each mask
+  long long bytes = 0;
+  unsigned char* dev = nullptr;
+  long long dev_cap = 0;
+  bool rendered = false;
+  pxg::Prim* dprims = nullptr;  // device copy of prims
+  long long dcap = 0;
+  bool dirty = true;
+  GraphCacheHolder* graph = nullptr;
+  ~pxg_masks();
+};
+
+// A recorded sequence of fillPath/strokePath calls (primitives built on the
+// host at record time), painted in order by pxg_image_draw_scene.
+struct pxg_scene {
+  std::vector<pxg::Prim> prims;
+  std::vector<pxg::PathJob> jobs;
+  // device copy of prims, uploaded at the first draw after a change
+  mutable pxg::Prim* dprims = nullptr;
+  mutable long long dcap = 0;
+  mutable bool dirty = true;
+  ~pxg_scene() {
+    if (dprims) cudaFree(dprims);
+  }
+};
+
+// The serving engine: render jobs (a recorded scene painted onto a fresh
+// transparent canvas, then an optional blur) admitted against a device
+// memory budget and advanced together, a bounded chunk of each job's paths
+// per step (continuous batching: a job that arrives while others are on the
+// GPU joins the next step; one that finishes leaves and frees its memory).
+struct SrvJob {
+  int64_t id;
+  const pxg_scene* scene;
+  int64_t W, H;
+  int64_t blur;  // radius (0: none)
+  int state;     // 0 queued, 1 active, 2 done, 3 failed
+  int status;
+  size_t next;   // next path of the scene
+  long long bytes;
+  pxg_image canvas;
+  uint8_t* tmp;
+  double t_submit, t_admit, t_done;
+  std::string err;
+};
+struct pxg_server {
+  long long budget = 0, used = 0;
+  long long paths_per_job = 512;     // path chunk of one job in one step
+  long long paths_per_step = 16384;  // paths of all jobs in one step
+  int64_t next_id = 1;
+  std::deque<SrvJob*> queue;
+  std::vector<SrvJob*> active;
+  std::map<int64_t, SrvJob*> jobs;
+  std::vector<int64_t> finished;
+  long long steps = 0, peak_used = 0, peak_active = 0;
+  ~pxg_server();
+};
+
 namespace pxg {
 __global__ void k_setup(PathJob* jobs, Arena A, int maxBands);
-__global__ void k_rows(PathJob* jobs, int njobs, Arena A, const uint8_t* tbl, long long totalRows);
+const void* rows_kernel(int v);
+size_t rows_smem(int v);
+int rows_warps(int v);
+void launch_rows(int v, unsigned blocks, cudaStream_t st, PathJob* jobs, int njobs, const Arena& A,
+                 const uint8_t* tbl, long long items, int rpi);
 __global__ void k_rows_wide(PathJob* jobs, Arena A, const uint8_t* tbl);
 __global__ void k_xclears(PathJob* jobs, Arena A);
+__global__ void k_scene(PathJob* jobs, const SceneRun* runs, int nruns, long long totalRows, Arena A,
+                        const uint8_t* tbl, unsigned char* wide, long long wideSlots);
+size_t scene_wide_bytes();
+int scene_ctas_per_sm();
+int draw_masks_tiles();
+void launch_draw_masks(int tile, uint32_t* page, long long W, long long H, const void* items, int n,
+                       const uint8_t* masks, int mode, const uint8_t* tbl, cudaStream_t st);
 size_t rows_smem_fast();
 size_t rows_smem_wide();
 int rows_warps_fast();
@@ -108,6 +187,14 @@ struct Ctx {
   long long segband_cap = 0;
   Band* bands = nullptr;
   long long band_cap = 0;
+  int* bandseg = nullptr;
+  long long bandseg_cap = 0;
+  int* primcnt = nullptr;
+  long long primcnt_cap = 0;
+  MaskDraw* mdraw = nullptr;      // mask positions of pxg_image_draw_masks
+  long long mdraw_cap = 0;
+  unsigned char* wide = nullptr;  // per-warp wide row scratch of the scene kernel
+  long long wide_slots = 0;
   long long* ovf = nullptr;
   long long ovf_cap = 0;
   long long* xcl = nullptr;
@@ -121,8 +208,10 @@ struct Ctx {
   long long kern_cap = 0;
   unsigned char* scratch = nullptr;
   long long scratch_cap = 0;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evr0 = nullptr, evr1 = nullptr;
   float last_ms = 0;
+  long long stats[4] = {0, 0, 0, 0};  // last fill launch: paths, prims, segments, band entries
+  int rows_ctas_per_sm[2] = {1, 1};  // resident CTAs of each row-kernel variant
   bool blocking = true;  // image operations wait for their GPU work
   std::map<int64_t, uint16_t*> weights;  // gaussian weights per radius, on the device
 };
@@ -152,8 +241,14 @@ void init_locked(int device) {
   straight_alpha_table(t.data());
   CU(cudaMalloc(&g.tbl, 65536));
   CU(cudaMemcpy(g.tbl, t.data(), 65536, cudaMemcpyHostToDevice));
-  CU(cudaFuncSetAttribute(k_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem_fast()));
+  for (int v = 0; v < 2; v++) {
+    CU(cudaFuncSetAttribute(rows_kernel(v), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem(v)));
+    int per = 0;
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, rows_kernel(v), rows_warps(v) * 32, rows_smem(v)));
+    g.rows_ctas_per_sm[v] = std::max(1, per);
+  }
   CU(cudaFuncSetAttribute(k_rows_wide, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem_wide()));
+  CU(cudaFuncSetAttribute(k_scene, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem_fast()));
   g.setupSmemMax = allow_max_smem((const void*)k_setup);
   g.blurSmemMax = std::min(allow_max_smem((const void*)k_blur_x), allow_max_smem((const void*)k_blur_y));
   g.blurSmemMax = std::min(g.blurSmemMax, allow_max_smem((const void*)k_blurf_x));
@@ -162,6 +257,8 @@ void init_locked(int device) {
   g.blurSmemMax = std::min(g.blurSmemMax, allow_max_smem(blurb_kernel(false)));
   CU(cudaEventCreate(&g.ev0));
   CU(cudaEventCreate(&g.ev1));
+  CU(cudaEventCreate(&g.evr0));
+  CU(cudaEventCreate(&g.evr1));
   g.ready = true;
 }
 void ensure_init() {
@@ -214,84 +311,250 @@ const char* status_message(int st) {
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+// Nim's round(v).int: half away from zero; out of range -> INT64_MIN
+int64_t nim_round_int(float v) {
+  float r = roundf(v);
+  if (!(r >= -9223372036854775808.0f && r < 9223372036854775808.0f)) return INT64_MIN;
+  return (int64_t)r;
+}
+
+// Lanes per curve in the setup kernel's flattening: the 256 threads of a job's
+// CTA shared out over its curves (a power of two, 1..32).
+int curve_group(const std::vector<Prim>& prims, long long off, int n) {
+  long long curves = 0;
+  for (int i = 0; i < n; i++) curves += prims[(size_t)(off + i)].kind != kPrimLine;
+  int gsz = 1;
+  while (gsz < 32 && curves * gsz * 2 <= 256) gsz *= 2;
+  return gsz;
+}
+
+// Workspace of the fill kernels, grown on demand (never shrunk).
+void ensure_arena(long long seg_need, long long list_need, long long nbands, long long nprims, long long rows) {
+  dev_grow(g.segs, g.seg_cap, seg_need);
+  dev_grow(g.segw, g.segw_cap, g.seg_cap);
+  dev_grow(g.segband, g.segband_cap, g.seg_cap);
+  dev_grow(g.bands, g.band_cap, nbands);
+  dev_grow(g.bandseg, g.bandseg_cap, list_need);
+  dev_grow(g.primcnt, g.primcnt_cap, nprims + 1);
+  dev_grow(g.ovf, g.ovf_cap, rows);
+  dev_grow(g.xcl, g.xcl_cap, 3 * (2 * rows + 1024));
+}
+
+// One host->device copy of jobs | counters | extra | prims through the pinned
+// upload area.
+struct Staged {
+  PathJob* dj;
+  unsigned char* extra;
+  size_t jobsBytes, ctrBytes, extraBytes, upBytes;
+  Arena A;
+};
+Staged stage(const std::vector<PathJob>& run, const void* extra, size_t extraBytes,
+             const std::vector<Prim>& prims, bool copy = true) {
+  Staged S;
+  const size_t nr = run.size();
+  S.jobsBytes = align_up(sizeof(PathJob) * std::max<size_t>(nr, 1), 256);
+  S.ctrBytes = 256;
+  S.extraBytes = align_up(extraBytes, 256);
+  const size_t primBytes = sizeof(Prim) * std::max<size_t>(prims.size(), 1);
+  const size_t need = S.jobsBytes + S.ctrBytes + S.extraBytes + primBytes;
+  if (need > g.up_cap) {
+    CU(cudaStreamSynchronize(g.stream));  // the old area may still be in flight
+    if (g.d_up) cudaFree(g.d_up);
+    if (g.h_up) cudaFreeHost(g.h_up);
+    g.d_up = nullptr;
+    g.h_up = nullptr;
+    size_t cap = std::max(need, g.up_cap * 2);
+    CU(cudaMalloc(&g.d_up, cap));
+    CU(cudaMallocHost(&g.h_up, cap));
+    g.up_cap = cap;
+  }
+  if (nr) memcpy(g.h_up, run.data(), sizeof(PathJob) * nr);
+  {  // jobs without resident primitives read the staged ones
+    const size_t primAt0 = S.jobsBytes + S.ctrBytes + S.extraBytes;
+    PathJob* hj = reinterpret_cast<PathJob*>(g.h_up);
+    for (size_t i = 0; i < nr; i++)
+      if (!hj[i].prims) hj[i].prims = reinterpret_cast<const Prim*>(g.d_up + primAt0);
+  }
+  unsigned long long* hc = reinterpret_cast<unsigned long long*>(g.h_up + S.jobsBytes);
+  memset(hc, 0, S.ctrBytes);
+  hc[kCtrRowErr] = ~0ull;
+  if (extraBytes) memcpy(g.h_up + S.jobsBytes + S.ctrBytes, extra, extraBytes);
+  const size_t primAt = S.jobsBytes + S.ctrBytes + S.extraBytes;
+  if (!prims.empty()) memcpy(g.h_up + primAt, prims.data(), sizeof(Prim) * prims.size());
+  S.upBytes = need;
+  if (copy) CU(cudaMemcpyAsync(g.d_up, g.h_up, need, cudaMemcpyHostToDevice, g.stream));
+  S.dj = reinterpret_cast<PathJob*>(g.d_up);
+  S.extra = g.d_up + S.jobsBytes + S.ctrBytes;
+  Arena& A = S.A;
+  A.prims = reinterpret_cast<const Prim*>(g.d_up + primAt);
+  A.segs = g.segs;
+  A.segw = g.segw;
+  A.seg_cap = g.seg_cap;
+  A.segband = g.segband;
+  A.bands = g.bands;
+  A.band_cap = g.band_cap;
+  A.bandseg = g.bandseg;
+  A.bandseg_cap = g.bandseg_cap;
+  A.primcnt = g.primcnt;
+  A.primcnt_cap = g.primcnt_cap;
+  A.counters = reinterpret_cast<unsigned long long*>(g.d_up + S.jobsBytes);
+  A.ovf_rows = g.ovf;
+  A.ovf_cap = g.ovf_cap;
+  A.xclears = g.xcl;
+  A.xclear_cap = g.xcl_cap / 3;
+  return S;
+}
+
+void note_stats(long long paths, long long prims, const unsigned long long* ctr) {
+  g.stats[0] = paths;
+  g.stats[1] = prims;
+  g.stats[2] = (long long)ctr[kCtrSegs];
+  g.stats[3] = (long long)ctr[kCtrBandSegs];
+}
+
+int setup_max_bands(long long maxH) {
+  const int maxBands = (int)(std::max<long long>(1, maxH / 4) + 1);
+  if ((size_t)maxBands * 8 > g.setupSmemMax) throw ApiError{"Image too tall for the fill kernels"};
+  return maxBands;
+}
+
+// Grows the workspace after a launch in which some job ran out of it.
+void grow_needs(const unsigned long long* ctr, long long& seg_need, long long& list_need) {
+  seg_need = std::max<long long>(seg_need, (long long)ctr[kCtrSegs] * 2);
+  list_need = std::max<long long>(list_need, (long long)ctr[kCtrBandSegs] * 2);
+  if ((long long)ctr[kCtrSegs] <= g.seg_cap && (long long)ctr[kCtrBandSegs] <= g.bandseg_cap) {
+    seg_need *= 2;
+    list_need *= 2;
+  }
+}
+
 // Runs fill jobs whose primitives are already in `prims` (job.prim_off set).
 // Jobs must target distinct images: a job whose workspace ran out is rerun
 // alone, after the others were drawn.  Returns per-job status.
-void run_jobs(std::vector<PathJob>& jobs, const std::vector<Prim>& prims, std::vector<int>& status) {
+// Row-kernel configuration of a fill launch: scratch variant and rows per
+// work item.
+struct RowsCfg {
+  int variant = 0;
+  int rpi = 1;
+};
+
+// A captured launch sequence (upload, setup, rows, status read-back), replayed
+// while the launch's shape and buffers are unchanged.
+struct GraphCache {
+  cudaGraphExec_t exec = nullptr;
+  std::vector<long long> key;
+  void reset() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+    key.clear();
+  }
+};
+
+struct RunOpts {
+  RowsCfg cfg;
+  unsigned char* zero = nullptr;  // buffer cleared before the first launch (mask batches)
+  long long zero_bytes = 0;
+  GraphCache* graph = nullptr;    // capture / replay the first launch
+  float* rows_ms = nullptr;       // row-kernel time of the first launch (autotuning)
+  const Prim* dprims = nullptr;   // primitives already on the device (else staged)
+};
+
+// Runs fill jobs whose primitives are already in `prims` (job.prim_off set).
+// Jobs must target distinct images: a job whose workspace ran out is rerun
+// alone, after the others were drawn.  Returns per-job status.
+void run_jobs(std::vector<PathJob>& jobs, const std::vector<Prim>& prims, std::vector<int>& status,
+              const RunOpts& opts = RunOpts()) {
+  const RowsCfg cfg = opts.cfg;
   const int nj = (int)jobs.size();
   status.assign((size_t)nj, kOk);
   std::vector<int> todo(nj);
   for (int i = 0; i < nj; i++) todo[i] = i;
   long long seg_need = std::max<long long>(1 << 16, (long long)prims.size() * 8);
+  long long list_need = seg_need * 4;
   for (int attempt = 0; attempt < 12 && !todo.empty(); attempt++) {
     std::vector<PathJob> run;
     long long rows = 0, maxH = 1;
+    long long items = 0;
     for (int i : todo) {
       PathJob j = jobs[i];
-      j.row_off = rows;
+      if (j.group == 0) j.group = curve_group(prims, j.prim_off, j.nprims);
+      j.pc_off = j.prim_off;
+      if (!opts.dprims) j.prims = nullptr;  // the staged copy
+      else j.prims = opts.dprims;
+      j.row_off = items;
+      items += (j.H + cfg.rpi - 1) / cfg.rpi;
       rows += j.H;
       maxH = std::max<long long>(maxH, j.H);
       j.status = kOk;
       run.push_back(j);
     }
     const int nr = (int)run.size();
-    const int maxBands = (int)(std::max<long long>(1, maxH / 4) + 1);
-    const size_t setupSmem = (size_t)maxBands * 8;
-    if (setupSmem > g.setupSmemMax) throw ApiError{"Image too tall for the fill kernels"};
-
-    dev_grow(g.segs, g.seg_cap, seg_need);
-    dev_grow(g.segw, g.segw_cap, g.seg_cap);
-    dev_grow(g.segband, g.segband_cap, g.seg_cap);
-    dev_grow(g.bands, g.band_cap, (long long)nr * maxBands);
-    dev_grow(g.ovf, g.ovf_cap, rows);
-    dev_grow(g.xcl, g.xcl_cap, 3 * (2 * rows + 1024));
-
-    const size_t jobsBytes = align_up(sizeof(PathJob) * nr, 256);
-    const size_t ctrBytes = 256;
-    const size_t primBytes = sizeof(Prim) * std::max<size_t>(prims.size(), 1);
-    const size_t need = jobsBytes + ctrBytes + primBytes;
-    if (need > g.up_cap) {
-      if (g.d_up) cudaFree(g.d_up);
-      if (g.h_up) cudaFreeHost(g.h_up);
-      g.d_up = nullptr;
-      g.h_up = nullptr;
-      size_t cap = std::max(need, g.up_cap * 2);
-      CU(cudaMalloc(&g.d_up, cap));
-      CU(cudaMallocHost(&g.h_up, cap));
-      g.up_cap = cap;
-    }
-    memcpy(g.h_up, run.data(), sizeof(PathJob) * nr);
-    memset(g.h_up + jobsBytes, 0, ctrBytes);
-    if (!prims.empty()) memcpy(g.h_up + jobsBytes + ctrBytes, prims.data(), sizeof(Prim) * prims.size());
-    CU(cudaMemcpyAsync(g.d_up, g.h_up, need, cudaMemcpyHostToDevice, g.stream));
-
-    PathJob* dj = reinterpret_cast<PathJob*>(g.d_up);
-    Arena A;
-    A.prims = reinterpret_cast<const Prim*>(g.d_up + jobsBytes + ctrBytes);
-    A.segs = g.segs;
-    A.segw = g.segw;
-    A.seg_cap = g.seg_cap;
-    A.segband = g.segband;
-    A.bands = g.bands;
-    A.band_cap = g.band_cap;
-    A.counters = reinterpret_cast<unsigned long long*>(g.d_up + jobsBytes);
-    A.ovf_rows = g.ovf;
-    A.ovf_cap = g.ovf_cap;
-    A.xclears = g.xcl;
-    A.xclear_cap = g.xcl_cap / 3;
-
-    k_setup<<<nr, 256, setupSmem, g.stream>>>(dj, A, maxBands); note_launch();
-    CU(cudaGetLastError());
-    const int wpb = rows_warps_fast();
-    long long blocks = (rows + wpb - 1) / wpb;
-    blocks = std::min<long long>(blocks, (long long)g.nsm * 16);
+    const int maxBands = setup_max_bands(maxH);
+    ensure_arena(seg_need, list_need, (long long)nr * maxBands, (long long)prims.size(), rows);
+    const bool graphed = opts.graph && attempt == 0 && g.stream != nullptr;
+    Staged S = stage(run, nullptr, 0, opts.dprims ? std::vector<Prim>() : prims, false);
+    Arena& A = S.A;
+    PathJob* dj = S.dj;
+    const int v = cfg.variant;
+    long long blocks = (items + rows_warps(v) - 1) / rows_warps(v);
+    blocks = std::min<long long>(blocks, (long long)g.nsm * g.rows_ctas_per_sm[v]);
     blocks = std::max<long long>(blocks, 1);
-    k_rows<<<(unsigned)blocks, wpb * 32, rows_smem_fast(), g.stream>>>(dj, nr, A, g.tbl, rows); note_launch();
-    CU(cudaGetLastError());
-    CU(cudaMemcpyAsync(g.h_up, g.d_up, jobsBytes + ctrBytes, cudaMemcpyDeviceToHost, g.stream));
+    const bool timeRows = opts.rows_ms && attempt == 0 && !graphed;
+    auto issue = [&](bool count) {
+      if (attempt == 0 && opts.zero) CU(cudaMemsetAsync(opts.zero, 0, (size_t)opts.zero_bytes, g.stream));
+      CU(cudaMemcpyAsync(g.d_up, g.h_up, S.upBytes, cudaMemcpyHostToDevice, g.stream));
+      k_setup<<<nr, 256, (size_t)maxBands * 8, g.stream>>>(dj, A, maxBands);
+      if (count) note_launch();
+      CU(cudaGetLastError());
+      if (timeRows) CU(cudaEventRecord(g.evr0, g.stream));
+      launch_rows(v, (unsigned)blocks, g.stream, dj, nr, A, g.tbl, items, cfg.rpi);
+      if (count) note_launch();
+      CU(cudaGetLastError());
+      if (timeRows) CU(cudaEventRecord(g.evr1, g.stream));
+      CU(cudaMemcpyAsync(g.h_up, g.d_up, S.jobsBytes + S.ctrBytes, cudaMemcpyDeviceToHost, g.stream));
+    };
+    if (graphed) {
+      std::vector<long long> key = {nr, items, (long long)S.upBytes, (long long)(uintptr_t)g.d_up,
+                                    (long long)(uintptr_t)g.h_up, (long long)(uintptr_t)g.segs, g.seg_cap,
+                                    (long long)(uintptr_t)g.bandseg, g.bandseg_cap,
+                                    (long long)(uintptr_t)g.bands, g.band_cap, (long long)(uintptr_t)g.primcnt,
+                                    g.primcnt_cap, (long long)(uintptr_t)g.ovf, g.ovf_cap,
+                                    (long long)(uintptr_t)g.xcl, g.xcl_cap, v, cfg.rpi, blocks, maxBands,
+                                    (long long)(uintptr_t)opts.zero, opts.zero_bytes,
+                                    (long long)(uintptr_t)g.stream, (long long)(uintptr_t)opts.dprims};
+      GraphCache& gc = *opts.graph;
+      if (!gc.exec || gc.key != key) {
+        gc.reset();
+        CU(cudaStreamBeginCapture(g.stream, cudaStreamCaptureModeThreadLocal));
+        try {
+          issue(false);
+        } catch (...) {
+          cudaGraph_t gr = nullptr;
+          cudaStreamEndCapture(g.stream, &gr);
+          if (gr) cudaGraphDestroy(gr);
+          throw;
+        }
+        cudaGraph_t gr = nullptr;
+        CU(cudaStreamEndCapture(g.stream, &gr));
+        cudaError_t e = cudaGraphInstantiate(&gc.exec, gr, 0);
+        cudaGraphDestroy(gr);
+        if (e != cudaSuccess) {
+          gc.exec = nullptr;
+          CU(e);
+        }
+        gc.key = key;
+      }
+      CU(cudaGraphLaunch(gc.exec, g.stream));
+      note_launch();
+      note_launch();
+    } else {
+      issue(true);
+    }
     CU(cudaStreamSynchronize(g.stream));
+    if (timeRows) CU(cudaEventElapsedTime(opts.rows_ms, g.evr0, g.evr1));
     unsigned long long ctr[kNumCounters];
-    memcpy(ctr, g.h_up + jobsBytes, sizeof ctr);
+    memcpy(ctr, g.h_up + S.jobsBytes, sizeof ctr);
+    note_stats(nr, (long long)prims.size(), ctr);
     if (ctr[kCtrOvfRows] > 0 || ctr[kCtrXClears] > 0) {
       if ((long long)ctr[kCtrXClears] > A.xclear_cap) throw ApiError{"Out of workspace memory (cross-row clears)"};
       if (ctr[kCtrOvfRows] > 0) {
@@ -304,7 +567,7 @@ void run_jobs(std::vector<PathJob>& jobs, const std::vector<Prim>& prims, std::v
         k_xclears<<<(unsigned)b, 256, 0, g.stream>>>(dj, A); note_launch();
         CU(cudaGetLastError());
       }
-      CU(cudaMemcpyAsync(g.h_up, g.d_up, jobsBytes, cudaMemcpyDeviceToHost, g.stream));
+      CU(cudaMemcpyAsync(g.h_up, g.d_up, S.jobsBytes, cudaMemcpyDeviceToHost, g.stream));
       CU(cudaStreamSynchronize(g.stream));
     }
     const PathJob* out = reinterpret_cast<const PathJob*>(g.h_up);
@@ -321,12 +584,125 @@ void run_jobs(std::vector<PathJob>& jobs, const std::vector<Prim>& prims, std::v
         status[(size_t)i] = st == kNothing ? kOk : st;
       }
     }
-    if (grow) {
-      seg_need = std::max<long long>(seg_need * 4, (long long)ctr[kCtrSegs] * 2);
-    }
+    if (grow) grow_needs(ctr, seg_need, list_need);
     todo = again;
   }
   for (int i : todo) status[(size_t)i] = kErrArenaFull;
+}
+
+// A run of paths painted in order onto one canvas (a scene, or one serving
+// job's chunk of paths).
+struct HostRun {
+  pxg_image* canvas;
+  std::vector<PathJob>* jobs;  // the run's paths, in order; img/W/H are set here
+  const std::vector<Prim>* prims;  // host primitives (jobs' prim_off index them)
+  const Prim* dprims;              // the same primitives on the device
+  size_t j0, j1;               // paths still to paint
+  int status;                  // first failure (kOk when every path was painted)
+};
+
+// The scene's primitives on the device, uploaded once after each change.
+const Prim* scene_device_prims(const pxg_scene* sc) {
+  if (sc->dirty) {
+    dev_grow(sc->dprims, sc->dcap, std::max<long long>((long long)sc->prims.size(), 1));
+    if (!sc->prims.empty())
+      CU(cudaMemcpy(sc->dprims, sc->prims.data(), sizeof(Prim) * sc->prims.size(), cudaMemcpyHostToDevice));
+    sc->dirty = false;
+  }
+  return sc->dprims;
+}
+
+// Paints several runs (distinct canvases) in one setup + scene launch pair,
+// repeating for runs whose workspace ran out.  MaskBlend paths must not be
+// inside a run (their clears reach outside the rows the run owns).
+void run_scene_runs(std::vector<HostRun>& runs) {
+  long long prim_total = 0;
+  for (auto& r : runs) prim_total += (long long)r.prims->size();
+  long long seg_need = std::max<long long>(1 << 16, prim_total * 8);
+  long long list_need = seg_need * 4;
+  for (auto& r : runs) r.status = kOk;
+  for (int attempt = 0; attempt < 12; attempt++) {
+    std::vector<PathJob> dev;
+    long long pc = 0;
+    std::vector<SceneRun> sr;
+    std::vector<size_t> which;  // launch run -> runs index
+    long long rows = 0, maxH = 1;
+    for (size_t ri = 0; ri < runs.size(); ri++) {
+      HostRun& r = runs[ri];
+      if (r.status != kOk || r.j0 >= r.j1) continue;
+      SceneRun s;
+      s.row_off = rows;
+      s.H = r.canvas->height;
+      s.j0 = (int)dev.size();
+      for (size_t j = r.j0; j < r.j1; j++) {
+        PathJob pj = (*r.jobs)[j];
+        if (pj.group == 0) pj.group = curve_group(*r.prims, pj.prim_off, pj.nprims);
+        pj.prims = r.dprims;
+        pj.pc_off = pc;
+        pc += pj.nprims;
+        pj.img = r.canvas->data;
+        pj.W = r.canvas->width;
+        pj.H = r.canvas->height;
+        pj.status = kOk;
+        dev.push_back(pj);
+      }
+      s.j1 = (int)dev.size();
+      rows += s.H;
+      maxH = std::max<long long>(maxH, s.H);
+      sr.push_back(s);
+      which.push_back(ri);
+    }
+    if (sr.empty()) return;
+    const int nj = (int)dev.size();
+    const int maxBands = setup_max_bands(maxH);
+    ensure_arena(seg_need, list_need, (long long)nj * maxBands, pc, 1);
+    const int wpb = rows_warps_fast();
+    long long blocks = std::min<long long>((rows + wpb - 1) / wpb, (long long)g.nsm * scene_ctas_per_sm());
+    blocks = std::max<long long>(blocks, 1);
+    const long long slots = blocks * wpb;
+    if (slots > g.wide_slots) {
+      if (g.wide) cudaFree(g.wide);
+      g.wide = nullptr;
+      g.wide_slots = 0;
+      CU(cudaMalloc(&g.wide, (size_t)slots * scene_wide_bytes()));
+      g.wide_slots = slots;
+    }
+    Staged S = stage(dev, sr.data(), sizeof(SceneRun) * sr.size(), std::vector<Prim>());
+    if (nj > 0) {
+      k_setup<<<nj, 256, (size_t)maxBands * 8, g.stream>>>(S.dj, S.A, maxBands); note_launch();
+      CU(cudaGetLastError());
+    }
+    k_scene<<<(unsigned)blocks, wpb * 32, rows_smem_fast(), g.stream>>>(
+        S.dj, reinterpret_cast<const SceneRun*>(S.extra), (int)sr.size(), rows, S.A, g.tbl, g.wide, g.wide_slots);
+    note_launch();
+    CU(cudaGetLastError());
+    CU(cudaMemcpyAsync(g.h_up, g.d_up, S.jobsBytes + S.ctrBytes, cudaMemcpyDeviceToHost, g.stream));
+    CU(cudaStreamSynchronize(g.stream));
+    unsigned long long ctr[kNumCounters];
+    memcpy(ctr, g.h_up + S.jobsBytes, sizeof ctr);
+    note_stats(nj, pc, ctr);
+    const PathJob* out = reinterpret_cast<const PathJob*>(g.h_up);
+    bool grow = false;
+    for (size_t k = 0; k < sr.size(); k++) {
+      HostRun& r = runs[which[k]];
+      size_t done = r.j1;
+      for (int j = sr[k].j0; j < sr[k].j1; j++) {
+        const int st = out[j].status;
+        if (st == kOk || st == kNothing) continue;
+        done = r.j0 + (size_t)(j - sr[k].j0);
+        if (st == kErrArenaFull) grow = true;
+        else r.status = st;
+        break;
+      }
+      if (ctr[kCtrRowErr] != ~0ull && (int)ctr[kCtrRowErr] >= sr[k].j0 && (int)ctr[kCtrRowErr] < sr[k].j1)
+        r.status = kErrRowTooComplex;
+      r.j0 = r.status == kOk ? done : r.j1;
+    }
+    if (!grow) return;
+    grow_needs(ctr, seg_need, list_need);
+  }
+  for (auto& r : runs)
+    if (r.status == kOk && r.j0 < r.j1) r.status = kErrArenaFull;
 }
 
 PathJob make_job(pxg_image* img, uint32_t rgbx, int blend, const float* mat, float ps, int winding) {
@@ -338,9 +714,11 @@ PathJob make_job(pxg_image* img, uint32_t rgbx, int blend, const float* mat, flo
   j.mode = blend;
   j.rgbx = rgbx;
   memcpy(j.mat, mat, sizeof j.mat);
-  j.img = img->data;
-  j.W = img->width;
-  j.H = img->height;
+  if (img) {
+    j.img = img->data;
+    j.W = img->width;
+    j.H = img->height;
+  }
   return j;
 }
 
@@ -361,6 +739,22 @@ bool paint_color(const float* color, float& opacity, int blend, uint32_t& rgbx) 
   float c[4] = {color[0], color[1], color[2], color[3] * opacity};
   rgbx = color_to_rgbx(c);
   return true;
+}
+
+// Host-only work (recording geometry): no device needed.
+template <class F>
+int guarded_host(F&& f) {
+  try {
+    f();
+    return 0;
+  } catch (const ApiError& e) {
+    set_err(e.msg);
+  } catch (const GeomError& e) {
+    set_err(e.msg);
+  } catch (const std::exception& e) {
+    set_err(e.what());
+  }
+  return 1;
 }
 
 template <class F>
@@ -390,6 +784,295 @@ void run_single(pxg_image* img, std::vector<Prim>& prims, uint32_t rgbx, int ble
   run_jobs(jobs, prims, st);
   t.done();
   if (st[0] != kOk) throw ApiError{status_message(st[0])};
+}
+
+// ---------------------------------------------------------------------------
+// Serving engine
+// ---------------------------------------------------------------------------
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+void srv_release(pxg_server* sv, SrvJob* j) {
+  if (j->canvas.data) cudaFree(j->canvas.data);
+  if (j->tmp) cudaFree(j->tmp);
+  j->canvas.data = nullptr;
+  j->tmp = nullptr;
+  sv->used -= j->bytes;
+  j->bytes = 0;
+}
+
+// Admits queued jobs in arrival order while their canvases fit the budget.
+void srv_admit(pxg_server* sv) {
+  while (!sv->queue.empty()) {
+    SrvJob* j = sv->queue.front();
+    const long long need = j->W * j->H * 4 * (j->blur > 0 ? 2 : 1);
+    if (sv->used + need > sv->budget) break;
+    sv->queue.pop_front();
+    CU(cudaMalloc((void**)&j->canvas.data, (size_t)(j->W * j->H * 4)));
+    j->canvas.width = j->W;
+    j->canvas.height = j->H;
+    j->canvas.owned = 1;
+    if (j->blur > 0) CU(cudaMalloc((void**)&j->tmp, (size_t)(j->W * j->H * 4)));
+    CU(cudaMemsetAsync(j->canvas.data, 0, (size_t)(j->W * j->H * 4), g.stream));
+    j->bytes = need;
+    sv->used += need;
+    sv->peak_used = std::max(sv->peak_used, sv->used);
+    j->state = 1;
+    j->t_admit = now_s();
+    sv->active.push_back(j);
+  }
+  sv->peak_active = std::max<long long>(sv->peak_active, (long long)sv->active.size());
+}
+
+void srv_finish(pxg_server* sv, SrvJob* j, int status, const std::string& err) {
+  j->status = status;
+  j->err = err;
+  j->state = status == kOk ? 2 : 3;
+  j->t_done = now_s();
+  sv->finished.push_back(j->id);
+}
+
+// One step: every active job's next chunk of paths in one setup + scene
+// launch pair; MaskBlend paths run alone; finished jobs get their blur.
+void srv_step(pxg_server* sv) {
+  srv_admit(sv);
+  if (sv->active.empty()) return;
+  std::vector<HostRun> runs;
+  std::vector<SrvJob*> owners;
+  std::vector<std::vector<PathJob>*> jobvecs;
+  long long budget = sv->paths_per_step;
+  for (SrvJob* j : sv->active) {
+    if (budget <= 0) break;
+    const auto& pj = j->scene->jobs;
+    if (j->next < pj.size() && pj[j->next].mode == kMask) {
+      // a MaskBlend path: drawn alone
+      PathJob one = pj[j->next];
+      std::vector<Prim> sub(j->scene->prims.begin() + one.prim_off,
+                            j->scene->prims.begin() + one.prim_off + one.nprims);
+      one.prim_off = 0;
+      one.img = j->canvas.data;
+      one.W = j->W;
+      one.H = j->H;
+      std::vector<PathJob> v(1, one);
+      std::vector<int> st;
+      run_jobs(v, sub, st);
+      if (st[0] != kOk) {
+        srv_finish(sv, j, st[0], status_message(st[0]));
+        continue;
+      }
+      j->next++;
+      budget--;
+      continue;
+    }
+    size_t e = j->next;
+    const size_t lim = (size_t)std::min<long long>(sv->paths_per_job, budget);
+    while (e < pj.size() && e - j->next < lim && pj[e].mode != kMask) e++;
+    if (e == j->next) continue;
+    runs.push_back(HostRun{&j->canvas, const_cast<std::vector<PathJob>*>(&pj), &j->scene->prims,
+                           scene_device_prims(j->scene), j->next, e, kOk});
+    owners.push_back(j);
+    budget -= (long long)(e - j->next);
+  }
+  if (!runs.empty()) {
+    std::vector<size_t> ends;
+    for (auto& r : runs) ends.push_back(r.j1);
+    run_scene_runs(runs);
+    for (size_t k = 0; k < runs.size(); k++) {
+      SrvJob* j = owners[k];
+      if (j->state != 1) continue;
+      if (runs[k].status != kOk) srv_finish(sv, j, runs[k].status, status_message(runs[k].status));
+      else j->next = ends[k];
+    }
+  }
+  // jobs whose paths are all painted: blur, then done
+  std::vector<SrvJob*> still;
+  std::vector<SrvJob*> done;
+  for (SrvJob* j : sv->active) {
+    if (j->state != 1) {
+      srv_release(sv, j);
+      continue;
+    }
+    if (j->next >= j->scene->jobs.size()) {
+      if (j->blur > 0) {
+        const uint16_t* kern = weights_for(j->blur);
+        launch_blur((uint32_t*)j->canvas.data, (uint32_t*)j->tmp, j->W, j->H, (int)j->blur, kern, 0u, g.nsm,
+                    g.blurSmemMax, g.stream);
+        CU(cudaGetLastError());
+      }
+      done.push_back(j);
+    } else {
+      still.push_back(j);
+    }
+  }
+  if (!done.empty()) CU(cudaStreamSynchronize(g.stream));
+  for (SrvJob* j : done) {
+    srv_finish(sv, j, kOk, "");
+    if (j->tmp) {
+      cudaFree(j->tmp);
+      j->tmp = nullptr;
+      const long long half = j->W * j->H * 4;
+      sv->used -= half;
+      j->bytes -= half;
+    }
+  }
+  sv->active = still;
+  sv->steps++;
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner: per operation and shape class, the fastest of a few launch
+// configurations, found by timing each once the first time the class is
+// seen.  Every configuration computes the same bytes; only speed differs.
+// ---------------------------------------------------------------------------
+enum TuneOp { kTuneMaskRows = 0, kTuneMaskDraw = 1 };
+const RowsCfg kMaskRowsCands[] = {{0, 1}, {1, 1}, {1, 2}, {1, 4}};
+constexpr int kNumMaskRowsCands = 4;
+
+struct Tuner {
+  bool on = true;
+  std::map<std::pair<int, long long>, int> best;
+  std::map<std::pair<int, long long>, std::vector<float>> ms;
+};
+Tuner g_tune;
+
+int size_bucket(long long v) {  // 0: <=32, 1: <=64, ... 6: >1024
+  int b = 0;
+  long long lim = 32;
+  while (b < 6 && v > lim) {
+    lim *= 2;
+    b++;
+  }
+  return b;
+}
+int count_bucket(long long n) {
+  int b = 0;
+  while (b < 20 && (1LL << b) < n) b++;
+  return b;
+}
+long long mask_class(const pxg_masks* m) {
+  long long side = 1;
+  for (const PathJob& j : m->jobs) side = std::max<long long>(side, std::max<long long>(j.W, j.H));
+  return size_bucket(side) * 32 + count_bucket((long long)m->jobs.size());
+}
+
+}  // namespace
+
+struct GraphCacheHolder {
+  GraphCache gc;
+};
+pxg_server::~pxg_server() {
+  for (auto& kv : jobs) {
+    SrvJob* j = kv.second;
+    if (j->canvas.data) cudaFree(j->canvas.data);
+    if (j->tmp) cudaFree(j->tmp);
+    delete j;
+  }
+}
+pxg_masks::~pxg_masks() {
+  if (graph) {
+    graph->gc.reset();
+    delete graph;
+  }
+  if (dev) cudaFree(dev);
+  if (dprims) cudaFree(dprims);
+}
+
+namespace {
+
+const Prim* masks_device_prims(pxg_masks* m) {
+  if (m->dirty) {
+    dev_grow(m->dprims, m->dcap, std::max<long long>((long long)m->prims.size(), 1));
+    if (!m->prims.empty())
+      CU(cudaMemcpy(m->dprims, m->prims.data(), sizeof(Prim) * m->prims.size(), cudaMemcpyHostToDevice));
+    m->dirty = false;
+  }
+  return m->dprims;
+}
+
+void render_masks(pxg_masks* m) {
+  if (m->jobs.empty()) return;
+  dev_grow(m->dev, m->dev_cap, std::max<long long>(m->bytes, 16));
+  std::vector<PathJob> jobs = m->jobs;
+  for (size_t i = 0; i < jobs.size(); i++) jobs[i].img = m->dev + m->offs[i];
+  if (!m->graph) m->graph = new GraphCacheHolder();
+  const std::pair<int, long long> key{kTuneMaskRows, mask_class(m)};
+  auto it = g_tune.best.find(key);
+  std::vector<int> st;
+  if (g_tune.on && it == g_tune.best.end()) {
+    std::vector<float> t(kNumMaskRowsCands, 0.0f);
+    int best = 0;
+    for (int c = 0; c < kNumMaskRowsCands; c++) {
+      std::vector<PathJob> jc = jobs;
+      RunOpts o;
+      o.cfg = kMaskRowsCands[c];
+      o.zero = m->dev;
+      o.zero_bytes = m->bytes;
+      o.rows_ms = &t[(size_t)c];
+      o.dprims = masks_device_prims(m);
+      run_jobs(jc, m->prims, st, o);
+      if (t[(size_t)c] < t[(size_t)best]) best = c;
+    }
+    g_tune.best[key] = best;
+    g_tune.ms[key] = t;
+  } else {
+    RunOpts o;
+    o.cfg = kMaskRowsCands[it == g_tune.best.end() ? 1 : it->second];
+    o.zero = m->dev;
+    o.zero_bytes = m->bytes;
+    o.graph = &m->graph->gc;
+    o.dprims = masks_device_prims(m);
+    run_jobs(jobs, m->prims, st, o);
+  }
+  for (size_t i = 0; i < st.size(); i++)
+    if (st[i] != kOk) throw ApiError{status_message(st[i])};
+  m->rendered = true;
+}
+
+void draw_masks(pxg_image* page, const pxg_masks* m, const int64_t* xy, int blend) {
+  const int n = (int)m->jobs.size();
+  if (n == 0) return;
+  std::vector<MaskDraw> items((size_t)n);
+  for (int i = 0; i < n; i++) {
+    items[(size_t)i].off = m->offs[(size_t)i];
+    items[(size_t)i].x = xy[2 * i];
+    items[(size_t)i].y = xy[2 * i + 1];
+    items[(size_t)i].w = (int)m->jobs[(size_t)i].W;
+    items[(size_t)i].h = (int)m->jobs[(size_t)i].H;
+  }
+  // a pageable copy: the host vector may go away as soon as the call returns
+  dev_grow(g.mdraw, g.mdraw_cap, (long long)n);
+  CU(cudaMemcpyAsync(g.mdraw, items.data(), sizeof(MaskDraw) * (size_t)n, cudaMemcpyHostToDevice, g.stream));
+  struct {
+    const void* extra;
+  } S{g.mdraw};
+  const long long pxBytes = page->width * page->height * 4;
+  const std::pair<int, long long> key{kTuneMaskDraw, size_bucket(std::max(page->width, page->height)) * 32 +
+                                                        count_bucket(n)};
+  auto it = g_tune.best.find(key);
+  int tile = 2;
+  if (g_tune.on && it == g_tune.best.end()) {
+    // time every tile shape on a copy of the page, then draw with the fastest
+    unsigned char* tmp = (unsigned char*)scratch(pxBytes);
+    std::vector<float> t((size_t)draw_masks_tiles(), 0.0f);
+    for (int c = 0; c < draw_masks_tiles(); c++) {
+      CU(cudaMemcpyAsync(tmp, page->data, (size_t)pxBytes, cudaMemcpyDeviceToDevice, g.stream));
+      CU(cudaEventRecord(g.evr0, g.stream));
+      launch_draw_masks(c, (uint32_t*)tmp, page->width, page->height, S.extra, n, m->dev, blend, g.tbl, g.stream);
+      CU(cudaGetLastError());
+      CU(cudaEventRecord(g.evr1, g.stream));
+      CU(cudaEventSynchronize(g.evr1));
+      CU(cudaEventElapsedTime(&t[(size_t)c], g.evr0, g.evr1));
+      if (t[(size_t)c] < t[(size_t)tile]) tile = c;
+    }
+    g_tune.best[key] = tile;
+    g_tune.ms[key] = t;
+  } else if (it != g_tune.best.end()) {
+    tile = it->second;
+  }
+  launch_draw_masks(tile, (uint32_t*)page->data, page->width, page->height, S.extra, n, m->dev, blend, g.tbl,
+                    g.stream);
+  CU(cudaGetLastError());
 }
 
 }  // namespace
@@ -587,6 +1270,386 @@ int pxg_fill_paths_batch(pxg_image* const* images, int64_t nj, const float* cmds
   });
 }
 
+int pxg_last_fill_stats(int64_t* out4) {
+  if (!out4) {
+    set_err("Invalid output pointer");
+    return 1;
+  }
+  for (int i = 0; i < 4; i++) out4[i] = g.stats[i];
+  return 0;
+}
+
+pxg_scene* pxg_scene_new(void) {
+  try {
+    return new pxg_scene();
+  } catch (...) {
+    set_err("Out of host memory");
+    return nullptr;
+  }
+}
+
+void pxg_scene_free(pxg_scene* sc) { delete sc; }
+
+int pxg_scene_clear(pxg_scene* sc) {
+  if (!sc) {
+    set_err("Invalid scene handle");
+    return 1;
+  }
+  sc->prims.clear();
+  sc->jobs.clear();
+  sc->dirty = true;
+  return 0;
+}
+
+int64_t pxg_scene_len(const pxg_scene* sc) { return sc ? (int64_t)sc->jobs.size() : 0; }
+
+int pxg_scene_fill_path(pxg_scene* sc, const float* cmds, int64_t n, const float* color, float opacity,
+                        int blend, const float* transform, int winding) {
+  return guarded_host([&] {
+    if (!sc) throw ApiError{"Invalid scene handle"};
+    check_blend(blend);
+    if (winding != 0 && winding != 1) throw ApiError{"Invalid winding rule"};
+    if (n < 0 || (n > 0 && !cmds)) throw ApiError{"Invalid path commands"};
+    validate_commands(cmds, n);
+    uint32_t rgbx;
+    if (!paint_color(color, opacity, blend, rgbx)) return;
+    const float* mat = transform ? transform : kIdent;
+    float ps = pixel_scale(mat);
+    std::vector<Prim> prims;
+    build_fill_prims(cmds, n, ps, prims);
+    PathJob j = make_job(nullptr, rgbx, blend, mat, ps, winding);
+    j.prim_off = (long long)sc->prims.size();
+    j.nprims = (int)prims.size();
+    j.group = curve_group(prims, 0, j.nprims);
+    sc->prims.insert(sc->prims.end(), prims.begin(), prims.end());
+    sc->jobs.push_back(j);
+    sc->dirty = true;
+  });
+}
+
+int pxg_scene_stroke_path(pxg_scene* sc, const float* cmds, int64_t n, const float* color, float opacity,
+                          int blend, const float* transform, float width, int cap, int join,
+                          float miterLimit, const float* dashes, int64_t nd) {
+  return guarded_host([&] {
+    if (!sc) throw ApiError{"Invalid scene handle"};
+    check_blend(blend);
+    if (n < 0 || (n > 0 && !cmds)) throw ApiError{"Invalid path commands"};
+    validate_commands(cmds, n);
+    uint32_t rgbx;
+    if (!paint_color(color, opacity, blend, rgbx)) return;
+    const float* mat = transform ? transform : kIdent;
+    float ps = pixel_scale(mat);
+    std::vector<Prim> prims;
+    build_stroke_prims(cmds, n, ps, width, cap, join, miterLimit, dashes, nd, prims);
+    PathJob j = make_job(nullptr, rgbx, blend, mat, ps, 0);
+    j.prim_off = (long long)sc->prims.size();
+    j.nprims = (int)prims.size();
+    j.group = curve_group(prims, 0, j.nprims);
+    sc->prims.insert(sc->prims.end(), prims.begin(), prims.end());
+    sc->jobs.push_back(j);
+    sc->dirty = true;
+  });
+}
+
+int pxg_image_draw_scene(pxg_image* im, const pxg_scene* sc) {
+  return guarded([&] {
+    check_image(im);
+    if (!sc) throw ApiError{"Invalid scene handle"};
+    std::vector<PathJob> jobs = sc->jobs;
+    Timed t(true);
+    const Prim* dp = scene_device_prims(sc);
+    size_t i = 0;
+    while (i < jobs.size()) {
+      if (jobs[i].mode == kMask) {  // its clears cover rows outside its own: draw it alone
+        std::vector<Prim> sub(sc->prims.begin() + jobs[i].prim_off,
+                              sc->prims.begin() + jobs[i].prim_off + jobs[i].nprims);
+        PathJob j = jobs[i];
+        j.img = im->data;
+        j.W = im->width;
+        j.H = im->height;
+        j.prim_off = 0;
+        std::vector<PathJob> one(1, j);
+        std::vector<int> st;
+        run_jobs(one, sub, st);
+        if (st[0] != kOk) throw ApiError{status_message(st[0])};
+        i++;
+        continue;
+      }
+      size_t e = i;
+      while (e < jobs.size() && jobs[e].mode != kMask) e++;
+      std::vector<HostRun> runs(1);
+      runs[0] = HostRun{im, &jobs, &sc->prims, dp, i, e, kOk};
+      run_scene_runs(runs);
+      if (runs[0].status != kOk) throw ApiError{status_message(runs[0].status)};
+      i = e;
+    }
+    t.done();
+  });
+}
+
+pxg_masks* pxg_masks_new(void) {
+  try {
+    return new pxg_masks();
+  } catch (...) {
+    set_err("Out of host memory");
+    return nullptr;
+  }
+}
+
+void pxg_masks_free(pxg_masks* m) {
+  if (!m) return;
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  delete m;
+}
+
+int64_t pxg_masks_len(const pxg_masks* m) { return m ? (int64_t)m->jobs.size() : 0; }
+
+int pxg_masks_add_path(pxg_masks* m, const float* cmds, int64_t n, int64_t width, int64_t height,
+                       const float* transform, int winding) {
+  return guarded_host([&] {
+    if (!m) throw ApiError{"Invalid mask batch handle"};
+    if (width <= 0 || height <= 0) throw ApiError{"Image width and height must be > 0"};
+    if (width > (1 << 20) || height > (1 << 20)) throw ApiError{"Mask too large"};
+    if (winding != 0 && winding != 1) throw ApiError{"Invalid winding rule"};
+    if (n < 0 || (n > 0 && !cmds)) throw ApiError{"Invalid path commands"};
+    validate_commands(cmds, n);
+    const float* mat = transform ? transform : kIdent;
+    float ps = pixel_scale(mat);
+    std::vector<Prim> prims;
+    build_fill_prims(cmds, n, ps, prims);
+    static const float white[4] = {1, 1, 1, 1};
+    PathJob j = make_job(nullptr, color_to_rgbx(white), kNormal, mat, ps, winding);
+    j.a8 = 1;
+    j.W = width;
+    j.H = height;
+    j.prim_off = (long long)m->prims.size();
+    j.nprims = (int)prims.size();
+    j.group = curve_group(prims, 0, j.nprims);
+    m->prims.insert(m->prims.end(), prims.begin(), prims.end());
+    m->jobs.push_back(j);
+    m->dirty = true;
+    m->offs.push_back(m->bytes);
+    m->bytes += (width * height + 15) / 16 * 16;
+    m->rendered = false;
+  });
+}
+
+int pxg_masks_render(pxg_masks* m) {
+  return guarded([&] {
+    if (!m) throw ApiError{"Invalid mask batch handle"};
+    Timed t(true);
+    render_masks(m);
+    t.done();
+  });
+}
+
+int pxg_masks_render_config(pxg_masks* m, int variant, int rows_per_item) {
+  return guarded([&] {
+    if (!m) throw ApiError{"Invalid mask batch handle"};
+    if (variant < 0 || variant > 1 || rows_per_item < 1 || rows_per_item > 64) throw ApiError{"Invalid configuration"};
+    if (m->jobs.empty()) return;
+    dev_grow(m->dev, m->dev_cap, std::max<long long>(m->bytes, 16));
+    std::vector<PathJob> jobs = m->jobs;
+    for (size_t i = 0; i < jobs.size(); i++) jobs[i].img = m->dev + m->offs[i];
+    RunOpts o;
+    o.cfg.variant = variant;
+    o.cfg.rpi = rows_per_item;
+    o.zero = m->dev;
+    o.zero_bytes = m->bytes;
+    o.dprims = masks_device_prims(m);
+    std::vector<int> st;
+    Timed t(true);
+    run_jobs(jobs, m->prims, st, o);
+    t.done();
+    for (size_t i = 0; i < st.size(); i++)
+      if (st[i] != kOk) throw ApiError{status_message(st[i])};
+    m->rendered = true;
+  });
+}
+
+int pxg_masks_download(const pxg_masks* m, int64_t i, void* out, int64_t nbytes) {
+  return guarded([&] {
+    if (!m) throw ApiError{"Invalid mask batch handle"};
+    if (i < 0 || i >= (int64_t)m->jobs.size()) throw ApiError{"Mask index out of range"};
+    if (!m->rendered) throw ApiError{"Masks not rendered"};
+    const int64_t need = m->jobs[(size_t)i].W * m->jobs[(size_t)i].H;
+    if (!out || nbytes < need) throw ApiError{"Output buffer too small"};
+    CU(cudaStreamSynchronize(g.stream));
+    CU(cudaMemcpy(out, m->dev + m->offs[(size_t)i], (size_t)need, cudaMemcpyDeviceToHost));
+  });
+}
+
+const void* pxg_masks_device_ptr(const pxg_masks* m, int64_t i) {
+  if (!m || i < 0 || i >= (int64_t)m->jobs.size() || !m->dev) return nullptr;
+  return m->dev + m->offs[(size_t)i];
+}
+
+int pxg_image_draw_masks(pxg_image* page, const pxg_masks* m, const int64_t* xy, int blend) {
+  return guarded([&] {
+    check_image(page);
+    if (!m) throw ApiError{"Invalid mask batch handle"};
+    check_blend(blend);
+    if (blend == kMask) throw ApiError{"MaskBlend is not supported for mask batches"};
+    if (!m->rendered && !m->jobs.empty()) throw ApiError{"Masks not rendered"};
+    if (!xy && !m->jobs.empty()) throw ApiError{"Invalid positions"};
+    Timed t;
+    draw_masks(page, m, xy, blend);
+    t.done();
+  });
+}
+
+pxg_server* pxg_server_new(int64_t budget_bytes, int64_t paths_per_job, int64_t paths_per_step) {
+  try {
+    if (budget_bytes <= 0 || paths_per_job <= 0 || paths_per_step <= 0) {
+      set_err("Invalid server limits");
+      return nullptr;
+    }
+    pxg_server* sv = new pxg_server();
+    sv->budget = budget_bytes;
+    sv->paths_per_job = paths_per_job;
+    sv->paths_per_step = paths_per_step;
+    return sv;
+  } catch (...) {
+    set_err("Out of host memory");
+    return nullptr;
+  }
+}
+
+void pxg_server_free(pxg_server* sv) {
+  if (!sv) return;
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  if (g.ready) cudaStreamSynchronize(g.stream);
+  delete sv;
+}
+
+int64_t pxg_server_submit(pxg_server* sv, const pxg_scene* scene, int64_t width, int64_t height,
+                          float blur_radius) {
+  int64_t id = 0;
+  int rc = guarded([&] {
+    if (!sv || !scene) throw ApiError{"Invalid server or scene handle"};
+    if (width <= 0 || height <= 0) throw ApiError{"Image width and height must be > 0"};
+    const int64_t r = nim_round_int(blur_radius);
+    if (r < 0) throw ApiError{"Cannot apply negative blur"};
+    if (r > (1 << 20)) throw ApiError{"Blur radius too large"};
+    const long long need = width * height * 4 * (r > 0 ? 2 : 1);
+    if (need > sv->budget) throw ApiError{"Job larger than the server's memory budget"};
+    SrvJob* j = new SrvJob();
+    j->id = sv->next_id++;
+    j->scene = scene;
+    j->W = width;
+    j->H = height;
+    j->blur = r;
+    j->state = 0;
+    j->status = kOk;
+    j->next = 0;
+    j->bytes = 0;
+    j->canvas = pxg_image{nullptr, 0, 0, 0};
+    j->tmp = nullptr;
+    j->t_submit = now_s();
+    j->t_admit = j->t_done = 0;
+    sv->jobs[j->id] = j;
+    sv->queue.push_back(j);
+    id = j->id;
+  });
+  return rc == 0 ? id : 0;
+}
+
+int pxg_server_step(pxg_server* sv) {
+  return guarded([&] {
+    if (!sv) throw ApiError{"Invalid server handle"};
+    srv_step(sv);
+  });
+}
+
+int64_t pxg_server_pending(const pxg_server* sv) {
+  return sv ? (int64_t)(sv->queue.size() + sv->active.size()) : 0;
+}
+
+int64_t pxg_server_poll(pxg_server* sv, int64_t* ids, int64_t cap) {
+  if (!sv) return 0;
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  const int64_t n = std::min<int64_t>(cap, (int64_t)sv->finished.size());
+  for (int64_t i = 0; i < n; i++) ids[i] = sv->finished[(size_t)i];
+  sv->finished.erase(sv->finished.begin(), sv->finished.begin() + n);
+  return n;
+}
+
+int pxg_server_take(pxg_server* sv, int64_t id, void* out, int64_t nbytes, double* times3) {
+  return guarded([&] {
+    if (!sv) throw ApiError{"Invalid server handle"};
+    auto it = sv->jobs.find(id);
+    if (it == sv->jobs.end()) throw ApiError{"Unknown job"};
+    SrvJob* j = it->second;
+    if (j->state < 2) throw ApiError{"Job not finished"};
+    if (times3) {
+      times3[0] = j->t_submit;
+      times3[1] = j->t_admit;
+      times3[2] = j->t_done;
+    }
+    std::string err = j->err;
+    const int state = j->state;
+    if (state == 2 && out) {
+      if (nbytes < j->W * j->H * 4) throw ApiError{"Output buffer too small"};
+      CU(cudaMemcpy(out, j->canvas.data, (size_t)(j->W * j->H * 4), cudaMemcpyDeviceToHost));
+    }
+    srv_release(sv, j);
+    sv->jobs.erase(it);
+    delete j;
+    if (state == 3) throw ApiError{err};
+  });
+}
+
+int pxg_server_stats(const pxg_server* sv, int64_t* out6) {
+  if (!sv || !out6) {
+    set_err("Invalid server handle");
+    return 1;
+  }
+  out6[0] = sv->steps;
+  out6[1] = sv->used;
+  out6[2] = sv->peak_used;
+  out6[3] = sv->peak_active;
+  out6[4] = (int64_t)sv->queue.size();
+  out6[5] = (int64_t)sv->active.size();
+  return 0;
+}
+
+int pxg_autotune(int enable) {
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  g_tune.on = enable != 0;
+  return 0;
+}
+
+int64_t pxg_autotune_report(char* buf, int64_t cap) {
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  std::string r;
+  for (auto& kv : g_tune.best) {
+    char line[256];
+    const int op = kv.first.first;
+    const long long cls = kv.first.second;
+    int c = kv.second;
+    if (op == kTuneMaskRows)
+      snprintf(line, sizeof line, "mask_rows class(side<=%d,count<=%lld): variant=%d rows_per_item=%d",
+               32 << (int)(cls / 32), 1LL << (cls % 32), kMaskRowsCands[c].variant, kMaskRowsCands[c].rpi);
+    else
+      snprintf(line, sizeof line, "mask_draw class(side<=%d,count<=%lld): tile=%s", 32 << (int)(cls / 32),
+               1LL << (cls % 32), c == 0 ? "32x32" : (c == 1 ? "64x32" : "64x64"));
+    r += line;
+    auto t = g_tune.ms.find(kv.first);
+    if (t != g_tune.ms.end()) {
+      r += " ms=[";
+      for (size_t k = 0; k < t->second.size(); k++) {
+        char v[32];
+        snprintf(v, sizeof v, "%s%.4f", k ? "," : "", t->second[k]);
+        r += v;
+      }
+      r += "]";
+    }
+    r += "\n";
+  }
+  if (buf && cap > 0) snprintf(buf, (size_t)cap, "%s", r.c_str());
+  return (int64_t)r.size();
+}
+
 int pxg_image_draw(pxg_image* a, const pxg_image* b, int64_t tx, int64_t ty, int blend) {
   return guarded([&] {
     check_image(a);
@@ -600,11 +1663,6 @@ int pxg_image_draw(pxg_image* a, const pxg_image* b, int64_t tx, int64_t ty, int
   });
 }
 
-static int64_t nim_round_int(float v) {
-  float r = roundf(v);
-  if (!(r >= -9223372036854775808.0f && r < 9223372036854775808.0f)) return INT64_MIN;
-  return (int64_t)r;
-}
 
 int pxg_image_blur(pxg_image* im, float radius, const float* oob) {
   return guarded([&] {

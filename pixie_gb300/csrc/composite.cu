@@ -8,6 +8,7 @@
 #include <atomic>
 
 #include "pxg_device.cuh"
+#include "raster.cuh"
 
 namespace pxg {
 
@@ -187,5 +188,102 @@ void launch_blend_pixels(int mode, const uint8_t* tbl, const uint32_t* bd, const
   if (blocks < 1) blocks = 1;
   k_blend_pixels<<<(unsigned)blocks, 256, 0, st>>>(mode, tbl, bd, src, out, n); note_launch();
 }
+
+// ---------------------------------------------------------------------------
+// Ordered composite of a batch of 8-bit masks: for i = 0..n-1,
+// draw(page, mask_i as an RGBX image (a, a, a, a), translate(x_i, y_i), mode)
+// (images.nim:636-678 with blendRect :468-529).  One CTA owns a TW x TH tile
+// of the page; every thread owns TW*TH/256 pixels of it in registers, so the
+// masks that overlap the tile are applied to each pixel in batch order with
+// no synchronisation between them.  The CTA finds its masks by testing the
+// batch's rectangles 256 at a time and compacting the hits in order.
+// Tiles no mask touches are neither read nor written.
+// ---------------------------------------------------------------------------
+template <int TW, int TH>
+__global__ void __launch_bounds__(256) k_draw_masks(uint32_t* __restrict__ page, long long W, long long H,
+                                                    const MaskDraw* __restrict__ items, int n,
+                                                    const uint8_t* __restrict__ masks, int mode,
+                                                    const uint8_t* tbl) {
+  constexpr int PER = TW * TH / 256;  // pixels per thread
+  __shared__ int list[256];
+  __shared__ int s_warp[8];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const long long tx0 = (long long)blockIdx.x * TW, ty0 = (long long)blockIdx.y * TH;
+  const long long tx1 = min(tx0 + TW, W), ty1 = min(ty0 + TH, H);
+  uint32_t px[PER];
+  bool loaded = false;
+  for (int c0 = 0; c0 < n; c0 += 256) {
+    const int i = c0 + tid;
+    bool hit = false;
+    if (i < n) {
+      const MaskDraw m = items[i];
+      const long long x0 = max(m.x, 0LL), x1 = min(m.x + m.w, W);
+      const long long y0 = max(m.y, 0LL), y1 = min(m.y + m.h, H);
+      hit = max(x0, tx0) < min(x1, tx1) && max(y0, ty0) < min(y1, ty1);
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, hit);
+    if (lane == 0) s_warp[warp] = __popc(b);
+    __syncthreads();
+    int before = 0, cnt = 0;
+    for (int w = 0; w < 8; w++) {
+      if (w < warp) before += s_warp[w];
+      cnt += s_warp[w];
+    }
+    if (hit) list[before + __popc(b & ((1u << lane) - 1))] = i;
+    __syncthreads();
+    if (cnt > 0) {
+      if (!loaded) {
+#pragma unroll
+        for (int k = 0; k < PER; k++) {
+          const int p = tid + 256 * k;
+          const long long X = tx0 + p % TW, Y = ty0 + p / TW;
+          px[k] = (X < tx1 && Y < ty1) ? page[Y * W + X] : 0u;
+        }
+        loaded = true;
+      }
+      for (int j = 0; j < cnt; j++) {
+        const MaskDraw m = items[list[j]];
+#pragma unroll
+        for (int k = 0; k < PER; k++) {
+          const int p = tid + 256 * k;
+          const long long X = tx0 + p % TW, Y = ty0 + p / TW;
+          const long long u = X - m.x, v = Y - m.y;
+          if (X < tx1 && Y < ty1 && u >= 0 && u < m.w && v >= 0 && v < m.h) {
+            const uint32_t a = (uint32_t)masks[m.off + v * m.w + u] * 0x01010101u;
+            px[k] = mode == kNormal ? blendNormal(px[k], a) : (mode == kOverwrite ? a : blend_px(mode, tbl, px[k], a));
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (loaded) {
+#pragma unroll
+    for (int k = 0; k < PER; k++) {
+      const int p = tid + 256 * k;
+      const long long X = tx0 + p % TW, Y = ty0 + p / TW;
+      if (X < tx1 && Y < ty1) page[Y * W + X] = px[k];
+    }
+  }
+}
+
+// Tile shapes of the mask composite (the bin size): 0 = 32x32, 1 = 64x32, 2 = 64x64.
+int draw_masks_tiles() { return 3; }
+void launch_draw_masks(int tile, uint32_t* page, long long W, long long H, const void* items, int n,
+                       const uint8_t* masks, int mode, const uint8_t* tbl, cudaStream_t st) {
+  const MaskDraw* it = reinterpret_cast<const MaskDraw*>(items);
+  if (tile == 0) {
+    dim3 grid((unsigned)((W + 31) / 32), (unsigned)((H + 31) / 32));
+    k_draw_masks<32, 32><<<grid, 256, 0, st>>>(page, W, H, it, n, masks, mode, tbl);
+  } else if (tile == 1) {
+    dim3 grid((unsigned)((W + 63) / 64), (unsigned)((H + 31) / 32));
+    k_draw_masks<64, 32><<<grid, 256, 0, st>>>(page, W, H, it, n, masks, mode, tbl);
+  } else {
+    dim3 grid((unsigned)((W + 63) / 64), (unsigned)((H + 63) / 64));
+    k_draw_masks<64, 64><<<grid, 256, 0, st>>>(page, W, H, it, n, masks, mode, tbl);
+  }
+  note_launch();
+}
+size_t mask_draw_bytes() { return sizeof(MaskDraw); }
 
 }  // namespace pxg

@@ -436,7 +436,32 @@ void build_stroke_prims(const float* cmds, int64_t n, float ps, float strokeWidt
   enum { Butt = 0, RoundC = 1, Square = 2 };
   enum { Miter = 0, RoundJ = 1, Bevel = 2 };
 
-  auto circle = [&](P2 c) {  // ellipse(c, hs, hs) flattened (:604-616, :1938-1941)
+  // Outline shapes in the reference's order.  Round joins and caps are
+  // circles: pixie flattens ellipse(c, hs, hs) (:604-616, :1938-1941) with the
+  // same error margin, so they go to the GPU as their four cubics and are
+  // flattened there; the other shapes are polygons of lines.
+  struct OutShape {  // a polygon of at most 5 points, or a circle at c
+    P2 p[5];
+    int n;
+    bool circ;
+    P2 c;
+  };
+  auto poly5 = [](std::initializer_list<P2> pts) {
+    OutShape o;
+    o.n = 0;
+    for (P2 q : pts) o.p[o.n++] = q;
+    o.circ = false;
+    o.c = P2{0, 0};
+    return o;
+  };
+  auto circle = [&](P2 c) {
+    OutShape o;
+    o.n = 0;
+    o.circ = true;
+    o.c = c;
+    return o;
+  };
+  auto emit_circle = [&](P2 c) {
     const double mx = kCircleK * (double)hs, my = kCircleK * (double)hs;
     const float cx = c.x, cy = c.y;
     float e[] = {(float)kMove, cx + hs, cy,
@@ -445,14 +470,14 @@ void build_stroke_prims(const float* cmds, int64_t n, float ps, float strokeWidt
                  (float)kCubic, cx - hs, (float)(cy - my), (float)(cx - mx), cy - hs, cx, cy - hs,
                  (float)kCubic, (float)(cx + mx), cy - hs, cx + hs, (float)(cy - my), cx + hs, cy,
                  (float)kClose};
-    return walk_commands(e, (int64_t)(sizeof e / sizeof e[0]), true, ems, nullptr)[0];
+    walk_commands(e, (int64_t)(sizeof e / sizeof e[0]), true, ems, &out);
   };
   auto rect = [&](P2 a, P2 b) {  // :1943-1965
     P2 t = unit(sub(b, a));
     P2 nrm{t.y, t.x};
     P2 p0{a.x + nrm.x * hs, a.y - nrm.y * hs}, p1{b.x + nrm.x * hs, b.y - nrm.y * hs};
     P2 p2{b.x - nrm.x * hs, b.y + nrm.y * hs}, p3{a.x - nrm.x * hs, a.y + nrm.y * hs};
-    return Poly{p0, p1, p2, p3, p0};
+    return poly5({p0, p1, p2, p3, p0});
   };
   auto fixAngle = [](float a) {
     const float tau = (float)(kPI * 2);
@@ -460,7 +485,7 @@ void build_stroke_prims(const float* cmds, int64_t n, float ps, float strokeWidt
     while ((double)a < -kPI) a += tau;
     return a;
   };
-  auto join = [&](std::vector<Poly>& o, P2 prevPos, P2 pos, P2 nextPos) {  // :1967-2013
+  auto join = [&](std::vector<OutShape>& o, P2 prevPos, P2 pos, P2 nextPos) {  // :1967-2013
     if (lineJoin == RoundJ) {
       float area = (float)kPI * hs * hs;
       if (area > minArea) o.push_back(circle(pos));
@@ -489,11 +514,13 @@ void build_stroke_prims(const float* cmds, int64_t n, float ps, float strokeWidt
           P2 at = add(a0, scl(s1, t));
           float bls = len2(sub(at, pos));
           float areaSq = 0.25f * (len2(a) * bls + len2(b) * bls);
-          if (areaSq > (minArea * minArea)) o.push_back(Poly{add(pos, a), at, add(pos, b), pos, add(pos, a)});
+          if (areaSq > (minArea * minArea))
+            o.push_back(poly5({add(pos, a), at, add(pos, b), pos, add(pos, a)}));
         }
       } else if (lj == Bevel) {
         float areaSq = 0.25f * len2(a) * len2(b);
-        if (areaSq > (minArea * minArea)) o.push_back(Poly{add(a, pos), add(b, pos), pos, add(a, pos)});
+        if (areaSq > (minArea * minArea))
+          o.push_back(poly5({add(a, pos), add(b, pos), pos, add(a, pos)}));
       }
     }
   };
@@ -503,9 +530,14 @@ void build_stroke_prims(const float* cmds, int64_t n, float ps, float strokeWidt
     std::vector<float> d2 = dashes;
     dashes.insert(dashes.end(), d2.begin(), d2.end());
   }
-  std::vector<Poly> outline;
+  std::vector<OutShape> outline;
+  {
+    size_t pts = 0;
+    for (const Poly& s : shapes) pts += s.size();
+    outline.reserve(pts * 2 + 4 * shapes.size());
+  }
   for (const Poly& s : shapes) {  // :2015-2082
-    std::vector<Poly> st;
+    std::vector<OutShape>& st = outline;
     const bool open = !eq(s[0], s.back());
     if (open) {
       if (lineCap == RoundC) st.push_back(circle(s[0]));
@@ -548,9 +580,17 @@ void build_stroke_prims(const float* cmds, int64_t n, float ps, float strokeWidt
       P2 t = unit(sub(s.back(), s[s.size() - 2]));
       st.push_back(rect(add(s.back(), scl(t, hs)), s.back()));
     }
-    outline.insert(outline.end(), st.begin(), st.end());
   }
-  for (const Poly& p : outline) emit_polygon_lines(p, out);
+  out.reserve(out.size() + outline.size() * 5);
+  for (const OutShape& o : outline) {
+    if (o.circ) {
+      emit_circle(o.c);
+    } else if (o.n > 0) {  // emit_polygon_lines on the inline points
+      if (!eq(o.p[o.n - 1], o.p[0])) out.push_back(line_prim(o.p[o.n - 1], o.p[0]));
+      for (int i = 0; i + 1 < o.n; i++)
+        if (!eq(o.p[i], o.p[i + 1])) out.push_back(line_prim(o.p[i], o.p[i + 1]));
+    }
+  }
 }
 
 float pixel_scale(const float* m) {  // paths.nim:61-66

@@ -24,6 +24,7 @@ namespace pxg {
 
 static __device__ constexpr float kEps = (float)(0.0001 * 3.141592653589793);  // paths.nim:44
 static constexpr long long kIterCap = 1LL << 24;
+static constexpr int kSegTile = 1024;  // segment band ranges staged per pass of the band-list build
 
 struct V2 {
   float x, y;
@@ -53,72 +54,78 @@ __device__ __forceinline__ V2 quadAt(V2 a, V2 c, V2 to, float t) {
   return a * ((t2 - 2 * t) + 1) + c * (-2 * t2 + 2 * t) + to * t2;
 }
 
-// Calls emit(prev, next) for every segment addSegment would add (zero-length
-// segments are dropped as in paths.nim:669-675).  Returns a JobStatus.
+// The adaptive loops of addCubic/addQuadratic (paths.nim:677-762) with the
+// halvings of one search evaluated side by side.  After a segment is
+// accepted the loop tries steps s0, s0/2, s0/4, ... until one passes the
+// error test (or drops to float32 epsilon, which raises).  Every quantity the
+// test at level k reads -- next = f(t + s0/2^k), halfway = f(t + s0/2^(k+1)),
+// the tangent at t + s0/2^(k+1) -- depends only on (t, s0, prev): halving a
+// normal float is exact, so the sequential loop's recomputed `next = halfway`
+// and `t + step/4` equal these values bit for bit.  A group of G lanes tests
+// levels base..base+G-1 at once; the first level that accepts (or is at or
+// below epsilon) is the one the sequential loop would have stopped at.  With
+// G = 1 this is the reference's loop unchanged.  Calls emit(prev, next) for
+// every segment addSegment keeps (zero-length ones dropped, :669-675);
+// returns a JobStatus.  All G lanes of the group run the loop in lockstep.
+__device__ __forceinline__ float pow2neg(int k) {  // 2^-k for 0 <= k < 126
+  return __int_as_float((127 - k) << 23);
+}
 template <class Emit>
-__device__ int flatten_prim(const Prim& p, float ems, Emit&& emit) {
-  V2 at{p.x[0], p.y[0]};
-  if (p.kind == kPrimLine) {
-    V2 to{p.x[1], p.y[1]};
-    if (at.x - to.x != 0.0f || at.y - to.y != 0.0f) emit(at, to);
-    return kOk;
-  }
-  float t = 0, step = 1;
+__device__ int flatten_curve_group(const Prim& p, float ems, int G, int gl, int leader,
+                                   unsigned gmask, Emit&& emit) {
+  const bool cubic = p.kind == kPrimCubic;
+  const V2 at{p.x[0], p.y[0]}, c1{p.x[1], p.y[1]};
+  const V2 c2{p.x[2], p.y[2]}, to{cubic ? p.x[3] : p.x[2], cubic ? p.y[3] : p.y[2]};
+  float t = 0, s0 = 1;
+  bool halfStepping = false;
   V2 prev = at;
-  long long iters = 0;
-  if (p.kind == kPrimCubic) {
-    V2 c1{p.x[1], p.y[1]}, c2{p.x[2], p.y[2]}, to{p.x[3], p.y[3]};
-    V2 next = cubicAt(at, c1, c2, to, t + step);
-    V2 halfway = cubicAt(at, c1, c2, to, t + step / 2);
-    while (true) {
-      if (step <= FLT_EPSILON) return kErrCubic;
-      if (++iters > kIterCap) return kErrIterLimit;
-      V2 midpoint = (prev + next) / 2;
-      V2 lineTangent = midpoint - prev;
-      V2 curveTangent = cubicDeriv(at, c1, c2, to, t + step / 2);
-      V2 scaled = (curveTangent / length(curveTangent)) * length(lineTangent);
-      float error = lengthSq(midpoint - halfway);
-      float errorTangent = lengthSq(lineTangent - scaled);
-      if (error + errorTangent > ems) {
-        next = halfway;
-        halfway = cubicAt(at, c1, c2, to, t + step / 4);
-        step /= 2;
-      } else {
-        if (prev.x - next.x != 0.0f || prev.y - next.y != 0.0f) emit(prev, next);
-        t += step;
-        if (t == 1) break;
-        prev = next;
-        step = nmin(step * 2, 1 - t);
-        next = cubicAt(at, c1, c2, to, t + step);
-        halfway = cubicAt(at, c1, c2, to, t + step / 2);
+  long long rounds = 0;
+  while (true) {
+    int kdec = 0;
+    V2 nxt{0, 0};
+    for (int base = 0;; base += G) {
+      if (++rounds > kIterCap) return kErrIterLimit;
+      const int k = base + gl;
+      const float sk = k < 100 ? s0 * pow2neg(k) : 0.0f;
+      const bool invalid = sk <= FLT_EPSILON;
+      bool accept = false;
+      V2 nx{0, 0};
+      if (!invalid) {
+        const float sh = sk * 0.5f;
+        if (cubic) {
+          nx = cubicAt(at, c1, c2, to, t + sk);
+          const V2 halfway = cubicAt(at, c1, c2, to, t + sh);
+          const V2 midpoint = (prev + nx) / 2;
+          const V2 lineTangent = midpoint - prev;
+          const V2 curveTangent = cubicDeriv(at, c1, c2, to, t + sh);
+          const V2 scaled = (curveTangent / length(curveTangent)) * length(lineTangent);
+          const float error = lengthSq(midpoint - halfway);
+          const float errorTangent = lengthSq(lineTangent - scaled);
+          accept = !(error + errorTangent > ems);
+        } else {
+          nx = quadAt(at, c1, c2, t + sk);
+          const V2 halfway = quadAt(at, c1, c2, t + sh);
+          const V2 midpoint = (prev + nx) / 2;
+          accept = !(lengthSq(midpoint - halfway) > ems);
+        }
+      }
+      const unsigned dec = (__ballot_sync(gmask, invalid || accept) >> leader) & (G == 32 ? 0xffffffffu : ((1u << G) - 1));
+      if (dec) {
+        const int src = leader + __ffs(dec) - 1;
+        if (__shfl_sync(gmask, (int)invalid, src)) return cubic ? kErrCubic : kErrQuad;
+        nxt.x = __shfl_sync(gmask, nx.x, src);
+        nxt.y = __shfl_sync(gmask, nx.y, src);
+        kdec = base + __ffs(dec) - 1;
+        break;
       }
     }
-    return kOk;
-  }
-  // quadratic
-  V2 c{p.x[1], p.y[1]}, to{p.x[2], p.y[2]};
-  V2 next = quadAt(at, c, to, t + step);
-  V2 halfway = quadAt(at, c, to, t + step / 2);
-  bool halfStepping = false;
-  while (true) {
-    if (step <= FLT_EPSILON) return kErrQuad;
-    if (++iters > kIterCap) return kErrIterLimit;
-    V2 midpoint = (prev + next) / 2;
-    float error = lengthSq(midpoint - halfway);
-    if (error > ems) {
-      next = halfway;
-      halfway = quadAt(at, c, to, t + step / 4);
-      halfStepping = true;
-      step /= 2;
-    } else {
-      if (prev.x - next.x != 0.0f || prev.y - next.y != 0.0f) emit(prev, next);
-      t += step;
-      if (t == 1) break;
-      prev = next;
-      step = halfStepping ? nmin(step, 1 - t) : nmin(step * 2, 1 - t);
-      next = quadAt(at, c, to, t + step);
-      halfway = quadAt(at, c, to, t + step / 2);
-    }
+    const float step = s0 * pow2neg(kdec);
+    if (prev.x - nxt.x != 0.0f || prev.y - nxt.y != 0.0f) emit(prev, nxt);
+    t += step;
+    if (t == 1) break;
+    prev = nxt;
+    if (kdec > 0) halfStepping = true;
+    s0 = (!cubic && halfStepping) ? nmin(step, 1 - t) : nmin(step * 2, 1 - t);
   }
   return kOk;
 }
@@ -247,7 +254,9 @@ __global__ void __launch_bounds__(256) k_setup(PathJob* jobs, Arena A, int maxBa
   __shared__ long long s_warp[32];
   __shared__ long long s_err;
   __shared__ int s_status;
-  __shared__ long long s_segbase, s_bandbase, s_nseg;
+  __shared__ long long s_segbase, s_bandbase, s_nseg, s_listbase;
+  __shared__ uint2 s_tile[kSegTile];
+  __shared__ uint32_t s_lohi[66];
   __shared__ float s_red[4][32];
   __shared__ long long s_hdr[6];
 
@@ -259,35 +268,55 @@ __global__ void __launch_bounds__(256) k_setup(PathJob* jobs, Arena A, int maxBa
   }
   __syncthreads();
 
-  const Prim* P = A.prims + J.prim_off;
+  const Prim* P = J.prims + J.prim_off;
   const int np = J.nprims;
-  const int chunk = (np + T - 1) / T;
-  const int p0 = min(np, tid * chunk), p1 = min(np, p0 + chunk);
+  int* PC = A.primcnt + J.pc_off;
+  // curves: groups of G lanes (G divides 32), one curve per group at a time
+  const int G = J.group;
+  const int NG = T / G, gid = tid / G, gl = tid % G, leader = lane - gl;
+  const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1) << leader);
 
-  // Phase A: count the segments each thread's primitives emit
-  long long cnt = 0;
-  for (int p = p0; p < p1; p++) {
-    int st = flatten_prim(P[p], J.ems, [&](V2 a, V2 b) {
+  // Phase A: count the segments each primitive emits
+  for (int p = tid; p < np; p += T) {
+    if (P[p].kind != kPrimLine) continue;
+    float4 s;
+    int w;
+    V2 a{P[p].x[0], P[p].y[0]}, b{P[p].x[1], P[p].y[1]};
+    PC[p] = ((a.x - b.x != 0.0f || a.y - b.y != 0.0f) && make_seg(J, a, b, s, w)) ? 1 : 0;
+  }
+  for (int p = gid; p < np; p += NG) {
+    if (P[p].kind == kPrimLine) continue;
+    int cnt = 0;
+    int st = flatten_curve_group(P[p], J.ems, G, gl, leader, gmask, [&](V2 a, V2 b) {
       float4 s;
       int w;
       if (make_seg(J, a, b, s, w)) cnt++;
     });
     if (st != kOk) {  // the reference raises at the first failing primitive
-      atomicMin(&s_err, ((long long)p << 8) | st);
+      if (gl == 0) atomicMin(&s_err, ((long long)p << 8) | st);
       break;
     }
+    if (gl == 0) PC[p] = cnt;
   }
-  long long total;
-  long long excl = block_excl_scan(cnt, s_warp, total);
+  __syncthreads();
+  if (s_err != LLONG_MAX) {
+    if (tid == 0) J.status = (int)(s_err & 255);
+    return;
+  }
+  // exclusive prefix of the counts, in primitive order
+  long long total = 0;
+  for (int c0 = 0; c0 < np; c0 += T) {
+    const int p = c0 + tid;
+    long long v = p < np ? PC[p] : 0, tot;
+    long long ex = block_excl_scan(v, s_warp, tot);
+    if (p < np) PC[p] = (int)(total + ex);
+    total += tot;
+  }
   if (tid == 0) {
-    if (s_err != LLONG_MAX) {
-      s_status = (int)(s_err & 255);
-    } else {
-      unsigned long long base = atomicAdd(&A.counters[kCtrSegs], (unsigned long long)total);
-      s_segbase = (long long)base;
-      s_nseg = total;
-      if ((long long)base + total > A.seg_cap) s_status = kErrArenaFull;
-    }
+    unsigned long long base = atomicAdd(&A.counters[kCtrSegs], (unsigned long long)total);
+    s_segbase = (long long)base;
+    s_nseg = total;
+    if ((long long)base + total > A.seg_cap || total > INT_MAX) s_status = kErrArenaFull;
   }
   __syncthreads();
   if (s_status != kOk) {
@@ -297,23 +326,32 @@ __global__ void __launch_bounds__(256) k_setup(PathJob* jobs, Arena A, int maxBa
 
   // Phase B: emit the segments in order and reduce the bounds (:1098-1117)
   float xmin = INFINITY, xmax = -INFINITY, ymin = INFINITY, ymax = -INFINITY;
-  {
-    long long o = s_segbase + excl;
-    for (int p = p0; p < p1; p++) {
-      flatten_prim(P[p], J.ems, [&](V2 a, V2 b) {
-        float4 s;
-        int w;
-        if (make_seg(J, a, b, s, w)) {
-          A.segs[o] = s;
-          A.segw[o] = w;
-          o++;
-          xmin = nmin(xmin, nmin(s.x, s.z));
-          xmax = nmax(xmax, nmax(s.x, s.z));
-          ymin = nmin(ymin, s.y);
-          ymax = nmax(ymax, s.w);
-        }
-      });
-    }
+  auto put = [&](long long o, float4 s, int w) {
+    A.segs[o] = s;
+    A.segw[o] = w;
+    xmin = nmin(xmin, nmin(s.x, s.z));
+    xmax = nmax(xmax, nmax(s.x, s.z));
+    ymin = nmin(ymin, s.y);
+    ymax = nmax(ymax, s.w);
+  };
+  for (int p = tid; p < np; p += T) {
+    if (P[p].kind != kPrimLine) continue;
+    float4 s;
+    int w;
+    V2 a{P[p].x[0], P[p].y[0]}, b{P[p].x[1], P[p].y[1]};
+    if ((a.x - b.x != 0.0f || a.y - b.y != 0.0f) && make_seg(J, a, b, s, w)) put(s_segbase + PC[p], s, w);
+  }
+  for (int p = gid; p < np; p += NG) {
+    if (P[p].kind == kPrimLine) continue;
+    long long o = s_segbase + PC[p];
+    flatten_curve_group(P[p], J.ems, G, gl, leader, gmask, [&](V2 a, V2 b) {
+      float4 s;
+      int w;
+      if (make_seg(J, a, b, s, w)) {
+        if (gl == 0) put(o, s, w);
+        o++;
+      }
+    });
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -430,11 +468,75 @@ __global__ void __launch_bounds__(256) k_setup(PathJob* jobs, Arena A, int maxBa
     if (tid == 0) J.status = s_status;
     return;
   }
-  for (uint32_t k = tid; k < numP; k += T) {
-    Band bd;
-    bd.count = bandc[k];
-    bd.flags = bandf[k];
-    A.bands[s_bandbase + k] = bd;
+  // Phase E: each band's entry list, segment indices ascending -- the order in
+  // which partitionSegments appends them (:1215-1234).  Offsets by a scan of
+  // the counts; then every thread owns bands and walks the segments in order.
+  long long etotal = 0;
+  for (uint32_t c0 = 0; c0 < numP; c0 += T) {
+    const uint32_t k = c0 + tid;
+    long long v = k < numP ? bandc[k] : 0, tot;
+    long long ex = block_excl_scan(v, s_warp, tot);
+    if (k < numP) {
+      Band bd;
+      bd.off = etotal + ex;  // relative until the base is known
+      bd.count = bandc[k];
+      bd.flags = bandf[k];
+      A.bands[s_bandbase + k] = bd;
+      bandc[k] = (int)(etotal + ex);  // cursor
+    }
+    etotal += tot;
+  }
+  if (tid == 0) {
+    unsigned long long base = atomicAdd(&A.counters[kCtrBandSegs], (unsigned long long)etotal);
+    s_listbase = (long long)base;
+    if ((long long)base + etotal > A.bandseg_cap || etotal > INT_MAX) s_status = kErrArenaFull;
+  }
+  __syncthreads();
+  if (s_status != kOk) {
+    if (tid == 0) J.status = s_status;
+    return;
+  }
+  int* L = A.bandseg + s_listbase;
+  for (uint32_t k = tid; k < numP; k += T) A.bands[s_bandbase + k].off += s_listbase;
+  for (long long t0 = 0; t0 < nseg; t0 += kSegTile) {
+    const int tl = (int)min((long long)kSegTile, nseg - t0);
+    uint32_t lo = UINT_MAX, hi = 0;
+    for (int j = tid; j < tl; j += T) {
+      uint2 r = A.segband[segbase + t0 + j];
+      s_tile[j] = r;
+      lo = min(lo, r.x);
+      hi = max(hi, r.y);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+      hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if (lane == 0) {
+      s_lohi[warp] = lo;
+      s_lohi[32 + warp] = hi;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      for (int i = 1; i < (T + 31) / 32; i++) {
+        lo = min(lo, s_lohi[i]);
+        hi = max(hi, s_lohi[32 + i]);
+      }
+      s_lohi[64] = lo;
+      s_lohi[65] = hi;
+    }
+    __syncthreads();
+    const uint32_t tlo = s_lohi[64], thi = s_lohi[65];
+    for (uint32_t k = tid; k < numP; k += T) {
+      if (k < tlo || k > thi) continue;
+      int cur = bandc[k];
+      for (int j = 0; j < tl; j++) {
+        const uint2 r = s_tile[j];
+        if (r.x <= k && k <= r.y) L[cur++] = (int)(t0 + j);
+      }
+      bandc[k] = cur;
+    }
+    __syncthreads();
   }
   if (tid == 0) {
     J.band_off = s_bandbase;
@@ -496,9 +598,38 @@ __device__ __forceinline__ int stable_rank_f(const float* keys, int n, int i) {
   return r;
 }
 
+// One row of the destination: premultiplied RGBX (4 bytes per pixel), or an
+// 8-bit alpha mask (A8) read as (a, a, a, a) and written as the alpha byte.
+// A mask render paints a white opaque colour with NormalBlend onto a
+// transparent mask, so every pixel keeps four equal channels and the alpha
+// byte holds the whole RGBX value.
+template <bool A8>
+struct PxRef {
+  unsigned char* p;
+  __device__ __forceinline__ operator uint32_t() const {
+    if (A8) return (uint32_t)*p * 0x01010101u;
+    return *reinterpret_cast<const uint32_t*>(p);
+  }
+  __device__ __forceinline__ const PxRef& operator=(uint32_t v) const {
+    if (A8) *p = (unsigned char)(v >> 24);
+    else *reinterpret_cast<uint32_t*>(p) = v;
+    return *this;
+  }
+};
+template <bool A8>
+struct RowPx {
+  unsigned char* base;
+  __device__ __forceinline__ PxRef<A8> operator[](long long x) const { return PxRef<A8>{base + x * (A8 ? 1 : 4)}; }
+};
+template <bool A8>
+__device__ __forceinline__ RowPx<A8> row_of(const PathJob& J, long long y) {
+  return RowPx<A8>{J.img + y * J.W * (A8 ? 1 : 4)};
+}
+
 // Linear-index clear of [y*W + a, y*W + b) (clearUnsafe :1433-1440 with
 // startY == toY).  Pixels before row y are recorded for the cross-row pass.
-__device__ void clear_span_linear(const PathJob& J, const Arena& A, int job, uint32_t* row,
+template <bool A8>
+__device__ void clear_span_linear(const PathJob& J, const Arena& A, int job, RowPx<A8> row,
                                   long long y, long long a, long long b, int lane) {
   if (a == J.W) return;
   if (b <= a) return;
@@ -517,11 +648,13 @@ __device__ void clear_span_linear(const PathJob& J, const Arena& A, int job, uin
   }
 }
 
-template <int MAXH, int XT>
-__device__ void process_row(const PathJob& J, const Arena& A, const uint8_t* tbl, int job,
+// Draws row y of job J.  Returns false, having drawn nothing, when the row's
+// crossings exceed MAXH (the caller retries it with a larger scratch).
+template <int MAXH, int XT, bool A8>
+__device__ bool process_row(const PathJob& J, const Arena& A, const uint8_t* tbl, int job,
                             long long y, RowScratch<MAXH, XT>& S, int lane) {
   const long long W = J.W;
-  uint32_t* row = reinterpret_cast<uint32_t*>(J.img) + y * W;
+  const RowPx<A8> row = row_of<A8>(J, y);
   const int mode = J.mode;
   const uint32_t rgbx = J.rgbx;
   const bool maskMode = mode == kMask;
@@ -536,27 +669,17 @@ __device__ void process_row(const PathJob& J, const Arena& A, const uint8_t* tbl
   const float bottom = (float)(k == J.nb - 1 ? J.pathHeight : J.startY + (k + 1) * (long long)J.ph);
   const float4* SG = A.segs + J.seg_off;
   const int* SW = A.segw + J.seg_off;
-  const uint2* SB = A.segband + J.seg_off;
-  const uint32_t kk = (uint32_t)k;
-  const int nseg = J.nseg;
+  const int* BL = A.bandseg + bd.off;  // the band's segments, ascending
+  const int nb = bd.count;
   Entry* E = S.ent;
 
   // a band of exactly two entries: are they two non-intersecting segments
   // spanning the band (:1250-1262)?
   bool two = false;
-  if (bd.count == 2) {
-    int got = 0;
-    for (int c0 = 0; c0 < nseg && got < 2; c0 += 32) {
-      int i = c0 + lane;
-      bool in = false;
-      if (i < nseg) {
-        uint2 r = SB[i];
-        in = r.x <= kk && kk <= r.y;
-      }
-      unsigned m = __ballot_sync(0xffffffffu, in);
-      int pos = got + __popc(m & lt);
-      if (in && pos < 2) E[pos] = make_entry(SG[i], SW[i], top, bottom);
-      got += __popc(m);
+  if (nb == 2) {
+    if (lane < 2) {
+      const int i = BL[lane];
+      E[lane] = make_entry(SG[i], SW[i], top, bottom);
     }
     __syncwarp();
     Entry e0 = E[0], e1 = E[1];
@@ -582,7 +705,7 @@ __device__ void process_row(const PathJob& J, const Arena& A, const uint8_t* tbl
       if (x >= minX && x < maxX) row[x] = op_fill(mode, tbl, row[x], rgbx);
       else if (maskMode) row[x] = 0u;
     }
-    return;
+    return true;
   }
 
   // entries overlapping the scanline [y, y+1) in band order (:1677-1693)
@@ -591,17 +714,15 @@ __device__ void process_row(const PathJob& J, const Arena& A, const uint8_t* tbl
   if (two) {
     n = 2;
   } else {
-    for (int c0 = 0; c0 < nseg; c0 += 32) {
-      int i = c0 + lane;
+    for (int c0 = 0; c0 < nb; c0 += 32) {
+      const int j = c0 + lane;
       bool pred = false, ns = false;
       Entry e;
-      if (i < nseg) {
-        uint2 r = SB[i];
-        if (r.x <= kk && kk <= r.y) {
-          e = make_entry(SG[i], SW[i], top, bottom);
-          pred = !(e.by <= scanTop || e.ay >= scanBottom);
-          ns = e.ay > scanTop || e.by < scanBottom;
-        }
+      if (j < nb) {
+        const int i = BL[j];
+        e = make_entry(SG[i], SW[i], top, bottom);
+        pred = !(e.by <= scanTop || e.ay >= scanBottom);
+        ns = e.ay > scanTop || e.by < scanBottom;
       }
       unsigned m = __ballot_sync(0xffffffffu, pred);
       if (__any_sync(0xffffffffu, pred && ns)) allSpan = false;
@@ -611,13 +732,7 @@ __device__ void process_row(const PathJob& J, const Arena& A, const uint8_t* tbl
     }
   }
   for (int i = lane; i < min(n, MAXH); i += 32) S.idx[i] = i;
-  if (n > MAXH) {  // too many crossings for this kernel: hand the row to the wide kernel
-    if (lane == 0) {
-      unsigned long long slot = atomicAdd(&A.counters[kCtrOvfRows], 1ull);
-      if ((long long)slot < A.ovf_cap) A.ovf_rows[slot] = ((long long)job << 32) | y;
-    }
-    return;
-  }
+  if (n > MAXH) return false;  // too many crossings for this scratch
   __syncwarp();
 
   // (ii) trapezoid fast path (:1695-1872)
@@ -750,7 +865,7 @@ __device__ void process_row(const PathJob& J, const Arena& A, const uint8_t* tbl
         filledTo = nim_int(ceilf(nmax(tr0, tr1)));
       }
       if (maskMode) clear_span_linear(J, A, job, row, y, min(filledTo, W), W, lane);
-      return;
+      return true;
     }
   }
 
@@ -913,19 +1028,28 @@ __device__ void process_row(const PathJob& J, const Arena& A, const uint8_t* tbl
       }
     }
   }
+  return true;
 }
 
 constexpr int kFastMaxH = 256, kFastXT = 1024, kFastWarps = 4;
 constexpr int kWideMaxH = 2048, kWideXT = 1024;
 
-__global__ void __launch_bounds__(kFastWarps * 32) k_rows(PathJob* jobs, int njobs, Arena A,
-                                                          const uint8_t* tbl, long long totalRows) {
+// The persistent row kernel: every warp takes work items -- RPI consecutive
+// rows of one job -- from a device queue (one atomic per item) until the
+// queue is empty, so jobs of uneven height share the GPU evenly.  Rows whose
+// crossings exceed MAXH go to the wide kernel.
+template <int MAXH, int XT, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_rows(PathJob* jobs, int njobs, Arena A,
+                                                     const uint8_t* tbl, long long totalItems, int rpi) {
   extern __shared__ __align__(16) unsigned char rsm[];
-  using Scratch = RowScratch<kFastMaxH, kFastXT>;
+  using Scratch = RowScratch<MAXH, XT>;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   Scratch& S = reinterpret_cast<Scratch*>(rsm)[warp];
-  for (long long item = (long long)blockIdx.x * kFastWarps + warp; item < totalRows;
-       item += (long long)gridDim.x * kFastWarps) {
+  while (true) {
+    unsigned long long q = 0;
+    if (lane == 0) q = atomicAdd(&A.counters[kCtrQueue], 1ull);
+    const long long item = (long long)__shfl_sync(0xffffffffu, q, 0);
+    if (item >= totalItems) break;
     int lo = 0, hi = njobs - 1;  // job with row_off <= item
     while (lo < hi) {
       int mid = (lo + hi + 1) >> 1;
@@ -933,18 +1057,31 @@ __global__ void __launch_bounds__(kFastWarps * 32) k_rows(PathJob* jobs, int njo
       else hi = mid - 1;
     }
     const PathJob& J = jobs[lo];
-    const long long y = item - J.row_off;
-    if (J.status != kOk || y >= J.H) continue;
-    if (y < J.startY || y >= J.pathHeight) {
-      if (J.mode == kMask) {  // :1910-1912
-        uint32_t* row = reinterpret_cast<uint32_t*>(J.img) + y * J.W;
-        for (long long x = lane; x < J.W; x += 32) row[x] = 0u;
+    if (J.status != kOk) continue;
+    const long long y0 = (item - J.row_off) * rpi;
+    for (long long y = y0; y < y0 + rpi && y < J.H; y++) {
+      if (y < J.startY || y >= J.pathHeight) {
+        if (J.mode == kMask) {  // :1910-1912 (never an A8 job)
+          const RowPx<false> row = row_of<false>(J, y);
+          for (long long x = lane; x < J.W; x += 32) row[x] = 0u;
+        }
+        continue;
       }
-      continue;
+      const bool ok = J.a8 ? process_row<MAXH, XT, true>(J, A, tbl, lo, y, S, lane)
+                           : process_row<MAXH, XT, false>(J, A, tbl, lo, y, S, lane);
+      if (!ok && lane == 0) {
+        // too many crossings for this kernel: hand the row to the wide kernel
+        unsigned long long slot = atomicAdd(&A.counters[kCtrOvfRows], 1ull);
+        if ((long long)slot < A.ovf_cap) A.ovf_rows[slot] = ((long long)lo << 32) | y;
+      }
+      __syncwarp();
     }
-    process_row<kFastMaxH, kFastXT>(J, A, tbl, lo, y, S, lane);
   }
 }
+
+constexpr int kSmallMaxH = 32, kSmallXT = 256, kSmallWarps = 8;
+template __global__ void k_rows<kFastMaxH, kFastXT, kFastWarps>(PathJob*, int, Arena, const uint8_t*, long long, int);
+template __global__ void k_rows<kSmallMaxH, kSmallXT, kSmallWarps>(PathJob*, int, Arena, const uint8_t*, long long, int);
 
 // Rows whose crossings exceed the fast kernel's capacity: one warp per CTA
 // with room for kWideMaxH crossings.
@@ -967,7 +1104,9 @@ __global__ void __launch_bounds__(32) k_rows_wide(PathJob* jobs, Arena A, const 
       if (lane == 0) J.status = kErrRowTooComplex;
       continue;
     }
-    process_row<kWideMaxH, kWideXT>(J, A, tbl, job, y, S, lane);
+    const bool ok = J.a8 ? process_row<kWideMaxH, kWideXT, true>(J, A, tbl, job, y, S, lane)
+                         : process_row<kWideMaxH, kWideXT, false>(J, A, tbl, job, y, S, lane);
+    if (!ok && lane == 0) J.status = kErrRowTooComplex;
   }
 }
 
@@ -984,8 +1123,74 @@ __global__ void k_xclears(PathJob* jobs, Arena A) {
   }
 }
 
+// Dense scenes: one warp owns one canvas row and paints every path of its run
+// into it in submission order, so each pixel sees the paths in the order the
+// reference's sequence of fillPath/strokePath calls applies them.  A path that
+// failed in setup stops its run there (the reference raises at that call);
+// rows with more crossings than the shared-memory scratch holds take a
+// per-warp global-memory scratch of kWideMaxH.
+__global__ void __launch_bounds__(kFastWarps * 32) k_scene(PathJob* jobs, const SceneRun* runs, int nruns,
+                                                           long long totalRows, Arena A, const uint8_t* tbl,
+                                                           unsigned char* wide, long long wideSlots) {
+  extern __shared__ __align__(16) unsigned char rsm[];
+  using Scratch = RowScratch<kFastMaxH, kFastXT>;
+  using Wide = RowScratch<kWideMaxH, kWideXT>;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  Scratch& S = reinterpret_cast<Scratch*>(rsm)[warp];
+  const long long gw = (long long)blockIdx.x * kFastWarps + warp;
+  for (long long item = gw; item < totalRows; item += (long long)gridDim.x * kFastWarps) {
+    int lo = 0, hi = nruns - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (runs[mid].row_off <= item) lo = mid;
+      else hi = mid - 1;
+    }
+    const SceneRun R = runs[lo];
+    const long long y = item - R.row_off;
+    if (y >= R.H) continue;
+    for (int j = R.j0; j < R.j1; j++) {
+      const PathJob& J = jobs[j];
+      const int st = J.status;
+      if (st != kOk) {
+        if (st == kNothing) continue;
+        break;
+      }
+      if (y < J.startY || y >= J.pathHeight) continue;
+      bool ok = process_row<kFastMaxH, kFastXT, false>(J, A, tbl, j, y, S, lane);
+      if (!ok && gw < wideSlots) {
+        __syncwarp();
+        ok = process_row<kWideMaxH, kWideXT, false>(J, A, tbl, j, y, reinterpret_cast<Wide*>(wide)[gw], lane);
+      }
+      if (!ok && lane == 0) atomicMin(&A.counters[kCtrRowErr], (unsigned long long)j);
+      __syncwarp();
+    }
+  }
+}
+
+size_t scene_wide_bytes() { return sizeof(RowScratch<kWideMaxH, kWideXT>); }
+int scene_ctas_per_sm() { return 2; }  // two CTAs of kFastWarps row scratches fit one SM's shared memory
+
 size_t rows_smem_fast() { return sizeof(RowScratch<kFastMaxH, kFastXT>) * kFastWarps; }
 size_t rows_smem_wide() { return sizeof(RowScratch<kWideMaxH, kWideXT>); }
 int rows_warps_fast() { return kFastWarps; }
+
+// Row kernel variants: 0 = 256 crossings / 1024-px coverage tiles / 4 warps
+// per CTA, 1 = 32 crossings / 256-px tiles / 8 warps (small paths such as
+// glyphs: eight times less shared memory per warp, more warps per SM).
+const void* rows_kernel(int v) {
+  return v == 1 ? (const void*)k_rows<kSmallMaxH, kSmallXT, kSmallWarps>
+                : (const void*)k_rows<kFastMaxH, kFastXT, kFastWarps>;
+}
+size_t rows_smem(int v) {
+  return v == 1 ? sizeof(RowScratch<kSmallMaxH, kSmallXT>) * kSmallWarps : rows_smem_fast();
+}
+int rows_warps(int v) { return v == 1 ? kSmallWarps : kFastWarps; }
+void launch_rows(int v, unsigned blocks, cudaStream_t st, PathJob* jobs, int njobs, const Arena& A,
+                 const uint8_t* tbl, long long items, int rpi) {
+  if (v == 1)
+    k_rows<kSmallMaxH, kSmallXT, kSmallWarps><<<blocks, kSmallWarps * 32, rows_smem(1), st>>>(jobs, njobs, A, tbl, items, rpi);
+  else
+    k_rows<kFastMaxH, kFastXT, kFastWarps><<<blocks, kFastWarps * 32, rows_smem(0), st>>>(jobs, njobs, A, tbl, items, rpi);
+}
 
 }  // namespace pxg

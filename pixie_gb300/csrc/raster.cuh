@@ -5,10 +5,10 @@
 // path commands into primitives (lines, quadratics, cubics; arcs and stroke
 // outlines arrive as lines), the setup kernel (one CTA per job) flattens them
 // into pixie's segments, reduces the bounds and derives the row-band
-// partitions (each segment's band range, each band's entry count and
-// anti-aliasing flag); the row kernel (one warp per image row) collects its
-// band's entries in segment order, runs the reference's per-row decision and
-// writes the pixels.
+// partitions (each band's entry list in segment order, its count and
+// anti-aliasing flag); the row kernel (one warp per image row) reads its
+// band's entries, runs the reference's per-row decision and writes the
+// pixels.
 #pragma once
 #include <vector_types.h>
 
@@ -28,7 +28,8 @@ struct Entry {  // PartitionEntry (paths.nim:28-31): clipped segment, line m/b, 
   int w, pad;
 };
 
-struct Band {  // Partition (paths.nim:33-36): entry count and flags
+struct Band {  // Partition (paths.nim:33-36): its entries' segment indices, count and flags
+  long long off;  // first index in Arena::bandseg
   int count, flags;
 };
 enum BandFlags { kBandAA = 1, kBandTwoSpanning = 2 };
@@ -46,16 +47,19 @@ enum JobStatus {
 
 struct PathJob {
   // inputs (host)
+  const Prim* prims;  // device primitives of the job's path: prims[prim_off ..]
+  long long pc_off;   // the job's slice of Arena::primcnt
   long long prim_off;
   int nprims, winding;
   float ems;  // errorMarginSq = pow(0.2 / pixelScale, 2)  (paths.nim:667)
   int identity, mode;
   uint32_t rgbx;  // premultiplied paint colour
   float mat[9];
-  int pad0;
-  uint8_t* img;  // RGBX, row-major, W*H pixels
+  int group;     // lanes that flatten one curve together (1, 2, 4, 8, 16 or 32)
+  int a8;        // img is an 8-bit alpha mask (white NormalBlend fills only), else RGBX
+  uint8_t* img;  // RGBX or A8, row-major, W*H pixels
   long long W, H;
-  long long row_off;  // prefix of work rows over the batch
+  long long row_off;  // prefix of row-kernel work items over the batch
   // outputs (setup kernel)
   int status, nseg, nb;
   uint32_t ph;
@@ -63,8 +67,23 @@ struct PathJob {
   long long startX, startY, pathWidth, pathHeight;
 };
 
+// Paths [j0, j1) of the job array painted in order onto one canvas (the
+// jobs' img/W/H).  A launch may carry several runs on distinct canvases.
+struct SceneRun {
+  long long row_off;  // prefix of canvas rows over the launch's runs
+  long long H;
+  int j0, j1;
+};
+
+// One mask of a batch drawn onto a page at an integer offset.
+struct MaskDraw {
+  long long off;  // byte offset of the mask in the batch's mask buffer
+  long long x, y;
+  int w, h;
+};
+
 enum ArenaCounter {
-  kCtrSegs = 0, kCtrBands, kCtrOvfRows, kCtrXClears, kNumCounters
+  kCtrSegs = 0, kCtrBands, kCtrOvfRows, kCtrXClears, kCtrBandSegs, kCtrRowErr, kCtrQueue, kNumCounters
 };
 
 struct Arena {
@@ -75,6 +94,10 @@ struct Arena {
   long long seg_cap;
   Band* bands;
   long long band_cap;
+  int* bandseg;    // per band, the indices (within the job) of its segments, ascending
+  long long bandseg_cap;
+  int* primcnt;    // per primitive: segments emitted, then their exclusive prefix
+  long long primcnt_cap;
   unsigned long long* counters;
   long long* ovf_rows;  // packed (job << 32 | y) rows whose crossings exceed the fast kernel
   long long ovf_cap;

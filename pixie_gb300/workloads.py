@@ -171,3 +171,23 @@ def glyph_batch(seed: int, n: int = 4096, page: int = 4096):
     glyphs = [glyph(seed * 100003 + i) for i in range(n)]
     pos = randint(seed * 13 + 1, 2 * n, 0, page - 1).reshape(n, 2)
     return glyphs, pos
+
+
+# -- serving ----------------------------------------------------------------------
+def serving_job(seed: int, min_side: int = 256, max_side: int = 4096, min_paths: int = 10,
+                max_paths: int = 5000, blur_share: float = 0.2):
+    """One render job: canvas side log-uniform in [min_side, max_side], a dense
+    scene of min_paths..max_paths paths over the canvas, and on blur_share of
+    jobs a blur of radius uniform in {2..32}."""
+    a = uniform(seed * 2654435761 + 17, 4, 0.0, 1.0)
+    side = int(min_side * math.exp(float(a[0]) * math.log(max_side / min_side)))
+    n = min_paths + int(float(a[1]) * (max_paths - min_paths + 1))
+    n = min(n, max_paths)
+    blur = 2 + int(float(a[2]) * 31) if float(a[3]) < blur_share else 0
+    return {"side": side, "items": dense_scene(seed, n_paths=n, size=float(side)), "blur": blur}
+
+
+def poisson_arrivals(seed: int, rate: float, n: int) -> np.ndarray:
+    """n arrival times (seconds from 0) of a Poisson process of `rate` jobs/s."""
+    u = uniform01(seed * 7 + 3, n).astype(np.float64)
+    return np.cumsum(-np.log1p(-u) / rate)
