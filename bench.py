@@ -122,8 +122,11 @@ def dist_setup():
     if ws > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+        else:  # host-only replicas (tests of the N>1 timing path)
+            dist.init_process_group("gloo")
     return ws, rank, local
 
 
@@ -138,7 +141,8 @@ def max_over_ranks(ws, v):
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -587,6 +591,22 @@ def run_case(case: str):
         for _ in range(2):
             px.fill_paths_batch(imgs, [g[0] for g in glyphs], [[1, 1, 1, 1]] * len(glyphs),
                                 winding_rules=[g[3] for g in glyphs])
+    elif case in ("scene", "scene_small"):  # dense scene: 2000 paths on 1024^2 (small: 400 on 512^2)
+        n, side = (2000, 1024) if case == "scene" else (400, 512)
+        sc, _ = record_scene(px, wl.dense_scene(7, n_paths=n, size=float(side)))
+        img = px.Image(side, side)
+        for _ in range(2):
+            img.draw_scene(sc)
+    elif case == "masks":  # 4096 glyph masks rendered, then composited onto a 4096^2 page
+        glyphs, pos = wl.glyph_batch(7, n=4096)
+        m = px.Masks()
+        for cmds, w, h, wind in glyphs:
+            m.add_path(cmds, w, h, None, wind)
+        px.autotune(False)
+        page = px.Image(4096, 4096)
+        for _ in range(2):
+            m.render()
+            page.draw_masks(m, pos)
     else:
         raise SystemExit(f"unknown case {case}")
     px.synchronize()
@@ -606,7 +626,7 @@ def main():
     ap.add_argument("--no-fill", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--case", default=None,
-                    help="run one small operation for profiling: fill512 | blur64 | draw | glyphs")
+                    help="run one small operation for profiling: fill512 | blur64 | draw | glyphs | scene | scene_small | masks")
     args = ap.parse_args()
     if args.case:
         run_case(args.case)

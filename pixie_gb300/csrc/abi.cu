@@ -1315,7 +1315,7 @@ int pxg_scene_fill_path(pxg_scene* sc, const float* cmds, int64_t n, const float
     if (!paint_color(color, opacity, blend, rgbx)) return;
     const float* mat = transform ? transform : kIdent;
     float ps = pixel_scale(mat);
-    std::vector<Prim> prims;
+    thread_local std::vector<Prim> prims;  // keeps its capacity between recordings
     build_fill_prims(cmds, n, ps, prims);
     PathJob j = make_job(nullptr, rgbx, blend, mat, ps, winding);
     j.prim_off = (long long)sc->prims.size();
@@ -1339,7 +1339,7 @@ int pxg_scene_stroke_path(pxg_scene* sc, const float* cmds, int64_t n, const flo
     if (!paint_color(color, opacity, blend, rgbx)) return;
     const float* mat = transform ? transform : kIdent;
     float ps = pixel_scale(mat);
-    std::vector<Prim> prims;
+    thread_local std::vector<Prim> prims;  // keeps its capacity between recordings
     build_stroke_prims(cmds, n, ps, width, cap, join, miterLimit, dashes, nd, prims);
     PathJob j = make_job(nullptr, rgbx, blend, mat, ps, 0);
     j.prim_off = (long long)sc->prims.size();

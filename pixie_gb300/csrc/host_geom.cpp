@@ -461,16 +461,28 @@ void build_stroke_prims(const float* cmds, int64_t n, float ps, float strokeWidt
     o.c = c;
     return o;
   };
+  // The commands of ellipse(c, hs, hs) are Move + 4 cubics + Close, a closed
+  // arc-free subpath: the command walk turns them into exactly these four
+  // cubic primitives (the last cubic ends on the start point, so no closing
+  // line), built here directly.
   auto emit_circle = [&](P2 c) {
     const double mx = kCircleK * (double)hs, my = kCircleK * (double)hs;
     const float cx = c.x, cy = c.y;
-    float e[] = {(float)kMove, cx + hs, cy,
-                 (float)kCubic, cx + hs, (float)(cy + my), (float)(cx + mx), cy + hs, cx, cy + hs,
-                 (float)kCubic, (float)(cx - mx), cy + hs, cx - hs, (float)(cy + my), cx - hs, cy,
-                 (float)kCubic, cx - hs, (float)(cy - my), (float)(cx - mx), cy - hs, cx, cy - hs,
-                 (float)kCubic, (float)(cx + mx), cy - hs, cx + hs, (float)(cy - my), cx + hs, cy,
-                 (float)kClose};
-    walk_commands(e, (int64_t)(sizeof e / sizeof e[0]), true, ems, &out);
+    const float q[4][8] = {
+        {cx + hs, cy, cx + hs, (float)(cy + my), (float)(cx + mx), cy + hs, cx, cy + hs},
+        {cx, cy + hs, (float)(cx - mx), cy + hs, cx - hs, (float)(cy + my), cx - hs, cy},
+        {cx - hs, cy, cx - hs, (float)(cy - my), (float)(cx - mx), cy - hs, cx, cy - hs},
+        {cx, cy - hs, (float)(cx + mx), cy - hs, cx + hs, (float)(cy - my), cx + hs, cy}};
+    for (int k = 0; k < 4; k++) {
+      Prim p;
+      memset(&p, 0, sizeof p);
+      p.kind = kPrimCubic;
+      for (int i = 0; i < 4; i++) {
+        p.x[i] = q[k][2 * i];
+        p.y[i] = q[k][2 * i + 1];
+      }
+      out.push_back(p);
+    }
   };
   auto rect = [&](P2 a, P2 b) {  // :1943-1965
     P2 t = unit(sub(b, a));
