@@ -100,10 +100,13 @@ void launch_rows(int v, unsigned blocks, cudaStream_t st, PathJob* jobs, int njo
                  const uint8_t* tbl, long long items, int rpi);
 __global__ void k_rows_wide(PathJob* jobs, Arena A, const uint8_t* tbl);
 __global__ void k_xclears(PathJob* jobs, Arena A);
-__global__ void k_scene(PathJob* jobs, const SceneRun* runs, int nruns, long long totalRows, Arena A,
-                        const uint8_t* tbl, unsigned char* wide, long long wideSlots);
+const void* scene_kernel(int v);
+size_t scene_smem(int v);
+int scene_warps();
+void launch_scene(int v, unsigned blocks, cudaStream_t st, PathJob* jobs, const SceneRun* runs, int nruns,
+                  long long items, const Arena& A, const uint8_t* tbl, unsigned char* wide, long long slots,
+                  int sliceW);
 size_t scene_wide_bytes();
-int scene_ctas_per_sm();
 int draw_masks_tiles();
 void launch_draw_masks(int tile, uint32_t* page, long long W, long long H, const void* items, int n,
                        const uint8_t* masks, int mode, const uint8_t* tbl, cudaStream_t st);
@@ -212,6 +215,8 @@ struct Ctx {
   float last_ms = 0;
   long long stats[4] = {0, 0, 0, 0};  // last fill launch: paths, prims, segments, band entries
   int rows_ctas_per_sm[2] = {1, 1};  // resident CTAs of each row-kernel variant
+  int scene_ctas_per_sm[2] = {1, 1};
+  int scene_variant = 1, scene_slice = 256;  // scene kernel configuration
   bool blocking = true;  // image operations wait for their GPU work
   std::map<int64_t, uint16_t*> weights;  // gaussian weights per radius, on the device
 };
@@ -248,7 +253,12 @@ void init_locked(int device) {
     g.rows_ctas_per_sm[v] = std::max(1, per);
   }
   CU(cudaFuncSetAttribute(k_rows_wide, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem_wide()));
-  CU(cudaFuncSetAttribute(k_scene, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem_fast()));
+  for (int v = 0; v < 2; v++) {
+    CU(cudaFuncSetAttribute(scene_kernel(v), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scene_smem(v)));
+    int per = 0;
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, scene_kernel(v), scene_warps() * 32, scene_smem(v)));
+    g.scene_ctas_per_sm[v] = std::max(1, per);
+  }
   g.setupSmemMax = allow_max_smem((const void*)k_setup);
   g.blurSmemMax = std::min(allow_max_smem((const void*)k_blur_x), allow_max_smem((const void*)k_blur_y));
   g.blurSmemMax = std::min(g.blurSmemMax, allow_max_smem((const void*)k_blurf_x));
@@ -632,6 +642,7 @@ void run_scene_runs(std::vector<HostRun>& runs) {
       if (r.status != kOk || r.j0 >= r.j1) continue;
       SceneRun s;
       s.row_off = rows;
+      s.W = r.canvas->width;
       s.H = r.canvas->height;
       s.j0 = (int)dev.size();
       for (size_t j = r.j0; j < r.j1; j++) {
@@ -647,7 +658,7 @@ void run_scene_runs(std::vector<HostRun>& runs) {
         dev.push_back(pj);
       }
       s.j1 = (int)dev.size();
-      rows += s.H;
+      rows += s.H * ((s.W + g.scene_slice - 1) / g.scene_slice);
       maxH = std::max<long long>(maxH, s.H);
       sr.push_back(s);
       which.push_back(ri);
@@ -656,8 +667,9 @@ void run_scene_runs(std::vector<HostRun>& runs) {
     const int nj = (int)dev.size();
     const int maxBands = setup_max_bands(maxH);
     ensure_arena(seg_need, list_need, (long long)nj * maxBands, pc, 1);
-    const int wpb = rows_warps_fast();
-    long long blocks = std::min<long long>((rows + wpb - 1) / wpb, (long long)g.nsm * scene_ctas_per_sm());
+    const int sv = g.scene_variant;
+    const int wpb = scene_warps();
+    long long blocks = std::min<long long>((rows + wpb - 1) / wpb, (long long)g.nsm * g.scene_ctas_per_sm[sv]);
     blocks = std::max<long long>(blocks, 1);
     const long long slots = blocks * wpb;
     if (slots > g.wide_slots) {
@@ -672,8 +684,8 @@ void run_scene_runs(std::vector<HostRun>& runs) {
       k_setup<<<nj, 256, (size_t)maxBands * 8, g.stream>>>(S.dj, S.A, maxBands); note_launch();
       CU(cudaGetLastError());
     }
-    k_scene<<<(unsigned)blocks, wpb * 32, rows_smem_fast(), g.stream>>>(
-        S.dj, reinterpret_cast<const SceneRun*>(S.extra), (int)sr.size(), rows, S.A, g.tbl, g.wide, g.wide_slots);
+    launch_scene(sv, (unsigned)blocks, g.stream, S.dj, reinterpret_cast<const SceneRun*>(S.extra), (int)sr.size(),
+                 rows, S.A, g.tbl, g.wide, g.wide_slots, g.scene_slice);
     note_launch();
     CU(cudaGetLastError());
     CU(cudaMemcpyAsync(g.h_up, g.d_up, S.jobsBytes + S.ctrBytes, cudaMemcpyDeviceToHost, g.stream));
@@ -1611,6 +1623,15 @@ int pxg_server_stats(const pxg_server* sv, int64_t* out6) {
   out6[4] = (int64_t)sv->queue.size();
   out6[5] = (int64_t)sv->active.size();
   return 0;
+}
+
+int pxg_scene_config(int variant, int slice_width) {
+  return guarded([&] {
+    if (variant < 0 || variant > 1 || slice_width < 32 || slice_width > (1 << 20))
+      throw ApiError{"Invalid scene configuration"};
+    g.scene_variant = variant;
+    g.scene_slice = slice_width;
+  });
 }
 
 int pxg_autotune(int enable) {

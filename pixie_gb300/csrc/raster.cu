@@ -630,11 +630,12 @@ __device__ __forceinline__ RowPx<A8> row_of(const PathJob& J, long long y) {
 // startY == toY).  Pixels before row y are recorded for the cross-row pass.
 template <bool A8>
 __device__ void clear_span_linear(const PathJob& J, const Arena& A, int job, RowPx<A8> row,
-                                  long long y, long long a, long long b, int lane) {
+                                  long long y, long long a, long long b, int lane, long long xa,
+                                  long long xb) {
   if (a == J.W) return;
   if (b <= a) return;
-  for (long long x = max(a, 0LL) + lane; x < b; x += 32) row[x] = 0u;
-  if (a < 0 && lane == 0) {
+  for (long long x = max(max(a, 0LL), xa) + lane; x < min(b, xb); x += 32) row[x] = 0u;
+  if (a < 0 && lane == 0 && xa == 0) {
     long long lo = y * J.W + a, hi = y * J.W + min(b, 0LL);
     if (lo < 0) lo = 0;
     if (hi > lo) {
@@ -648,11 +649,13 @@ __device__ void clear_span_linear(const PathJob& J, const Arena& A, int job, Row
   }
 }
 
-// Draws row y of job J.  Returns false, having drawn nothing, when the row's
-// crossings exceed MAXH (the caller retries it with a larger scratch).
+// Draws the pixels [xa, xb) of row y of job J (the whole row: 0, W).
+// Returns false, having drawn nothing, when the row's crossings exceed MAXH
+// (the caller retries it with a larger scratch).
 template <int MAXH, int XT, bool A8>
 __device__ bool process_row(const PathJob& J, const Arena& A, const uint8_t* tbl, int job,
-                            long long y, RowScratch<MAXH, XT>& S, int lane) {
+                            long long y, RowScratch<MAXH, XT>& S, int lane, long long xa,
+                            long long xb) {
   const long long W = J.W;
   const RowPx<A8> row = row_of<A8>(J, y);
   const int mode = J.mode;
@@ -701,7 +704,7 @@ __device__ bool process_row(const PathJob& J, const Arena& A, const uint8_t* tbl
   if (two && !(bd.flags & kBandAA)) {
     long long minX = min(max(nim_int(E[0].ax), 0LL), W);
     long long maxX = min(max(nim_int(E[1].ax), 0LL), W);
-    for (long long x = lane; x < W; x += 32) {
+    for (long long x = xa + lane; x < xb; x += 32) {
       if (x >= minX && x < maxX) row[x] = op_fill(mode, tbl, row[x], rgbx);
       else if (maskMode) row[x] = 0u;
     }
@@ -818,7 +821,7 @@ __device__ bool process_row(const PathJob& J, const Arena& A, const uint8_t* tbl
           const bool inv = tl0 < tl1;
           const float sliverStart = nmin(tl0, tl1), rectStart = leftMaxX;
           const long long xs = nim_int(sliverStart), xe = nim_int(ceilf(rectStart));
-          for (long long x = max(xs, 0LL) + lane; x < min(xe, W); x += 32) {
+          for (long long x = max(max(xs, 0LL), xa) + lane; x < min(min(xe, W), xb); x += 32) {
             float prevPen = x == xs ? sliverStart : (float)x;
             float pen = (float)(x + 1);
             float rightRectArea = 0;
@@ -839,7 +842,7 @@ __device__ bool process_row(const PathJob& J, const Arena& A, const uint8_t* tbl
           const bool inv = tr0 > tr1;
           const float rectEnd = rightMinX, sliverEnd = nmax(tr0, tr1);
           const long long xs = nim_int(rectEnd), xe = nim_int(ceilf(sliverEnd));
-          for (long long x = max(xs, 0LL) + lane; x < min(xe, W); x += 32) {
+          for (long long x = max(max(xs, 0LL), xa) + lane; x < min(min(xe, W), xb); x += 32) {
             float prevPen = x == xs ? rectEnd : (float)x;
             float pen = (float)(x + 1);
             float ap = fabsf(prevPen);
@@ -855,16 +858,16 @@ __device__ bool process_row(const PathJob& J, const Arena& A, const uint8_t* tbl
           }
         }
         {  // the fully covered middle (:1830-1835)
-          long long fb = min(max(leftCoverEnd, 0LL), W), fe = min(max(rightCoverBegin, 0LL), W);
+          long long fb = max(min(max(leftCoverEnd, 0LL), W), xa), fe = min(min(max(rightCoverBegin, 0LL), W), xb);
           for (long long x = fb + lane; x < fe; x += 32) row[x] = op_fill(mode, tbl, row[x], rgbx);
         }
         if (maskMode) {  // :1837-1845
           long long clearTo = nim_int(nmin(tl0, tl1));
-          clear_span_linear(J, A, job, row, y, min(filledTo, W), min(clearTo, W), lane);
+          clear_span_linear(J, A, job, row, y, min(filledTo, W), min(clearTo, W), lane, xa, xb);
         }
         filledTo = nim_int(ceilf(nmax(tr0, tr1)));
       }
-      if (maskMode) clear_span_linear(J, A, job, row, y, min(filledTo, W), W, lane);
+      if (maskMode) clear_span_linear(J, A, job, row, y, min(filledTo, W), W, lane, xa, xb);
       return true;
     }
   }
@@ -909,7 +912,45 @@ __device__ bool process_row(const PathJob& J, const Arena& A, const uint8_t* tbl
       S.a3[r] = S.a1[i];
     }
     __syncwarp();
-    if (lane == 0) {  // walk (:1298-1334)
+    // walk (:1298-1334).  Without two adjacent hits at the same position the
+    // look-ahead that skips a cancelling pair never fires, and every hit's
+    // part in the walk follows from the winding count before it (a prefix
+    // sum): the warp walks 32 hits at a time.  Otherwise lane 0 walks.
+    bool adjEq = false;
+    for (int i = lane; i + 1 < nh; i += 32) adjEq |= S.a2[i] == S.a2[i + 1];
+    if (!__any_sync(0xffffffffu, adjEq)) {
+      int ns = S.nsp, carry = 0, prevCarry = 0;
+      for (int c0 = 0; c0 < nh; c0 += 32) {
+        const int i = c0 + lane;
+        const bool valid = i < nh;
+        const int at = valid ? S.a2[i] : 0, w = valid ? S.a3[i] : 0;
+        int incl = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int t = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += t;
+        }
+        const int count = carry + incl - w;
+        const bool pos = valid && at > 0;
+        const bool fill = shouldFill(J.winding, count);
+        const bool shortcut = fill && i < nh - 1 && J.winding == 0 && count + w != 0;
+        const bool emit = pos && fill && !shortcut;
+        const bool upd = pos && (!fill || emit);  // hits that set prevAt
+        const unsigned um = __ballot_sync(0xffffffffu, upd);
+        const unsigned below = um & lt;
+        const int src = below ? 31 - __clz(below) : lane;
+        const int pa = __shfl_sync(0xffffffffu, at, src);
+        const int prevAt = below ? pa : prevCarry;
+        const unsigned em = __ballot_sync(0xffffffffu, emit);
+        const int slot = ns + __popc(em & lt);
+        if (emit && slot < RowScratch<MAXH, XT>::SPCAP) S.sp[slot] = make_int2(prevAt, at);
+        ns += __popc(em);
+        carry += __shfl_sync(0xffffffffu, incl, 31);
+        if (um) prevCarry = __shfl_sync(0xffffffffu, at, 31 - __clz(um));
+      }
+      __syncwarp();
+      if (lane == 0) S.nsp = ns;
+    } else if (lane == 0) {
       int i = 0, ns = S.nsp;
       long long count = 0;
       int prevAt = 0;
@@ -945,10 +986,11 @@ __device__ bool process_row(const PathJob& J, const Arena& A, const uint8_t* tbl
 
   if (aa) {
     // coverage row over [startX, startX + pathWidth) in tiles of XT pixels
-    const long long cx0 = J.startX, cx1 = J.startX + J.pathWidth;
+    const long long px0 = J.startX, px1 = J.startX + J.pathWidth;
+    const long long cx0 = max(px0, xa), cx1 = min(px1, xb);
     if (maskMode) {
-      for (long long x = lane; x < W; x += 32)
-        if (x < cx0 || x >= cx1) row[x] = 0u;
+      for (long long x = xa + lane; x < xb; x += 32)
+        if (x < px0 || x >= px1) row[x] = 0u;
     }
     for (long long tx0 = cx0; tx0 < cx1; tx0 += XT) {
       const long long tx1 = min(tx0 + (long long)XT, cx1);
@@ -1005,9 +1047,10 @@ __device__ bool process_row(const PathJob& J, const Arena& A, const uint8_t* tbl
       }
       __syncwarp();
       for (int i = lane; i < L; i += 32) {
-        uint32_t cov = (uint32_t)S.acc[i] & 255u;
-        long long x = tx0 + i;
-        row[x] = op_cov(mode, tbl, row[x], rgbx, cov);
+        const uint32_t cov = (uint32_t)S.acc[i] & 255u;
+        const long long x = tx0 + i;
+        // pixels op_cov leaves unchanged are neither read nor written
+        if (maskMode ? cov != 255u : cov != 0u) row[x] = op_cov(mode, tbl, row[x], rgbx, cov);
       }
       __syncwarp();
     }
@@ -1015,7 +1058,7 @@ __device__ bool process_row(const PathJob& J, const Arena& A, const uint8_t* tbl
     // fillHits with the single sample's spans (:1540-1591); spans are sorted
     // and disjoint, so a pixel is inside at most one.
     const long long startX = J.startX;
-    for (long long x = lane; x < W; x += 32) {
+    for (long long x = xa + lane; x < xb; x += 32) {
       bool inside = false;
       for (int j = 0; j < nsp && !inside; j++) {
         long long fs = S.sp[j].x / 256, fe = S.sp[j].y / 256;
@@ -1067,8 +1110,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_rows(PathJob* jobs, int njobs, A
         }
         continue;
       }
-      const bool ok = J.a8 ? process_row<MAXH, XT, true>(J, A, tbl, lo, y, S, lane)
-                           : process_row<MAXH, XT, false>(J, A, tbl, lo, y, S, lane);
+      const bool ok = J.a8 ? process_row<MAXH, XT, true>(J, A, tbl, lo, y, S, lane, 0, J.W)
+                           : process_row<MAXH, XT, false>(J, A, tbl, lo, y, S, lane, 0, J.W);
       if (!ok && lane == 0) {
         // too many crossings for this kernel: hand the row to the wide kernel
         unsigned long long slot = atomicAdd(&A.counters[kCtrOvfRows], 1ull);
@@ -1104,8 +1147,8 @@ __global__ void __launch_bounds__(32) k_rows_wide(PathJob* jobs, Arena A, const 
       if (lane == 0) J.status = kErrRowTooComplex;
       continue;
     }
-    const bool ok = J.a8 ? process_row<kWideMaxH, kWideXT, true>(J, A, tbl, job, y, S, lane)
-                         : process_row<kWideMaxH, kWideXT, false>(J, A, tbl, job, y, S, lane);
+    const bool ok = J.a8 ? process_row<kWideMaxH, kWideXT, true>(J, A, tbl, job, y, S, lane, 0, J.W)
+                         : process_row<kWideMaxH, kWideXT, false>(J, A, tbl, job, y, S, lane, 0, J.W);
     if (!ok && lane == 0) J.status = kErrRowTooComplex;
   }
 }
@@ -1123,22 +1166,31 @@ __global__ void k_xclears(PathJob* jobs, Arena A) {
   }
 }
 
-// Dense scenes: one warp owns one canvas row and paints every path of its run
-// into it in submission order, so each pixel sees the paths in the order the
-// reference's sequence of fillPath/strokePath calls applies them.  A path that
-// failed in setup stops its run there (the reference raises at that call);
-// rows with more crossings than the shared-memory scratch holds take a
-// per-warp global-memory scratch of kWideMaxH.
-__global__ void __launch_bounds__(kFastWarps * 32) k_scene(PathJob* jobs, const SceneRun* runs, int nruns,
-                                                           long long totalRows, Arena A, const uint8_t* tbl,
-                                                           unsigned char* wide, long long wideSlots) {
+// Dense scenes: a warp owns a slice of one canvas row (sliceW pixels) and
+// paints every path of its run into it in submission order, so each pixel
+// sees the paths in the order the reference's sequence of fillPath/strokePath
+// calls applies them.  Work items (row, slice) come from a device queue.  A
+// path that failed in setup stops its run there (the reference raises at that
+// call); a path whose bounds miss the slice is skipped (outside its bounds a
+// non-mask fill writes nothing); rows with more crossings than the
+// shared-memory scratch holds take a per-warp global-memory scratch of
+// kWideMaxH.  Each warp still computes the whole row's crossings and walk,
+// and draws only its slice.
+template <int MAXH, int XT, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_scene(PathJob* jobs, const SceneRun* runs, int nruns,
+                                                      long long totalItems, Arena A, const uint8_t* tbl,
+                                                      unsigned char* wide, long long wideSlots, int sliceW) {
   extern __shared__ __align__(16) unsigned char rsm[];
-  using Scratch = RowScratch<kFastMaxH, kFastXT>;
+  using Scratch = RowScratch<MAXH, XT>;
   using Wide = RowScratch<kWideMaxH, kWideXT>;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   Scratch& S = reinterpret_cast<Scratch*>(rsm)[warp];
-  const long long gw = (long long)blockIdx.x * kFastWarps + warp;
-  for (long long item = gw; item < totalRows; item += (long long)gridDim.x * kFastWarps) {
+  const long long gw = (long long)blockIdx.x * WARPS + warp;
+  while (true) {
+    unsigned long long q = 0;
+    if (lane == 0) q = atomicAdd(&A.counters[kCtrQueue], 1ull);
+    const long long item = (long long)__shfl_sync(0xffffffffu, q, 0);
+    if (item >= totalItems) break;
     int lo = 0, hi = nruns - 1;
     while (lo < hi) {
       int mid = (lo + hi + 1) >> 1;
@@ -1146,7 +1198,10 @@ __global__ void __launch_bounds__(kFastWarps * 32) k_scene(PathJob* jobs, const 
       else hi = mid - 1;
     }
     const SceneRun R = runs[lo];
-    const long long y = item - R.row_off;
+    const long long ns = (R.W + sliceW - 1) / sliceW;
+    const long long local = item - R.row_off;
+    const long long y = local / ns;
+    const long long xa = (local % ns) * sliceW, xb = min(xa + sliceW, R.W);
     if (y >= R.H) continue;
     for (int j = R.j0; j < R.j1; j++) {
       const PathJob& J = jobs[j];
@@ -1156,10 +1211,12 @@ __global__ void __launch_bounds__(kFastWarps * 32) k_scene(PathJob* jobs, const 
         break;
       }
       if (y < J.startY || y >= J.pathHeight) continue;
-      bool ok = process_row<kFastMaxH, kFastXT, false>(J, A, tbl, j, y, S, lane);
+      if (J.startX >= xb || J.startX + J.pathWidth <= xa) continue;
+      bool ok = process_row<MAXH, XT, false>(J, A, tbl, j, y, S, lane, xa, xb);
       if (!ok && gw < wideSlots) {
         __syncwarp();
-        ok = process_row<kWideMaxH, kWideXT, false>(J, A, tbl, j, y, reinterpret_cast<Wide*>(wide)[gw], lane);
+        ok = process_row<kWideMaxH, kWideXT, false>(J, A, tbl, j, y, reinterpret_cast<Wide*>(wide)[gw], lane,
+                                                    xa, xb);
       }
       if (!ok && lane == 0) atomicMin(&A.counters[kCtrRowErr], (unsigned long long)j);
       __syncwarp();
@@ -1167,8 +1224,30 @@ __global__ void __launch_bounds__(kFastWarps * 32) k_scene(PathJob* jobs, const 
   }
 }
 
+// Scene kernel variants: 0 = 256 crossings / 1024-px tiles, 1 = 128 / 256
+// (half the shared memory per warp: twice the warps per SM).
+constexpr int kSceneMaxH1 = 128, kSceneXT1 = 256;
+const void* scene_kernel(int v) {
+  return v == 1 ? (const void*)k_scene<kSceneMaxH1, kSceneXT1, kFastWarps>
+                : (const void*)k_scene<kFastMaxH, kFastXT, kFastWarps>;
+}
+size_t scene_smem(int v) {
+  return v == 1 ? sizeof(RowScratch<kSceneMaxH1, kSceneXT1>) * kFastWarps
+                : sizeof(RowScratch<kFastMaxH, kFastXT>) * kFastWarps;
+}
+int scene_warps() { return kFastWarps; }
+void launch_scene(int v, unsigned blocks, cudaStream_t st, PathJob* jobs, const SceneRun* runs, int nruns,
+                  long long items, const Arena& A, const uint8_t* tbl, unsigned char* wide, long long slots,
+                  int sliceW) {
+  if (v == 1)
+    k_scene<kSceneMaxH1, kSceneXT1, kFastWarps><<<blocks, kFastWarps * 32, scene_smem(1), st>>>(
+        jobs, runs, nruns, items, A, tbl, wide, slots, sliceW);
+  else
+    k_scene<kFastMaxH, kFastXT, kFastWarps><<<blocks, kFastWarps * 32, scene_smem(0), st>>>(
+        jobs, runs, nruns, items, A, tbl, wide, slots, sliceW);
+}
+
 size_t scene_wide_bytes() { return sizeof(RowScratch<kWideMaxH, kWideXT>); }
-int scene_ctas_per_sm() { return 2; }  // two CTAs of kFastWarps row scratches fit one SM's shared memory
 
 size_t rows_smem_fast() { return sizeof(RowScratch<kFastMaxH, kFastXT>) * kFastWarps; }
 size_t rows_smem_wide() { return sizeof(RowScratch<kWideMaxH, kWideXT>); }

@@ -70,8 +70,8 @@ struct PathJob {
 // Paths [j0, j1) of the job array painted in order onto one canvas (the
 // jobs' img/W/H).  A launch may carry several runs on distinct canvases.
 struct SceneRun {
-  long long row_off;  // prefix of canvas rows over the launch's runs
-  long long H;
+  long long row_off;  // prefix of (row, slice) work items over the launch's runs
+  long long W, H;
   int j0, j1;
 };
 

@@ -176,3 +176,17 @@ def test_scene_reuse_and_clear():
     b = px.Image(128, 128)
     b.draw_scene(sc)
     assert not b.to_numpy().any()
+
+
+@pytest.mark.parametrize("variant,slice_w", [(0, 1 << 20), (0, 256), (1, 256), (1, 64), (1, 100)])
+def test_every_scene_configuration_writes_the_same_bytes(variant, slice_w):
+    items = wl.dense_scene(23, n_paths=120, size=300.0)
+    ref = oracle_scene(items, 300, 300)
+    sc = record(items)
+    px.scene_config(variant, slice_w)
+    try:
+        img = px.Image(300, 300)
+        img.draw_scene(sc)
+    finally:
+        px.scene_config(1, 256)
+    assert_same(img.to_numpy(), ref, f"scene config {variant}/{slice_w}")
