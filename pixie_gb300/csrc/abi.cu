@@ -107,6 +107,7 @@ void launch_scene(int v, unsigned blocks, cudaStream_t st, PathJob* jobs, const 
                   long long items, const Arena& A, const uint8_t* tbl, unsigned char* wide, long long slots,
                   int sliceW);
 size_t scene_wide_bytes();
+size_t setup_smem(int maxBands);
 int draw_masks_tiles();
 void launch_draw_masks(int tile, uint32_t* page, long long W, long long H, const void* items, int n,
                        const uint8_t* masks, int mode, const uint8_t* tbl, cudaStream_t st);
@@ -424,7 +425,7 @@ void note_stats(long long paths, long long prims, const unsigned long long* ctr)
 
 int setup_max_bands(long long maxH) {
   const int maxBands = (int)(std::max<long long>(1, maxH / 4) + 1);
-  if ((size_t)maxBands * 8 > g.setupSmemMax) throw ApiError{"Image too tall for the fill kernels"};
+  if (setup_smem(maxBands) > g.setupSmemMax) throw ApiError{"Image too tall for the fill kernels"};
   return maxBands;
 }
 
@@ -513,7 +514,7 @@ void run_jobs(std::vector<PathJob>& jobs, const std::vector<Prim>& prims, std::v
     auto issue = [&](bool count) {
       if (attempt == 0 && opts.zero) CU(cudaMemsetAsync(opts.zero, 0, (size_t)opts.zero_bytes, g.stream));
       CU(cudaMemcpyAsync(g.d_up, g.h_up, S.upBytes, cudaMemcpyHostToDevice, g.stream));
-      k_setup<<<nr, 256, (size_t)maxBands * 8, g.stream>>>(dj, A, maxBands);
+      k_setup<<<nr, 256, setup_smem(maxBands), g.stream>>>(dj, A, maxBands);
       if (count) note_launch();
       CU(cudaGetLastError());
       if (timeRows) CU(cudaEventRecord(g.evr0, g.stream));
@@ -681,7 +682,7 @@ void run_scene_runs(std::vector<HostRun>& runs) {
     }
     Staged S = stage(dev, sr.data(), sizeof(SceneRun) * sr.size(), std::vector<Prim>());
     if (nj > 0) {
-      k_setup<<<nj, 256, (size_t)maxBands * 8, g.stream>>>(S.dj, S.A, maxBands); note_launch();
+      k_setup<<<nj, 256, setup_smem(maxBands), g.stream>>>(S.dj, S.A, maxBands); note_launch();
       CU(cudaGetLastError());
     }
     launch_scene(sv, (unsigned)blocks, g.stream, S.dj, reinterpret_cast<const SceneRun*>(S.extra), (int)sr.size(),

@@ -25,6 +25,7 @@ namespace pxg {
 static __device__ constexpr float kEps = (float)(0.0001 * 3.141592653589793);  // paths.nim:44
 static constexpr long long kIterCap = 1LL << 24;
 static constexpr int kSegTile = 1024;  // segment band ranges staged per pass of the band-list build
+static constexpr int kBallotBands = 1024;  // band count up to which the ballot band-list build runs
 
 struct V2 {
   float x, y;
@@ -262,6 +263,7 @@ __global__ void __launch_bounds__(256) k_setup(PathJob* jobs, Arena A, int maxBa
 
   PathJob& J = jobs[blockIdx.x];
   const int tid = threadIdx.x, T = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  const unsigned lt32 = (1u << lane) - 1;
   if (tid == 0) {
     s_err = LLONG_MAX;
     s_status = kOk;
@@ -498,6 +500,64 @@ __global__ void __launch_bounds__(256) k_setup(PathJob* jobs, Arena A, int maxBa
   }
   int* L = A.bandseg + s_listbase;
   for (uint32_t k = tid; k < numP; k += T) A.bands[s_bandbase + k].off += s_listbase;
+  if (numP <= (uint32_t)kBallotBands && maxBands <= kBallotBands) {
+    // Each warp owns a contiguous range of segments and walks it 32 at a
+    // time; for every band the 32 segments touch, a ballot orders them.  A
+    // first pass counts each warp's entries per band (giving every warp its
+    // start in every band), the second writes them: O(entries) work.
+    const int NW = T >> 5;
+    int* wc = dsm + 2 * maxBands;  // [warp][band]
+    for (int k = tid; k < NW * (int)numP; k += T) wc[k] = 0;
+    __syncthreads();
+    const long long per = ((nseg + NW - 1) / NW + 31) / 32 * 32;
+    const long long s0 = min(nseg, (long long)warp * per), s1 = min(nseg, s0 + per);
+    int* mine = wc + warp * (int)numP;
+    for (int pass = 0; pass < 2; pass++) {
+      if (pass == 1) {
+        __syncthreads();
+        for (uint32_t k = tid; k < numP; k += T) {
+          int run = bandc[k];
+          for (int w = 0; w < NW; w++) {
+            const int t = wc[w * numP + k];
+            wc[w * numP + k] = run;
+            run += t;
+          }
+        }
+        __syncthreads();
+      }
+      for (long long c0 = s0; c0 < s1; c0 += 32) {
+        const long long i = c0 + lane;
+        const bool valid = i < s1;
+        uint2 r = make_uint2(UINT_MAX, 0u);
+        if (valid) r = A.segband[segbase + i];
+        uint32_t lo = r.x, hi = r.y;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+          hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        }
+        for (uint32_t k = lo; k <= hi; k++) {
+          const bool in = valid && r.x <= k && k <= r.y;
+          const unsigned m = __ballot_sync(0xffffffffu, in);
+          if (!m) continue;
+          if (pass == 0) {
+            if (lane == 0) mine[k] += __popc(m);
+          } else {
+            const int base = mine[k];
+            if (in) L[base + __popc(m & lt32)] = (int)i;
+            __syncwarp();
+            if (lane == 0) mine[k] = base + __popc(m);
+          }
+          __syncwarp();
+        }
+      }
+    }
+    if (tid == 0) {
+      J.band_off = s_bandbase;
+      J.status = kOk;
+    }
+    return;
+  }
   for (long long t0 = 0; t0 < nseg; t0 += kSegTile) {
     const int tl = (int)min((long long)kSegTile, nseg - t0);
     uint32_t lo = UINT_MAX, hi = 0;
@@ -1245,6 +1305,13 @@ void launch_scene(int v, unsigned blocks, cudaStream_t st, PathJob* jobs, const 
   else
     k_scene<kFastMaxH, kFastXT, kFastWarps><<<blocks, kFastWarps * 32, scene_smem(0), st>>>(
         jobs, runs, nruns, items, A, tbl, wide, slots, sliceW);
+}
+
+// Dynamic shared memory of k_setup for a launch whose images have at most
+// maxBands bands: per band a count and flags, plus per warp and band a cursor
+// for the ballot band-list build.
+size_t setup_smem(int maxBands) {
+  return (size_t)maxBands * 8 + (maxBands <= kBallotBands ? (size_t)(256 / 32) * maxBands * 4 : 0);
 }
 
 size_t scene_wide_bytes() { return sizeof(RowScratch<kWideMaxH, kWideXT>); }
