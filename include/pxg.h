@@ -148,10 +148,10 @@ int pxg_scene_stroke_path(pxg_scene* scene, const float* commands, int64_t n_com
                           const float transform[9], float stroke_width, int line_cap,
                           int line_join, float miter_limit, const float* dashes, int64_t n_dashes);
 int pxg_image_draw_scene(pxg_image* image, const pxg_scene* scene);
-/* Scene kernel configuration (every choice writes the same bytes): variant 0
- * holds 256 crossings per row in shared memory, 1 holds 128 (more warps per
- * SM); slice_width is the row slice one warp draws (>= 32). */
-int pxg_scene_config(int variant, int slice_width);
+/* Scene drawing configuration (every choice writes the same bytes):
+ * slice_width is the part of a canvas row one warp of the drawing pass owns
+ * (>= 32 pixels; default 256). */
+int pxg_scene_config(int slice_width);
 
 /* Mask batches: many paths, each filled with color(1, 1, 1, 1) onto a
  * transparent image of its own size, kept as the 8-bit alpha of that image

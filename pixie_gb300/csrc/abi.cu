@@ -100,12 +100,16 @@ void launch_rows(int v, unsigned blocks, cudaStream_t st, PathJob* jobs, int njo
                  const uint8_t* tbl, long long items, int rpi);
 __global__ void k_rows_wide(PathJob* jobs, Arena A, const uint8_t* tbl);
 __global__ void k_xclears(PathJob* jobs, Arena A);
-const void* scene_kernel(int v);
-size_t scene_smem(int v);
+const void* scene_rec_kernel();
+size_t scene_rec_smem();
+int scene_rec_warps();
+const void* scene_kernel();
 int scene_warps();
-void launch_scene(int v, unsigned blocks, cudaStream_t st, PathJob* jobs, const SceneRun* runs, int nruns,
-                  long long items, const Arena& A, const uint8_t* tbl, unsigned char* wide, long long slots,
-                  int sliceW);
+int scene_tile();
+void launch_scene_rec(unsigned blocks, cudaStream_t st, PathJob* jobs, int njobs, long long items, const Arena& A,
+                      unsigned char* wide, long long slots);
+void launch_scene(unsigned blocks, cudaStream_t st, PathJob* jobs, const SceneRun* runs, int nruns, long long items,
+                  const Arena& A, const uint8_t* tbl, int sliceW);
 size_t scene_wide_bytes();
 size_t setup_smem(int maxBands);
 int draw_masks_tiles();
@@ -197,7 +201,11 @@ struct Ctx {
   long long primcnt_cap = 0;
   MaskDraw* mdraw = nullptr;      // mask positions of pxg_image_draw_masks
   long long mdraw_cap = 0;
-  unsigned char* wide = nullptr;  // per-warp wide row scratch of the scene kernel
+  int4* prog = nullptr;           // scene row programs
+  long long prog_cap = 0;
+  long long* rowidx = nullptr;    // scene rows -> program
+  long long rowidx_cap = 0;
+  unsigned char* wide = nullptr;  // per-warp wide row scratch of the scene recording kernel
   long long wide_slots = 0;
   long long* ovf = nullptr;
   long long ovf_cap = 0;
@@ -216,8 +224,8 @@ struct Ctx {
   float last_ms = 0;
   long long stats[4] = {0, 0, 0, 0};  // last fill launch: paths, prims, segments, band entries
   int rows_ctas_per_sm[2] = {1, 1};  // resident CTAs of each row-kernel variant
-  int scene_ctas_per_sm[2] = {1, 1};
-  int scene_variant = 1, scene_slice = 256;  // scene kernel configuration
+  int scene_ctas_per_sm[2] = {1, 1};  // resident CTAs of the scene recording and drawing kernels
+  int scene_slice = 256;              // pixels of a row one warp of the drawing pass owns
   bool blocking = true;  // image operations wait for their GPU work
   std::map<int64_t, uint16_t*> weights;  // gaussian weights per radius, on the device
 };
@@ -254,11 +262,14 @@ void init_locked(int device) {
     g.rows_ctas_per_sm[v] = std::max(1, per);
   }
   CU(cudaFuncSetAttribute(k_rows_wide, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem_wide()));
-  for (int v = 0; v < 2; v++) {
-    CU(cudaFuncSetAttribute(scene_kernel(v), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scene_smem(v)));
+  {
+    CU(cudaFuncSetAttribute(scene_rec_kernel(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scene_rec_smem()));
     int per = 0;
-    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, scene_kernel(v), scene_warps() * 32, scene_smem(v)));
-    g.scene_ctas_per_sm[v] = std::max(1, per);
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, scene_rec_kernel(), scene_rec_warps() * 32,
+                                                     scene_rec_smem()));
+    g.scene_ctas_per_sm[0] = std::max(1, per);
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, scene_kernel(), scene_warps() * 32, 0));
+    g.scene_ctas_per_sm[1] = std::max(1, per);
   }
   g.setupSmemMax = allow_max_smem((const void*)k_setup);
   g.blurSmemMax = std::min(allow_max_smem((const void*)k_blur_x), allow_max_smem((const void*)k_blur_y));
@@ -408,6 +419,9 @@ Staged stage(const std::vector<PathJob>& run, const void* extra, size_t extraByt
   A.bandseg_cap = g.bandseg_cap;
   A.primcnt = g.primcnt;
   A.primcnt_cap = g.primcnt_cap;
+  A.prog = g.prog;
+  A.prog_cap = g.prog_cap;
+  A.rowidx = g.rowidx;
   A.counters = reinterpret_cast<unsigned long long*>(g.d_up + S.jobsBytes);
   A.ovf_rows = g.ovf;
   A.ovf_cap = g.ovf_cap;
@@ -631,18 +645,20 @@ void run_scene_runs(std::vector<HostRun>& runs) {
   for (auto& r : runs) prim_total += (long long)r.prims->size();
   long long seg_need = std::max<long long>(1 << 16, prim_total * 8);
   long long list_need = seg_need * 4;
+  long long prog_need = 0;
   for (auto& r : runs) r.status = kOk;
-  for (int attempt = 0; attempt < 12; attempt++) {
+  for (int attempt = 0; attempt < 16; attempt++) {
     std::vector<PathJob> dev;
     long long pc = 0;
     std::vector<SceneRun> sr;
     std::vector<size_t> which;  // launch run -> runs index
-    long long rows = 0, maxH = 1;
+    long long items = 0, recItems = 0, maxH = 1;
+    const int slice = g.scene_slice;
     for (size_t ri = 0; ri < runs.size(); ri++) {
       HostRun& r = runs[ri];
       if (r.status != kOk || r.j0 >= r.j1) continue;
       SceneRun s;
-      s.row_off = rows;
+      s.row_off = items;
       s.W = r.canvas->width;
       s.H = r.canvas->height;
       s.j0 = (int)dev.size();
@@ -655,11 +671,14 @@ void run_scene_runs(std::vector<HostRun>& runs) {
         pj.img = r.canvas->data;
         pj.W = r.canvas->width;
         pj.H = r.canvas->height;
+        pj.row_off = recItems;  // recording items: one per row of the canvas
+        pj.ri_off = recItems;
+        recItems += pj.H;
         pj.status = kOk;
         dev.push_back(pj);
       }
       s.j1 = (int)dev.size();
-      rows += s.H * ((s.W + g.scene_slice - 1) / g.scene_slice);
+      items += s.H * ((s.W + slice - 1) / slice);
       maxH = std::max<long long>(maxH, s.H);
       sr.push_back(s);
       which.push_back(ri);
@@ -668,11 +687,13 @@ void run_scene_runs(std::vector<HostRun>& runs) {
     const int nj = (int)dev.size();
     const int maxBands = setup_max_bands(maxH);
     ensure_arena(seg_need, list_need, (long long)nj * maxBands, pc, 1);
-    const int sv = g.scene_variant;
-    const int wpb = scene_warps();
-    long long blocks = std::min<long long>((rows + wpb - 1) / wpb, (long long)g.nsm * g.scene_ctas_per_sm[sv]);
-    blocks = std::max<long long>(blocks, 1);
-    const long long slots = blocks * wpb;
+    if (prog_need == 0) prog_need = std::max<long long>(1 << 20, recItems * 8);
+    dev_grow(g.prog, g.prog_cap, prog_need);
+    dev_grow(g.rowidx, g.rowidx_cap, std::max<long long>(recItems, 1));
+    const long long recBlocks = std::max<long long>(
+        1, std::min<long long>((recItems + scene_rec_warps() - 1) / scene_rec_warps(),
+                               (long long)g.nsm * g.scene_ctas_per_sm[0]));
+    const long long slots = recBlocks * scene_rec_warps();
     if (slots > g.wide_slots) {
       if (g.wide) cudaFree(g.wide);
       g.wide = nullptr;
@@ -680,13 +701,15 @@ void run_scene_runs(std::vector<HostRun>& runs) {
       CU(cudaMalloc(&g.wide, (size_t)slots * scene_wide_bytes()));
       g.wide_slots = slots;
     }
+    const long long blocks = std::max<long long>(
+        1, std::min<long long>((items + scene_warps() - 1) / scene_warps(), (long long)g.nsm * g.scene_ctas_per_sm[1]));
     Staged S = stage(dev, sr.data(), sizeof(SceneRun) * sr.size(), std::vector<Prim>());
-    if (nj > 0) {
-      k_setup<<<nj, 256, setup_smem(maxBands), g.stream>>>(S.dj, S.A, maxBands); note_launch();
-      CU(cudaGetLastError());
-    }
-    launch_scene(sv, (unsigned)blocks, g.stream, S.dj, reinterpret_cast<const SceneRun*>(S.extra), (int)sr.size(),
-                 rows, S.A, g.tbl, g.wide, g.wide_slots, g.scene_slice);
+    k_setup<<<nj, 256, setup_smem(maxBands), g.stream>>>(S.dj, S.A, maxBands); note_launch();
+    CU(cudaGetLastError());
+    launch_scene_rec((unsigned)recBlocks, g.stream, S.dj, nj, recItems, S.A, g.wide, g.wide_slots); note_launch();
+    CU(cudaGetLastError());
+    launch_scene((unsigned)blocks, g.stream, S.dj, reinterpret_cast<const SceneRun*>(S.extra), (int)sr.size(), items,
+                 S.A, g.tbl, slice);
     note_launch();
     CU(cudaGetLastError());
     CU(cudaMemcpyAsync(g.h_up, g.d_up, S.jobsBytes + S.ctrBytes, cudaMemcpyDeviceToHost, g.stream));
@@ -694,6 +717,10 @@ void run_scene_runs(std::vector<HostRun>& runs) {
     unsigned long long ctr[kNumCounters];
     memcpy(ctr, g.h_up + S.jobsBytes, sizeof ctr);
     note_stats(nj, pc, ctr);
+    if (ctr[kCtrProgFull]) {  // nothing was drawn: rerun with room for every program
+      prog_need = std::max<long long>(prog_need * 2, (long long)(ctr[kCtrProg] + ctr[kCtrProg] / 4));
+      continue;
+    }
     const PathJob* out = reinterpret_cast<const PathJob*>(g.h_up);
     bool grow = false;
     for (size_t k = 0; k < sr.size(); k++) {
@@ -1626,11 +1653,9 @@ int pxg_server_stats(const pxg_server* sv, int64_t* out6) {
   return 0;
 }
 
-int pxg_scene_config(int variant, int slice_width) {
+int pxg_scene_config(int slice_width) {
   return guarded([&] {
-    if (variant < 0 || variant > 1 || slice_width < 32 || slice_width > (1 << 20))
-      throw ApiError{"Invalid scene configuration"};
-    g.scene_variant = variant;
+    if (slice_width < 32 || slice_width > (1 << 20)) throw ApiError{"Invalid scene configuration"};
     g.scene_slice = slice_width;
   });
 }

@@ -709,10 +709,183 @@ __device__ void clear_span_linear(const PathJob& J, const Arena& A, int job, Row
   }
 }
 
+// The trapezoid path's pixels for one pair of entries, left (Lm, Lb) and
+// right (Rm, Rb), crossing the row at tl0/tl1 and tr0/tr1 (:1752-1835), drawn
+// within [xa, xb).
+template <bool A8>
+__device__ __forceinline__ void apply_trap_pair(RowPx<A8> row, int mode, const uint8_t* tbl, uint32_t rgbx,
+                                                long long y, long long W, float Lm, float Lb, float Rm,
+                                                float Rb, float tl0, float tl1, float tr0, float tr1,
+                                                long long xa, long long xb, int lane) {
+  const float leftMaxX = nmax(tl0, tl1), rightMinX = nmin(tr0, tr1);
+  const long long leftCoverEnd = nim_int(ceilf(leftMaxX));
+  const long long rightCoverBegin = nim_int(truncf(rightMinX));
+  {  // left sliver (:1752-1788)
+    const bool inv = tl0 < tl1;
+    const float sliverStart = nmin(tl0, tl1), rectStart = leftMaxX;
+    const long long xs = nim_int(sliverStart), xe = nim_int(ceilf(rectStart));
+    for (long long x = max(max(xs, 0LL), xa) + lane; x < min(min(xe, W), xb); x += 32) {
+      float prevPen = x == xs ? sliverStart : (float)x;
+      float pen = (float)(x + 1);
+      float rightRectArea = 0;
+      if (pen > rectStart) {
+        rightRectArea = pen - rectStart;
+        pen = rectStart;
+      }
+      float prevPenY = x == xs ? (inv ? (float)y : (float)(y + 1)) : Lm * (float)x + Lb;
+      float penY = Lm * pen + Lb;
+      float run = pen - prevPen;
+      float tri = 0.5f * run * fabsf(penY - prevPenY);
+      float rect = inv ? (prevPenY - (float)y) * run : ((float)(y + 1) - prevPenY) * run;
+      float area = tri + rect + rightRectArea;
+      row[x] = blend_px(mode, tbl, row[x], mul_f(rgbx, area));
+    }
+  }
+  {  // right sliver (:1790-1828)
+    const bool inv = tr0 > tr1;
+    const float rectEnd = rightMinX, sliverEnd = nmax(tr0, tr1);
+    const long long xs = nim_int(rectEnd), xe = nim_int(ceilf(sliverEnd));
+    for (long long x = max(max(xs, 0LL), xa) + lane; x < min(min(xe, W), xb); x += 32) {
+      float prevPen = x == xs ? rectEnd : (float)x;
+      float pen = (float)(x + 1);
+      float ap = fabsf(prevPen);
+      float leftRectArea = ap - floorf(ap);  // vmath fractional: fractional part of |v|
+      if (pen > sliverEnd) pen = sliverEnd;
+      float prevPenY = x == xs ? (inv ? (float)(y + 1) : (float)y) : Rm * (float)x + Rb;
+      float penY = Rm * pen + Rb;
+      float run = pen - prevPen;
+      float tri = 0.5f * run * fabsf(penY - prevPenY);
+      float rect = inv ? (penY - (float)y) * run : ((float)(y + 1) - penY) * run;
+      float area = leftRectArea + tri + rect;
+      row[x] = blend_px(mode, tbl, row[x], mul_f(rgbx, area));
+    }
+  }
+  {  // the fully covered middle (:1830-1835)
+    long long fb = max(min(max(leftCoverEnd, 0LL), W), xa), fe = min(min(max(rightCoverBegin, 0LL), W), xb);
+    for (long long x = fb + lane; x < fe; x += 32) row[x] = op_fill(mode, tbl, row[x], rgbx);
+  }
+}
+
+// computeCoverage's accumulation of the sample spans (prevAt, at) in 24.8
+// fixed point (:1398-1431) and fillCoverage (:1442-1526) over [cx0, cx1), in
+// tiles of XT pixels through the difference array acc (XT + 1 ints).
+template <bool A8, int XT>
+__device__ void apply_cov(RowPx<A8> row, int mode, const uint8_t* tbl, uint32_t rgbx, const int2* sp, int nsp,
+                          int sc, long long cx0, long long cx1, int* acc, int lane) {
+  const bool maskMode = mode == kMask;
+  for (long long tx0 = cx0; tx0 < cx1; tx0 += XT) {
+    const long long tx1 = min(tx0 + (long long)XT, cx1);
+    const int L = (int)(tx1 - tx0);
+    for (int i = lane; i <= L; i += 32) acc[i] = 0;
+    __syncwarp();
+    for (int j = lane; j < nsp; j += 32) {
+      const int2 spj = sp[j];
+      int prevAt = spj.x, at = spj.y;
+      long long pi = prevAt / 256, ai = at / 256;
+      long long fillStart = pi;
+      bool crossed = ai != pi;
+      int leftCover = crossed ? (prevAt / 256) * 256 + 256 - prevAt : at - prevAt;
+      if (leftCover != 0) {
+        fillStart++;
+        int v = ((leftCover * sc) / 256) & 255;
+        if (pi >= tx0 && pi < tx1) {
+          atomicAdd(&acc[pi - tx0], v);
+          atomicAdd(&acc[pi - tx0 + 1], -v);
+        }
+      }
+      if (crossed) {
+        int rightCover = at - (at / 256) * 256;
+        if (rightCover > 0) {
+          int v = ((rightCover * sc) / 256) & 255;
+          if (ai >= tx0 && ai < tx1) {
+            atomicAdd(&acc[ai - tx0], v);
+            atomicAdd(&acc[ai - tx0 + 1], -v);
+          }
+        }
+      }
+      long long fe = ai;
+      long long lo = max(fillStart, tx0), hi = min(fe, tx1);
+      if (hi > lo) {
+        atomicAdd(&acc[lo - tx0], sc);
+        atomicAdd(&acc[hi - tx0], -sc);
+      }
+    }
+    __syncwarp();
+    // prefix sum of the difference array; coverage = sum mod 256
+    const int C = (L + 31) / 32;
+    int base = lane * C, s = 0;
+    for (int i = base; i < min(base + C, L); i++) s += acc[i];
+    int incl = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    int run = incl - s;
+    __syncwarp();
+    for (int i = base; i < min(base + C, L); i++) {
+      run += acc[i];
+      acc[i] = run;
+    }
+    __syncwarp();
+    for (int i = lane; i < L; i += 32) {
+      const uint32_t cov = (uint32_t)acc[i] & 255u;
+      const long long x = tx0 + i;
+      // pixels op_cov leaves unchanged are neither read nor written
+      if (maskMode ? cov != 255u : cov != 0u) row[x] = op_cov(mode, tbl, row[x], rgbx, cov);
+    }
+    __syncwarp();
+  }
+}
+
+// fillHits (:1540-1591) for a non-mask mode: the single sample's spans are
+// sorted and disjoint, so a pixel is inside at most one.
+template <bool A8>
+__device__ void apply_hits(RowPx<A8> row, int mode, const uint8_t* tbl, uint32_t rgbx, const int2* sp, int nsp,
+                           long long xa, long long xb, int lane) {
+  for (long long x = xa + lane; x < xb; x += 32) {
+    bool inside = false;
+    for (int j = 0; j < nsp && !inside; j++) {
+      long long fs = sp[j].x / 256, fe = sp[j].y / 256;
+      if (fe - fs > 0 && x >= fs && x < fe) inside = true;
+    }
+    if (inside) row[x] = op_fill(mode, tbl, row[x], rgbx);
+  }
+}
+
+// Row programs: what a row of a path draws, recorded by the scene's first
+// pass and replayed by its second.  A program is a header unit then data:
+//   kRecFill  [minX, maxX) filled            (the non-AA two-edge case)
+//   kRecCov   n sample spans, coverage step  (computeCoverage + fillCoverage)
+//   kRecHits  n spans                        (fillHits, non-AA)
+//   kRecTrap  n pairs: {Lm, Lb, Rm, Rb}, {tl0, tl1, tr0, tr1} per pair
+enum RecKind { kRecFill = 1, kRecCov = 2, kRecHits = 3, kRecTrap = 4 };
+
+// Allocates `units` 16-byte units for row y of job J's program, stores its
+// index for the row, and returns it (lane-uniform); -1 if the arena is full.
+__device__ __forceinline__ long long rec_alloc(const PathJob& J, const Arena& A, long long y, int units,
+                                               int lane) {
+  unsigned long long base = 0;
+  if (lane == 0) {
+    base = atomicAdd(&A.counters[kCtrProg], (unsigned long long)units);
+    if ((long long)(base + units) > A.prog_cap) {
+      atomicOr(&A.counters[kCtrProgFull], 1ull);
+      A.rowidx[J.ri_off + y] = -1;
+      base = ~0ull;
+    } else {
+      A.rowidx[J.ri_off + y] = (long long)base;
+    }
+  }
+  base = __shfl_sync(0xffffffffu, base, 0);
+  return base == ~0ull ? -1 : (long long)base;
+}
+
 // Draws the pixels [xa, xb) of row y of job J (the whole row: 0, W).
 // Returns false, having drawn nothing, when the row's crossings exceed MAXH
 // (the caller retries it with a larger scratch).
-template <int MAXH, int XT, bool A8>
+// With REC the row is not drawn: its program is recorded instead (non-mask
+// modes only).
+template <int MAXH, int XT, bool A8, bool REC = false>
 __device__ bool process_row(const PathJob& J, const Arena& A, const uint8_t* tbl, int job,
                             long long y, RowScratch<MAXH, XT>& S, int lane, long long xa,
                             long long xb) {
@@ -764,6 +937,11 @@ __device__ bool process_row(const PathJob& J, const Arena& A, const uint8_t* tbl
   if (two && !(bd.flags & kBandAA)) {
     long long minX = min(max(nim_int(E[0].ax), 0LL), W);
     long long maxX = min(max(nim_int(E[1].ax), 0LL), W);
+    if (REC) {
+      const long long at = rec_alloc(J, A, y, 1, lane);
+      if (at >= 0 && lane == 0) A.prog[at] = make_int4(kRecFill, 0, (int)minX, (int)maxX);
+      return true;
+    }
     for (long long x = xa + lane; x < xb; x += 32) {
       if (x >= minX && x < maxX) row[x] = op_fill(mode, tbl, row[x], rgbx);
       else if (maskMode) row[x] = 0u;
@@ -806,11 +984,11 @@ __device__ bool process_row(const PathJob& J, const Arena& A, const uint8_t* tbl
     bool anyNaN = false;
     for (int i = lane; i < n; i += 32) {
       Entry e = E[S.idx[i]];
-      float xa = e.m == 0 ? e.b : (scanTop - e.b) / e.m;   // solveX :1137-1141
-      float xb = e.m == 0 ? e.b : (scanBottom - e.b) / e.m;
-      t0[i] = xa;
-      t1[i] = xb;
-      key[i] = (xa + xb) * 0.5f;
+      float xt = e.m == 0 ? e.b : (scanTop - e.b) / e.m;   // solveX :1137-1141
+      float xbt = e.m == 0 ? e.b : (scanBottom - e.b) / e.m;
+      t0[i] = xt;
+      t1[i] = xbt;
+      key[i] = (xt + xbt) * 0.5f;
       anyNaN |= isnan(key[i]);
     }
     anyNaN = __any_sync(0xffffffffu, anyNaN);
@@ -869,58 +1047,27 @@ __device__ bool process_row(const PathJob& J, const Arena& A, const uint8_t* tbl
       }
       simple = __shfl_sync(0xffffffffu, ok, 0) != 0;
     }
+    if (simple && REC) {
+      const int np = n / 2;
+      const long long at = rec_alloc(J, A, y, 1 + 2 * np, lane);
+      if (at >= 0) {
+        if (lane == 0) A.prog[at] = make_int4(kRecTrap, np, 0, 0);
+        for (int p = lane; p < np; p += 32) {
+          const Entry L = E[S.idx[2 * p]], R = E[S.idx[2 * p + 1]];
+          A.prog[at + 1 + 2 * p] = make_int4(__float_as_int(L.m), __float_as_int(L.b), __float_as_int(R.m),
+                                             __float_as_int(R.b));
+          A.prog[at + 2 + 2 * p] = make_int4(__float_as_int(t0[2 * p]), __float_as_int(t1[2 * p]),
+                                             __float_as_int(t0[2 * p + 1]), __float_as_int(t1[2 * p + 1]));
+        }
+      }
+      return true;
+    }
     if (simple) {
       long long filledTo = 0;
       for (int i = 0; i < n; i += 2) {
         const Entry L = E[S.idx[i]], R = E[S.idx[i + 1]];
         const float tl0 = t0[i], tl1 = t1[i], tr0 = t0[i + 1], tr1 = t1[i + 1];
-        const float leftMaxX = nmax(tl0, tl1), rightMinX = nmin(tr0, tr1);
-        const long long leftCoverEnd = nim_int(ceilf(leftMaxX));
-        const long long rightCoverBegin = nim_int(truncf(rightMinX));
-        {  // left sliver (:1752-1788)
-          const bool inv = tl0 < tl1;
-          const float sliverStart = nmin(tl0, tl1), rectStart = leftMaxX;
-          const long long xs = nim_int(sliverStart), xe = nim_int(ceilf(rectStart));
-          for (long long x = max(max(xs, 0LL), xa) + lane; x < min(min(xe, W), xb); x += 32) {
-            float prevPen = x == xs ? sliverStart : (float)x;
-            float pen = (float)(x + 1);
-            float rightRectArea = 0;
-            if (pen > rectStart) {
-              rightRectArea = pen - rectStart;
-              pen = rectStart;
-            }
-            float prevPenY = x == xs ? (inv ? (float)y : (float)(y + 1)) : L.m * (float)x + L.b;
-            float penY = L.m * pen + L.b;
-            float run = pen - prevPen;
-            float tri = 0.5f * run * fabsf(penY - prevPenY);
-            float rect = inv ? (prevPenY - (float)y) * run : ((float)(y + 1) - prevPenY) * run;
-            float area = tri + rect + rightRectArea;
-            row[x] = blend_px(mode, tbl, row[x], mul_f(rgbx, area));
-          }
-        }
-        {  // right sliver (:1790-1828)
-          const bool inv = tr0 > tr1;
-          const float rectEnd = rightMinX, sliverEnd = nmax(tr0, tr1);
-          const long long xs = nim_int(rectEnd), xe = nim_int(ceilf(sliverEnd));
-          for (long long x = max(max(xs, 0LL), xa) + lane; x < min(min(xe, W), xb); x += 32) {
-            float prevPen = x == xs ? rectEnd : (float)x;
-            float pen = (float)(x + 1);
-            float ap = fabsf(prevPen);
-            float leftRectArea = ap - floorf(ap);  // vmath fractional: fractional part of |v|
-            if (pen > sliverEnd) pen = sliverEnd;
-            float prevPenY = x == xs ? (inv ? (float)(y + 1) : (float)y) : R.m * (float)x + R.b;
-            float penY = R.m * pen + R.b;
-            float run = pen - prevPen;
-            float tri = 0.5f * run * fabsf(penY - prevPenY);
-            float rect = inv ? (penY - (float)y) * run : ((float)(y + 1) - penY) * run;
-            float area = leftRectArea + tri + rect;
-            row[x] = blend_px(mode, tbl, row[x], mul_f(rgbx, area));
-          }
-        }
-        {  // the fully covered middle (:1830-1835)
-          long long fb = max(min(max(leftCoverEnd, 0LL), W), xa), fe = min(min(max(rightCoverBegin, 0LL), W), xb);
-          for (long long x = fb + lane; x < fe; x += 32) row[x] = op_fill(mode, tbl, row[x], rgbx);
-        }
+        apply_trap_pair<A8>(row, mode, tbl, rgbx, y, W, L.m, L.b, R.m, R.b, tl0, tl1, tr0, tr1, xa, xb, lane);
         if (maskMode) {  // :1837-1845
           long long clearTo = nim_int(nmin(tl0, tl1));
           clear_span_linear(J, A, job, row, y, min(filledTo, W), min(clearTo, W), lane, xa, xb);
@@ -1044,77 +1191,25 @@ __device__ bool process_row(const PathJob& J, const Arena& A, const uint8_t* tbl
   }
   const int nsp = min(S.nsp, RowScratch<MAXH, XT>::SPCAP);
 
+  if (REC) {
+    const long long at = nsp > 0 ? rec_alloc(J, A, y, 1 + (nsp + 1) / 2, lane) : -1;
+    if (nsp == 0 && lane == 0) A.rowidx[J.ri_off + y] = -1;
+    if (at >= 0) {
+      if (lane == 0) A.prog[at] = make_int4(aa ? kRecCov : kRecHits, nsp, sc, 0);
+      int2* d = reinterpret_cast<int2*>(A.prog + at + 1);
+      for (int j = lane; j < nsp; j += 32) d[j] = S.sp[j];
+    }
+    return true;
+  }
   if (aa) {
     // coverage row over [startX, startX + pathWidth) in tiles of XT pixels
     const long long px0 = J.startX, px1 = J.startX + J.pathWidth;
-    const long long cx0 = max(px0, xa), cx1 = min(px1, xb);
     if (maskMode) {
       for (long long x = xa + lane; x < xb; x += 32)
         if (x < px0 || x >= px1) row[x] = 0u;
     }
-    for (long long tx0 = cx0; tx0 < cx1; tx0 += XT) {
-      const long long tx1 = min(tx0 + (long long)XT, cx1);
-      const int L = (int)(tx1 - tx0);
-      for (int i = lane; i <= L; i += 32) S.acc[i] = 0;
-      __syncwarp();
-      for (int j = lane; j < nsp; j += 32) {
-        int prevAt = S.sp[j].x, at = S.sp[j].y;
-        long long pi = prevAt / 256, ai = at / 256;
-        long long fillStart = pi;
-        bool crossed = ai != pi;
-        int leftCover = crossed ? (prevAt / 256) * 256 + 256 - prevAt : at - prevAt;
-        if (leftCover != 0) {
-          fillStart++;
-          int v = ((leftCover * sc) / 256) & 255;
-          if (pi >= tx0 && pi < tx1) {
-            atomicAdd(&S.acc[pi - tx0], v);
-            atomicAdd(&S.acc[pi - tx0 + 1], -v);
-          }
-        }
-        if (crossed) {
-          int rightCover = at - (at / 256) * 256;
-          if (rightCover > 0) {
-            int v = ((rightCover * sc) / 256) & 255;
-            if (ai >= tx0 && ai < tx1) {
-              atomicAdd(&S.acc[ai - tx0], v);
-              atomicAdd(&S.acc[ai - tx0 + 1], -v);
-            }
-          }
-        }
-        long long fe = ai;
-        long long lo = max(fillStart, tx0), hi = min(fe, tx1);
-        if (hi > lo) {
-          atomicAdd(&S.acc[lo - tx0], sc);
-          atomicAdd(&S.acc[hi - tx0], -sc);
-        }
-      }
-      __syncwarp();
-      // prefix sum of the difference array; coverage = sum mod 256
-      const int C = (L + 31) / 32;
-      int base = lane * C, s = 0;
-      for (int i = base; i < min(base + C, L); i++) s += S.acc[i];
-      int incl = s;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        int t = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += t;
-      }
-      int run = incl - s;
-      __syncwarp();
-      for (int i = base; i < min(base + C, L); i++) {
-        run += S.acc[i];
-        S.acc[i] = run;
-      }
-      __syncwarp();
-      for (int i = lane; i < L; i += 32) {
-        const uint32_t cov = (uint32_t)S.acc[i] & 255u;
-        const long long x = tx0 + i;
-        // pixels op_cov leaves unchanged are neither read nor written
-        if (maskMode ? cov != 255u : cov != 0u) row[x] = op_cov(mode, tbl, row[x], rgbx, cov);
-      }
-      __syncwarp();
-    }
-  } else {
+    apply_cov<A8, XT>(row, mode, tbl, rgbx, S.sp, nsp, sc, max(px0, xa), min(px1, xb), S.acc, lane);
+  } else if (maskMode) {
     // fillHits with the single sample's spans (:1540-1591); spans are sorted
     // and disjoint, so a pixel is inside at most one.
     const long long startX = J.startX;
@@ -1124,12 +1219,10 @@ __device__ bool process_row(const PathJob& J, const Arena& A, const uint8_t* tbl
         long long fs = S.sp[j].x / 256, fe = S.sp[j].y / 256;
         if (fe - fs > 0 && x >= fs && x < fe) inside = true;
       }
-      if (maskMode) {
-        row[x] = (x >= startX && inside) ? op_fill(mode, tbl, row[x], rgbx) : 0u;
-      } else if (inside) {
-        row[x] = op_fill(mode, tbl, row[x], rgbx);
-      }
+      row[x] = (x >= startX && inside) ? op_fill(mode, tbl, row[x], rgbx) : 0u;
     }
+  } else {
+    apply_hits<A8>(row, mode, tbl, rgbx, S.sp, nsp, xa, xb, lane);
   }
   return true;
 }
@@ -1226,22 +1319,25 @@ __global__ void k_xclears(PathJob* jobs, Arena A) {
   }
 }
 
-// Dense scenes: a warp owns a slice of one canvas row (sliceW pixels) and
-// paints every path of its run into it in submission order, so each pixel
-// sees the paths in the order the reference's sequence of fillPath/strokePath
-// calls applies them.  Work items (row, slice) come from a device queue.  A
-// path that failed in setup stops its run there (the reference raises at that
-// call); a path whose bounds miss the slice is skipped (outside its bounds a
-// non-mask fill writes nothing); rows with more crossings than the
-// shared-memory scratch holds take a per-warp global-memory scratch of
-// kWideMaxH.  Each warp still computes the whole row's crossings and walk,
-// and draws only its slice.
-template <int MAXH, int XT, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) k_scene(PathJob* jobs, const SceneRun* runs, int nruns,
-                                                      long long totalItems, Arena A, const uint8_t* tbl,
-                                                      unsigned char* wide, long long wideSlots, int sliceW) {
+// Dense scenes, in two passes.
+// k_scene_rec: every (path, row) of the launch, independent of the pixels, so
+// all of them run in parallel from a device queue: the row's band entries,
+// crossings, sort and walk, recorded as the row's program (RecKind).  Rows
+// with more crossings than the shared-memory scratch holds take a per-warp
+// global-memory scratch of kWideMaxH.
+// k_scene: a warp owns a slice of one canvas row (sliceW pixels) and replays
+// every path's program for that row in submission order, so each pixel sees
+// the paths in the order the reference's sequence of fillPath/strokePath
+// calls applies them.  A path that failed in setup stops its run there (the
+// reference raises at that call); a path whose bounds miss the slice is
+// skipped (outside its bounds a non-mask fill writes nothing).  If the
+// program arena overflowed, k_scene draws nothing and the host reruns the
+// launch with a larger arena.
+template <int MAXH, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_scene_rec(PathJob* jobs, int njobs, long long totalItems, Arena A,
+                                                          unsigned char* wide, long long wideSlots) {
   extern __shared__ __align__(16) unsigned char rsm[];
-  using Scratch = RowScratch<MAXH, XT>;
+  using Scratch = RowScratch<MAXH, 32>;
   using Wide = RowScratch<kWideMaxH, kWideXT>;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   Scratch& S = reinterpret_cast<Scratch*>(rsm)[warp];
@@ -1249,6 +1345,42 @@ __global__ void __launch_bounds__(WARPS * 32) k_scene(PathJob* jobs, const Scene
   while (true) {
     unsigned long long q = 0;
     if (lane == 0) q = atomicAdd(&A.counters[kCtrQueue], 1ull);
+    const long long item = (long long)__shfl_sync(0xffffffffu, q, 0);
+    if (item >= totalItems) break;
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (jobs[mid].row_off <= item) lo = mid;
+      else hi = mid - 1;
+    }
+    const PathJob& J = jobs[lo];
+    const long long y = item - J.row_off;
+    if (J.status != kOk || y < J.startY || y >= J.pathHeight || y >= J.H) continue;
+    bool ok = process_row<MAXH, 32, false, true>(J, A, nullptr, lo, y, S, lane, 0, J.W);
+    if (!ok && gw < wideSlots) {
+      __syncwarp();
+      ok = process_row<kWideMaxH, kWideXT, false, true>(J, A, nullptr, lo, y, reinterpret_cast<Wide*>(wide)[gw],
+                                                        lane, 0, J.W);
+    }
+    if (!ok && lane == 0) {
+      atomicMin(&A.counters[kCtrRowErr], (unsigned long long)lo);
+      A.rowidx[J.ri_off + y] = -1;
+    }
+    __syncwarp();
+  }
+}
+
+template <int XT, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_scene(PathJob* jobs, const SceneRun* runs, int nruns,
+                                                      long long totalItems, Arena A, const uint8_t* tbl,
+                                                      int sliceW) {
+  __shared__ int accs[WARPS][XT + 1];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int* acc = accs[warp];
+  if (A.counters[kCtrProgFull]) return;  // programs incomplete: the host reruns the launch
+  while (true) {
+    unsigned long long q = 0;
+    if (lane == 0) q = atomicAdd(&A.counters[kCtrQueue2], 1ull);
     const long long item = (long long)__shfl_sync(0xffffffffu, q, 0);
     if (item >= totalItems) break;
     int lo = 0, hi = nruns - 1;
@@ -1272,39 +1404,52 @@ __global__ void __launch_bounds__(WARPS * 32) k_scene(PathJob* jobs, const Scene
       }
       if (y < J.startY || y >= J.pathHeight) continue;
       if (J.startX >= xb || J.startX + J.pathWidth <= xa) continue;
-      bool ok = process_row<MAXH, XT, false>(J, A, tbl, j, y, S, lane, xa, xb);
-      if (!ok && gw < wideSlots) {
-        __syncwarp();
-        ok = process_row<kWideMaxH, kWideXT, false>(J, A, tbl, j, y, reinterpret_cast<Wide*>(wide)[gw], lane,
-                                                    xa, xb);
+      const long long at = A.rowidx[J.ri_off + y];
+      if (at < 0) continue;
+      const int4 h = A.prog[at];
+      const RowPx<false> row = row_of<false>(J, y);
+      const int mode = J.mode;
+      const uint32_t rgbx = J.rgbx;
+      if (h.x == kRecFill) {
+        for (long long x = max((long long)h.z, xa) + lane; x < min((long long)h.w, xb); x += 32)
+          row[x] = op_fill(mode, tbl, row[x], rgbx);
+      } else if (h.x == kRecCov) {
+        const long long px0 = J.startX, px1 = J.startX + J.pathWidth;
+        apply_cov<false, XT>(row, mode, tbl, rgbx, reinterpret_cast<const int2*>(A.prog + at + 1), h.y, h.z,
+                             max(px0, xa), min(px1, xb), acc, lane);
+      } else if (h.x == kRecHits) {
+        apply_hits<false>(row, mode, tbl, rgbx, reinterpret_cast<const int2*>(A.prog + at + 1), h.y, xa, xb, lane);
+      } else if (h.x == kRecTrap) {
+        for (int p = 0; p < h.y; p++) {
+          const int4 e = A.prog[at + 1 + 2 * p], t = A.prog[at + 2 + 2 * p];
+          apply_trap_pair<false>(row, mode, tbl, rgbx, y, J.W, __int_as_float(e.x), __int_as_float(e.y),
+                                 __int_as_float(e.z), __int_as_float(e.w), __int_as_float(t.x), __int_as_float(t.y),
+                                 __int_as_float(t.z), __int_as_float(t.w), xa, xb, lane);
+        }
       }
-      if (!ok && lane == 0) atomicMin(&A.counters[kCtrRowErr], (unsigned long long)j);
       __syncwarp();
     }
   }
 }
 
-// Scene kernel variants: 0 = 256 crossings / 1024-px tiles, 1 = 128 / 256
-// (half the shared memory per warp: twice the warps per SM).
-constexpr int kSceneMaxH1 = 128, kSceneXT1 = 256;
-const void* scene_kernel(int v) {
-  return v == 1 ? (const void*)k_scene<kSceneMaxH1, kSceneXT1, kFastWarps>
-                : (const void*)k_scene<kFastMaxH, kFastXT, kFastWarps>;
+// Scene kernels: the recording pass holds 128 crossings per row in shared
+// memory (8 warps per CTA); the drawing pass keeps one 256-pixel coverage
+// tile per warp.
+constexpr int kRecMaxH = 128, kRecWarps = 8, kSceneXT = 256, kSceneWarps = 8;
+const void* scene_rec_kernel() { return (const void*)k_scene_rec<kRecMaxH, kRecWarps>; }
+size_t scene_rec_smem() { return sizeof(RowScratch<kRecMaxH, 32>) * kRecWarps; }
+int scene_rec_warps() { return kRecWarps; }
+const void* scene_kernel() { return (const void*)k_scene<kSceneXT, kSceneWarps>; }
+int scene_warps() { return kSceneWarps; }
+int scene_tile() { return kSceneXT; }
+void launch_scene_rec(unsigned blocks, cudaStream_t st, PathJob* jobs, int njobs, long long items, const Arena& A,
+                      unsigned char* wide, long long slots) {
+  k_scene_rec<kRecMaxH, kRecWarps><<<blocks, kRecWarps * 32, scene_rec_smem(), st>>>(jobs, njobs, items, A, wide,
+                                                                                    slots);
 }
-size_t scene_smem(int v) {
-  return v == 1 ? sizeof(RowScratch<kSceneMaxH1, kSceneXT1>) * kFastWarps
-                : sizeof(RowScratch<kFastMaxH, kFastXT>) * kFastWarps;
-}
-int scene_warps() { return kFastWarps; }
-void launch_scene(int v, unsigned blocks, cudaStream_t st, PathJob* jobs, const SceneRun* runs, int nruns,
-                  long long items, const Arena& A, const uint8_t* tbl, unsigned char* wide, long long slots,
-                  int sliceW) {
-  if (v == 1)
-    k_scene<kSceneMaxH1, kSceneXT1, kFastWarps><<<blocks, kFastWarps * 32, scene_smem(1), st>>>(
-        jobs, runs, nruns, items, A, tbl, wide, slots, sliceW);
-  else
-    k_scene<kFastMaxH, kFastXT, kFastWarps><<<blocks, kFastWarps * 32, scene_smem(0), st>>>(
-        jobs, runs, nruns, items, A, tbl, wide, slots, sliceW);
+void launch_scene(unsigned blocks, cudaStream_t st, PathJob* jobs, const SceneRun* runs, int nruns, long long items,
+                  const Arena& A, const uint8_t* tbl, int sliceW) {
+  k_scene<kSceneXT, kSceneWarps><<<blocks, kSceneWarps * 32, 0, st>>>(jobs, runs, nruns, items, A, tbl, sliceW);
 }
 
 // Dynamic shared memory of k_setup for a launch whose images have at most

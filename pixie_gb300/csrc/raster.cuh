@@ -60,6 +60,7 @@ struct PathJob {
   uint8_t* img;  // RGBX or A8, row-major, W*H pixels
   long long W, H;
   long long row_off;  // prefix of row-kernel work items over the batch
+  long long ri_off;   // scenes: the job's rows in Arena::rowidx
   // outputs (setup kernel)
   int status, nseg, nb;
   uint32_t ph;
@@ -83,7 +84,8 @@ struct MaskDraw {
 };
 
 enum ArenaCounter {
-  kCtrSegs = 0, kCtrBands, kCtrOvfRows, kCtrXClears, kCtrBandSegs, kCtrRowErr, kCtrQueue, kNumCounters
+  kCtrSegs = 0, kCtrBands, kCtrOvfRows, kCtrXClears, kCtrBandSegs, kCtrRowErr, kCtrQueue,
+  kCtrProg, kCtrProgFull, kCtrQueue2, kNumCounters
 };
 
 struct Arena {
@@ -98,6 +100,9 @@ struct Arena {
   long long bandseg_cap;
   int* primcnt;    // per primitive: segments emitted, then their exclusive prefix
   long long primcnt_cap;
+  int4* prog;          // scenes: row programs (16-byte units)
+  long long prog_cap;
+  long long* rowidx;   // scenes: per job and row, the first unit of its program (-1: none)
   unsigned long long* counters;
   long long* ovf_rows;  // packed (job << 32 | y) rows whose crossings exceed the fast kernel
   long long ovf_cap;
