@@ -203,7 +203,7 @@ struct Ctx {
   long long mdraw_cap = 0;
   int4* prog = nullptr;           // scene row programs
   long long prog_cap = 0;
-  long long* rowidx = nullptr;    // scene rows -> program
+  int* rowidx = nullptr;          // scene rows -> program
   long long rowidx_cap = 0;
   unsigned char* wide = nullptr;  // per-warp wide row scratch of the scene recording kernel
   long long wide_slots = 0;
@@ -652,7 +652,7 @@ void run_scene_runs(std::vector<HostRun>& runs) {
     long long pc = 0;
     std::vector<SceneRun> sr;
     std::vector<size_t> which;  // launch run -> runs index
-    long long items = 0, recItems = 0, maxH = 1;
+    long long items = 0, recItems = 0, riTotal = 0, maxH = 1;
     const int slice = g.scene_slice;
     for (size_t ri = 0; ri < runs.size(); ri++) {
       HostRun& r = runs[ri];
@@ -661,7 +661,10 @@ void run_scene_runs(std::vector<HostRun>& runs) {
       s.row_off = items;
       s.W = r.canvas->width;
       s.H = r.canvas->height;
+      s.img = r.canvas->data;
       s.j0 = (int)dev.size();
+      s.ri_base = riTotal;
+      const long long nrun = (long long)(r.j1 - r.j0);
       for (size_t j = r.j0; j < r.j1; j++) {
         PathJob pj = (*r.jobs)[j];
         if (pj.group == 0) pj.group = curve_group(*r.prims, pj.prim_off, pj.nprims);
@@ -672,12 +675,14 @@ void run_scene_runs(std::vector<HostRun>& runs) {
         pj.W = r.canvas->width;
         pj.H = r.canvas->height;
         pj.row_off = recItems;  // recording items: one per row of the canvas
-        pj.ri_off = recItems;
         recItems += pj.H;
+        pj.ri_off = s.ri_base + (long long)(j - r.j0);
+        pj.ri_stride = nrun;
         pj.status = kOk;
         dev.push_back(pj);
       }
       s.j1 = (int)dev.size();
+      riTotal += s.H * nrun;
       items += s.H * ((s.W + slice - 1) / slice);
       maxH = std::max<long long>(maxH, s.H);
       sr.push_back(s);
@@ -689,7 +694,7 @@ void run_scene_runs(std::vector<HostRun>& runs) {
     ensure_arena(seg_need, list_need, (long long)nj * maxBands, pc, 1);
     if (prog_need == 0) prog_need = std::max<long long>(1 << 20, recItems * 8);
     dev_grow(g.prog, g.prog_cap, prog_need);
-    dev_grow(g.rowidx, g.rowidx_cap, std::max<long long>(recItems, 1));
+    dev_grow(g.rowidx, g.rowidx_cap, std::max<long long>(riTotal, 1));
     const long long recBlocks = std::max<long long>(
         1, std::min<long long>((recItems + scene_rec_warps() - 1) / scene_rec_warps(),
                                (long long)g.nsm * g.scene_ctas_per_sm[0]));
@@ -706,6 +711,7 @@ void run_scene_runs(std::vector<HostRun>& runs) {
     Staged S = stage(dev, sr.data(), sizeof(SceneRun) * sr.size(), std::vector<Prim>());
     k_setup<<<nj, 256, setup_smem(maxBands), g.stream>>>(S.dj, S.A, maxBands); note_launch();
     CU(cudaGetLastError());
+    CU(cudaMemsetAsync(g.rowidx, 0xff, sizeof(int) * (size_t)std::max<long long>(riTotal, 1), g.stream));
     launch_scene_rec((unsigned)recBlocks, g.stream, S.dj, nj, recItems, S.A, g.wide, g.wide_slots); note_launch();
     CU(cudaGetLastError());
     launch_scene((unsigned)blocks, g.stream, S.dj, reinterpret_cast<const SceneRun*>(S.extra), (int)sr.size(), items,

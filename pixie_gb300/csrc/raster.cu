@@ -131,6 +131,115 @@ __device__ int flatten_curve_group(const Prim& p, float ems, int G, int gl, int 
   return kOk;
 }
 
+// Every group of a warp flattens its curves (primitives gid, gid + NG, ...,
+// lines skipped) with the search of flatten_curve_group, but the groups step
+// together: one search window per iteration of a warp-wide loop, so the warp
+// never serialises its groups' divergent loops.  A group that finishes a
+// curve starts its next one in the same loop.  emit(p, prev, next) is called
+// by every lane of the group for each segment addSegment keeps.  Returns the
+// lane's group's error status for the first failing curve it met (kOk if
+// none) and that curve's index in errp.
+template <class Emit, class Done>
+__device__ int flatten_curves_converged(const Prim* P, int np, float ems, int G, int gid, int NG, int gl, int leader,
+                                        int& errp, Emit&& emit, Done&& done) {
+  const unsigned gbits = G == 32 ? 0xffffffffu : ((1u << G) - 1);
+  auto next_curve = [&](int q) {
+    while (q < np && P[q].kind == kPrimLine) q += NG;
+    return q;
+  };
+  int p = next_curve(gid);
+  bool cubic = false;
+  V2 at{0, 0}, c1{0, 0}, c2{0, 0}, to{0, 0}, prev{0, 0};
+  float t = 0, s0 = 1;
+  bool halfStepping = false;
+  int base = 0;
+  long long rounds = 0;
+  auto start = [&]() {
+    if (p >= np) return;
+    const Prim& q = P[p];
+    cubic = q.kind == kPrimCubic;
+    at = V2{q.x[0], q.y[0]};
+    c1 = V2{q.x[1], q.y[1]};
+    c2 = V2{q.x[2], q.y[2]};
+    to = V2{cubic ? q.x[3] : q.x[2], cubic ? q.y[3] : q.y[2]};
+    t = 0;
+    s0 = 1;
+    prev = at;
+    halfStepping = false;
+    base = 0;
+    rounds = 0;
+  };
+  start();
+  int status = kOk;
+  while (true) {
+    const bool active = p < np;
+    if (!__any_sync(0xffffffffu, active)) break;
+    const int k = base + gl;
+    const float sk = k < 100 ? s0 * pow2neg(k) : 0.0f;
+    const bool invalid = sk <= FLT_EPSILON;
+    bool accept = false;
+    V2 nx{0, 0};
+    if (active && !invalid) {
+      const float sh = sk * 0.5f;
+      if (cubic) {
+        nx = cubicAt(at, c1, c2, to, t + sk);
+        const V2 halfway = cubicAt(at, c1, c2, to, t + sh);
+        const V2 midpoint = (prev + nx) / 2;
+        const V2 lineTangent = midpoint - prev;
+        const V2 curveTangent = cubicDeriv(at, c1, c2, to, t + sh);
+        const V2 scaled = (curveTangent / length(curveTangent)) * length(lineTangent);
+        const float error = lengthSq(midpoint - halfway);
+        const float errorTangent = lengthSq(lineTangent - scaled);
+        accept = !(error + errorTangent > ems);
+      } else {
+        nx = quadAt(at, c1, c2, t + sk);
+        const V2 halfway = quadAt(at, c1, c2, t + sh);
+        const V2 midpoint = (prev + nx) / 2;
+        accept = !(lengthSq(midpoint - halfway) > ems);
+      }
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, active && (invalid || accept));
+    const unsigned mine = (b >> leader) & gbits;
+    const int src = leader + (mine ? __ffs(mine) - 1 : 0);
+    const int srcInvalid = __shfl_sync(0xffffffffu, (int)invalid, src);
+    const float nxx = __shfl_sync(0xffffffffu, nx.x, src);
+    const float nxy = __shfl_sync(0xffffffffu, nx.y, src);
+    if (!active) continue;
+    if (++rounds > kIterCap) {
+      status = kErrIterLimit;
+      errp = p;
+      p = np;
+      continue;
+    }
+    if (!mine) {
+      base += G;
+      continue;
+    }
+    if (srcInvalid) {
+      status = cubic ? kErrCubic : kErrQuad;
+      errp = p;
+      p = np;
+      continue;
+    }
+    const int kdec = base + __ffs(mine) - 1;
+    const float step = s0 * pow2neg(kdec);
+    const V2 nxt{nxx, nxy};
+    if (prev.x - nxt.x != 0.0f || prev.y - nxt.y != 0.0f) emit(p, prev, nxt);
+    t += step;
+    if (t == 1) {
+      done(p);
+      p = next_curve(p + NG);
+      start();
+      continue;
+    }
+    prev = nxt;
+    if (kdec > 0) halfStepping = true;
+    s0 = (!cubic && halfStepping) ? nmin(step, 1 - t) : nmin(step * 2, 1 - t);
+    base = 0;
+  }
+  return status;
+}
+
 // transform + shapesToSegments for one emitted pair (paths.nim:1059-1096).
 // vmath quantize(v, 1/256) = sign(v) * floor(|v| / n) * n.
 __device__ __forceinline__ float quantize256(float v) {
@@ -286,19 +395,21 @@ __global__ void __launch_bounds__(256) k_setup(PathJob* jobs, Arena A, int maxBa
     V2 a{P[p].x[0], P[p].y[0]}, b{P[p].x[1], P[p].y[1]};
     PC[p] = ((a.x - b.x != 0.0f || a.y - b.y != 0.0f) && make_seg(J, a, b, s, w)) ? 1 : 0;
   }
-  for (int p = gid; p < np; p += NG) {
-    if (P[p].kind == kPrimLine) continue;
-    int cnt = 0;
-    int st = flatten_curve_group(P[p], J.ems, G, gl, leader, gmask, [&](V2 a, V2 b) {
-      float4 s;
-      int w;
-      if (make_seg(J, a, b, s, w)) cnt++;
-    });
-    if (st != kOk) {  // the reference raises at the first failing primitive
-      if (gl == 0) atomicMin(&s_err, ((long long)p << 8) | st);
-      break;
-    }
-    if (gl == 0) PC[p] = cnt;
+  {
+    int cnt = 0, errp = 0;
+    const int st = flatten_curves_converged(
+        P, np, J.ems, G, gid, NG, gl, leader, errp,
+        [&](int, V2 a, V2 b) {
+          float4 s;
+          int w;
+          if (make_seg(J, a, b, s, w)) cnt++;
+        },
+        [&](int p) {
+          if (gl == 0) PC[p] = cnt;
+          cnt = 0;
+        });
+    if (st != kOk && gl == 0)  // the reference raises at the first failing primitive
+      atomicMin(&s_err, ((long long)errp << 8) | st);
   }
   __syncthreads();
   if (s_err != LLONG_MAX) {
@@ -343,17 +454,19 @@ __global__ void __launch_bounds__(256) k_setup(PathJob* jobs, Arena A, int maxBa
     V2 a{P[p].x[0], P[p].y[0]}, b{P[p].x[1], P[p].y[1]};
     if ((a.x - b.x != 0.0f || a.y - b.y != 0.0f) && make_seg(J, a, b, s, w)) put(s_segbase + PC[p], s, w);
   }
-  for (int p = gid; p < np; p += NG) {
-    if (P[p].kind == kPrimLine) continue;
-    long long o = s_segbase + PC[p];
-    flatten_curve_group(P[p], J.ems, G, gl, leader, gmask, [&](V2 a, V2 b) {
-      float4 s;
-      int w;
-      if (make_seg(J, a, b, s, w)) {
-        if (gl == 0) put(o, s, w);
-        o++;
-      }
-    });
+  {
+    int cnt = 0, errp = 0;
+    flatten_curves_converged(
+        P, np, J.ems, G, gid, NG, gl, leader, errp,
+        [&](int p, V2 a, V2 b) {
+          float4 s;
+          int w;
+          if (make_seg(J, a, b, s, w)) {
+            if (gl == 0) put(s_segbase + PC[p] + cnt, s, w);
+            cnt++;
+          }
+        },
+        [&](int) { cnt = 0; });
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -676,14 +789,19 @@ struct PxRef {
     return *this;
   }
 };
+// base holds pixel x0 (0 for a whole image row; a row slice staged in shared
+// memory starts at its first pixel).
 template <bool A8>
 struct RowPx {
   unsigned char* base;
-  __device__ __forceinline__ PxRef<A8> operator[](long long x) const { return PxRef<A8>{base + x * (A8 ? 1 : 4)}; }
+  long long x0;
+  __device__ __forceinline__ PxRef<A8> operator[](long long x) const {
+    return PxRef<A8>{base + (x - x0) * (A8 ? 1 : 4)};
+  }
 };
 template <bool A8>
 __device__ __forceinline__ RowPx<A8> row_of(const PathJob& J, long long y) {
-  return RowPx<A8>{J.img + y * J.W * (A8 ? 1 : 4)};
+  return RowPx<A8>{J.img + y * J.W * (A8 ? 1 : 4), 0};
 }
 
 // Linear-index clear of [y*W + a, y*W + b) (clearUnsafe :1433-1440 with
@@ -828,11 +946,22 @@ __device__ void apply_cov(RowPx<A8> row, int mode, const uint8_t* tbl, uint32_t 
       acc[i] = run;
     }
     __syncwarp();
-    for (int i = lane; i < L; i += 32) {
-      const uint32_t cov = (uint32_t)acc[i] & 255u;
-      const long long x = tx0 + i;
-      // pixels op_cov leaves unchanged are neither read nor written
-      if (maskMode ? cov != 255u : cov != 0u) row[x] = op_cov(mode, tbl, row[x], rgbx, cov);
+    // pixels op_cov leaves unchanged are neither read nor written; the
+    // backdrops of 8 pixels per lane are loaded before any is blended
+    for (int i0 = 0; i0 < L; i0 += 256) {
+      uint32_t bd[8], cv[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const int i = i0 + lane + 32 * u;
+        cv[u] = i < L ? ((uint32_t)acc[i] & 255u) : (maskMode ? 255u : 0u);
+        bd[u] = 0u;
+        if (maskMode ? cv[u] != 255u : cv[u] != 0u) bd[u] = row[tx0 + i];
+      }
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const int i = i0 + lane + 32 * u;
+        if (maskMode ? cv[u] != 255u : cv[u] != 0u) row[tx0 + i] = op_cov(mode, tbl, bd[u], rgbx, cv[u]);
+      }
     }
     __syncwarp();
   }
@@ -868,12 +997,12 @@ __device__ __forceinline__ long long rec_alloc(const PathJob& J, const Arena& A,
   unsigned long long base = 0;
   if (lane == 0) {
     base = atomicAdd(&A.counters[kCtrProg], (unsigned long long)units);
-    if ((long long)(base + units) > A.prog_cap) {
+    if ((long long)(base + units) > A.prog_cap || base + units > (unsigned long long)INT_MAX) {
       atomicOr(&A.counters[kCtrProgFull], 1ull);
-      A.rowidx[J.ri_off + y] = -1;
+      A.rowidx[J.ri_off + y * J.ri_stride] = -1;
       base = ~0ull;
     } else {
-      A.rowidx[J.ri_off + y] = (long long)base;
+      A.rowidx[J.ri_off + y * J.ri_stride] = (int)base;
     }
   }
   base = __shfl_sync(0xffffffffu, base, 0);
@@ -1193,7 +1322,7 @@ __device__ bool process_row(const PathJob& J, const Arena& A, const uint8_t* tbl
 
   if (REC) {
     const long long at = nsp > 0 ? rec_alloc(J, A, y, 1 + (nsp + 1) / 2, lane) : -1;
-    if (nsp == 0 && lane == 0) A.rowidx[J.ri_off + y] = -1;
+    if (nsp == 0 && lane == 0) A.rowidx[J.ri_off + y * J.ri_stride] = -1;
     if (at >= 0) {
       if (lane == 0) A.prog[at] = make_int4(aa ? kRecCov : kRecHits, nsp, sc, 0);
       int2* d = reinterpret_cast<int2*>(A.prog + at + 1);
@@ -1364,7 +1493,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_scene_rec(PathJob* jobs, int njo
     }
     if (!ok && lane == 0) {
       atomicMin(&A.counters[kCtrRowErr], (unsigned long long)lo);
-      A.rowidx[J.ri_off + y] = -1;
+      A.rowidx[J.ri_off + y * J.ri_stride] = -1;
     }
     __syncwarp();
   }
@@ -1375,8 +1504,10 @@ __global__ void __launch_bounds__(WARPS * 32) k_scene(PathJob* jobs, const Scene
                                                       long long totalItems, Arena A, const uint8_t* tbl,
                                                       int sliceW) {
   __shared__ int accs[WARPS][XT + 1];
+  __shared__ uint32_t pix[WARPS][XT];  // the warp's row slice while its paths are applied
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int* acc = accs[warp];
+  const bool staged = sliceW <= XT;
   if (A.counters[kCtrProgFull]) return;  // programs incomplete: the host reruns the launch
   while (true) {
     unsigned long long q = 0;
@@ -1395,38 +1526,69 @@ __global__ void __launch_bounds__(WARPS * 32) k_scene(PathJob* jobs, const Scene
     const long long y = local / ns;
     const long long xa = (local % ns) * sliceW, xb = min(xa + sliceW, R.W);
     if (y >= R.H) continue;
-    for (int j = R.j0; j < R.j1; j++) {
-      const PathJob& J = jobs[j];
-      const int st = J.status;
-      if (st != kOk) {
-        if (st == kNothing) continue;
-        break;
+    uint32_t* grow = reinterpret_cast<uint32_t*>(R.img) + y * R.W;
+    if (staged) {
+      for (long long x = xa + lane; x < xb; x += 32) pix[warp][x - xa] = grow[x];
+      __syncwarp();
+    }
+    const RowPx<false> row = staged ? RowPx<false>{reinterpret_cast<unsigned char*>(pix[warp]), xa}
+                                    : RowPx<false>{reinterpret_cast<unsigned char*>(grow), 0};
+    // 32 paths at a time: each lane loads one path's row program index and
+    // header (the row's indices are contiguous), then the warp replays the
+    // programs in path order.
+    const long long rb = R.ri_base + y * (long long)(R.j1 - R.j0);
+    for (int c0 = R.j0; c0 < R.j1; c0 += 32) {
+      const int j = c0 + lane;
+      const bool valid = j < R.j1;
+      int st = kNothing, at = -1, mode = 0;
+      uint32_t rgbx = 0;
+      long long sx = 0, pw = 0;
+      if (valid) {
+        const PathJob& J = jobs[j];
+        st = J.status;
+        at = A.rowidx[rb + (j - R.j0)];
+        sx = J.startX;
+        pw = J.pathWidth;
+        mode = J.mode;
+        rgbx = J.rgbx;
       }
-      if (y < J.startY || y >= J.pathHeight) continue;
-      if (J.startX >= xb || J.startX + J.pathWidth <= xa) continue;
-      const long long at = A.rowidx[J.ri_off + y];
-      if (at < 0) continue;
-      const int4 h = A.prog[at];
-      const RowPx<false> row = row_of<false>(J, y);
-      const int mode = J.mode;
-      const uint32_t rgbx = J.rgbx;
-      if (h.x == kRecFill) {
-        for (long long x = max((long long)h.z, xa) + lane; x < min((long long)h.w, xb); x += 32)
-          row[x] = op_fill(mode, tbl, row[x], rgbx);
-      } else if (h.x == kRecCov) {
-        const long long px0 = J.startX, px1 = J.startX + J.pathWidth;
-        apply_cov<false, XT>(row, mode, tbl, rgbx, reinterpret_cast<const int2*>(A.prog + at + 1), h.y, h.z,
-                             max(px0, xa), min(px1, xb), acc, lane);
-      } else if (h.x == kRecHits) {
-        apply_hits<false>(row, mode, tbl, rgbx, reinterpret_cast<const int2*>(A.prog + at + 1), h.y, xa, xb, lane);
-      } else if (h.x == kRecTrap) {
-        for (int p = 0; p < h.y; p++) {
-          const int4 e = A.prog[at + 1 + 2 * p], t = A.prog[at + 2 + 2 * p];
-          apply_trap_pair<false>(row, mode, tbl, rgbx, y, J.W, __int_as_float(e.x), __int_as_float(e.y),
-                                 __int_as_float(e.z), __int_as_float(e.w), __int_as_float(t.x), __int_as_float(t.y),
-                                 __int_as_float(t.z), __int_as_float(t.w), xa, xb, lane);
+      // the first failed path stops the run: it and the paths after it draw nothing
+      const unsigned bad = __ballot_sync(0xffffffffu, valid && st != kOk && st != kNothing);
+      const int lim = bad ? __ffs(bad) - 1 : 32;
+      const bool draws = valid && lane < lim && st == kOk && at >= 0 && sx < xb && sx + pw > xa;
+      int4 h = make_int4(0, 0, 0, 0);
+      if (draws) h = A.prog[at];
+      unsigned dm = __ballot_sync(0xffffffffu, draws);
+      while (dm) {
+        const int i = __ffs(dm) - 1;
+        dm &= dm - 1;
+        const int hx = __shfl_sync(0xffffffffu, h.x, i), hy = __shfl_sync(0xffffffffu, h.y, i);
+        const int hz = __shfl_sync(0xffffffffu, h.z, i), hw = __shfl_sync(0xffffffffu, h.w, i);
+        const int ai = __shfl_sync(0xffffffffu, at, i), mi = __shfl_sync(0xffffffffu, mode, i);
+        const uint32_t ci = __shfl_sync(0xffffffffu, rgbx, i);
+        const long long sxi = __shfl_sync(0xffffffffu, sx, i), pwi = __shfl_sync(0xffffffffu, pw, i);
+        if (hx == kRecFill) {
+          for (long long x = max((long long)hz, xa) + lane; x < min((long long)hw, xb); x += 32)
+            row[x] = op_fill(mi, tbl, row[x], ci);
+        } else if (hx == kRecCov) {
+          apply_cov<false, XT>(row, mi, tbl, ci, reinterpret_cast<const int2*>(A.prog + ai + 1), hy, hz,
+                               max(sxi, xa), min(sxi + pwi, xb), acc, lane);
+        } else if (hx == kRecHits) {
+          apply_hits<false>(row, mi, tbl, ci, reinterpret_cast<const int2*>(A.prog + ai + 1), hy, xa, xb, lane);
+        } else if (hx == kRecTrap) {
+          for (int p = 0; p < hy; p++) {
+            const int4 e = A.prog[ai + 1 + 2 * p], t = A.prog[ai + 2 + 2 * p];
+            apply_trap_pair<false>(row, mi, tbl, ci, y, R.W, __int_as_float(e.x), __int_as_float(e.y),
+                                   __int_as_float(e.z), __int_as_float(e.w), __int_as_float(t.x),
+                                   __int_as_float(t.y), __int_as_float(t.z), __int_as_float(t.w), xa, xb, lane);
+          }
         }
+        __syncwarp();
       }
+      if (bad) break;
+    }
+    if (staged) {
+      for (long long x = xa + lane; x < xb; x += 32) grow[x] = pix[warp][x - xa];
       __syncwarp();
     }
   }

@@ -60,7 +60,8 @@ struct PathJob {
   uint8_t* img;  // RGBX or A8, row-major, W*H pixels
   long long W, H;
   long long row_off;  // prefix of row-kernel work items over the batch
-  long long ri_off;   // scenes: the job's rows in Arena::rowidx
+  long long ri_off;     // scenes: row y of the job is Arena::rowidx[ri_off + y * ri_stride]
+  long long ri_stride;
   // outputs (setup kernel)
   int status, nseg, nb;
   uint32_t ph;
@@ -73,6 +74,8 @@ struct PathJob {
 struct SceneRun {
   long long row_off;  // prefix of (row, slice) work items over the launch's runs
   long long W, H;
+  uint8_t* img;       // the canvas (RGBX)
+  long long ri_base;  // row y, path j: Arena::rowidx[ri_base + y * (j1 - j0) + j - j0]
   int j0, j1;
 };
 
@@ -102,7 +105,7 @@ struct Arena {
   long long primcnt_cap;
   int4* prog;          // scenes: row programs (16-byte units)
   long long prog_cap;
-  long long* rowidx;   // scenes: per job and row, the first unit of its program (-1: none)
+  int* rowidx;         // scenes: per row and job, the first unit of its program (-1: none)
   unsigned long long* counters;
   long long* ovf_rows;  // packed (job << 32 | y) rows whose crossings exceed the fast kernel
   long long ovf_cap;
