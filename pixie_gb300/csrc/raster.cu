@@ -946,21 +946,19 @@ __device__ void apply_cov(RowPx<A8> row, int mode, const uint8_t* tbl, uint32_t 
       acc[i] = run;
     }
     __syncwarp();
-    // pixels op_cov leaves unchanged are neither read nor written; the
-    // backdrops of 8 pixels per lane are loaded before any is blended
-    for (int i0 = 0; i0 < L; i0 += 256) {
-      uint32_t bd[8], cv[8];
-#pragma unroll
-      for (int u = 0; u < 8; u++) {
-        const int i = i0 + lane + 32 * u;
-        cv[u] = i < L ? ((uint32_t)acc[i] & 255u) : (maskMode ? 255u : 0u);
-        bd[u] = 0u;
-        if (maskMode ? cv[u] != 255u : cv[u] != 0u) bd[u] = row[tx0 + i];
-      }
-#pragma unroll
-      for (int u = 0; u < 8; u++) {
-        const int i = i0 + lane + 32 * u;
-        if (maskMode ? cv[u] != 255u : cv[u] != 0u) row[tx0 + i] = op_cov(mode, tbl, bd[u], rgbx, cv[u]);
+    // pixels op_cov leaves unchanged are neither read nor written; the next
+    // pixel's backdrop is loaded while the current one is blended
+    {
+      const uint32_t keep = maskMode ? 255u : 0u;
+      uint32_t cvN = lane < L ? ((uint32_t)acc[lane] & 255u) : keep;
+      uint32_t bdN = cvN != keep ? (uint32_t)row[tx0 + lane] : 0u;
+#pragma unroll 1
+      for (int i = lane; i < L; i += 32) {
+        const uint32_t cv = cvN, bd = bdN;
+        const int in = i + 32;
+        cvN = in < L ? ((uint32_t)acc[in] & 255u) : keep;
+        bdN = cvN != keep ? (uint32_t)row[tx0 + in] : 0u;
+        if (cv != keep) row[tx0 + i] = op_cov(mode, tbl, bd, rgbx, cv);
       }
     }
     __syncwarp();
