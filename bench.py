@@ -566,7 +566,7 @@ def run_reference(args, ws, rank):
             "ms_per_step": per_step_single * 1e3 / cores}
 
 
-def run_case(case: str):
+def run_case(case: str, slice_w: int = 0):
     """One small, self-contained invocation of a single operation (used for
     ncu captures of one kernel on a small case)."""
     import pixie_gb300 as px
@@ -593,6 +593,8 @@ def run_case(case: str):
                                 winding_rules=[g[3] for g in glyphs])
     elif case in ("scene", "scene_small"):  # dense scene: 2000 paths on 1024^2 (small: 400 on 512^2)
         n, side = (2000, 1024) if case == "scene" else (400, 512)
+        if slice_w:
+            px.scene_config(slice_w)
         sc, _ = record_scene(px, wl.dense_scene(7, n_paths=n, size=float(side)))
         img = px.Image(side, side)
         for _ in range(2):
@@ -625,11 +627,12 @@ def main():
     ap.add_argument("--serve-pool", type=int, default=12, help="distinct recorded jobs the arrivals draw from")
     ap.add_argument("--no-fill", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--slice", type=int, default=0, help="scene row slice width for --case scene*")
     ap.add_argument("--case", default=None,
                     help="run one small operation for profiling: fill512 | blur64 | draw | glyphs | scene | scene_small | masks")
     args = ap.parse_args()
     if args.case:
-        run_case(args.case)
+        run_case(args.case, args.slice)
         return
     ws, rank, local = dist_setup()
 

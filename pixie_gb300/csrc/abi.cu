@@ -692,7 +692,7 @@ void run_scene_runs(std::vector<HostRun>& runs) {
     const int nj = (int)dev.size();
     const int maxBands = setup_max_bands(maxH);
     ensure_arena(seg_need, list_need, (long long)nj * maxBands, pc, 1);
-    if (prog_need == 0) prog_need = std::max<long long>(1 << 20, recItems * 8);
+    if (prog_need == 0) prog_need = std::max<long long>(1 << 20, recItems * 24);
     dev_grow(g.prog, g.prog_cap, prog_need);
     dev_grow(g.rowidx, g.rowidx_cap, std::max<long long>(riTotal, 1));
     const long long recBlocks = std::max<long long>(
