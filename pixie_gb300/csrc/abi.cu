@@ -251,10 +251,15 @@ void init_locked(int device) {
   g.smemOptin = prop.sharedMemPerBlockOptin;
   CU(cudaStreamCreateWithFlags(&g.own, cudaStreamNonBlocking));
   g.stream = g.own;
-  std::vector<uint8_t> t(65536);
+  // the straight-alpha table (256 x 256 bytes), then v / 255.0f for v = 0..255
+  std::vector<uint8_t> t(kTblBytes);
   straight_alpha_table(t.data());
-  CU(cudaMalloc(&g.tbl, 65536));
-  CU(cudaMemcpy(g.tbl, t.data(), 65536, cudaMemcpyHostToDevice));
+  for (int v = 0; v < 256; v++) {
+    const float f = (float)v / 255.0f;
+    memcpy(t.data() + kTblUnitOff + 4 * v, &f, 4);
+  }
+  CU(cudaMalloc(&g.tbl, kTblBytes));
+  CU(cudaMemcpy(g.tbl, t.data(), kTblBytes, cudaMemcpyHostToDevice));
   for (int v = 0; v < 2; v++) {
     CU(cudaFuncSetAttribute(rows_kernel(v), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem(v)));
     int per = 0;

@@ -102,6 +102,10 @@ __device__ __forceinline__ uint32_t premul8(uint32_t sv) {  // internal.nim:86-9
   if (s.a == 255) return sv;
   return pack((s.r * s.a + 127) / 255, (s.g * s.a + 127) / 255, (s.b * s.a + 127) / 255, s.a);
 }
+// The device table: the straight-alpha table (256 x 256 bytes, row = alpha),
+// then 256 floats v / 255.0f (the float division, done once on the host).
+constexpr size_t kTblUnitOff = 65536, kTblBytes = 65536 + 1024;
+
 __device__ __forceinline__ Px straight8(const uint8_t* tbl, uint32_t v) {
   Px p = unpack(v);
   const uint8_t* row = tbl + p.a * 256;
@@ -175,9 +179,10 @@ __device__ __forceinline__ float softLight1(float cb, float cs) {
 }
 static __device__ __noinline__ uint32_t blendFloat(const uint8_t* tbl, uint32_t bp, uint32_t sp, int mode) {
   Px b8 = straight8(tbl, bp), s8 = straight8(tbl, sp);
-  F3 cb{b8.r / 255.0f, b8.g / 255.0f, b8.b / 255.0f};
-  F3 cs{s8.r / 255.0f, s8.g / 255.0f, s8.b / 255.0f};
-  float ab = b8.a / 255.0f, as = s8.a / 255.0f;
+  const float* u = reinterpret_cast<const float*>(tbl + kTblUnitOff);  // u[v] = v / 255.0f
+  F3 cb{u[b8.r], u[b8.g], u[b8.b]};
+  F3 cs{u[s8.r], u[s8.g], u[s8.b]};
+  float ab = u[b8.a], as = u[s8.a];
   F3 m;
   switch (mode) {
     case kSoftLight:

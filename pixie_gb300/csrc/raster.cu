@@ -723,13 +723,22 @@ __global__ void __launch_bounds__(256) k_setup(PathJob* jobs, Arena A, int maxBa
 __device__ __forceinline__ bool shouldFill(int rule, long long count) {  // :1288-1296
   return rule == 0 ? count != 0 : (count % 2 != 0);
 }
+// The generic blender, kept out of line: the row code calls it from several
+// places, and one copy keeps the kernels small enough for the instruction
+// cache.  NormalBlend stays inline at every call site.
+static __device__ __noinline__ uint32_t blend_any(int mode, const uint8_t* tbl, uint32_t b, uint32_t s) {
+  return blend_px(mode, tbl, b, s);
+}
+__device__ __forceinline__ uint32_t blend_row(int mode, const uint8_t* tbl, uint32_t b, uint32_t s) {
+  return mode == kNormal ? blendNormal(b, s) : blend_any(mode, tbl, b, s);
+}
 // FILL: a fillHits span (:1540-1591)
 __device__ __forceinline__ uint32_t op_fill(int mode, const uint8_t* tbl, uint32_t b, uint32_t c) {
   switch (mode) {
     case kOverwrite: return c;
     case kNormal: return (c >> 24) == 255 ? c : blendNormal(b, c);
     case kMask: return (c >> 24) != 255 ? blendMaskPx(b, c) : b;
-    default: return blend_px(mode, tbl, b, c);
+    default: return blend_any(mode, tbl, b, c);
   }
 }
 // COV: fillCoverage with coverage k (:1442-1526)
@@ -738,7 +747,7 @@ __device__ __forceinline__ uint32_t op_cov(int mode, const uint8_t* tbl, uint32_
   if (k == 0) return b;
   if (mode == kOverwrite) return mul_c(c, k);
   if (mode == kNormal) return blendNormal(b, mul_c(c, k));
-  return blend_px(mode, tbl, b, mul_c(c, k));
+  return blend_any(mode, tbl, b, mul_c(c, k));
 }
 
 template <int MAXH, int XT>
@@ -856,7 +865,7 @@ __device__ __forceinline__ void apply_trap_pair(RowPx<A8> row, int mode, const u
       float tri = 0.5f * run * fabsf(penY - prevPenY);
       float rect = inv ? (prevPenY - (float)y) * run : ((float)(y + 1) - prevPenY) * run;
       float area = tri + rect + rightRectArea;
-      row[x] = blend_px(mode, tbl, row[x], mul_f(rgbx, area));
+      row[x] = blend_row(mode, tbl, row[x], mul_f(rgbx, area));
     }
   }
   {  // right sliver (:1790-1828)
@@ -875,7 +884,7 @@ __device__ __forceinline__ void apply_trap_pair(RowPx<A8> row, int mode, const u
       float tri = 0.5f * run * fabsf(penY - prevPenY);
       float rect = inv ? (penY - (float)y) * run : ((float)(y + 1) - penY) * run;
       float area = leftRectArea + tri + rect;
-      row[x] = blend_px(mode, tbl, row[x], mul_f(rgbx, area));
+      row[x] = blend_row(mode, tbl, row[x], mul_f(rgbx, area));
     }
   }
   {  // the fully covered middle (:1830-1835)
@@ -929,21 +938,22 @@ __device__ void apply_cov(RowPx<A8> row, int mode, const uint8_t* tbl, uint32_t 
       }
     }
     __syncwarp();
-    // prefix sum of the difference array; coverage = sum mod 256
-    const int C = (L + 31) / 32;
-    int base = lane * C, s = 0;
-    for (int i = base; i < min(base + C, L); i++) s += acc[i];
-    int incl = s;
+    // prefix sum of the difference array, 32 entries per step (lane i holds
+    // entry c0 + i: no bank conflicts); coverage = sum mod 256
+    {
+      int carry = 0;
+      for (int c0 = 0; c0 < L; c0 += 32) {
+        const int i = c0 + lane;
+        int v = i < L ? acc[i] : 0;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      int t = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += t;
-    }
-    int run = incl - s;
-    __syncwarp();
-    for (int i = base; i < min(base + C, L); i++) {
-      run += acc[i];
-      acc[i] = run;
+        for (int o = 1; o < 32; o <<= 1) {
+          const int t = __shfl_up_sync(0xffffffffu, v, o);
+          if (lane >= o) v += t;
+        }
+        v += carry;
+        if (i < L) acc[i] = v;
+        carry = __shfl_sync(0xffffffffu, v, 31);
+      }
     }
     __syncwarp();
     // pixels op_cov leaves unchanged are neither read nor written; the next
@@ -1498,7 +1508,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_scene_rec(PathJob* jobs, int njo
 }
 
 template <int XT, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) k_scene(PathJob* jobs, const SceneRun* runs, int nruns,
+__global__ void __launch_bounds__(WARPS * 32, 3) k_scene(PathJob* jobs, const SceneRun* runs, int nruns,
                                                       long long totalItems, Arena A, const uint8_t* tbl,
                                                       int sliceW) {
   __shared__ int accs[WARPS][XT + 1];
