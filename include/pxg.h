@@ -150,7 +150,8 @@ int pxg_scene_stroke_path(pxg_scene* scene, const float* commands, int64_t n_com
 int pxg_image_draw_scene(pxg_image* image, const pxg_scene* scene);
 /* Scene drawing configuration (every choice writes the same bytes):
  * slice_width is the part of a canvas row one warp of the drawing pass owns
- * (>= 32 pixels; default 256). */
+ * (>= 32 pixels), or 0 (the default) to choose it per launch from the
+ * canvas rows and the GPU's resident warps. */
 int pxg_scene_config(int slice_width);
 
 /* Mask batches: many paths, each filled with color(1, 1, 1, 1) onto a

@@ -225,7 +225,7 @@ struct Ctx {
   long long stats[4] = {0, 0, 0, 0};  // last fill launch: paths, prims, segments, band entries
   int rows_ctas_per_sm[2] = {1, 1};  // resident CTAs of each row-kernel variant
   int scene_ctas_per_sm[2] = {1, 1};  // resident CTAs of the scene recording and drawing kernels
-  int scene_slice = 256;              // pixels of a row one warp of the drawing pass owns
+  int scene_slice = 0;                // pixels of a row one warp of the drawing pass owns (0: chosen per launch)
   bool blocking = true;  // image operations wait for their GPU work
   std::map<int64_t, uint16_t*> weights;  // gaussian weights per radius, on the device
 };
@@ -642,6 +642,26 @@ const Prim* scene_device_prims(const pxg_scene* sc) {
   return sc->dprims;
 }
 
+// The row slice of the drawing pass.  Each work item replays every path of
+// its run, so items are long and the kernel lasts as long as its busiest
+// warp: the slice is chosen so that the launch has about three items per
+// resident warp (at most 256 pixels, the shared-memory stage), unless a
+// width was set with pxg_scene_config.
+int scene_slice_for(const std::vector<HostRun>& runs) {
+  if (g.scene_slice > 0) return g.scene_slice;
+  long long rows = 0, wmax = 1;
+  for (const HostRun& r : runs) {
+    if (r.status != kOk || r.j0 >= r.j1) continue;
+    rows += r.canvas->height;
+    wmax = std::max<long long>(wmax, r.canvas->width);
+  }
+  const long long slots = (long long)g.nsm * g.scene_ctas_per_sm[1] * scene_warps();
+  const long long per_row = std::max<long long>(1, (3 * slots + rows - 1) / std::max<long long>(rows, 1));
+  long long w = (wmax + per_row - 1) / per_row;
+  w = std::max<long long>(32, std::min<long long>(w, scene_tile()));
+  return (int)w;
+}
+
 // Paints several runs (distinct canvases) in one setup + scene launch pair,
 // repeating for runs whose workspace ran out.  MaskBlend paths must not be
 // inside a run (their clears reach outside the rows the run owns).
@@ -658,7 +678,7 @@ void run_scene_runs(std::vector<HostRun>& runs) {
     std::vector<SceneRun> sr;
     std::vector<size_t> which;  // launch run -> runs index
     long long items = 0, recItems = 0, riTotal = 0, maxH = 1;
-    const int slice = g.scene_slice;
+    const int slice = scene_slice_for(runs);
     for (size_t ri = 0; ri < runs.size(); ri++) {
       HostRun& r = runs[ri];
       if (r.status != kOk || r.j0 >= r.j1) continue;
@@ -844,9 +864,22 @@ double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
+// Canvases come from the device's stream-ordered memory pool: allocation and
+// release are ordered on the library's stream and never synchronise the
+// device, and freed blocks stay in the pool for the next admissions.
+void srv_pool_init() {
+  static bool done = false;
+  if (done) return;
+  cudaMemPool_t pool;
+  CU(cudaDeviceGetDefaultMemPool(&pool, g.dev));
+  uint64_t keep = ~0ull;
+  CU(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+  done = true;
+}
+
 void srv_release(pxg_server* sv, SrvJob* j) {
-  if (j->canvas.data) cudaFree(j->canvas.data);
-  if (j->tmp) cudaFree(j->tmp);
+  if (j->canvas.data) cudaFreeAsync(j->canvas.data, g.stream);
+  if (j->tmp) cudaFreeAsync(j->tmp, g.stream);
   j->canvas.data = nullptr;
   j->tmp = nullptr;
   sv->used -= j->bytes;
@@ -860,11 +893,12 @@ void srv_admit(pxg_server* sv) {
     const long long need = j->W * j->H * 4 * (j->blur > 0 ? 2 : 1);
     if (sv->used + need > sv->budget) break;
     sv->queue.pop_front();
-    CU(cudaMalloc((void**)&j->canvas.data, (size_t)(j->W * j->H * 4)));
+    srv_pool_init();
+    CU(cudaMallocAsync((void**)&j->canvas.data, (size_t)(j->W * j->H * 4), g.stream));
     j->canvas.width = j->W;
     j->canvas.height = j->H;
     j->canvas.owned = 1;
-    if (j->blur > 0) CU(cudaMalloc((void**)&j->tmp, (size_t)(j->W * j->H * 4)));
+    if (j->blur > 0) CU(cudaMallocAsync((void**)&j->tmp, (size_t)(j->W * j->H * 4), g.stream));
     CU(cudaMemsetAsync(j->canvas.data, 0, (size_t)(j->W * j->H * 4), g.stream));
     j->bytes = need;
     sv->used += need;
@@ -960,7 +994,7 @@ void srv_step(pxg_server* sv) {
   for (SrvJob* j : done) {
     srv_finish(sv, j, kOk, "");
     if (j->tmp) {
-      cudaFree(j->tmp);
+      cudaFreeAsync(j->tmp, g.stream);
       j->tmp = nullptr;
       const long long half = j->W * j->H * 4;
       sv->used -= half;
@@ -1015,10 +1049,11 @@ struct GraphCacheHolder {
 pxg_server::~pxg_server() {
   for (auto& kv : jobs) {
     SrvJob* j = kv.second;
-    if (j->canvas.data) cudaFree(j->canvas.data);
-    if (j->tmp) cudaFree(j->tmp);
+    if (j->canvas.data) cudaFreeAsync(j->canvas.data, g.stream);
+    if (j->tmp) cudaFreeAsync(j->tmp, g.stream);
     delete j;
   }
+  if (g.ready) cudaStreamSynchronize(g.stream);
 }
 pxg_masks::~pxg_masks() {
   if (graph) {
@@ -1641,7 +1676,8 @@ int pxg_server_take(pxg_server* sv, int64_t id, void* out, int64_t nbytes, doubl
     const int state = j->state;
     if (state == 2 && out) {
       if (nbytes < j->W * j->H * 4) throw ApiError{"Output buffer too small"};
-      CU(cudaMemcpy(out, j->canvas.data, (size_t)(j->W * j->H * 4), cudaMemcpyDeviceToHost));
+      CU(cudaMemcpyAsync(out, j->canvas.data, (size_t)(j->W * j->H * 4), cudaMemcpyDeviceToHost, g.stream));
+      CU(cudaStreamSynchronize(g.stream));
     }
     srv_release(sv, j);
     sv->jobs.erase(it);
@@ -1666,7 +1702,8 @@ int pxg_server_stats(const pxg_server* sv, int64_t* out6) {
 
 int pxg_scene_config(int slice_width) {
   return guarded([&] {
-    if (slice_width < 32 || slice_width > (1 << 20)) throw ApiError{"Invalid scene configuration"};
+    if (slice_width != 0 && (slice_width < 32 || slice_width > (1 << 20)))
+      throw ApiError{"Invalid scene configuration"};
     g.scene_slice = slice_width;
   });
 }
