@@ -150,9 +150,13 @@ int pxg_scene_stroke_path(pxg_scene* scene, const float* commands, int64_t n_com
 int pxg_image_draw_scene(pxg_image* image, const pxg_scene* scene);
 /* Scene drawing configuration (every choice writes the same bytes):
  * slice_width is the part of a canvas row one warp of the drawing pass owns
- * (>= 32 pixels), or 0 (the default) to choose it per launch from the
- * canvas rows and the GPU's resident warps. */
-int pxg_scene_config(int slice_width);
+ * (>= 32 pixels; default 256), or 0 to choose it per launch from the canvas
+ * rows and the GPU's resident warps.  coverage_bytes >= 0 replaces the arena
+ * in which the recording pass stores rows' coverage bytes (default: 4 GB or
+ * an eighth of free memory); rows that do not fit are recorded as sample
+ * spans and accumulated by the drawing pass instead; a negative value keeps
+ * the current arena. */
+int pxg_scene_config(int slice_width, int64_t coverage_bytes);
 
 /* Mask batches: many paths, each filled with color(1, 1, 1, 1) onto a
  * transparent image of its own size, kept as the 8-bit alpha of that image

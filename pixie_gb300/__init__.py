@@ -114,7 +114,7 @@ def lib():
         L.pxg_scene_fill_path.argtypes = [P, P, I64, P, F, I, P, I]
         L.pxg_scene_stroke_path.argtypes = [P, P, I64, P, F, I, P, F, I, I, F, P, I64]
         L.pxg_image_draw_scene.argtypes = [P, P]
-        L.pxg_scene_config.argtypes = [I]
+        L.pxg_scene_config.argtypes = [I, I64]
         L.pxg_last_fill_stats.argtypes = [P]
         L.pxg_masks_new.restype = P
         L.pxg_masks_free.argtypes = [P]
@@ -443,9 +443,9 @@ class Server:
                         [int(x) for x in v]))
 
 
-def scene_config(slice_width: int):
+def scene_config(slice_width: int = 256, coverage_bytes: int = -1):
     """Scene drawing configuration (see pxg_scene_config)."""
-    _check(lib().pxg_scene_config(int(slice_width)))
+    _check(lib().pxg_scene_config(int(slice_width), int(coverage_bytes)))
 
 
 def autotune(enable: bool):

@@ -205,6 +205,8 @@ struct Ctx {
   long long prog_cap = 0;
   int* rowidx = nullptr;          // scene rows -> program
   long long rowidx_cap = 0;
+  uint8_t* cov8 = nullptr;        // scene coverage bytes (rows that fit; the rest keep spans)
+  long long cov8_cap = 0;
   unsigned char* wide = nullptr;  // per-warp wide row scratch of the scene recording kernel
   long long wide_slots = 0;
   long long* ovf = nullptr;
@@ -225,7 +227,7 @@ struct Ctx {
   long long stats[4] = {0, 0, 0, 0};  // last fill launch: paths, prims, segments, band entries
   int rows_ctas_per_sm[2] = {1, 1};  // resident CTAs of each row-kernel variant
   int scene_ctas_per_sm[2] = {1, 1};  // resident CTAs of the scene recording and drawing kernels
-  int scene_slice = 0;                // pixels of a row one warp of the drawing pass owns (0: chosen per launch)
+  int scene_slice = 256;              // pixels of a row one warp of the drawing pass owns (0: chosen per launch)
   bool blocking = true;  // image operations wait for their GPU work
   std::map<int64_t, uint16_t*> weights;  // gaussian weights per radius, on the device
 };
@@ -427,6 +429,8 @@ Staged stage(const std::vector<PathJob>& run, const void* extra, size_t extraByt
   A.prog = g.prog;
   A.prog_cap = g.prog_cap;
   A.rowidx = g.rowidx;
+  A.cov8 = g.cov8;
+  A.cov8_cap = g.cov8_cap;
   A.counters = reinterpret_cast<unsigned long long*>(g.d_up + S.jobsBytes);
   A.ovf_rows = g.ovf;
   A.ovf_cap = g.ovf_cap;
@@ -720,6 +724,14 @@ void run_scene_runs(std::vector<HostRun>& runs) {
     if (prog_need == 0) prog_need = std::max<long long>(1 << 20, recItems * 24);
     dev_grow(g.prog, g.prog_cap, prog_need);
     dev_grow(g.rowidx, g.rowidx_cap, std::max<long long>(riTotal, 1));
+    if (!g.cov8) {  // coverage-byte arena: up to 4 GB, at most an eighth of the free memory
+      size_t fr = 0, tot = 0;
+      CU(cudaMemGetInfo(&fr, &tot));
+      long long cap = std::min<long long>(4LL << 30, (long long)(fr / 8));
+      cap = std::max<long long>(cap, 1 << 20);
+      CU(cudaMalloc(&g.cov8, (size_t)cap));
+      g.cov8_cap = cap;
+    }
     const long long recBlocks = std::max<long long>(
         1, std::min<long long>((recItems + scene_rec_warps() - 1) / scene_rec_warps(),
                                (long long)g.nsm * g.scene_ctas_per_sm[0]));
@@ -1700,11 +1712,19 @@ int pxg_server_stats(const pxg_server* sv, int64_t* out6) {
   return 0;
 }
 
-int pxg_scene_config(int slice_width) {
+int pxg_scene_config(int slice_width, int64_t coverage_bytes) {
   return guarded([&] {
     if (slice_width != 0 && (slice_width < 32 || slice_width > (1 << 20)))
       throw ApiError{"Invalid scene configuration"};
     g.scene_slice = slice_width;
+    if (coverage_bytes >= 0) {  // a new coverage-byte arena (0: spans only)
+      CU(cudaStreamSynchronize(g.stream));
+      if (g.cov8) cudaFree(g.cov8);
+      g.cov8 = nullptr;
+      g.cov8_cap = 0;
+      CU(cudaMalloc(&g.cov8, (size_t)std::max<int64_t>(coverage_bytes, 16)));
+      g.cov8_cap = coverage_bytes;
+    }
   });
 }
 

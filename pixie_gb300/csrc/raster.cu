@@ -896,6 +896,67 @@ __device__ __forceinline__ void apply_trap_pair(RowPx<A8> row, int mode, const u
 // computeCoverage's accumulation of the sample spans (prevAt, at) in 24.8
 // fixed point (:1398-1431) and fillCoverage (:1442-1526) over [cx0, cx1), in
 // tiles of XT pixels through the difference array acc (XT + 1 ints).
+// computeCoverage's accumulation of the sample spans (prevAt, at) in 24.8
+// fixed point (:1398-1431) over the pixels [tx0, tx1) (at most XT): leaves
+// acc[i] = coverage of pixel tx0 + i, modulo 256.
+template <int XT>
+__device__ void cov_tile(const int2* sp, int nsp, int sc, long long tx0, long long tx1, int* acc, int lane) {
+  const int L = (int)(tx1 - tx0);
+  for (int i = lane; i <= L; i += 32) acc[i] = 0;
+  __syncwarp();
+  for (int j = lane; j < nsp; j += 32) {
+    const int2 spj = sp[j];
+    int prevAt = spj.x, at = spj.y;
+    long long pi = prevAt / 256, ai = at / 256;
+    long long fillStart = pi;
+    bool crossed = ai != pi;
+    int leftCover = crossed ? (prevAt / 256) * 256 + 256 - prevAt : at - prevAt;
+    if (leftCover != 0) {
+      fillStart++;
+      int v = ((leftCover * sc) / 256) & 255;
+      if (pi >= tx0 && pi < tx1) {
+        atomicAdd(&acc[pi - tx0], v);
+        atomicAdd(&acc[pi - tx0 + 1], -v);
+      }
+    }
+    if (crossed) {
+      int rightCover = at - (at / 256) * 256;
+      if (rightCover > 0) {
+        int v = ((rightCover * sc) / 256) & 255;
+        if (ai >= tx0 && ai < tx1) {
+          atomicAdd(&acc[ai - tx0], v);
+          atomicAdd(&acc[ai - tx0 + 1], -v);
+        }
+      }
+    }
+    long long fe = ai;
+    long long lo = max(fillStart, tx0), hi = min(fe, tx1);
+    if (hi > lo) {
+      atomicAdd(&acc[lo - tx0], sc);
+      atomicAdd(&acc[hi - tx0], -sc);
+    }
+  }
+  __syncwarp();
+  // prefix sum of the difference array, 32 entries per step (lane i holds
+  // entry c0 + i: no bank conflicts)
+  int carry = 0;
+  for (int c0 = 0; c0 < L; c0 += 32) {
+    const int i = c0 + lane;
+    int v = i < L ? acc[i] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += t;
+    }
+    v += carry;
+    if (i < L) acc[i] = v;
+    carry = __shfl_sync(0xffffffffu, v, 31);
+  }
+  __syncwarp();
+}
+
+// fillCoverage (:1442-1526) of the sample spans over [cx0, cx1), in tiles of
+// XT pixels through the difference array acc (XT + 1 ints).
 template <bool A8, int XT>
 __device__ void apply_cov(RowPx<A8> row, int mode, const uint8_t* tbl, uint32_t rgbx, const int2* sp, int nsp,
                           int sc, long long cx0, long long cx1, int* acc, int lane) {
@@ -903,59 +964,7 @@ __device__ void apply_cov(RowPx<A8> row, int mode, const uint8_t* tbl, uint32_t 
   for (long long tx0 = cx0; tx0 < cx1; tx0 += XT) {
     const long long tx1 = min(tx0 + (long long)XT, cx1);
     const int L = (int)(tx1 - tx0);
-    for (int i = lane; i <= L; i += 32) acc[i] = 0;
-    __syncwarp();
-    for (int j = lane; j < nsp; j += 32) {
-      const int2 spj = sp[j];
-      int prevAt = spj.x, at = spj.y;
-      long long pi = prevAt / 256, ai = at / 256;
-      long long fillStart = pi;
-      bool crossed = ai != pi;
-      int leftCover = crossed ? (prevAt / 256) * 256 + 256 - prevAt : at - prevAt;
-      if (leftCover != 0) {
-        fillStart++;
-        int v = ((leftCover * sc) / 256) & 255;
-        if (pi >= tx0 && pi < tx1) {
-          atomicAdd(&acc[pi - tx0], v);
-          atomicAdd(&acc[pi - tx0 + 1], -v);
-        }
-      }
-      if (crossed) {
-        int rightCover = at - (at / 256) * 256;
-        if (rightCover > 0) {
-          int v = ((rightCover * sc) / 256) & 255;
-          if (ai >= tx0 && ai < tx1) {
-            atomicAdd(&acc[ai - tx0], v);
-            atomicAdd(&acc[ai - tx0 + 1], -v);
-          }
-        }
-      }
-      long long fe = ai;
-      long long lo = max(fillStart, tx0), hi = min(fe, tx1);
-      if (hi > lo) {
-        atomicAdd(&acc[lo - tx0], sc);
-        atomicAdd(&acc[hi - tx0], -sc);
-      }
-    }
-    __syncwarp();
-    // prefix sum of the difference array, 32 entries per step (lane i holds
-    // entry c0 + i: no bank conflicts); coverage = sum mod 256
-    {
-      int carry = 0;
-      for (int c0 = 0; c0 < L; c0 += 32) {
-        const int i = c0 + lane;
-        int v = i < L ? acc[i] : 0;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const int t = __shfl_up_sync(0xffffffffu, v, o);
-          if (lane >= o) v += t;
-        }
-        v += carry;
-        if (i < L) acc[i] = v;
-        carry = __shfl_sync(0xffffffffu, v, 31);
-      }
-    }
-    __syncwarp();
+    cov_tile<XT>(sp, nsp, sc, tx0, tx1, acc, lane);
     // pixels op_cov leaves unchanged are neither read nor written; the next
     // pixel's backdrop is loaded while the current one is blended
     {
@@ -996,7 +1005,9 @@ __device__ void apply_hits(RowPx<A8> row, int mode, const uint8_t* tbl, uint32_t
 //   kRecCov   n sample spans, coverage step  (computeCoverage + fillCoverage)
 //   kRecHits  n spans                        (fillHits, non-AA)
 //   kRecTrap  n pairs: {Lm, Lb, Rm, Rb}, {tl0, tl1, tr0, tr1} per pair
-enum RecKind { kRecFill = 1, kRecCov = 2, kRecHits = 3, kRecTrap = 4 };
+//   kRecCov8  the coverage bytes of pixels [lo, hi), at a 64-bit offset in
+//             Arena::cov8 (the accumulation done once, at record time)
+enum RecKind { kRecFill = 1, kRecCov = 2, kRecHits = 3, kRecTrap = 4, kRecCov8 = 5 };
 
 // Allocates `units` 16-byte units for row y of job J's program, stores its
 // index for the row, and returns it (lane-uniform); -1 if the arena is full.
@@ -1329,6 +1340,49 @@ __device__ bool process_row(const PathJob& J, const Arena& A, const uint8_t* tbl
   const int nsp = min(S.nsp, RowScratch<MAXH, XT>::SPCAP);
 
   if (REC) {
+    if (nsp > 0 && aa) {
+      // the pixels the spans can touch, within the path's bounds
+      long long lo = LLONG_MAX, hi = LLONG_MIN;
+      for (int j = lane; j < nsp; j += 32) {
+        lo = min(lo, (long long)(S.sp[j].x / 256));
+        hi = max(hi, (long long)(S.sp[j].y / 256) + 1);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+      }
+      lo = max(lo, J.startX);
+      hi = min(hi, J.startX + J.pathWidth);
+      if (hi <= lo) {
+        if (lane == 0) A.rowidx[J.ri_off + y * J.ri_stride] = -1;
+        return true;
+      }
+      // coverage bytes when the arena has room (else the spans are recorded)
+      const unsigned long long nbytes = (unsigned long long)((hi - lo + 15) & ~15LL);
+      unsigned long long cb = 0;
+      if (lane == 0) {
+        cb = atomicAdd(&A.counters[kCtrCov8], nbytes);
+        if ((long long)(cb + nbytes) > A.cov8_cap) cb = ~0ull;
+      }
+      cb = __shfl_sync(0xffffffffu, cb, 0);
+      if (cb != ~0ull) {
+        const long long at = rec_alloc(J, A, y, 2, lane);
+        if (at < 0) return true;
+        if (lane == 0) {
+          A.prog[at] = make_int4(kRecCov8, 0, (int)lo, (int)hi);
+          A.prog[at + 1] = make_int4((int)(cb & 0xffffffffu), (int)(cb >> 32), 0, 0);
+        }
+        uint8_t* dst = A.cov8 + cb;
+        for (long long tx0 = lo; tx0 < hi; tx0 += XT) {
+          const long long tx1 = min(tx0 + (long long)XT, hi);
+          cov_tile<XT>(S.sp, nsp, sc, tx0, tx1, S.acc, lane);
+          for (int i = lane; i < (int)(tx1 - tx0); i += 32) dst[tx0 - lo + i] = (uint8_t)(S.acc[i] & 255);
+          __syncwarp();
+        }
+        return true;
+      }
+    }
     const long long at = nsp > 0 ? rec_alloc(J, A, y, 1 + (nsp + 1) / 2, lane) : -1;
     if (nsp == 0 && lane == 0) A.rowidx[J.ri_off + y * J.ri_stride] = -1;
     if (at >= 0) {
@@ -1470,11 +1524,12 @@ __global__ void k_xclears(PathJob* jobs, Arena A) {
 // skipped (outside its bounds a non-mask fill writes nothing).  If the
 // program arena overflowed, k_scene draws nothing and the host reruns the
 // launch with a larger arena.
+constexpr int kRecXT = 256;  // coverage tile of the recording pass
 template <int MAXH, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) k_scene_rec(PathJob* jobs, int njobs, long long totalItems, Arena A,
                                                           unsigned char* wide, long long wideSlots) {
   extern __shared__ __align__(16) unsigned char rsm[];
-  using Scratch = RowScratch<MAXH, 32>;
+  using Scratch = RowScratch<MAXH, kRecXT>;
   using Wide = RowScratch<kWideMaxH, kWideXT>;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   Scratch& S = reinterpret_cast<Scratch*>(rsm)[warp];
@@ -1493,7 +1548,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_scene_rec(PathJob* jobs, int njo
     const PathJob& J = jobs[lo];
     const long long y = item - J.row_off;
     if (J.status != kOk || y < J.startY || y >= J.pathHeight || y >= J.H) continue;
-    bool ok = process_row<MAXH, 32, false, true>(J, A, nullptr, lo, y, S, lane, 0, J.W);
+    bool ok = process_row<MAXH, kRecXT, false, true>(J, A, nullptr, lo, y, S, lane, 0, J.W);
     if (!ok && gw < wideSlots) {
       __syncwarp();
       ok = process_row<kWideMaxH, kWideXT, false, true>(J, A, nullptr, lo, y, reinterpret_cast<Wide*>(wide)[gw],
@@ -1581,6 +1636,25 @@ __global__ void __launch_bounds__(WARPS * 32, 3) k_scene(PathJob* jobs, const Sc
         } else if (hx == kRecCov) {
           apply_cov<false, XT>(row, mi, tbl, ci, reinterpret_cast<const int2*>(A.prog + ai + 1), hy, hz,
                                max(sxi, xa), min(sxi + pwi, xb), acc, lane);
+        } else if (hx == kRecCov8) {
+          const int4 u = A.prog[ai + 1];
+          const uint8_t* cv8 = A.cov8 + (((long long)(unsigned)u.y << 32) | (unsigned)u.x) - hz;
+          const long long x0 = max((long long)hz, xa), x1 = min((long long)hw, xb);
+          uint32_t cvN = 0, bdN = 0;
+          if (x0 + lane < x1) {
+            cvN = cv8[x0 + lane];
+            if (cvN) bdN = row[x0 + lane];
+          }
+#pragma unroll 1
+          for (long long x = x0 + lane; x < x1; x += 32) {
+            const uint32_t cv = cvN, bd = bdN;
+            cvN = 0;
+            if (x + 32 < x1) {
+              cvN = cv8[x + 32];
+              if (cvN) bdN = row[x + 32];
+            }
+            if (cv) row[x] = op_cov(mi, tbl, bd, ci, cv);
+          }
         } else if (hx == kRecHits) {
           apply_hits<false>(row, mi, tbl, ci, reinterpret_cast<const int2*>(A.prog + ai + 1), hy, xa, xb, lane);
         } else if (hx == kRecTrap) {
@@ -1607,7 +1681,7 @@ __global__ void __launch_bounds__(WARPS * 32, 3) k_scene(PathJob* jobs, const Sc
 // tile per warp.
 constexpr int kRecMaxH = 128, kRecWarps = 8, kSceneXT = 256, kSceneWarps = 8;
 const void* scene_rec_kernel() { return (const void*)k_scene_rec<kRecMaxH, kRecWarps>; }
-size_t scene_rec_smem() { return sizeof(RowScratch<kRecMaxH, 32>) * kRecWarps; }
+size_t scene_rec_smem() { return sizeof(RowScratch<kRecMaxH, kRecXT>) * kRecWarps; }
 int scene_rec_warps() { return kRecWarps; }
 const void* scene_kernel() { return (const void*)k_scene<kSceneXT, kSceneWarps>; }
 int scene_warps() { return kSceneWarps; }

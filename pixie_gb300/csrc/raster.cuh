@@ -88,7 +88,7 @@ struct MaskDraw {
 
 enum ArenaCounter {
   kCtrSegs = 0, kCtrBands, kCtrOvfRows, kCtrXClears, kCtrBandSegs, kCtrRowErr, kCtrQueue,
-  kCtrProg, kCtrProgFull, kCtrQueue2, kNumCounters
+  kCtrProg, kCtrProgFull, kCtrQueue2, kCtrCov8, kNumCounters
 };
 
 struct Arena {
@@ -106,6 +106,8 @@ struct Arena {
   int4* prog;          // scenes: row programs (16-byte units)
   long long prog_cap;
   int* rowidx;         // scenes: per row and job, the first unit of its program (-1: none)
+  uint8_t* cov8;       // scenes: coverage bytes of rows recorded as kRecCov8
+  long long cov8_cap;
   unsigned long long* counters;
   long long* ovf_rows;  // packed (job << 32 | y) rows whose crossings exceed the fast kernel
   long long ovf_cap;

@@ -188,5 +188,21 @@ def test_every_scene_configuration_writes_the_same_bytes(slice_w):
         img = px.Image(300, 300)
         img.draw_scene(sc)
     finally:
-        px.scene_config(0)
+        px.scene_config(256)
     assert_same(img.to_numpy(), ref, f"scene slice {slice_w}")
+
+
+@pytest.mark.parametrize("cov_bytes", [0, 200000])
+def test_scene_rows_recorded_as_spans_when_the_coverage_arena_is_small(cov_bytes):
+    # 0: every row keeps its sample spans; 200 kB: some rows get coverage
+    # bytes and the rest spans
+    items = wl.dense_scene(29, n_paths=150, size=400.0)
+    ref = oracle_scene(items, 400, 400)
+    sc = record(items)
+    px.scene_config(256, cov_bytes)
+    try:
+        img = px.Image(400, 400)
+        img.draw_scene(sc)
+    finally:
+        px.scene_config(256, 64 << 20)
+    assert_same(img.to_numpy(), ref, f"coverage arena {cov_bytes}")
