@@ -591,11 +591,16 @@ def run_case(case: str, slice_w: int = 0):
         for _ in range(2):
             px.fill_paths_batch(imgs, [g[0] for g in glyphs], [[1, 1, 1, 1]] * len(glyphs),
                                 winding_rules=[g[3] for g in glyphs])
-    elif case in ("scene", "scene_small"):  # dense scene: 2000 paths on 1024^2 (small: 400 on 512^2)
-        n, side = (2000, 1024) if case == "scene" else (400, 512)
+    elif case in ("scene", "scene_small", "scene_normal"):
+        # dense scene: 2000 paths on 1024^2 (small: 400 on 512^2; normal: every path NormalBlend)
+        n, side = (400, 512) if case == "scene_small" else (2000, 1024)
         if slice_w:
             px.scene_config(slice_w)
-        sc, _ = record_scene(px, wl.dense_scene(7, n_paths=n, size=float(side)))
+        items = wl.dense_scene(7, n_paths=n, size=float(side))
+        if case == "scene_normal":
+            for it in items:
+                it["blend"] = 0
+        sc, _ = record_scene(px, items)
         img = px.Image(side, side)
         for _ in range(2):
             img.draw_scene(sc)

@@ -96,8 +96,8 @@ __global__ void k_setup(PathJob* jobs, Arena A, int maxBands);
 const void* rows_kernel(int v);
 size_t rows_smem(int v);
 int rows_warps(int v);
-void launch_rows(int v, unsigned blocks, cudaStream_t st, PathJob* jobs, int njobs, const Arena& A,
-                 const uint8_t* tbl, long long items, int rpi);
+void launch_rows(int v, unsigned blocks, cudaStream_t st, PathJob* jobs, const long long* offs, int njobs,
+                 const Arena& A, const uint8_t* tbl, long long items, int rpi);
 __global__ void k_rows_wide(PathJob* jobs, Arena A, const uint8_t* tbl);
 __global__ void k_xclears(PathJob* jobs, Arena A);
 const void* scene_rec_kernel();
@@ -106,8 +106,8 @@ int scene_rec_warps();
 const void* scene_kernel();
 int scene_warps();
 int scene_tile();
-void launch_scene_rec(unsigned blocks, cudaStream_t st, PathJob* jobs, int njobs, long long items, const Arena& A,
-                      unsigned char* wide, long long slots);
+void launch_scene_rec(unsigned blocks, cudaStream_t st, PathJob* jobs, const SceneRun* runs, int nruns,
+                      long long items, const Arena& A, unsigned char* wide, long long slots);
 void launch_scene(unsigned blocks, cudaStream_t st, PathJob* jobs, const SceneRun* runs, int nruns, long long items,
                   const Arena& A, const uint8_t* tbl, int sliceW);
 size_t scene_wide_bytes();
@@ -526,7 +526,10 @@ void run_jobs(std::vector<PathJob>& jobs, const std::vector<Prim>& prims, std::v
     const int maxBands = setup_max_bands(maxH);
     ensure_arena(seg_need, list_need, (long long)nr * maxBands, (long long)prims.size(), rows);
     const bool graphed = opts.graph && attempt == 0 && g.stream != nullptr;
-    Staged S = stage(run, nullptr, 0, opts.dprims ? std::vector<Prim>() : prims, false);
+    std::vector<long long> offs((size_t)nr);
+    for (int r = 0; r < nr; r++) offs[(size_t)r] = run[(size_t)r].row_off;
+    Staged S = stage(run, offs.data(), sizeof(long long) * offs.size(), opts.dprims ? std::vector<Prim>() : prims,
+                     false);
     Arena& A = S.A;
     PathJob* dj = S.dj;
     const int v = cfg.variant;
@@ -541,7 +544,8 @@ void run_jobs(std::vector<PathJob>& jobs, const std::vector<Prim>& prims, std::v
       if (count) note_launch();
       CU(cudaGetLastError());
       if (timeRows) CU(cudaEventRecord(g.evr0, g.stream));
-      launch_rows(v, (unsigned)blocks, g.stream, dj, nr, A, g.tbl, items, cfg.rpi);
+      launch_rows(v, (unsigned)blocks, g.stream, dj, reinterpret_cast<const long long*>(S.extra), nr, A, g.tbl, items,
+                  cfg.rpi);
       if (count) note_launch();
       CU(cudaGetLastError());
       if (timeRows) CU(cudaEventRecord(g.evr1, g.stream));
@@ -693,6 +697,7 @@ void run_scene_runs(std::vector<HostRun>& runs) {
       s.img = r.canvas->data;
       s.j0 = (int)dev.size();
       s.ri_base = riTotal;
+      s.rec_off = recItems;
       const long long nrun = (long long)(r.j1 - r.j0);
       for (size_t j = r.j0; j < r.j1; j++) {
         PathJob pj = (*r.jobs)[j];
@@ -749,7 +754,9 @@ void run_scene_runs(std::vector<HostRun>& runs) {
     k_setup<<<nj, 256, setup_smem(maxBands), g.stream>>>(S.dj, S.A, maxBands); note_launch();
     CU(cudaGetLastError());
     CU(cudaMemsetAsync(g.rowidx, 0xff, sizeof(int) * (size_t)std::max<long long>(riTotal, 1), g.stream));
-    launch_scene_rec((unsigned)recBlocks, g.stream, S.dj, nj, recItems, S.A, g.wide, g.wide_slots); note_launch();
+    launch_scene_rec((unsigned)recBlocks, g.stream, S.dj, reinterpret_cast<const SceneRun*>(S.extra), (int)sr.size(),
+                     recItems, S.A, g.wide, g.wide_slots);
+    note_launch();
     CU(cudaGetLastError());
     launch_scene((unsigned)blocks, g.stream, S.dj, reinterpret_cast<const SceneRun*>(S.extra), (int)sr.size(), items,
                  S.A, g.tbl, slice);

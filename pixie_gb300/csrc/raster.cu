@@ -1426,7 +1426,7 @@ constexpr int kWideMaxH = 2048, kWideXT = 1024;
 // queue is empty, so jobs of uneven height share the GPU evenly.  Rows whose
 // crossings exceed MAXH go to the wide kernel.
 template <int MAXH, int XT, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) k_rows(PathJob* jobs, int njobs, Arena A,
+__global__ void __launch_bounds__(WARPS * 32) k_rows(PathJob* jobs, const long long* offs, int njobs, Arena A,
                                                      const uint8_t* tbl, long long totalItems, int rpi) {
   extern __shared__ __align__(16) unsigned char rsm[];
   using Scratch = RowScratch<MAXH, XT>;
@@ -1437,10 +1437,10 @@ __global__ void __launch_bounds__(WARPS * 32) k_rows(PathJob* jobs, int njobs, A
     if (lane == 0) q = atomicAdd(&A.counters[kCtrQueue], 1ull);
     const long long item = (long long)__shfl_sync(0xffffffffu, q, 0);
     if (item >= totalItems) break;
-    int lo = 0, hi = njobs - 1;  // job with row_off <= item
+    int lo = 0, hi = njobs - 1;  // job with row_off <= item (offs: the jobs' row_off, packed)
     while (lo < hi) {
       int mid = (lo + hi + 1) >> 1;
-      if (jobs[mid].row_off <= item) lo = mid;
+      if (offs[mid] <= item) lo = mid;
       else hi = mid - 1;
     }
     const PathJob& J = jobs[lo];
@@ -1467,8 +1467,10 @@ __global__ void __launch_bounds__(WARPS * 32) k_rows(PathJob* jobs, int njobs, A
 }
 
 constexpr int kSmallMaxH = 32, kSmallXT = 256, kSmallWarps = 8;
-template __global__ void k_rows<kFastMaxH, kFastXT, kFastWarps>(PathJob*, int, Arena, const uint8_t*, long long, int);
-template __global__ void k_rows<kSmallMaxH, kSmallXT, kSmallWarps>(PathJob*, int, Arena, const uint8_t*, long long, int);
+template __global__ void k_rows<kFastMaxH, kFastXT, kFastWarps>(PathJob*, const long long*, int, Arena,
+                                                                 const uint8_t*, long long, int);
+template __global__ void k_rows<kSmallMaxH, kSmallXT, kSmallWarps>(PathJob*, const long long*, int, Arena,
+                                                                   const uint8_t*, long long, int);
 
 // Rows whose crossings exceed the fast kernel's capacity: one warp per CTA
 // with room for kWideMaxH crossings.
@@ -1526,8 +1528,9 @@ __global__ void k_xclears(PathJob* jobs, Arena A) {
 // launch with a larger arena.
 constexpr int kRecXT = 256;  // coverage tile of the recording pass
 template <int MAXH, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) k_scene_rec(PathJob* jobs, int njobs, long long totalItems, Arena A,
-                                                          unsigned char* wide, long long wideSlots) {
+__global__ void __launch_bounds__(WARPS * 32) k_scene_rec(PathJob* jobs, const SceneRun* runs, int nruns,
+                                                          long long totalItems, Arena A, unsigned char* wide,
+                                                          long long wideSlots) {
   extern __shared__ __align__(16) unsigned char rsm[];
   using Scratch = RowScratch<MAXH, kRecXT>;
   using Wide = RowScratch<kWideMaxH, kWideXT>;
@@ -1539,15 +1542,18 @@ __global__ void __launch_bounds__(WARPS * 32) k_scene_rec(PathJob* jobs, int njo
     if (lane == 0) q = atomicAdd(&A.counters[kCtrQueue], 1ull);
     const long long item = (long long)__shfl_sync(0xffffffffu, q, 0);
     if (item >= totalItems) break;
-    int lo = 0, hi = njobs - 1;
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (jobs[mid].row_off <= item) lo = mid;
-      else hi = mid - 1;
+    // items run by run, path by path, row by row: rec_off + (j - j0) * H + y
+    int r0 = 0, r1 = nruns - 1;
+    while (r0 < r1) {
+      int mid = (r0 + r1 + 1) >> 1;
+      if (runs[mid].rec_off <= item) r0 = mid;
+      else r1 = mid - 1;
     }
+    const long long local = item - runs[r0].rec_off, H = runs[r0].H;
+    const int lo = runs[r0].j0 + (int)(local / H);
+    const long long y = local % H;
     const PathJob& J = jobs[lo];
-    const long long y = item - J.row_off;
-    if (J.status != kOk || y < J.startY || y >= J.pathHeight || y >= J.H) continue;
+    if (J.status != kOk || y < J.startY || y >= J.pathHeight) continue;
     bool ok = process_row<MAXH, kRecXT, false, true>(J, A, nullptr, lo, y, S, lane, 0, J.W);
     if (!ok && gw < wideSlots) {
       __syncwarp();
@@ -1686,10 +1692,10 @@ int scene_rec_warps() { return kRecWarps; }
 const void* scene_kernel() { return (const void*)k_scene<kSceneXT, kSceneWarps>; }
 int scene_warps() { return kSceneWarps; }
 int scene_tile() { return kSceneXT; }
-void launch_scene_rec(unsigned blocks, cudaStream_t st, PathJob* jobs, int njobs, long long items, const Arena& A,
-                      unsigned char* wide, long long slots) {
-  k_scene_rec<kRecMaxH, kRecWarps><<<blocks, kRecWarps * 32, scene_rec_smem(), st>>>(jobs, njobs, items, A, wide,
-                                                                                    slots);
+void launch_scene_rec(unsigned blocks, cudaStream_t st, PathJob* jobs, const SceneRun* runs, int nruns,
+                      long long items, const Arena& A, unsigned char* wide, long long slots) {
+  k_scene_rec<kRecMaxH, kRecWarps><<<blocks, kRecWarps * 32, scene_rec_smem(), st>>>(jobs, runs, nruns, items, A,
+                                                                                    wide, slots);
 }
 void launch_scene(unsigned blocks, cudaStream_t st, PathJob* jobs, const SceneRun* runs, int nruns, long long items,
                   const Arena& A, const uint8_t* tbl, int sliceW) {
@@ -1720,12 +1726,14 @@ size_t rows_smem(int v) {
   return v == 1 ? sizeof(RowScratch<kSmallMaxH, kSmallXT>) * kSmallWarps : rows_smem_fast();
 }
 int rows_warps(int v) { return v == 1 ? kSmallWarps : kFastWarps; }
-void launch_rows(int v, unsigned blocks, cudaStream_t st, PathJob* jobs, int njobs, const Arena& A,
-                 const uint8_t* tbl, long long items, int rpi) {
+void launch_rows(int v, unsigned blocks, cudaStream_t st, PathJob* jobs, const long long* offs, int njobs,
+                 const Arena& A, const uint8_t* tbl, long long items, int rpi) {
   if (v == 1)
-    k_rows<kSmallMaxH, kSmallXT, kSmallWarps><<<blocks, kSmallWarps * 32, rows_smem(1), st>>>(jobs, njobs, A, tbl, items, rpi);
+    k_rows<kSmallMaxH, kSmallXT, kSmallWarps><<<blocks, kSmallWarps * 32, rows_smem(1), st>>>(jobs, offs, njobs, A,
+                                                                                              tbl, items, rpi);
   else
-    k_rows<kFastMaxH, kFastXT, kFastWarps><<<blocks, kFastWarps * 32, rows_smem(0), st>>>(jobs, njobs, A, tbl, items, rpi);
+    k_rows<kFastMaxH, kFastXT, kFastWarps><<<blocks, kFastWarps * 32, rows_smem(0), st>>>(jobs, offs, njobs, A, tbl,
+                                                                                          items, rpi);
 }
 
 }  // namespace pxg

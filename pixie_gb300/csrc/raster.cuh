@@ -76,6 +76,7 @@ struct SceneRun {
   long long W, H;
   uint8_t* img;       // the canvas (RGBX)
   long long ri_base;  // row y, path j: Arena::rowidx[ri_base + y * (j1 - j0) + j - j0]
+  long long rec_off;  // recording items of the run: rec_off + (j - j0) * H + y
   int j0, j1;
 };
 
