@@ -494,8 +494,10 @@ def run_scene(px, wl, seed=7, n_paths=2000, size=1024, reps=3):
     painted = len(sc)
     return {"paths_recorded": painted, "paths_raising_in_reference": failed,
             "segments": stats["segments"], "primitives": stats["primitives"],
+            "covered_pixel_blends": stats["pixel_blends"],
             "gpu_ms_per_scene": round(g, 3), "paths_per_s_gpu": round(painted / (g / 1e3), 1),
             "edges_per_s_gpu": round(stats["segments"] / (g / 1e3), 1),
+            "covered_gpix_per_s_gpu": round(stats["pixel_blends"] / (g / 1e3) / 1e9, 3),
             "draw_call_ms": round(w * 1e3, 3), "record_ms_host": round(rec_s * 1e3, 1),
             "note": "gpu_ms covers the primitive upload, setup and scene launches of draw_scene; "
                     "record_ms is the host command walk and stroke outlining of all paths"}

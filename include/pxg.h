@@ -227,9 +227,10 @@ int pxg_autotune(int enable);
 int64_t pxg_autotune_report(char* buf, int64_t capacity);
 
 /* Counts of the last fill launch (fillPath, strokePath, batch or scene):
- * out[0] paths, out[1] primitives uploaded, out[2] segments after
- * flattening, out[3] band entries.  No counterpart in the reference. */
-int pxg_last_fill_stats(int64_t out[4]);
+ * out[0] paths, out[1] primitives, out[2] segments after flattening, out[3]
+ * band entries, out[4] pixel blends of a scene's drawing pass (0 for other
+ * launches).  No counterpart in the reference. */
+int pxg_last_fill_stats(int64_t out[5]);
 
 /* Blur without allocating: the same result as pxg_image_blur, for callers
  * that cannot call cudaMalloc (programs whose device memory is owned by their

@@ -224,7 +224,7 @@ struct Ctx {
   long long scratch_cap = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evr0 = nullptr, evr1 = nullptr;
   float last_ms = 0;
-  long long stats[4] = {0, 0, 0, 0};  // last fill launch: paths, prims, segments, band entries
+  long long stats[5] = {0, 0, 0, 0, 0};  // last fill launch: paths, prims, segments, band entries, blends
   int rows_ctas_per_sm[2] = {1, 1};  // resident CTAs of each row-kernel variant
   int scene_ctas_per_sm[2] = {1, 1};  // resident CTAs of the scene recording and drawing kernels
   int scene_slice = 256;              // pixels of a row one warp of the drawing pass owns (0: chosen per launch)
@@ -444,6 +444,7 @@ void note_stats(long long paths, long long prims, const unsigned long long* ctr)
   g.stats[1] = prims;
   g.stats[2] = (long long)ctr[kCtrSegs];
   g.stats[3] = (long long)ctr[kCtrBandSegs];
+  g.stats[4] = (long long)ctr[kCtrPainted];
 }
 
 int setup_max_bands(long long maxH) {
@@ -1375,12 +1376,12 @@ int pxg_fill_paths_batch(pxg_image* const* images, int64_t nj, const float* cmds
   });
 }
 
-int pxg_last_fill_stats(int64_t* out4) {
-  if (!out4) {
+int pxg_last_fill_stats(int64_t* out5) {
+  if (!out5) {
     set_err("Invalid output pointer");
     return 1;
   }
-  for (int i = 0; i < 4; i++) out4[i] = g.stats[i];
+  for (int i = 0; i < 5; i++) out5[i] = g.stats[i];
   return 0;
 }
 

@@ -215,22 +215,50 @@ __global__ void __launch_bounds__(kBWarps * 32, 2)
   const long long a0 = (long long)blockIdx.x * kBT, c0 = (long long)blockIdx.y * 32;
   const long long alen = XPASS ? W : H, clen = XPASS ? H : W;
   const float4 o = px4(oob), zero = make_float4(0.f, 0.f, 0.f, 0.f);
-  for (int i = tid; i < span * 32; i += kBWarps * 32) {
-    int p, c;
-    if (XPASS) {  // consecutive threads read consecutive x of one row
-      c = i / span;
-      p = i - c * span;
-    } else {  // consecutive threads read consecutive x of one row
-      p = i >> 5;
-      c = i & 31;
+  // Stage the tile: 8 loads per thread in flight before any is converted, so
+  // the staging does not wait on L2/HBM latency one pixel at a time.
+  constexpr int kU = 8;
+  const int total = span * 32;
+  for (int i0 = tid; i0 < total; i0 += kU * kBWarps * 32) {
+    uint32_t raw[kU];
+    int kind[kU];  // 0: zero padding, 1: out of bounds, 2: pixel
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const int i = i0 + u * kBWarps * 32;
+      int p, c;
+      if (XPASS) {  // consecutive threads read consecutive x of one row
+        c = i / span;
+        p = i - c * span;
+      } else {  // consecutive threads read consecutive x of one row
+        p = i >> 5;
+        c = i & 31;
+      }
+      const long long ga = a0 - r + p, gc = c0 + c;
+      kind[u] = 0;
+      raw[u] = 0u;
+      if (i < total && p < kBT + 2 * r && gc < clen) {
+        if (ga >= 0 && ga < alen) {
+          raw[u] = XPASS ? in[gc * W + ga] : in[ga * W + gc];
+          kind[u] = 2;
+        } else {
+          kind[u] = 1;
+        }
+      }
     }
-    long long ga = a0 - r + p, gc = c0 + c;
-    float4 v = zero;
-    if (p < kBT + 2 * r && gc < clen) {
-      if (ga >= 0 && ga < alen) v = px4(XPASS ? in[gc * W + ga] : in[ga * W + gc]);
-      else v = o;
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const int i = i0 + u * kBWarps * 32;
+      if (i >= total) break;
+      int p, c;
+      if (XPASS) {
+        c = i / span;
+        p = i - c * span;
+      } else {
+        p = i >> 5;
+        c = i & 31;
+      }
+      px[p * 32 + c] = kind[u] == 2 ? px4(raw[u]) : (kind[u] == 1 ? o : zero);
     }
-    px[p * 32 + c] = v;
   }
   for (int i = tid; i < ntap + kBP; i += kBWarps * 32) kw[i] = i < ntap ? (float)kern[i] : 0.f;
   __syncthreads();

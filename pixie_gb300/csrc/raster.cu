@@ -843,7 +843,7 @@ template <bool A8>
 __device__ __forceinline__ void apply_trap_pair(RowPx<A8> row, int mode, const uint8_t* tbl, uint32_t rgbx,
                                                 long long y, long long W, float Lm, float Lb, float Rm,
                                                 float Rb, float tl0, float tl1, float tr0, float tr1,
-                                                long long xa, long long xb, int lane) {
+                                                long long xa, long long xb, int lane, unsigned* cnt = nullptr) {
   const float leftMaxX = nmax(tl0, tl1), rightMinX = nmin(tr0, tr1);
   const long long leftCoverEnd = nim_int(ceilf(leftMaxX));
   const long long rightCoverBegin = nim_int(truncf(rightMinX));
@@ -866,6 +866,7 @@ __device__ __forceinline__ void apply_trap_pair(RowPx<A8> row, int mode, const u
       float rect = inv ? (prevPenY - (float)y) * run : ((float)(y + 1) - prevPenY) * run;
       float area = tri + rect + rightRectArea;
       row[x] = blend_row(mode, tbl, row[x], mul_f(rgbx, area));
+      if (cnt) ++*cnt;
     }
   }
   {  // right sliver (:1790-1828)
@@ -885,11 +886,15 @@ __device__ __forceinline__ void apply_trap_pair(RowPx<A8> row, int mode, const u
       float rect = inv ? (penY - (float)y) * run : ((float)(y + 1) - penY) * run;
       float area = leftRectArea + tri + rect;
       row[x] = blend_row(mode, tbl, row[x], mul_f(rgbx, area));
+      if (cnt) ++*cnt;
     }
   }
   {  // the fully covered middle (:1830-1835)
     long long fb = max(min(max(leftCoverEnd, 0LL), W), xa), fe = min(min(max(rightCoverBegin, 0LL), W), xb);
-    for (long long x = fb + lane; x < fe; x += 32) row[x] = op_fill(mode, tbl, row[x], rgbx);
+    for (long long x = fb + lane; x < fe; x += 32) {
+      row[x] = op_fill(mode, tbl, row[x], rgbx);
+      if (cnt) ++*cnt;
+    }
   }
 }
 
@@ -959,7 +964,7 @@ __device__ void cov_tile(const int2* sp, int nsp, int sc, long long tx0, long lo
 // XT pixels through the difference array acc (XT + 1 ints).
 template <bool A8, int XT>
 __device__ void apply_cov(RowPx<A8> row, int mode, const uint8_t* tbl, uint32_t rgbx, const int2* sp, int nsp,
-                          int sc, long long cx0, long long cx1, int* acc, int lane) {
+                          int sc, long long cx0, long long cx1, int* acc, int lane, unsigned* cnt = nullptr) {
   const bool maskMode = mode == kMask;
   for (long long tx0 = cx0; tx0 < cx1; tx0 += XT) {
     const long long tx1 = min(tx0 + (long long)XT, cx1);
@@ -977,7 +982,10 @@ __device__ void apply_cov(RowPx<A8> row, int mode, const uint8_t* tbl, uint32_t 
         const int in = i + 32;
         cvN = in < L ? ((uint32_t)acc[in] & 255u) : keep;
         bdN = cvN != keep ? (uint32_t)row[tx0 + in] : 0u;
-        if (cv != keep) row[tx0 + i] = op_cov(mode, tbl, bd, rgbx, cv);
+        if (cv != keep) {
+          row[tx0 + i] = op_cov(mode, tbl, bd, rgbx, cv);
+          if (cnt) ++*cnt;
+        }
       }
     }
     __syncwarp();
@@ -988,14 +996,17 @@ __device__ void apply_cov(RowPx<A8> row, int mode, const uint8_t* tbl, uint32_t 
 // sorted and disjoint, so a pixel is inside at most one.
 template <bool A8>
 __device__ void apply_hits(RowPx<A8> row, int mode, const uint8_t* tbl, uint32_t rgbx, const int2* sp, int nsp,
-                           long long xa, long long xb, int lane) {
+                           long long xa, long long xb, int lane, unsigned* cnt = nullptr) {
   for (long long x = xa + lane; x < xb; x += 32) {
     bool inside = false;
     for (int j = 0; j < nsp && !inside; j++) {
       long long fs = sp[j].x / 256, fe = sp[j].y / 256;
       if (fe - fs > 0 && x >= fs && x < fe) inside = true;
     }
-    if (inside) row[x] = op_fill(mode, tbl, row[x], rgbx);
+    if (inside) {
+      row[x] = op_fill(mode, tbl, row[x], rgbx);
+      if (cnt) ++*cnt;
+    }
   }
 }
 
@@ -1602,6 +1613,7 @@ __global__ void __launch_bounds__(WARPS * 32, 3) k_scene(PathJob* jobs, const Sc
     }
     const RowPx<false> row = staged ? RowPx<false>{reinterpret_cast<unsigned char*>(pix[warp]), xa}
                                     : RowPx<false>{reinterpret_cast<unsigned char*>(grow), 0};
+    unsigned painted = 0;  // pixel blends of this item (reported as a launch counter)
     // 32 paths at a time: each lane loads one path's row program index and
     // header (the row's indices are contiguous), then the warp replays the
     // programs in path order.
@@ -1637,11 +1649,13 @@ __global__ void __launch_bounds__(WARPS * 32, 3) k_scene(PathJob* jobs, const Sc
         const uint32_t ci = __shfl_sync(0xffffffffu, rgbx, i);
         const long long sxi = __shfl_sync(0xffffffffu, sx, i), pwi = __shfl_sync(0xffffffffu, pw, i);
         if (hx == kRecFill) {
-          for (long long x = max((long long)hz, xa) + lane; x < min((long long)hw, xb); x += 32)
+          for (long long x = max((long long)hz, xa) + lane; x < min((long long)hw, xb); x += 32) {
             row[x] = op_fill(mi, tbl, row[x], ci);
+            ++painted;
+          }
         } else if (hx == kRecCov) {
           apply_cov<false, XT>(row, mi, tbl, ci, reinterpret_cast<const int2*>(A.prog + ai + 1), hy, hz,
-                               max(sxi, xa), min(sxi + pwi, xb), acc, lane);
+                               max(sxi, xa), min(sxi + pwi, xb), acc, lane, &painted);
         } else if (hx == kRecCov8) {
           const int4 u = A.prog[ai + 1];
           const uint8_t* cv8 = A.cov8 + (((long long)(unsigned)u.y << 32) | (unsigned)u.x) - hz;
@@ -1659,16 +1673,21 @@ __global__ void __launch_bounds__(WARPS * 32, 3) k_scene(PathJob* jobs, const Sc
               cvN = cv8[x + 32];
               if (cvN) bdN = row[x + 32];
             }
-            if (cv) row[x] = op_cov(mi, tbl, bd, ci, cv);
+            if (cv) {
+              row[x] = op_cov(mi, tbl, bd, ci, cv);
+              ++painted;
+            }
           }
         } else if (hx == kRecHits) {
-          apply_hits<false>(row, mi, tbl, ci, reinterpret_cast<const int2*>(A.prog + ai + 1), hy, xa, xb, lane);
+          apply_hits<false>(row, mi, tbl, ci, reinterpret_cast<const int2*>(A.prog + ai + 1), hy, xa, xb, lane,
+                            &painted);
         } else if (hx == kRecTrap) {
           for (int p = 0; p < hy; p++) {
             const int4 e = A.prog[ai + 1 + 2 * p], t = A.prog[ai + 2 + 2 * p];
             apply_trap_pair<false>(row, mi, tbl, ci, y, R.W, __int_as_float(e.x), __int_as_float(e.y),
                                    __int_as_float(e.z), __int_as_float(e.w), __int_as_float(t.x),
-                                   __int_as_float(t.y), __int_as_float(t.z), __int_as_float(t.w), xa, xb, lane);
+                                   __int_as_float(t.y), __int_as_float(t.z), __int_as_float(t.w), xa, xb, lane,
+                                   &painted);
           }
         }
         __syncwarp();
@@ -1679,6 +1698,9 @@ __global__ void __launch_bounds__(WARPS * 32, 3) k_scene(PathJob* jobs, const Sc
       for (long long x = xa + lane; x < xb; x += 32) grow[x] = pix[warp][x - xa];
       __syncwarp();
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) painted += __shfl_xor_sync(0xffffffffu, painted, o);
+    if (lane == 0 && painted) atomicAdd(&A.counters[kCtrPainted], (unsigned long long)painted);
   }
 }
 

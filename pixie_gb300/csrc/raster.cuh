@@ -89,7 +89,7 @@ struct MaskDraw {
 
 enum ArenaCounter {
   kCtrSegs = 0, kCtrBands, kCtrOvfRows, kCtrXClears, kCtrBandSegs, kCtrRowErr, kCtrQueue,
-  kCtrProg, kCtrProgFull, kCtrQueue2, kCtrCov8, kNumCounters
+  kCtrProg, kCtrProgFull, kCtrQueue2, kCtrCov8, kCtrPainted, kNumCounters
 };
 
 struct Arena {
