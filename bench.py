@@ -494,7 +494,7 @@ def run_scene(px, wl, seed=7, n_paths=2000, size=1024, reps=3):
     painted = len(sc)
     return {"paths_recorded": painted, "paths_raising_in_reference": failed,
             "segments": stats["segments"], "primitives": stats["primitives"],
-            "covered_pixel_blends": stats["pixel_blends"],
+            "covered_pixel_blends": stats["pixel_blends"], "wide_rows": stats["wide_rows"],
             "gpu_ms_per_scene": round(g, 3), "paths_per_s_gpu": round(painted / (g / 1e3), 1),
             "edges_per_s_gpu": round(stats["segments"] / (g / 1e3), 1),
             "covered_gpix_per_s_gpu": round(stats["pixel_blends"] / (g / 1e3) / 1e9, 3),
@@ -606,6 +606,7 @@ def run_case(case: str, slice_w: int = 0):
         img = px.Image(side, side)
         for _ in range(2):
             img.draw_scene(sc)
+        print(json.dumps(px.last_fill_stats()))
     elif case == "masks":  # 4096 glyph masks rendered, then composited onto a 4096^2 page
         glyphs, pos = wl.glyph_batch(7, n=4096)
         m = px.Masks()

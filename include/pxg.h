@@ -197,8 +197,9 @@ int pxg_image_draw_masks(pxg_image* page, const pxg_masks* masks, const int64_t*
  * until the job's result is taken) and returns its id (0 on error).
  * pxg_server_step admits queued jobs in arrival order while their canvases
  * (and blur work space) fit the budget, then advances every admitted job by
- * up to paths_per_job of its paths -- at most paths_per_step in all -- in
- * one setup launch and one scene launch; jobs whose paths are all painted
+ * up to paths_per_job of its paths -- at most paths_per_step paths and 8M
+ * path-rows (paths x canvas height) in all -- in one scene launch sequence
+ * (setup, recording, drawing); jobs whose paths are all painted
  * are blurred and finish, freeing their memory for the next admissions.
  * pxg_server_poll returns finished job ids; pxg_server_take copies a
  * finished job's canvas to the host (out may be NULL), reports its submit,
@@ -229,8 +230,9 @@ int64_t pxg_autotune_report(char* buf, int64_t capacity);
 /* Counts of the last fill launch (fillPath, strokePath, batch or scene):
  * out[0] paths, out[1] primitives, out[2] segments after flattening, out[3]
  * band entries, out[4] pixel blends of a scene's drawing pass (0 for other
- * launches).  No counterpart in the reference. */
-int pxg_last_fill_stats(int64_t out[5]);
+ * launches), out[5] rows whose crossings exceeded the shared-memory scratch.
+ * No counterpart in the reference. */
+int pxg_last_fill_stats(int64_t out[6]);
 
 /* Blur without allocating: the same result as pxg_image_blur, for callers
  * that cannot call cudaMalloc (programs whose device memory is owned by their

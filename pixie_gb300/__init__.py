@@ -493,10 +493,10 @@ def last_gpu_ms() -> float:
 def last_fill_stats() -> dict:
     """Counts of the last fill launch: paths, primitives, segments, band
     entries and (scenes) the drawing pass's pixel blends."""
-    v = np.zeros(5, np.int64)
+    v = np.zeros(6, np.int64)
     _check(lib().pxg_last_fill_stats(_ptr(v)))
     return {"paths": int(v[0]), "primitives": int(v[1]), "segments": int(v[2]), "band_entries": int(v[3]),
-            "pixel_blends": int(v[4])}
+            "pixel_blends": int(v[4]), "wide_rows": int(v[5])}
 
 
 def set_blocking(blocking: bool):

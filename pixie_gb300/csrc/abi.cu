@@ -224,7 +224,7 @@ struct Ctx {
   long long scratch_cap = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evr0 = nullptr, evr1 = nullptr;
   float last_ms = 0;
-  long long stats[5] = {0, 0, 0, 0, 0};  // last fill launch: paths, prims, segments, band entries, blends
+  long long stats[6] = {0, 0, 0, 0, 0, 0};  // last fill launch: paths, prims, segments, entries, blends, wide rows
   int rows_ctas_per_sm[2] = {1, 1};  // resident CTAs of each row-kernel variant
   int scene_ctas_per_sm[2] = {1, 1};  // resident CTAs of the scene recording and drawing kernels
   int scene_slice = 256;              // pixels of a row one warp of the drawing pass owns (0: chosen per launch)
@@ -445,6 +445,7 @@ void note_stats(long long paths, long long prims, const unsigned long long* ctr)
   g.stats[2] = (long long)ctr[kCtrSegs];
   g.stats[3] = (long long)ctr[kCtrBandSegs];
   g.stats[4] = (long long)ctr[kCtrPainted];
+  g.stats[5] = (long long)ctr[kCtrOvfRows];
 }
 
 int setup_max_bands(long long maxH) {
@@ -675,9 +676,10 @@ int scene_slice_for(const std::vector<HostRun>& runs) {
 // repeating for runs whose workspace ran out.  MaskBlend paths must not be
 // inside a run (their clears reach outside the rows the run owns).
 void run_scene_runs(std::vector<HostRun>& runs) {
-  long long prim_total = 0;
-  for (auto& r : runs) prim_total += (long long)r.prims->size();
-  long long seg_need = std::max<long long>(1 << 16, prim_total * 8);
+  long long prim_total = 0;  // primitives of the paths this launch draws
+  for (auto& r : runs)
+    for (size_t j = r.j0; j < r.j1; j++) prim_total += (*r.jobs)[j].nprims;
+  long long seg_need = std::max<long long>(1 << 16, prim_total * 4);
   long long list_need = seg_need * 4;
   long long prog_need = 0;
   for (auto& r : runs) r.status = kOk;
@@ -727,7 +729,7 @@ void run_scene_runs(std::vector<HostRun>& runs) {
     const int nj = (int)dev.size();
     const int maxBands = setup_max_bands(maxH);
     ensure_arena(seg_need, list_need, (long long)nj * maxBands, pc, 1);
-    if (prog_need == 0) prog_need = std::max<long long>(1 << 20, recItems * 24);
+    if (prog_need == 0) prog_need = std::max<long long>(1 << 20, std::min<long long>(recItems * 3, 1LL << 27));
     dev_grow(g.prog, g.prog_cap, prog_need);
     dev_grow(g.rowidx, g.rowidx_cap, std::max<long long>(riTotal, 1));
     if (!g.cov8) {  // coverage-byte arena: up to 4 GB, at most an eighth of the free memory
@@ -897,6 +899,8 @@ void srv_pool_init() {
   done = true;
 }
 
+constexpr long long kStepPathRows = 8LL << 20;
+
 void srv_release(pxg_server* sv, SrvJob* j) {
   if (j->canvas.data) cudaFreeAsync(j->canvas.data, g.stream);
   if (j->tmp) cudaFreeAsync(j->tmp, g.stream);
@@ -947,8 +951,9 @@ void srv_step(pxg_server* sv) {
   std::vector<SrvJob*> owners;
   std::vector<std::vector<PathJob>*> jobvecs;
   long long budget = sv->paths_per_step;
+  long long rowBudget = kStepPathRows;  // path-rows of the step: bounds its row programs
   for (SrvJob* j : sv->active) {
-    if (budget <= 0) break;
+    if (budget <= 0 || rowBudget <= 0) break;
     const auto& pj = j->scene->jobs;
     if (j->next < pj.size() && pj[j->next].mode == kMask) {
       // a MaskBlend path: drawn alone
@@ -971,9 +976,11 @@ void srv_step(pxg_server* sv) {
       continue;
     }
     size_t e = j->next;
-    const size_t lim = (size_t)std::min<long long>(sv->paths_per_job, budget);
+    const size_t lim = (size_t)std::max<long long>(
+        1, std::min<long long>(std::min<long long>(sv->paths_per_job, budget), rowBudget / j->H));
     while (e < pj.size() && e - j->next < lim && pj[e].mode != kMask) e++;
     if (e == j->next) continue;
+    rowBudget -= (long long)(e - j->next) * j->H;
     runs.push_back(HostRun{&j->canvas, const_cast<std::vector<PathJob>*>(&pj), &j->scene->prims,
                            scene_device_prims(j->scene), j->next, e, kOk});
     owners.push_back(j);
@@ -1376,12 +1383,12 @@ int pxg_fill_paths_batch(pxg_image* const* images, int64_t nj, const float* cmds
   });
 }
 
-int pxg_last_fill_stats(int64_t* out5) {
-  if (!out5) {
+int pxg_last_fill_stats(int64_t* out6) {
+  if (!out6) {
     set_err("Invalid output pointer");
     return 1;
   }
-  for (int i = 0; i < 5; i++) out5[i] = g.stats[i];
+  for (int i = 0; i < 6; i++) out6[i] = g.stats[i];
   return 0;
 }
 

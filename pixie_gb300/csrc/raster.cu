@@ -1567,6 +1567,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_scene_rec(PathJob* jobs, const S
     if (J.status != kOk || y < J.startY || y >= J.pathHeight) continue;
     bool ok = process_row<MAXH, kRecXT, false, true>(J, A, nullptr, lo, y, S, lane, 0, J.W);
     if (!ok && gw < wideSlots) {
+      if (lane == 0) atomicAdd(&A.counters[kCtrOvfRows], 1ull);  // rows taking the wide scratch
       __syncwarp();
       ok = process_row<kWideMaxH, kWideXT, false, true>(J, A, nullptr, lo, y, reinterpret_cast<Wide*>(wide)[gw],
                                                         lane, 0, J.W);
