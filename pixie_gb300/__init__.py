@@ -142,6 +142,7 @@ def lib():
         L.pxg_server_take.argtypes = [P, I64, P, I64, P]
         L.pxg_server_stats.argtypes = [P, P]
         L.pxg_autotune.argtypes = [I]
+        L.pxg_blur_config.argtypes = [I]
         L.pxg_autotune_report.argtypes = [P, I64]
         L.pxg_autotune_report.restype = I64
         _lib = L
@@ -446,6 +447,11 @@ class Server:
 def scene_config(slice_width: int = 256, coverage_bytes: int = -1):
     """Scene drawing configuration (see pxg_scene_config)."""
     _check(lib().pxg_scene_config(int(slice_width), int(coverage_bytes)))
+
+
+def blur_config(use_tensor_cores: bool):
+    """True (default): blur radii 1..128 on the tensor cores; False: CUDA cores."""
+    _check(lib().pxg_blur_config(1 if use_tensor_cores else 0))
 
 
 def autotune(enable: bool):

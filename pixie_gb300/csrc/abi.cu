@@ -136,6 +136,9 @@ void* blurb_kernel(bool x);
 unsigned long long launch_count();
 void note_launch();
 size_t blur_y_smem(int r);
+bool launch_blur_tc(uint32_t* img, uint32_t* tmp, long long W, long long H, int r, const uint16_t* kern,
+                    uint32_t oob, int nsm, size_t maxSmem, int* err, cudaStream_t st);
+const void* tc_blur_kernel(bool x, int n);
 __global__ void k_blur_x(const uint32_t*, uint32_t*, long long, long long, int, const uint16_t*, uint32_t);
 __global__ void k_blur_y(const uint32_t*, uint32_t*, long long, long long, int, const uint16_t*, uint32_t);
 __global__ void k_blurf_x(const uint32_t*, uint32_t*, long long, long long, int, const uint16_t*, uint32_t);
@@ -223,6 +226,10 @@ struct Ctx {
   unsigned char* scratch = nullptr;
   long long scratch_cap = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evr0 = nullptr, evr1 = nullptr;
+  int* dev_err = nullptr;   // device-side error flag (a tensor-core wait that ran out)
+  int* host_err = nullptr;  // its pinned mirror
+  bool blur_tensor = true;  // blur radii 1..128 on the tensor cores
+  size_t tcSmemMax = 0;
   float last_ms = 0;
   long long stats[6] = {0, 0, 0, 0, 0, 0};  // last fill launch: paths, prims, segments, entries, blends, wide rows
   int rows_ctas_per_sm[2] = {1, 1};  // resident CTAs of each row-kernel variant
@@ -288,6 +295,14 @@ void init_locked(int device) {
   CU(cudaEventCreate(&g.ev1));
   CU(cudaEventCreate(&g.evr0));
   CU(cudaEventCreate(&g.evr1));
+  CU(cudaMalloc(&g.dev_err, sizeof(int)));
+  CU(cudaMemset(g.dev_err, 0, sizeof(int)));
+  CU(cudaMallocHost(&g.host_err, sizeof(int)));
+  *g.host_err = 0;
+  g.tcSmemMax = allow_max_smem(tc_blur_kernel(true, 128));
+  g.tcSmemMax = std::min(g.tcSmemMax, allow_max_smem(tc_blur_kernel(false, 128)));
+  g.tcSmemMax = std::min(g.tcSmemMax, allow_max_smem(tc_blur_kernel(true, 64)));
+  g.tcSmemMax = std::min(g.tcSmemMax, allow_max_smem(tc_blur_kernel(false, 64)));
   g.ready = true;
 }
 void ensure_init() {
@@ -325,6 +340,18 @@ struct Timed {
     g.last_ms = ms;
   }
 };
+
+// Reads (and clears) the device error flag; throws if a kernel reported a
+// wait that ran out.
+void check_device_error() {
+  CU(cudaMemcpyAsync(g.host_err, g.dev_err, sizeof(int), cudaMemcpyDeviceToHost, g.stream));
+  CU(cudaStreamSynchronize(g.stream));
+  if (*g.host_err) {
+    *g.host_err = 0;
+    CU(cudaMemsetAsync(g.dev_err, 0, sizeof(int), g.stream));
+    throw ApiError{"GPU wait timed out (tensor-core blur)"};
+  }
+}
 
 const char* status_message(int st) {
   switch (st) {
@@ -1743,6 +1770,10 @@ int pxg_scene_config(int slice_width, int64_t coverage_bytes) {
   });
 }
 
+int pxg_blur_config(int use_tensor_cores) {
+  return guarded([&] { g.blur_tensor = use_tensor_cores != 0; });
+}
+
 int pxg_autotune(int enable) {
   std::lock_guard<std::recursive_mutex> lk(g.mu);
   g_tune.on = enable != 0;
@@ -1806,10 +1837,13 @@ int pxg_image_blur(pxg_image* im, float radius, const float* oob) {
     const uint16_t* kern = weights_for(r);
     uint32_t* tmp = (uint32_t*)scratch(im->width * im->height * 4);
     Timed t;
-    launch_blur((uint32_t*)im->data, tmp, im->width, im->height, (int)r, kern, o, g.nsm,
-                g.blurSmemMax, g.stream);
+    if (!(g.blur_tensor && launch_blur_tc((uint32_t*)im->data, tmp, im->width, im->height, (int)r, kern, o,
+                                          g.nsm, g.tcSmemMax, g.dev_err, g.stream)))
+      launch_blur((uint32_t*)im->data, tmp, im->width, im->height, (int)r, kern, o, g.nsm,
+                  g.blurSmemMax, g.stream);
     CU(cudaGetLastError());
     t.done();
+    if (g.blocking) check_device_error();
   });
 }
 

@@ -1,0 +1,288 @@
+// Gaussian blur passes on the 5th-generation tensor cores (tcgen05, TMEM).
+//
+// One pass of pixie's blur (images.nim:304-365) is, for every channel,
+//   out[x] = (sum_t w[t] * p[x - r + t]) div 256 div 255,   t = 0 .. 2r
+// with 8-bit pixels p and 16-bit weights w.  Over a tile of N outputs and the
+// K = N + 2r inputs they read, that is a product with a banded (Toeplitz)
+// matrix B[n][k] = w[k - n]:  D[m][n] = sum_k A[m][k] * B[n][k], where a row m
+// of A is one channel of one image row (X pass) or column (Y pass).
+//
+// The arithmetic is exact.  Each weight is split into bytes, w = 256 * wh +
+// wl, so A (pixels, <= 255) and both weight matrices hold integers <= 255,
+// exact in f16; every product is an integer <= 65025 and every sum an integer
+// below 2^24 (at most 2r + 1 <= 257 products), exact in the f32 accumulator.
+// The epilogue forms 256 * D_hi + D_lo in integers and divides by 65280 --
+// bit for bit the reference's integer sums (tests compare every byte with
+// the oracle).
+//
+// Layout: one CTA (one warpgroup, 128 threads) per SM, persistent over tiles.
+// Shared memory holds B_hi and B_lo (built once per CTA) and the A tile, all
+// K-major without swizzle: 8 x 8 f16 core matrices of 128 contiguous bytes,
+// adjacent in K 128 bytes apart (LBO), adjacent in M/N (K / 8) * 128 bytes
+// apart (SBO).  Each tile: the threads convert the tile's pixels to f16 into
+// A; one thread issues K/16 MMAs of 128 x N x 16 for each weight byte into
+// two TMEM accumulators (N columns each); tcgen05.commit signals an mbarrier;
+// the warps read their 32 TMEM lanes back (tcgen05.ld), combine, quantise and
+// stage the tile in shared memory for coalesced stores.  Every wait is
+// bounded; a wait that runs out sets *err, and the CTA still frees its TMEM.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "pxg_device.cuh"
+
+namespace pxg {
+
+void note_launch();
+
+namespace {
+
+constexpr int kTcThreads = 128;          // one warpgroup: TMEM lanes 0..127
+constexpr long long kWaitCap = 1 << 22;  // mbarrier polls before giving up (far above a tile's MMA time)
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// tcgen05 shared-memory matrix descriptor: K-major, no swizzle.
+__device__ __forceinline__ uint64_t mat_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: f16 A and B (K-major), f32 D, M x N.
+__host__ __device__ constexpr uint32_t instr_desc(int M, int N) {
+  return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// Byte offset of element (row, k) in a K-major no-swizzle operand with K
+// columns.
+__device__ __forceinline__ uint32_t canon_off(int row, int k, int K) {
+  return (uint32_t)((row >> 3) * (K >> 3) * 128 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                        uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
+               : "memory");
+}
+
+// Waits for the mbarrier to complete the phase with the given parity;
+// returns false if it did not within kWaitCap polls.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+  for (long long i = 0; i < kWaitCap; i++) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// 32 lanes x 32 columns of f32 from TMEM (this warp's lane quarter).
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ uint16_t f16_bits(uint32_t v) {  // an integer 0..255 as f16
+  return __half_as_ushort(__uint2half_rn(v));
+}
+
+}  // namespace
+
+// One pass.  XPASS: rows of A are (image row, channel) pairs, 32 image rows
+// per tile, K runs along x; else (image column, channel), 32 columns per
+// tile, K along y.  N outputs per tile along the pass axis.
+template <bool XPASS, int N>
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_blur_tc(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, long long W, long long H, int r,
+              int K, const uint16_t* __restrict__ kern, uint32_t oob, int* err) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t bBytes = (uint32_t)N * K * 2, aBytes = 128u * K * 2;
+  unsigned char* bhi = sm;
+  unsigned char* blo = sm + bBytes;
+  unsigned char* abuf = sm + 2 * bBytes;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(abuf + aBytes);
+  uint32_t* taddr_s = reinterpret_cast<uint32_t*>(mbar + 1);
+
+  // The Toeplitz weight bytes, once per CTA.
+  for (int i = tid; i < N * K; i += kTcThreads) {
+    const int n = i / K, k = i - n * K, t = k - n;
+    const uint32_t w = (t >= 0 && t <= 2 * r) ? kern[t] : 0u;
+    *reinterpret_cast<uint16_t*>(bhi + canon_off(n, k, K)) = f16_bits(w >> 8);
+    *reinterpret_cast<uint16_t*>(blo + canon_off(n, k, K)) = f16_bits(w & 255u);
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(mbar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 0) {  // 2N TMEM columns: D_hi then D_lo
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(taddr_s)),
+                 "r"(2 * N)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = *taddr_s;
+  const uint32_t idesc = instr_desc(128, N);
+  const uint32_t sbo = (uint32_t)(K >> 3) * 128u;
+
+  const long long alen = XPASS ? W : H;     // along the pass
+  const long long clen = XPASS ? H : W;     // across it
+  const long long ntA = (alen + N - 1) / N, ntC = (clen + 31) / 32;
+  uint32_t phase = 0;
+  bool ok = true;
+  for (long long tile = blockIdx.x; tile < ntA * ntC && ok; tile += gridDim.x) {
+    const long long a0 = (tile % ntA) * N, c0 = (tile / ntA) * 32;
+    // A tile: row m = 4 * j + channel for the j-th line across, K inputs along
+    for (int i = tid; i < 32 * K; i += kTcThreads) {
+      int j, k;
+      if (XPASS) {  // consecutive threads read consecutive x of one row
+        j = i / K;
+        k = i - j * K;
+      } else {  // consecutive threads read consecutive x (j) of one row (k)
+        k = i >> 5;
+        j = i & 31;
+      }
+      const long long ga = a0 - r + k, gc = c0 + j;
+      uint32_t px = 0u;
+      if (gc < clen) {
+        if (ga >= 0 && ga < alen) px = XPASS ? in[gc * W + ga] : in[ga * W + gc];
+        else px = oob;
+      }
+#pragma unroll
+      for (int c = 0; c < 4; c++)
+        *reinterpret_cast<uint16_t*>(abuf + canon_off(4 * j + c, k, K)) = f16_bits((px >> (8 * c)) & 255u);
+    }
+    // the generic-proxy stores must be visible to the tensor core's reads
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (tid == 0) {
+      const uint32_t a = smem_u32(abuf), bh = smem_u32(bhi), bl = smem_u32(blo);
+      for (int s = 0; s < K / 16; s++) {
+        const uint32_t off = (uint32_t)s * 256u;  // two core matrices along K per step
+        mma_f16(tmem, mat_desc(a + off, 128, sbo), mat_desc(bh + off, 128, sbo), idesc, s > 0);
+        mma_f16(tmem + N, mat_desc(a + off, 128, sbo), mat_desc(bl + off, 128, sbo), idesc, s > 0);
+      }
+      mma_commit(smem_u32(mbar));
+    }
+    const bool waited = mbar_wait(smem_u32(mbar), phase);
+    if (!waited && lane == 0) atomicExch(err, 1);
+    phase ^= 1u;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (__syncthreads_or(!waited)) {  // every thread leaves together, then frees TMEM below
+      ok = false;
+      break;
+    }
+    // epilogue: this warp's TMEM lanes are rows m = 32 * warp + lane
+    const int m = 32 * warp + lane, j = m >> 2, c = m & 3;
+    unsigned char* stage = abuf;  // the A tile is no longer read: reuse it as [j][n][c] bytes
+#pragma unroll 1
+    for (int cc = 0; cc < N; cc += 32) {
+      float hi[32], lo[32];
+      tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)cc, hi);
+      tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(N + cc), lo);
+#pragma unroll
+      for (int q = 0; q < 32; q++) {
+        const uint32_t v = (uint32_t)hi[q] * 256u + (uint32_t)lo[q];
+        stage[(j * N + cc + q) * 4 + c] = (unsigned char)(v / 65280u);
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    const uint32_t* st = reinterpret_cast<const uint32_t*>(stage);
+    for (int i = tid; i < 32 * N; i += kTcThreads) {
+      int jj, n;
+      if (XPASS) {  // a row's N outputs are contiguous
+        jj = i / N;
+        n = i - jj * N;
+      } else {  // 32 columns of one output row are contiguous
+        n = i >> 5;
+        jj = i & 31;
+      }
+      const long long ga = a0 + n, gc = c0 + jj;
+      if (ga < alen && gc < clen) {
+        if (XPASS) out[gc * W + ga] = st[jj * N + n];
+        else out[ga * W + gc] = st[jj * N + n];
+      }
+    }
+    __syncthreads();
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(2 * N) : "memory");
+}
+
+// Tile width along the pass and the padded input span for radius r, or 0 when
+// the tensor path does not take r (it keeps every sum below 2^24 for r <= 128).
+int tc_blur_n(int r) { return r < 1 || r > 128 ? 0 : (r <= 64 ? 128 : 64); }
+int tc_blur_k(int r) {
+  const int n = tc_blur_n(r);
+  return n ? (n + 2 * r + 15) / 16 * 16 : 0;
+}
+size_t tc_blur_smem(int r) {
+  const int n = tc_blur_n(r), k = tc_blur_k(r);
+  return n ? (size_t)2 * n * k * 2 + (size_t)128 * k * 2 + 16 : 0;
+}
+const void* tc_blur_kernel(bool x, int n) {
+  if (n == 128) return x ? (const void*)k_blur_tc<true, 128> : (const void*)k_blur_tc<false, 128>;
+  return x ? (const void*)k_blur_tc<true, 64> : (const void*)k_blur_tc<false, 64>;
+}
+
+// Both passes (img -> tmp -> img).  Returns false if r is not for this path.
+bool launch_blur_tc(uint32_t* img, uint32_t* tmp, long long W, long long H, int r, const uint16_t* kern,
+                    uint32_t oob, int nsm, size_t maxSmem, int* err, cudaStream_t st) {
+  const int n = tc_blur_n(r), k = tc_blur_k(r);
+  const size_t smem = tc_blur_smem(r);
+  if (!n || smem > maxSmem) return false;
+  const long long tilesX = ((W + n - 1) / n) * ((H + 31) / 32);
+  const long long tilesY = ((H + n - 1) / n) * ((W + 31) / 32);
+  const unsigned gx = (unsigned)std::max<long long>(1, std::min<long long>(tilesX, nsm));
+  const unsigned gy = (unsigned)std::max<long long>(1, std::min<long long>(tilesY, nsm));
+  if (n == 128) {
+    k_blur_tc<true, 128><<<gx, kTcThreads, smem, st>>>(img, tmp, W, H, r, k, kern, oob, err);
+    k_blur_tc<false, 128><<<gy, kTcThreads, smem, st>>>(tmp, img, W, H, r, k, kern, oob, err);
+  } else {
+    k_blur_tc<true, 64><<<gx, kTcThreads, smem, st>>>(img, tmp, W, H, r, k, kern, oob, err);
+    k_blur_tc<false, 64><<<gy, kTcThreads, smem, st>>>(tmp, img, W, H, r, k, kern, oob, err);
+  }
+  note_launch();
+  note_launch();
+  return true;
+}
+
+}  // namespace pxg
