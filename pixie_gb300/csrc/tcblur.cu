@@ -15,14 +15,14 @@
 // bit for bit the reference's integer sums (tests compare every byte with
 // the oracle).
 //
-// Layout: one CTA (one warpgroup, 128 threads) per SM, persistent over tiles.
+// Layout: one or two CTAs (256 threads) per SM, persistent over tiles.
 // Shared memory holds B_hi and B_lo (built once per CTA) and the A tile, all
 // K-major without swizzle: 8 x 8 f16 core matrices of 128 contiguous bytes,
 // adjacent in K 128 bytes apart (LBO), adjacent in M/N (K / 8) * 128 bytes
 // apart (SBO).  Each tile: the threads convert the tile's pixels to f16 into
 // A; one thread issues K/16 MMAs of 128 x N x 16 for each weight byte into
 // two TMEM accumulators (N columns each); tcgen05.commit signals an mbarrier;
-// the warps read their 32 TMEM lanes back (tcgen05.ld), combine, quantise and
+// the warps read their TMEM lanes back (tcgen05.ld), combine, quantise and
 // stage the tile in shared memory for coalesced stores.  Every wait is
 // bounded; a wait that runs out sets *err, and the CTA still frees its TMEM.
 #include <cuda_fp16.h>
@@ -39,7 +39,7 @@ void note_launch();
 
 namespace {
 
-constexpr int kTcThreads = 128;          // one warpgroup: TMEM lanes 0..127
+constexpr int kTcThreads = 256;          // two warpgroups: warps w and w + 4 share TMEM lanes 32 * (w % 4)
 constexpr long long kWaitCap = 1 << 22;  // mbarrier polls before giving up (far above a tile's MMA time)
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -121,7 +121,7 @@ __device__ __forceinline__ uint16_t f16_bits(uint32_t v) {  // an integer 0..255
 // per tile, K runs along x; else (image column, channel), 32 columns per
 // tile, K along y.  N outputs per tile along the pass axis.
 template <bool XPASS, int N>
-__global__ void __launch_bounds__(kTcThreads, 1)
+__global__ void __launch_bounds__(kTcThreads, 2)
     k_blur_tc(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, long long W, long long H, int r,
               int K, const uint16_t* __restrict__ kern, uint32_t oob, int* err) {
   extern __shared__ __align__(1024) unsigned char sm[];
@@ -164,25 +164,39 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   bool ok = true;
   for (long long tile = blockIdx.x; tile < ntA * ntC && ok; tile += gridDim.x) {
     const long long a0 = (tile % ntA) * N, c0 = (tile / ntA) * 32;
-    // A tile: row m = 4 * j + channel for the j-th line across, K inputs along
-    for (int i = tid; i < 32 * K; i += kTcThreads) {
-      int j, k;
-      if (XPASS) {  // consecutive threads read consecutive x of one row
-        j = i / K;
-        k = i - j * K;
-      } else {  // consecutive threads read consecutive x (j) of one row (k)
-        k = i >> 5;
-        j = i & 31;
+    // A tile: row m = 4 * j + channel for the j-th line across, K inputs
+    // along.  An item is 8 consecutive inputs of one line: 8 loads in flight,
+    // then one 16-byte store (a core-matrix row) per channel.
+    const int KG = K >> 3;
+    for (int it = tid; it < 32 * KG; it += kTcThreads) {
+      int j, kg;
+      if (XPASS) {  // consecutive threads: consecutive 8-pixel runs of one row
+        j = it / KG;
+        kg = it - j * KG;
+      } else {  // consecutive threads: consecutive columns j
+        kg = it >> 5;
+        j = it & 31;
       }
-      const long long ga = a0 - r + k, gc = c0 + j;
-      uint32_t px = 0u;
-      if (gc < clen) {
-        if (ga >= 0 && ga < alen) px = XPASS ? in[gc * W + ga] : in[ga * W + gc];
-        else px = oob;
+      const long long gc = c0 + j;
+      uint32_t px[8];
+#pragma unroll
+      for (int t = 0; t < 8; t++) {
+        const long long ga = a0 - r + 8 * kg + t;
+        px[t] = 0u;
+        if (gc < clen) {
+          if (ga >= 0 && ga < alen) px[t] = XPASS ? in[gc * W + ga] : in[ga * W + gc];
+          else px[t] = oob;
+        }
       }
 #pragma unroll
-      for (int c = 0; c < 4; c++)
-        *reinterpret_cast<uint16_t*>(abuf + canon_off(4 * j + c, k, K)) = f16_bits((px >> (8 * c)) & 255u);
+      for (int c = 0; c < 4; c++) {
+        uint32_t h[4];
+#pragma unroll
+        for (int t = 0; t < 4; t++)
+          h[t] = (uint32_t)f16_bits((px[2 * t] >> (8 * c)) & 255u) |
+                 ((uint32_t)f16_bits((px[2 * t + 1] >> (8 * c)) & 255u) << 16);
+        *reinterpret_cast<uint4*>(abuf + canon_off(4 * j + c, 8 * kg, K)) = make_uint4(h[0], h[1], h[2], h[3]);
+      }
     }
     // the generic-proxy stores must be visible to the tensor core's reads
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
@@ -206,18 +220,22 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       ok = false;
       break;
     }
-    // epilogue: this warp's TMEM lanes are rows m = 32 * warp + lane
-    const int m = 32 * warp + lane, j = m >> 2, c = m & 3;
-    unsigned char* stage = abuf;  // the A tile is no longer read: reuse it as [j][n][c] bytes
+    // epilogue: warp w reads TMEM lanes m = 32 * (w % 4) + lane, columns
+    // [(w / 4) * N / 2, + N / 2); the tile is staged as bytes [j][n][c] with a
+    // row stride of 4 * N + 16 bytes (quads of lanes land in different banks)
+    const int q = warp & 3, half = warp >> 2;
+    const int m = 32 * q + lane, j = m >> 2, c = m & 3;
+    unsigned char* stage = abuf;  // the A tile is no longer read
+    const int rs = 4 * N + 16;
 #pragma unroll 1
-    for (int cc = 0; cc < N; cc += 32) {
+    for (int cc = half * (N / 2); cc < (half + 1) * (N / 2); cc += 32) {
       float hi[32], lo[32];
-      tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)cc, hi);
-      tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(N + cc), lo);
+      tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)cc, hi);
+      tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(N + cc), lo);
 #pragma unroll
-      for (int q = 0; q < 32; q++) {
-        const uint32_t v = (uint32_t)hi[q] * 256u + (uint32_t)lo[q];
-        stage[(j * N + cc + q) * 4 + c] = (unsigned char)(v / 65280u);
+      for (int t = 0; t < 32; t++) {
+        const uint32_t v = (uint32_t)hi[t] * 256u + (uint32_t)lo[t];
+        stage[j * rs + (cc + t) * 4 + c] = (unsigned char)(v / 65280u);
       }
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -234,8 +252,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
       const long long ga = a0 + n, gc = c0 + jj;
       if (ga < alen && gc < clen) {
-        if (XPASS) out[gc * W + ga] = st[jj * N + n];
-        else out[ga * W + gc] = st[jj * N + n];
+        const uint32_t v = st[jj * (rs / 4) + n];
+        if (XPASS) out[gc * W + ga] = v;
+        else out[ga * W + gc] = v;
       }
     }
     __syncthreads();
@@ -271,8 +290,11 @@ bool launch_blur_tc(uint32_t* img, uint32_t* tmp, long long W, long long H, int 
   if (!n || smem > maxSmem) return false;
   const long long tilesX = ((W + n - 1) / n) * ((H + 31) / 32);
   const long long tilesY = ((H + n - 1) / n) * ((W + 31) / 32);
-  const unsigned gx = (unsigned)std::max<long long>(1, std::min<long long>(tilesX, nsm));
-  const unsigned gy = (unsigned)std::max<long long>(1, std::min<long long>(tilesY, nsm));
+  // two CTAs per SM when both fit in shared memory (their TMEM, 2 x 2N
+  // columns, always fits the SM's 512): one stages while the other computes
+  const int per = smem * 2 + 2048 <= 228 * 1024 ? 2 : 1;
+  const unsigned gx = (unsigned)std::max<long long>(1, std::min<long long>(tilesX, (long long)nsm * per));
+  const unsigned gy = (unsigned)std::max<long long>(1, std::min<long long>(tilesY, (long long)nsm * per));
   if (n == 128) {
     k_blur_tc<true, 128><<<gx, kTcThreads, smem, st>>>(img, tmp, W, H, r, k, kern, oob, err);
     k_blur_tc<false, 128><<<gy, kTcThreads, smem, st>>>(tmp, img, W, H, r, k, kern, oob, err);
