@@ -450,7 +450,7 @@ def scene_config(slice_width: int = 256, coverage_bytes: int = -1):
 
 
 def blur_config(use_tensor_cores: bool):
-    """True (default): blur radii 1..128 on the tensor cores; False: CUDA cores."""
+    """True (default): blur radii 8..128 on the tensor cores; False: CUDA cores."""
     _check(lib().pxg_blur_config(1 if use_tensor_cores else 0))
 
 

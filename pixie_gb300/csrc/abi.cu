@@ -228,7 +228,7 @@ struct Ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evr0 = nullptr, evr1 = nullptr;
   int* dev_err = nullptr;   // device-side error flag (a tensor-core wait that ran out)
   int* host_err = nullptr;  // its pinned mirror
-  bool blur_tensor = true;  // blur radii 1..128 on the tensor cores
+  bool blur_tensor = true;  // blur radii 8..128 on the tensor cores
   size_t tcSmemMax = 0;
   float last_ms = 0;
   long long stats[6] = {0, 0, 0, 0, 0, 0};  // last fill launch: paths, prims, segments, entries, blends, wide rows

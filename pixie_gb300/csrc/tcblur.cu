@@ -267,8 +267,10 @@ __global__ void __launch_bounds__(kTcThreads, 2)
 }
 
 // Tile width along the pass and the padded input span for radius r, or 0 when
-// the tensor path does not take r (it keeps every sum below 2^24 for r <= 128).
-int tc_blur_n(int r) { return r < 1 || r > 128 ? 0 : (r <= 64 ? 128 : 64); }
+// the tensor path does not take r: it keeps every sum below 2^24 for r <= 128,
+// and below r = 8 the CUDA-core kernels, which are not compute-bound there,
+// are faster.
+int tc_blur_n(int r) { return r < 8 || r > 128 ? 0 : (r <= 64 ? 128 : 64); }
 int tc_blur_k(int r) {
   const int n = tc_blur_n(r);
   return n ? (n + 2 * r + 15) / 16 * 16 : 0;
