@@ -449,9 +449,10 @@ def scene_config(slice_width: int = 256, coverage_bytes: int = -1):
     _check(lib().pxg_scene_config(int(slice_width), int(coverage_bytes)))
 
 
-def blur_config(use_tensor_cores: bool):
-    """True (default): blur radii 8..128 on the tensor cores; False: CUDA cores."""
-    _check(lib().pxg_blur_config(1 if use_tensor_cores else 0))
+def blur_config(mode):
+    """1/True (default): pipelined tensor-core blur (radii 1..128); 2: the
+    single-stage tensor-core kernel (radii 8..128); 0/False: CUDA cores."""
+    _check(lib().pxg_blur_config(int(mode)))
 
 
 def autotune(enable: bool):

@@ -139,6 +139,9 @@ size_t blur_y_smem(int r);
 bool launch_blur_tc(uint32_t* img, uint32_t* tmp, long long W, long long H, int r, const uint16_t* kern,
                     uint32_t oob, int nsm, size_t maxSmem, int* err, cudaStream_t st);
 const void* tc_blur_kernel(bool x, int n);
+bool launch_blur_tcp(uint32_t* img, uint32_t* tmp, long long W, long long H, int r, const uint16_t* kern,
+                     uint32_t oob, int nsm, size_t maxSmem, int* err, cudaStream_t st);
+const void* tcp_blur_kernel(bool x, int n);
 __global__ void k_blur_x(const uint32_t*, uint32_t*, long long, long long, int, const uint16_t*, uint32_t);
 __global__ void k_blur_y(const uint32_t*, uint32_t*, long long, long long, int, const uint16_t*, uint32_t);
 __global__ void k_blurf_x(const uint32_t*, uint32_t*, long long, long long, int, const uint16_t*, uint32_t);
@@ -228,7 +231,7 @@ struct Ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evr0 = nullptr, evr1 = nullptr;
   int* dev_err = nullptr;   // device-side error flag (a tensor-core wait that ran out)
   int* host_err = nullptr;  // its pinned mirror
-  bool blur_tensor = true;  // blur radii 8..128 on the tensor cores
+  int blur_tensor = 1;      // 1: pipelined tensor-core blur, 2: single-stage one, 0: CUDA cores
   size_t tcSmemMax = 0;
   float last_ms = 0;
   long long stats[6] = {0, 0, 0, 0, 0, 0};  // last fill launch: paths, prims, segments, entries, blends, wide rows
@@ -303,6 +306,10 @@ void init_locked(int device) {
   g.tcSmemMax = std::min(g.tcSmemMax, allow_max_smem(tc_blur_kernel(false, 128)));
   g.tcSmemMax = std::min(g.tcSmemMax, allow_max_smem(tc_blur_kernel(true, 64)));
   g.tcSmemMax = std::min(g.tcSmemMax, allow_max_smem(tc_blur_kernel(false, 64)));
+  g.tcSmemMax = std::min(g.tcSmemMax, allow_max_smem(tcp_blur_kernel(true, 64)));
+  g.tcSmemMax = std::min(g.tcSmemMax, allow_max_smem(tcp_blur_kernel(false, 64)));
+  g.tcSmemMax = std::min(g.tcSmemMax, allow_max_smem(tcp_blur_kernel(true, 32)));
+  g.tcSmemMax = std::min(g.tcSmemMax, allow_max_smem(tcp_blur_kernel(false, 32)));
   g.ready = true;
 }
 void ensure_init() {
@@ -1771,7 +1778,10 @@ int pxg_scene_config(int slice_width, int64_t coverage_bytes) {
 }
 
 int pxg_blur_config(int use_tensor_cores) {
-  return guarded([&] { g.blur_tensor = use_tensor_cores != 0; });
+  return guarded([&] {
+    if (use_tensor_cores < 0 || use_tensor_cores > 2) throw ApiError{"Invalid blur configuration"};
+    g.blur_tensor = use_tensor_cores;
+  });
 }
 
 int pxg_autotune(int enable) {
@@ -1837,8 +1847,12 @@ int pxg_image_blur(pxg_image* im, float radius, const float* oob) {
     const uint16_t* kern = weights_for(r);
     uint32_t* tmp = (uint32_t*)scratch(im->width * im->height * 4);
     Timed t;
-    if (!(g.blur_tensor && launch_blur_tc((uint32_t*)im->data, tmp, im->width, im->height, (int)r, kern, o,
-                                          g.nsm, g.tcSmemMax, g.dev_err, g.stream)))
+    const bool tc = g.blur_tensor == 2 ? launch_blur_tc((uint32_t*)im->data, tmp, im->width, im->height, (int)r,
+                                                        kern, o, g.nsm, g.tcSmemMax, g.dev_err, g.stream)
+                    : g.blur_tensor == 1 && launch_blur_tcp((uint32_t*)im->data, tmp, im->width, im->height,
+                                                            (int)r, kern, o, g.nsm, g.tcSmemMax, g.dev_err,
+                                                            g.stream);
+    if (!tc)
       launch_blur((uint32_t*)im->data, tmp, im->width, im->height, (int)r, kern, o, g.nsm,
                   g.blurSmemMax, g.stream);
     CU(cudaGetLastError());

@@ -266,6 +266,230 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(2 * N) : "memory");
 }
 
+// The pipelined pass: warp-specialised and double-buffered, so that loading
+// and converting tile i + 1, the MMAs of tile i and the epilogue of tile i - 1
+// run at the same time.
+//   warps 0-3  producers: global loads -> f16 A tile in A[i % 2], then arrive
+//              on full[i % 2]; before refilling a slot they wait empty[slot]
+//   warp 8     one thread issues the MMAs of a tile into accumulator pair
+//              i % 2 (TMEM) and commits to empty[slot] and tfull[pair]
+//   warps 4-7  epilogue: wait tfull[pair], read TMEM lanes 32 * (w % 4),
+//              arrive on tempty[pair], quantise, stage and store the tile
+// Every mbarrier wait is bounded; a role whose wait runs out sets *err and
+// stops, the others' waits then run out too, and the CTA frees its TMEM.
+constexpr int kPipeThreads = 288;
+
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(mbar), "r"(count) : "memory");
+}
+// bar.red.or over the 128 epilogue threads (named barrier 1): every thread
+// gets the same answer, so they leave a loop together.
+__device__ __forceinline__ bool epi_bar_or(bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.or.pred q, 1, 128, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}\n"
+      : "=r"(r)
+      : "r"((uint32_t)v)
+      : "memory");
+  return r != 0;
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(mbar) : "memory");
+}
+
+template <bool XPASS, int N>
+__global__ void __launch_bounds__(kPipeThreads, 1)
+    k_blur_tcp(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, long long W, long long H, int r,
+               int K, const uint16_t* __restrict__ kern, uint32_t oob, int* err) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t bBytes = (uint32_t)N * K * 2, aBytes = 128u * K * 2;
+  const int rs = 4 * N + 16;  // output staging row stride (bytes)
+  unsigned char* bhi = sm;
+  unsigned char* blo = sm + bBytes;
+  unsigned char* abuf0 = sm + 2 * bBytes;
+  unsigned char* stage = abuf0 + 2 * aBytes;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(stage + 32 * rs);  // full[2] empty[2] tfull[2] tempty[2]
+  uint32_t* taddr_s = reinterpret_cast<uint32_t*>(bars + 8);
+  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + 2), tfull0 = smem_u32(bars + 4),
+                 tempty0 = smem_u32(bars + 6);
+
+  for (int i = tid; i < N * K; i += kPipeThreads) {
+    const int n = i / K, k = i - n * K, t = k - n;
+    const uint32_t w = (t >= 0 && t <= 2 * r) ? kern[t] : 0u;
+    *reinterpret_cast<uint16_t*>(bhi + canon_off(n, k, K)) = f16_bits(w >> 8);
+    *reinterpret_cast<uint16_t*>(blo + canon_off(n, k, K)) = f16_bits(w & 255u);
+  }
+  if (tid == 0) {
+    for (int b = 0; b < 2; b++) {
+      mbar_init(full0 + 8 * b, 128);
+      mbar_init(empty0 + 8 * b, 1);
+      mbar_init(tfull0 + 8 * b, 1);
+      mbar_init(tempty0 + 8 * b, 128);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 0) {  // two accumulator pairs: (D_hi, D_lo) x 2
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(taddr_s)),
+                 "r"(4 * N)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // B, for the tensor core
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = *taddr_s;
+
+  const long long alen = XPASS ? W : H, clen = XPASS ? H : W;
+  const long long ntA = (alen + N - 1) / N, ntC = (clen + 31) / 32, ntiles = ntA * ntC;
+  const long long nmine = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+
+  if (warp < 4) {
+    // producers
+    const int KG = K >> 3;
+    for (long long i = 0; i < nmine; i++) {
+      const int slot = (int)(i & 1);
+      if (i >= 2 && !mbar_wait(empty0 + 8 * slot, (uint32_t)(((i >> 1) - 1) & 1))) {
+        if (lane == 0) atomicExch(err, 1);
+        break;
+      }
+      const long long tile = blockIdx.x + i * gridDim.x;
+      const long long a0 = (tile % ntA) * N, c0 = (tile / ntA) * 32;
+      unsigned char* abuf = abuf0 + slot * aBytes;
+      for (int it = tid; it < 32 * KG; it += 128) {
+        int j, kg;
+        if (XPASS) {
+          j = it / KG;
+          kg = it - j * KG;
+        } else {
+          kg = it >> 5;
+          j = it & 31;
+        }
+        const long long gc = c0 + j;
+        uint32_t px[8];
+#pragma unroll
+        for (int t = 0; t < 8; t++) {
+          const long long ga = a0 - r + 8 * kg + t;
+          px[t] = 0u;
+          if (gc < clen) {
+            if (ga >= 0 && ga < alen) px[t] = XPASS ? in[gc * W + ga] : in[ga * W + gc];
+            else px[t] = oob;
+          }
+        }
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          uint32_t h[4];
+#pragma unroll
+          for (int t = 0; t < 4; t++)
+            h[t] = (uint32_t)f16_bits((px[2 * t] >> (8 * c)) & 255u) |
+                   ((uint32_t)f16_bits((px[2 * t + 1] >> (8 * c)) & 255u) << 16);
+          *reinterpret_cast<uint4*>(abuf + canon_off(4 * j + c, 8 * kg, K)) = make_uint4(h[0], h[1], h[2], h[3]);
+        }
+      }
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+      mbar_arrive(full0 + 8 * slot);
+    }
+  } else if (warp == 8) {
+    // the MMA issuer
+    if (lane == 0) {
+      const uint32_t idesc = instr_desc(128, N);
+      const uint32_t sbo = (uint32_t)(K >> 3) * 128u;
+      const uint32_t bh = smem_u32(bhi), bl = smem_u32(blo);
+      for (long long i = 0; i < nmine; i++) {
+        const int slot = (int)(i & 1);
+        if (!mbar_wait(full0 + 8 * slot, (uint32_t)((i >> 1) & 1)) ||
+            (i >= 2 && !mbar_wait(tempty0 + 8 * slot, (uint32_t)(((i >> 1) - 1) & 1)))) {
+          atomicExch(err, 1);
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const uint32_t a = smem_u32(abuf0 + slot * aBytes);
+        const uint32_t dh = tmem + (uint32_t)(slot * 2 * N), dl = dh + (uint32_t)N;
+        for (int s2 = 0; s2 < K / 16; s2++) {
+          const uint32_t off = (uint32_t)s2 * 256u;
+          mma_f16(dh, mat_desc(a + off, 128, sbo), mat_desc(bh + off, 128, sbo), idesc, s2 > 0);
+          mma_f16(dl, mat_desc(a + off, 128, sbo), mat_desc(bl + off, 128, sbo), idesc, s2 > 0);
+        }
+        mma_commit(empty0 + 8 * slot);
+        mma_commit(tfull0 + 8 * slot);
+      }
+    }
+    __syncwarp();
+  } else {
+    // epilogue: warps 4-7, TMEM lanes 32 * (warp % 4)
+    const int q = warp & 3;
+    const int m = 32 * q + lane, j = m >> 2, c = m & 3;
+    const int etid = tid - 128;  // 0..127
+    for (long long i = 0; i < nmine; i++) {
+      const int slot = (int)(i & 1);
+      const bool ready = mbar_wait(tfull0 + 8 * slot, (uint32_t)((i >> 1) & 1));
+      if (!ready && lane == 0) atomicExch(err, 1);
+      // also: the staging buffer is free (the previous tile's stores are done)
+      if (epi_bar_or(!ready)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      const uint32_t dh = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(slot * 2 * N);
+#pragma unroll 1
+      for (int cc = 0; cc < N; cc += 32) {
+        float hi[32], lo[32];
+        tmem_ld32(dh + (uint32_t)cc, hi);
+        tmem_ld32(dh + (uint32_t)(N + cc), lo);
+#pragma unroll
+        for (int t = 0; t < 32; t++) {
+          const uint32_t v = (uint32_t)hi[t] * 256u + (uint32_t)lo[t];
+          stage[j * rs + (cc + t) * 4 + c] = (unsigned char)(v / 65280u);
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+      mbar_arrive(tempty0 + 8 * slot);
+      asm volatile("bar.sync 1, 128;\n" ::: "memory");
+      const long long tile = blockIdx.x + i * gridDim.x;
+      const long long a0 = (tile % ntA) * N, c0 = (tile / ntA) * 32;
+      const uint32_t* st = reinterpret_cast<const uint32_t*>(stage);
+      for (int e = etid; e < 32 * N; e += 128) {
+        int jj, n;
+        if (XPASS) {
+          jj = e / N;
+          n = e - jj * N;
+        } else {
+          n = e >> 5;
+          jj = e & 31;
+        }
+        const long long ga = a0 + n, gc = c0 + jj;
+        if (ga < alen && gc < clen) {
+          const uint32_t v = st[jj * (rs / 4) + n];
+          if (XPASS) out[gc * W + ga] = v;
+          else out[ga * W + gc] = v;
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(4 * N) : "memory");
+}
+
+// The pipelined pass's tile width: 64 outputs for r <= 64, 32 up to 128
+// (two A tiles, B and the output stage fit 227 KB of shared memory).
+int tcp_blur_n(int r) { return r < 1 || r > 128 ? 0 : (r <= 64 ? 64 : 32); }
+int tcp_blur_k(int r) {
+  const int n = tcp_blur_n(r);
+  return n ? (n + 2 * r + 15) / 16 * 16 : 0;
+}
+size_t tcp_blur_smem(int r) {
+  const int n = tcp_blur_n(r), k = tcp_blur_k(r);
+  return n ? (size_t)2 * n * k * 2 + (size_t)2 * 128 * k * 2 + (size_t)32 * (4 * n + 16) + 8 * 8 + 16 : 0;
+}
+const void* tcp_blur_kernel(bool x, int n) {
+  if (n == 64) return x ? (const void*)k_blur_tcp<true, 64> : (const void*)k_blur_tcp<false, 64>;
+  return x ? (const void*)k_blur_tcp<true, 32> : (const void*)k_blur_tcp<false, 32>;
+}
+
 // Tile width along the pass and the padded input span for radius r, or 0 when
 // the tensor path does not take r: it keeps every sum below 2^24 for r <= 128,
 // and below r = 8 the CUDA-core kernels, which are not compute-bound there,
@@ -282,6 +506,28 @@ size_t tc_blur_smem(int r) {
 const void* tc_blur_kernel(bool x, int n) {
   if (n == 128) return x ? (const void*)k_blur_tc<true, 128> : (const void*)k_blur_tc<false, 128>;
   return x ? (const void*)k_blur_tc<true, 64> : (const void*)k_blur_tc<false, 64>;
+}
+
+// Both passes with the pipelined kernel.  Returns false if r is not for it.
+bool launch_blur_tcp(uint32_t* img, uint32_t* tmp, long long W, long long H, int r, const uint16_t* kern,
+                     uint32_t oob, int nsm, size_t maxSmem, int* err, cudaStream_t st) {
+  const int n = tcp_blur_n(r), k = tcp_blur_k(r);
+  const size_t smem = tcp_blur_smem(r);
+  if (!n || smem > maxSmem) return false;
+  const long long tilesX = ((W + n - 1) / n) * ((H + 31) / 32);
+  const long long tilesY = ((H + n - 1) / n) * ((W + 31) / 32);
+  const unsigned gx = (unsigned)std::max<long long>(1, std::min<long long>(tilesX, nsm));
+  const unsigned gy = (unsigned)std::max<long long>(1, std::min<long long>(tilesY, nsm));
+  if (n == 64) {
+    k_blur_tcp<true, 64><<<gx, kPipeThreads, smem, st>>>(img, tmp, W, H, r, k, kern, oob, err);
+    k_blur_tcp<false, 64><<<gy, kPipeThreads, smem, st>>>(tmp, img, W, H, r, k, kern, oob, err);
+  } else {
+    k_blur_tcp<true, 32><<<gx, kPipeThreads, smem, st>>>(img, tmp, W, H, r, k, kern, oob, err);
+    k_blur_tcp<false, 32><<<gy, kPipeThreads, smem, st>>>(tmp, img, W, H, r, k, kern, oob, err);
+  }
+  note_launch();
+  note_launch();
+  return true;
 }
 
 // Both passes (img -> tmp -> img).  Returns false if r is not for this path.
