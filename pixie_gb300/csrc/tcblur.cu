@@ -115,6 +115,17 @@ __device__ __forceinline__ uint16_t f16_bits(uint32_t v) {  // an integer 0..255
   return __half_as_ushort(__uint2half_rn(v));
 }
 
+// Channel c of two RGBX pixels as an f16 pair (x's in the low half): the
+// bytes are placed under the f16 exponent of 1024 (0x64), where the mantissa
+// step is 1, giving 1024 + v exactly; subtracting 1024 leaves v.
+__device__ __forceinline__ uint32_t f16_pair(uint32_t x, uint32_t y, int c) {
+  const uint32_t p = __byte_perm(x, y, (uint32_t)c | ((uint32_t)(c + 4) << 4));  // [x_c, y_c, ., .]
+  const uint32_t q = __byte_perm(p, 0x64646464u, 0x5140u);                      // [x_c, 64, y_c, 64]
+  const __half2 h = __hsub2(*reinterpret_cast<const __half2*>(&q), __halves2half2(__ushort_as_half(0x6400),
+                                                                                  __ushort_as_half(0x6400)));
+  return *reinterpret_cast<const uint32_t*>(&h);
+}
+
 }  // namespace
 
 // One pass.  XPASS: rows of A are (image row, channel) pairs, 32 image rows
@@ -192,9 +203,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       for (int c = 0; c < 4; c++) {
         uint32_t h[4];
 #pragma unroll
-        for (int t = 0; t < 4; t++)
-          h[t] = (uint32_t)f16_bits((px[2 * t] >> (8 * c)) & 255u) |
-                 ((uint32_t)f16_bits((px[2 * t + 1] >> (8 * c)) & 255u) << 16);
+        for (int t = 0; t < 4; t++) h[t] = f16_pair(px[2 * t], px[2 * t + 1], c);
         *reinterpret_cast<uint4*>(abuf + canon_off(4 * j + c, 8 * kg, K)) = make_uint4(h[0], h[1], h[2], h[3]);
       }
     }
@@ -269,15 +278,17 @@ __global__ void __launch_bounds__(kTcThreads, 2)
 // The pipelined pass: warp-specialised and double-buffered, so that loading
 // and converting tile i + 1, the MMAs of tile i and the epilogue of tile i - 1
 // run at the same time.
-//   warps 0-3  producers: global loads -> f16 A tile in A[i % 2], then arrive
-//              on full[i % 2]; before refilling a slot they wait empty[slot]
-//   warp 8     one thread issues the MMAs of a tile into accumulator pair
-//              i % 2 (TMEM) and commits to empty[slot] and tfull[pair]
-//   warps 4-7  epilogue: wait tfull[pair], read TMEM lanes 32 * (w % 4),
-//              arrive on tempty[pair], quantise, stage and store the tile
+//   warps 0-7   producers: global loads -> f16 A tile in A[i % 2], then
+//               arrive on full[i % 2]; before refilling a slot they wait
+//               empty[slot]
+//   warp 12     one thread issues the MMAs of a tile into accumulator pair
+//               i % 2 (TMEM) and commits to empty[slot] and tfull[pair]
+//   warps 8-11  epilogue: wait tfull[pair], read TMEM lanes 32 * (w % 4),
+//               arrive on tempty[pair], quantise, stage and store the tile
 // Every mbarrier wait is bounded; a role whose wait runs out sets *err and
 // stops, the others' waits then run out too, and the CTA frees its TMEM.
-constexpr int kPipeThreads = 288;
+constexpr int kPipeThreads = 416;  // 8 producer warps, 4 epilogue warps, 1 MMA warp
+constexpr int kProducers = 256;
 
 __device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(mbar), "r"(count) : "memory");
@@ -325,7 +336,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
   }
   if (tid == 0) {
     for (int b = 0; b < 2; b++) {
-      mbar_init(full0 + 8 * b, 128);
+      mbar_init(full0 + 8 * b, kProducers);
       mbar_init(empty0 + 8 * b, 1);
       mbar_init(tfull0 + 8 * b, 1);
       mbar_init(tempty0 + 8 * b, 128);
@@ -348,7 +359,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
   const long long ntA = (alen + N - 1) / N, ntC = (clen + 31) / 32, ntiles = ntA * ntC;
   const long long nmine = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
 
-  if (warp < 4) {
+  if (tid < kProducers) {
     // producers
     const int KG = K >> 3;
     for (long long i = 0; i < nmine; i++) {
@@ -360,7 +371,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
       const long long tile = blockIdx.x + i * gridDim.x;
       const long long a0 = (tile % ntA) * N, c0 = (tile / ntA) * 32;
       unsigned char* abuf = abuf0 + slot * aBytes;
-      for (int it = tid; it < 32 * KG; it += 128) {
+      for (int it = tid; it < 32 * KG; it += kProducers) {
         int j, kg;
         if (XPASS) {
           j = it / KG;
@@ -384,16 +395,14 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
         for (int c = 0; c < 4; c++) {
           uint32_t h[4];
 #pragma unroll
-          for (int t = 0; t < 4; t++)
-            h[t] = (uint32_t)f16_bits((px[2 * t] >> (8 * c)) & 255u) |
-                   ((uint32_t)f16_bits((px[2 * t + 1] >> (8 * c)) & 255u) << 16);
+          for (int t = 0; t < 4; t++) h[t] = f16_pair(px[2 * t], px[2 * t + 1], c);
           *reinterpret_cast<uint4*>(abuf + canon_off(4 * j + c, 8 * kg, K)) = make_uint4(h[0], h[1], h[2], h[3]);
         }
       }
       asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
       mbar_arrive(full0 + 8 * slot);
     }
-  } else if (warp == 8) {
+  } else if (warp == 12) {
     // the MMA issuer
     if (lane == 0) {
       const uint32_t idesc = instr_desc(128, N);
@@ -420,10 +429,10 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
     }
     __syncwarp();
   } else {
-    // epilogue: warps 4-7, TMEM lanes 32 * (warp % 4)
+    // epilogue: warps 8-11, TMEM lanes 32 * (warp % 4)
     const int q = warp & 3;
     const int m = 32 * q + lane, j = m >> 2, c = m & 3;
-    const int etid = tid - 128;  // 0..127
+    const int etid = tid - kProducers;  // 0..127
     for (long long i = 0; i < nmine; i++) {
       const int slot = (int)(i & 1);
       const bool ready = mbar_wait(tfull0 + 8 * slot, (uint32_t)((i >> 1) & 1));
