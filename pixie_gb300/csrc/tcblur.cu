@@ -281,26 +281,27 @@ __global__ void __launch_bounds__(kTcThreads, 2)
 //   warps 0-7   producers: global loads -> f16 A tile in A[i % 2], then
 //               arrive on full[i % 2]; before refilling a slot they wait
 //               empty[slot]
-//   warp 12     one thread issues the MMAs of a tile into accumulator pair
+//   warp 16     one thread issues the MMAs of a tile into accumulator pair
 //               i % 2 (TMEM) and commits to empty[slot] and tfull[pair]
-//   warps 8-11  epilogue: wait tfull[pair], read TMEM lanes 32 * (w % 4),
-//               arrive on tempty[pair], quantise, stage and store the tile
+//   warps 8-15  epilogue: wait tfull[pair], read TMEM lanes 32 * (w % 4)
+//               (warps w and w + 4 split the columns), arrive on
+//               tempty[pair], quantise, stage and store the tile
 // Every mbarrier wait is bounded; a role whose wait runs out sets *err and
 // stops, the others' waits then run out too, and the CTA frees its TMEM.
-constexpr int kPipeThreads = 416;  // 8 producer warps, 4 epilogue warps, 1 MMA warp
-constexpr int kProducers = 256;
+constexpr int kPipeThreads = 544;  // 8 producer warps, 8 epilogue warps, 1 MMA warp
+constexpr int kProducers = 256, kEpilogue = 256;
 
 __device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(mbar), "r"(count) : "memory");
 }
-// bar.red.or over the 128 epilogue threads (named barrier 1): every thread
+// bar.red.or over the 256 epilogue threads (named barrier 1): every thread
 // gets the same answer, so they leave a loop together.
 __device__ __forceinline__ bool epi_bar_or(bool v) {
   uint32_t r;
   asm volatile(
       "{\n\t.reg .pred p, q;\n\t"
       "setp.ne.u32 p, %1, 0;\n\t"
-      "bar.red.or.pred q, 1, 128, p;\n\t"
+      "bar.red.or.pred q, 1, 256, p;\n\t"
       "selp.u32 %0, 1, 0, q;\n\t}\n"
       : "=r"(r)
       : "r"((uint32_t)v)
@@ -339,7 +340,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
       mbar_init(full0 + 8 * b, kProducers);
       mbar_init(empty0 + 8 * b, 1);
       mbar_init(tfull0 + 8 * b, 1);
-      mbar_init(tempty0 + 8 * b, 128);
+      mbar_init(tempty0 + 8 * b, kEpilogue);
     }
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
@@ -402,7 +403,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
       asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
       mbar_arrive(full0 + 8 * slot);
     }
-  } else if (warp == 12) {
+  } else if (warp == 16) {
     // the MMA issuer
     if (lane == 0) {
       const uint32_t idesc = instr_desc(128, N);
@@ -429,10 +430,13 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
     }
     __syncwarp();
   } else {
-    // epilogue: warps 8-11, TMEM lanes 32 * (warp % 4)
-    const int q = warp & 3;
+    // epilogue: warps 8-15, TMEM lanes 32 * (warp % 4); warps w and w + 4
+    // take the two halves of the columns (when a half holds 32 columns)
+    const int q = warp & 3, half = (warp - 8) >> 2;
     const int m = 32 * q + lane, j = m >> 2, c = m & 3;
-    const int etid = tid - kProducers;  // 0..127
+    const int etid = tid - kProducers;  // 0..255
+    const int cols = N / 2 >= 32 ? N / 2 : (half ? 0 : N);
+    const int col0 = N / 2 >= 32 ? half * (N / 2) : 0;
     for (long long i = 0; i < nmine; i++) {
       const int slot = (int)(i & 1);
       const bool ready = mbar_wait(tfull0 + 8 * slot, (uint32_t)((i >> 1) & 1));
@@ -442,7 +446,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
       const uint32_t dh = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(slot * 2 * N);
 #pragma unroll 1
-      for (int cc = 0; cc < N; cc += 32) {
+      for (int cc = col0; cc < col0 + cols; cc += 32) {
         float hi[32], lo[32];
         tmem_ld32(dh + (uint32_t)cc, hi);
         tmem_ld32(dh + (uint32_t)(N + cc), lo);
@@ -454,11 +458,11 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
       }
       asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
       mbar_arrive(tempty0 + 8 * slot);
-      asm volatile("bar.sync 1, 128;\n" ::: "memory");
+      asm volatile("bar.sync 1, 256;\n" ::: "memory");
       const long long tile = blockIdx.x + i * gridDim.x;
       const long long a0 = (tile % ntA) * N, c0 = (tile / ntA) * 32;
       const uint32_t* st = reinterpret_cast<const uint32_t*>(stage);
-      for (int e = etid; e < 32 * N; e += 128) {
+      for (int e = etid; e < 32 * N; e += kEpilogue) {
         int jj, n;
         if (XPASS) {
           jj = e / N;
