@@ -275,12 +275,12 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(2 * N) : "memory");
 }
 
-// The pipelined pass: warp-specialised and double-buffered, so that loading
+// The pipelined pass: warp-specialised, with S (2..4) input slots, so that loading
 // and converting tile i + 1, the MMAs of tile i and the epilogue of tile i - 1
 // run at the same time.
-//   warps 0-7   producers: global loads -> f16 A tile in A[i % 2], then
-//               arrive on full[i % 2]; before refilling a slot they wait
-//               empty[slot]
+//   warps 0-7   producers (two groups taking alternate tiles): global loads
+//               -> f16 A tile in A[i % S], then arrive on full[i % S];
+//               before refilling a slot they wait empty[slot]
 //   warp 16     one thread issues the MMAs of a tile into accumulator pair
 //               i % 2 (TMEM) and commits to empty[slot] and tfull[pair]
 //   warps 8-15  epilogue: wait tfull[pair], read TMEM lanes 32 * (w % 4)
@@ -315,19 +315,19 @@ __device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
 template <bool XPASS, int N>
 __global__ void __launch_bounds__(kPipeThreads, 1)
     k_blur_tcp(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, long long W, long long H, int r,
-               int K, const uint16_t* __restrict__ kern, uint32_t oob, int* err) {
+               int K, int S, const uint16_t* __restrict__ kern, uint32_t oob, int* err) {
   extern __shared__ __align__(1024) unsigned char sm[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t bBytes = (uint32_t)N * K * 2, aBytes = 128u * K * 2;
   const int rs = 4 * N + 16;  // output staging row stride (bytes)
   unsigned char* bhi = sm;
   unsigned char* blo = sm + bBytes;
-  unsigned char* abuf0 = sm + 2 * bBytes;
-  unsigned char* stage = abuf0 + 2 * aBytes;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(stage + 32 * rs);  // full[2] empty[2] tfull[2] tempty[2]
-  uint32_t* taddr_s = reinterpret_cast<uint32_t*>(bars + 8);
-  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + 2), tfull0 = smem_u32(bars + 4),
-                 tempty0 = smem_u32(bars + 6);
+  unsigned char* abuf0 = sm + 2 * bBytes;  // S input slots
+  unsigned char* stage = abuf0 + (size_t)S * aBytes;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(stage + 32 * rs);  // full[4] empty[4] tfull[2] tempty[2]
+  uint32_t* taddr_s = reinterpret_cast<uint32_t*>(bars + 12);
+  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + 4), tfull0 = smem_u32(bars + 8),
+                 tempty0 = smem_u32(bars + 10);
 
   for (int i = tid; i < N * K; i += kPipeThreads) {
     const int n = i / K, k = i - n * K, t = k - n;
@@ -336,9 +336,11 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
     *reinterpret_cast<uint16_t*>(blo + canon_off(n, k, K)) = f16_bits(w & 255u);
   }
   if (tid == 0) {
-    for (int b = 0; b < 2; b++) {
-      mbar_init(full0 + 8 * b, kProducers);
+    for (int b = 0; b < 4; b++) {
+      mbar_init(full0 + 8 * b, kProducers / 2);
       mbar_init(empty0 + 8 * b, 1);
+    }
+    for (int b = 0; b < 2; b++) {
       mbar_init(tfull0 + 8 * b, 1);
       mbar_init(tempty0 + 8 * b, kEpilogue);
     }
@@ -361,18 +363,20 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
   const long long nmine = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
 
   if (tid < kProducers) {
-    // producers
+    // producers, in two groups of 128 threads taking alternate tiles, so two
+    // tiles' loads are in flight at once
     const int KG = K >> 3;
-    for (long long i = 0; i < nmine; i++) {
-      const int slot = (int)(i & 1);
-      if (i >= 2 && !mbar_wait(empty0 + 8 * slot, (uint32_t)(((i >> 1) - 1) & 1))) {
+    const int grp = tid >> 7, gtid = tid & 127;
+    for (long long i = grp; i < nmine; i += 2) {
+      const int slot = (int)(i % S);
+      if (i >= S && !mbar_wait(empty0 + 8 * slot, (uint32_t)((i / S - 1) & 1))) {
         if (lane == 0) atomicExch(err, 1);
         break;
       }
       const long long tile = blockIdx.x + i * gridDim.x;
       const long long a0 = (tile % ntA) * N, c0 = (tile / ntA) * 32;
       unsigned char* abuf = abuf0 + slot * aBytes;
-      for (int it = tid; it < 32 * KG; it += kProducers) {
+      for (int it = gtid; it < 32 * KG; it += 128) {
         int j, kg;
         if (XPASS) {
           j = it / KG;
@@ -410,22 +414,22 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
       const uint32_t sbo = (uint32_t)(K >> 3) * 128u;
       const uint32_t bh = smem_u32(bhi), bl = smem_u32(blo);
       for (long long i = 0; i < nmine; i++) {
-        const int slot = (int)(i & 1);
-        if (!mbar_wait(full0 + 8 * slot, (uint32_t)((i >> 1) & 1)) ||
-            (i >= 2 && !mbar_wait(tempty0 + 8 * slot, (uint32_t)(((i >> 1) - 1) & 1)))) {
+        const int slot = (int)(i % S), pair = (int)(i & 1);
+        if (!mbar_wait(full0 + 8 * slot, (uint32_t)((i / S) & 1)) ||
+            (i >= 2 && !mbar_wait(tempty0 + 8 * pair, (uint32_t)(((i >> 1) - 1) & 1)))) {
           atomicExch(err, 1);
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
         const uint32_t a = smem_u32(abuf0 + slot * aBytes);
-        const uint32_t dh = tmem + (uint32_t)(slot * 2 * N), dl = dh + (uint32_t)N;
+        const uint32_t dh = tmem + (uint32_t)(pair * 2 * N), dl = dh + (uint32_t)N;
         for (int s2 = 0; s2 < K / 16; s2++) {
           const uint32_t off = (uint32_t)s2 * 256u;
           mma_f16(dh, mat_desc(a + off, 128, sbo), mat_desc(bh + off, 128, sbo), idesc, s2 > 0);
           mma_f16(dl, mat_desc(a + off, 128, sbo), mat_desc(bl + off, 128, sbo), idesc, s2 > 0);
         }
         mma_commit(empty0 + 8 * slot);
-        mma_commit(tfull0 + 8 * slot);
+        mma_commit(tfull0 + 8 * pair);
       }
     }
     __syncwarp();
@@ -494,9 +498,15 @@ int tcp_blur_k(int r) {
   const int n = tcp_blur_n(r);
   return n ? (n + 2 * r + 15) / 16 * 16 : 0;
 }
-size_t tcp_blur_smem(int r) {
+size_t tcp_blur_smem(int r, int slots) {
   const int n = tcp_blur_n(r), k = tcp_blur_k(r);
-  return n ? (size_t)2 * n * k * 2 + (size_t)2 * 128 * k * 2 + (size_t)32 * (4 * n + 16) + 8 * 8 + 16 : 0;
+  return n ? (size_t)2 * n * k * 2 + (size_t)slots * 128 * k * 2 + (size_t)32 * (4 * n + 16) + 12 * 8 + 16 : 0;
+}
+// Input slots of the pipeline: as many as fit, up to 4.
+int tcp_blur_slots(int r, size_t maxSmem) {
+  int sl = 4;
+  while (sl > 2 && tcp_blur_smem(r, sl) > maxSmem) sl--;
+  return sl;
 }
 const void* tcp_blur_kernel(bool x, int n) {
   if (n == 64) return x ? (const void*)k_blur_tcp<true, 64> : (const void*)k_blur_tcp<false, 64>;
@@ -525,18 +535,19 @@ const void* tc_blur_kernel(bool x, int n) {
 bool launch_blur_tcp(uint32_t* img, uint32_t* tmp, long long W, long long H, int r, const uint16_t* kern,
                      uint32_t oob, int nsm, size_t maxSmem, int* err, cudaStream_t st) {
   const int n = tcp_blur_n(r), k = tcp_blur_k(r);
-  const size_t smem = tcp_blur_smem(r);
+  const int slots = tcp_blur_slots(r, maxSmem);
+  const size_t smem = tcp_blur_smem(r, slots);
   if (!n || smem > maxSmem) return false;
   const long long tilesX = ((W + n - 1) / n) * ((H + 31) / 32);
   const long long tilesY = ((H + n - 1) / n) * ((W + 31) / 32);
   const unsigned gx = (unsigned)std::max<long long>(1, std::min<long long>(tilesX, nsm));
   const unsigned gy = (unsigned)std::max<long long>(1, std::min<long long>(tilesY, nsm));
   if (n == 64) {
-    k_blur_tcp<true, 64><<<gx, kPipeThreads, smem, st>>>(img, tmp, W, H, r, k, kern, oob, err);
-    k_blur_tcp<false, 64><<<gy, kPipeThreads, smem, st>>>(tmp, img, W, H, r, k, kern, oob, err);
+    k_blur_tcp<true, 64><<<gx, kPipeThreads, smem, st>>>(img, tmp, W, H, r, k, slots, kern, oob, err);
+    k_blur_tcp<false, 64><<<gy, kPipeThreads, smem, st>>>(tmp, img, W, H, r, k, slots, kern, oob, err);
   } else {
-    k_blur_tcp<true, 32><<<gx, kPipeThreads, smem, st>>>(img, tmp, W, H, r, k, kern, oob, err);
-    k_blur_tcp<false, 32><<<gy, kPipeThreads, smem, st>>>(tmp, img, W, H, r, k, kern, oob, err);
+    k_blur_tcp<true, 32><<<gx, kPipeThreads, smem, st>>>(img, tmp, W, H, r, k, slots, kern, oob, err);
+    k_blur_tcp<false, 32><<<gy, kPipeThreads, smem, st>>>(tmp, img, W, H, r, k, slots, kern, oob, err);
   }
   note_launch();
   note_launch();
