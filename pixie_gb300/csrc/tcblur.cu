@@ -282,9 +282,9 @@ __global__ void __launch_bounds__(kTcThreads, 2)
 //               -> f16 A tile in A[i % S], then arrive on full[i % S];
 //               before refilling a slot they wait empty[slot]
 //   warp 16     one thread issues the MMAs of a tile into accumulator pair
-//               i % 2 (TMEM) and commits to empty[slot] and tfull[pair]
-//   warps 8-15  epilogue: wait tfull[pair], read TMEM lanes 32 * (w % 4)
-//               (warps w and w + 4 split the columns), arrive on
+//               i % 4 (TMEM) and commits to empty[slot] and tfull[pair]
+//   warps 8-15  epilogue, two groups of four warps on alternate tiles: wait
+//               tfull[pair], read TMEM lanes 32 * (w % 4), arrive on
 //               tempty[pair], quantise, stage and store the tile
 // Every mbarrier wait is bounded; a role whose wait runs out sets *err and
 // stops, the others' waits then run out too, and the CTA frees its TMEM.
@@ -294,19 +294,22 @@ constexpr int kProducers = 256, kEpilogue = 256;
 __device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(mbar), "r"(count) : "memory");
 }
-// bar.red.or over the 256 epilogue threads (named barrier 1): every thread
-// gets the same answer, so they leave a loop together.
-__device__ __forceinline__ bool epi_bar_or(bool v) {
+// bar.red.or over the 128 threads of epilogue group g (named barrier 1 + g):
+// every thread gets the same answer, so the group leaves a loop together.
+__device__ __forceinline__ bool epi_bar_or(int g, bool v) {
   uint32_t r;
   asm volatile(
       "{\n\t.reg .pred p, q;\n\t"
       "setp.ne.u32 p, %1, 0;\n\t"
-      "bar.red.or.pred q, 1, 256, p;\n\t"
+      "bar.red.or.pred q, %2, 128, p;\n\t"
       "selp.u32 %0, 1, 0, q;\n\t}\n"
       : "=r"(r)
-      : "r"((uint32_t)v)
+      : "r"((uint32_t)v), "r"(1 + g)
       : "memory");
   return r != 0;
+}
+__device__ __forceinline__ void epi_bar(int g) {
+  asm volatile("bar.sync %0, 128;\n" ::"r"(1 + g) : "memory");
 }
 __device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(mbar) : "memory");
@@ -324,10 +327,10 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
   unsigned char* blo = sm + bBytes;
   unsigned char* abuf0 = sm + 2 * bBytes;  // S input slots
   unsigned char* stage = abuf0 + (size_t)S * aBytes;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(stage + 32 * rs);  // full[4] empty[4] tfull[2] tempty[2]
-  uint32_t* taddr_s = reinterpret_cast<uint32_t*>(bars + 12);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(stage + 2 * 32 * rs);  // full[4] empty[4] tfull[4] tempty[4]
+  uint32_t* taddr_s = reinterpret_cast<uint32_t*>(bars + 16);
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + 4), tfull0 = smem_u32(bars + 8),
-                 tempty0 = smem_u32(bars + 10);
+                 tempty0 = smem_u32(bars + 12);
 
   for (int i = tid; i < N * K; i += kPipeThreads) {
     const int n = i / K, k = i - n * K, t = k - n;
@@ -339,16 +342,14 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
     for (int b = 0; b < 4; b++) {
       mbar_init(full0 + 8 * b, kProducers / 2);
       mbar_init(empty0 + 8 * b, 1);
-    }
-    for (int b = 0; b < 2; b++) {
       mbar_init(tfull0 + 8 * b, 1);
-      mbar_init(tempty0 + 8 * b, kEpilogue);
+      mbar_init(tempty0 + 8 * b, kEpilogue / 2);
     }
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
-  if (warp == 0) {  // two accumulator pairs: (D_hi, D_lo) x 2
+  if (warp == 0) {  // four accumulator pairs: (D_hi, D_lo) x 4
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(taddr_s)),
-                 "r"(4 * N)
+                 "r"(8 * N)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
   }
@@ -414,9 +415,9 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
       const uint32_t sbo = (uint32_t)(K >> 3) * 128u;
       const uint32_t bh = smem_u32(bhi), bl = smem_u32(blo);
       for (long long i = 0; i < nmine; i++) {
-        const int slot = (int)(i % S), pair = (int)(i & 1);
+        const int slot = (int)(i % S), pair = (int)(i & 3);
         if (!mbar_wait(full0 + 8 * slot, (uint32_t)((i / S) & 1)) ||
-            (i >= 2 && !mbar_wait(tempty0 + 8 * pair, (uint32_t)(((i >> 1) - 1) & 1)))) {
+            (i >= 4 && !mbar_wait(tempty0 + 8 * pair, (uint32_t)(((i >> 2) - 1) & 1)))) {
           atomicExch(err, 1);
           break;
         }
@@ -434,39 +435,38 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
     }
     __syncwarp();
   } else {
-    // epilogue: warps 8-15, TMEM lanes 32 * (warp % 4); warps w and w + 4
-    // take the two halves of the columns (when a half holds 32 columns)
-    const int q = warp & 3, half = (warp - 8) >> 2;
+    // epilogue: two groups of four warps (8-11, 12-15) take alternate tiles;
+    // in a group, warp w reads TMEM lanes 32 * (w % 4), every column
+    const int q = warp & 3, grp = (warp - 8) >> 2;
     const int m = 32 * q + lane, j = m >> 2, c = m & 3;
-    const int etid = tid - kProducers;  // 0..255
-    const int cols = N / 2 >= 32 ? N / 2 : (half ? 0 : N);
-    const int col0 = N / 2 >= 32 ? half * (N / 2) : 0;
-    for (long long i = 0; i < nmine; i++) {
-      const int slot = (int)(i & 1);
-      const bool ready = mbar_wait(tfull0 + 8 * slot, (uint32_t)((i >> 1) & 1));
+    const int etid = (tid - kProducers) & 127;
+    unsigned char* st8 = stage + grp * 32 * rs;
+    for (long long i = grp; i < nmine; i += 2) {
+      const int pair = (int)(i & 3);
+      const bool ready = mbar_wait(tfull0 + 8 * pair, (uint32_t)((i >> 2) & 1));
       if (!ready && lane == 0) atomicExch(err, 1);
-      // also: the staging buffer is free (the previous tile's stores are done)
-      if (epi_bar_or(!ready)) break;
+      // also: the group's staging buffer is free (its previous stores are done)
+      if (epi_bar_or(grp, !ready)) break;
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      const uint32_t dh = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(slot * 2 * N);
+      const uint32_t dh = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(pair * 2 * N);
 #pragma unroll 1
-      for (int cc = col0; cc < col0 + cols; cc += 32) {
+      for (int cc = 0; cc < N; cc += 32) {
         float hi[32], lo[32];
         tmem_ld32(dh + (uint32_t)cc, hi);
         tmem_ld32(dh + (uint32_t)(N + cc), lo);
 #pragma unroll
         for (int t = 0; t < 32; t++) {
           const uint32_t v = (uint32_t)hi[t] * 256u + (uint32_t)lo[t];
-          stage[j * rs + (cc + t) * 4 + c] = (unsigned char)(v / 65280u);
+          st8[j * rs + (cc + t) * 4 + c] = (unsigned char)(v / 65280u);
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-      mbar_arrive(tempty0 + 8 * slot);
-      asm volatile("bar.sync 1, 256;\n" ::: "memory");
+      mbar_arrive(tempty0 + 8 * pair);
+      epi_bar(grp);
       const long long tile = blockIdx.x + i * gridDim.x;
       const long long a0 = (tile % ntA) * N, c0 = (tile / ntA) * 32;
-      const uint32_t* st = reinterpret_cast<const uint32_t*>(stage);
-      for (int e = etid; e < 32 * N; e += kEpilogue) {
+      const uint32_t* st = reinterpret_cast<const uint32_t*>(st8);
+      for (int e = etid; e < 32 * N; e += 128) {
         int jj, n;
         if (XPASS) {
           jj = e / N;
@@ -488,7 +488,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(4 * N) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(8 * N) : "memory");
 }
 
 // The pipelined pass's tile width: 64 outputs for r <= 64, 32 up to 128
@@ -500,7 +500,8 @@ int tcp_blur_k(int r) {
 }
 size_t tcp_blur_smem(int r, int slots) {
   const int n = tcp_blur_n(r), k = tcp_blur_k(r);
-  return n ? (size_t)2 * n * k * 2 + (size_t)slots * 128 * k * 2 + (size_t)32 * (4 * n + 16) + 12 * 8 + 16 : 0;
+  return n ? (size_t)2 * n * k * 2 + (size_t)slots * 128 * k * 2 + (size_t)2 * 32 * (4 * n + 16) + 16 * 8 + 16
+           : 0;
 }
 // Input slots of the pipeline: as many as fit, up to 4.
 int tcp_blur_slots(int r, size_t maxSmem) {
