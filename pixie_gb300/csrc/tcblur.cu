@@ -368,6 +368,9 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
     // tiles' loads are in flight at once
     const int KG = K >> 3;
     const int grp = tid >> 7, gtid = tid & 127;
+    // 16-byte loads along x when every run of 8 starts on a 16-byte boundary
+    const bool vec = XPASS && (W & 3) == 0 && (r & 3) == 0 &&
+                     ((reinterpret_cast<uintptr_t>(in) & 15) == 0);
     for (long long i = grp; i < nmine; i += 2) {
       const int slot = (int)(i % S);
       if (i >= S && !mbar_wait(empty0 + 8 * slot, (uint32_t)((i / S - 1) & 1))) {
@@ -377,32 +380,54 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
       const long long tile = blockIdx.x + i * gridDim.x;
       const long long a0 = (tile % ntA) * N, c0 = (tile / ntA) * 32;
       unsigned char* abuf = abuf0 + slot * aBytes;
-      for (int it = gtid; it < 32 * KG; it += 128) {
-        int j, kg;
-        if (XPASS) {
-          j = it / KG;
-          kg = it - j * KG;
-        } else {
-          kg = it >> 5;
-          j = it & 31;
-        }
-        const long long gc = c0 + j;
-        uint32_t px[8];
+      // two items per round: 16 pixels' loads in flight before any is converted
+      for (int it0 = gtid; it0 < 32 * KG; it0 += 256) {
+        uint32_t px[2][8];
+        int jj[2], kk[2];
 #pragma unroll
-        for (int t = 0; t < 8; t++) {
-          const long long ga = a0 - r + 8 * kg + t;
-          px[t] = 0u;
-          if (gc < clen) {
-            if (ga >= 0 && ga < alen) px[t] = XPASS ? in[gc * W + ga] : in[ga * W + gc];
-            else px[t] = oob;
+        for (int u = 0; u < 2; u++) {
+          const int it = it0 + 128 * u;
+          int j = 0, kg = 0;
+          if (XPASS) {
+            j = it / KG;
+            kg = it - j * KG;
+          } else {
+            kg = it >> 5;
+            j = it & 31;
+          }
+          jj[u] = j;
+          kk[u] = kg;
+          const long long gc = c0 + j, g0 = a0 - r + 8 * kg;
+          const bool live = it < 32 * KG && gc < clen;
+          if (XPASS && live && vec && g0 >= 0 && g0 + 8 <= alen) {
+            // the run's 8 pixels as two aligned 16-byte loads
+            const uint4 v0 = *reinterpret_cast<const uint4*>(in + gc * W + g0);
+            const uint4 v1 = *reinterpret_cast<const uint4*>(in + gc * W + g0 + 4);
+            px[u][0] = v0.x; px[u][1] = v0.y; px[u][2] = v0.z; px[u][3] = v0.w;
+            px[u][4] = v1.x; px[u][5] = v1.y; px[u][6] = v1.z; px[u][7] = v1.w;
+          } else {
+#pragma unroll
+            for (int t = 0; t < 8; t++) {
+              const long long ga = g0 + t;
+              px[u][t] = 0u;
+              if (live) {
+                if (ga >= 0 && ga < alen) px[u][t] = XPASS ? in[gc * W + ga] : in[ga * W + gc];
+                else px[u][t] = oob;
+              }
+            }
           }
         }
 #pragma unroll
-        for (int c = 0; c < 4; c++) {
-          uint32_t h[4];
+        for (int u = 0; u < 2; u++) {
+          if (it0 + 128 * u >= 32 * KG) break;
 #pragma unroll
-          for (int t = 0; t < 4; t++) h[t] = f16_pair(px[2 * t], px[2 * t + 1], c);
-          *reinterpret_cast<uint4*>(abuf + canon_off(4 * j + c, 8 * kg, K)) = make_uint4(h[0], h[1], h[2], h[3]);
+          for (int c = 0; c < 4; c++) {
+            uint32_t h[4];
+#pragma unroll
+            for (int t = 0; t < 4; t++) h[t] = f16_pair(px[u][2 * t], px[u][2 * t + 1], c);
+            *reinterpret_cast<uint4*>(abuf + canon_off(4 * jj[u] + c, 8 * kk[u], K)) =
+                make_uint4(h[0], h[1], h[2], h[3]);
+          }
         }
       }
       asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
