@@ -91,11 +91,11 @@ int pxg_image_draw(pxg_image* a, const pxg_image* b, int64_t translate_x, int64_
  * (bindings/bindings.nim:133) */
 int pxg_image_blur(pxg_image* image, float radius, const float out_of_bounds[4]);
 
-/* Blur kernels: 1 (default) runs radii 1..128 on the tensor cores (tcgen05;
+/* Blur kernels: 1 (default) runs radii 8..128 on the tensor cores (tcgen05;
  * exact integer sums through byte-split weights) with the warp-specialised,
- * double-buffered kernel; 2 uses the single-stage tensor-core kernel (radii
- * 8..128); 0 the CUDA-core kernels.  All write the same bytes.  No
- * counterpart in the reference. */
+ * multi-buffered kernel; 2 uses the single-stage tensor-core kernel (radii
+ * 8..128); 0 the CUDA-core kernels (which every mode uses for the other
+ * radii).  All write the same bytes.  No counterpart in the reference. */
 int pxg_blur_config(int use_tensor_cores);
 
 /* spread(Image, float32)  src/pixie/images.nim:700-758 (private in the

@@ -450,7 +450,7 @@ def scene_config(slice_width: int = 256, coverage_bytes: int = -1):
 
 
 def blur_config(mode):
-    """1/True (default): pipelined tensor-core blur (radii 1..128); 2: the
+    """1/True (default): pipelined tensor-core blur (radii 8..128); 2: the
     single-stage tensor-core kernel (radii 8..128); 0/False: CUDA cores."""
     _check(lib().pxg_blur_config(int(mode)))
 

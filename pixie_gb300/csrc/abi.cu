@@ -133,7 +133,6 @@ void launch_shadow(const uint32_t* src, uint32_t* out, uint8_t* a0, uint8_t* a1,
                    uint32_t color, int nsm, cudaStream_t st);
 size_t blur_x_smem(int r);
 void* blurb_kernel(bool x);
-void* blur2d_kernel();
 unsigned long long launch_count();
 void note_launch();
 size_t blur_y_smem(int r);
@@ -295,7 +294,6 @@ void init_locked(int device) {
   g.blurSmemMax = std::min(g.blurSmemMax, allow_max_smem((const void*)k_blurf_y));
   g.blurSmemMax = std::min(g.blurSmemMax, allow_max_smem(blurb_kernel(true)));
   g.blurSmemMax = std::min(g.blurSmemMax, allow_max_smem(blurb_kernel(false)));
-  g.blurSmemMax = std::min(g.blurSmemMax, allow_max_smem(blur2d_kernel()));
   CU(cudaEventCreate(&g.ev0));
   CU(cudaEventCreate(&g.ev1));
   CU(cudaEventCreate(&g.evr0));

@@ -418,83 +418,10 @@ size_t blur_y_smem(int r) { return (size_t)(kTY + 2 * r) * kTX * 4 + (size_t)(2 
 
 // in -> tmp (X pass) -> in (Y pass); float32 tiles when they fit, then the
 // integer tiles, then the direct kernels.
-// Small radii (r < 8): both passes in one kernel over 64 x 32 output tiles.
-// The tile and its halo are read once into shared memory as float4 (out-of-
-// image taps take the out-of-bounds colour), the X pass fills the quantised
-// intermediate rows of the halo (rows outside the image are the out-of-bounds
-// colour, as the reference's Y pass sees them), the Y pass writes the tile:
-// the intermediate never goes to memory.  Sums are exact in float32 (< 2^24).
-constexpr int kB2X = 64, kB2Y = 32, kB2Threads = 256;
-size_t blur2d_smem(int r) {
-  return (size_t)(kB2Y + 2 * r) * (kB2X + 2 * r) * 16 + (size_t)(kB2Y + 2 * r) * kB2X * 16 + (2 * r + 1) * 4 + 16;
-}
-__global__ void __launch_bounds__(kB2Threads) k_blur2d(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
-                                                      long long W, long long H, int r,
-                                                      const uint16_t* __restrict__ kern, uint32_t oob) {
-  extern __shared__ __align__(16) unsigned char sm[];
-  const int AW = kB2X + 2 * r, AH = kB2Y + 2 * r;
-  float4* A = reinterpret_cast<float4*>(sm);  // AH x AW input
-  float4* B = A + AH * AW;                    // AH x kB2X intermediate
-  float* kw = reinterpret_cast<float*>(B + AH * kB2X);
-  const long long x0 = (long long)blockIdx.x * kB2X, y0 = (long long)blockIdx.y * kB2Y;
-  const float4 o = px4(oob);
-  for (int i = threadIdx.x; i <= 2 * r; i += kB2Threads) kw[i] = (float)kern[i];
-  for (int i = threadIdx.x; i < AH * AW; i += kB2Threads) {
-    const int ly = i / AW, lx = i - ly * AW;
-    const long long gy = y0 - r + ly, gx = x0 - r + lx;
-    A[i] = (gy >= 0 && gy < H && gx >= 0 && gx < W) ? px4(in[gy * W + gx]) : o;
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < AH * kB2X; i += kB2Threads) {
-    const int ly = i / kB2X, x = i - ly * kB2X;
-    const long long gy = y0 - r + ly;
-    float4 v = o;
-    if (gy >= 0 && gy < H) {
-      float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
-      const float4* rowp = A + ly * AW + x;
-      for (int t = 0; t <= 2 * r; t++) {
-        const float w = kw[t];
-        const float4 p = rowp[t];
-        a.x = fmaf(p.x, w, a.x);
-        a.y = fmaf(p.y, w, a.y);
-        a.z = fmaf(p.z, w, a.z);
-        a.w = fmaf(p.w, w, a.w);
-      }
-      v = px4(quantf(a));
-    }
-    B[i] = v;
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < kB2Y * kB2X; i += kB2Threads) {
-    const int y = i / kB2X, x = i - y * kB2X;
-    const long long gy = y0 + y, gx = x0 + x;
-    if (gy >= H || gx >= W) continue;
-    float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4* colp = B + y * kB2X + x;
-    for (int t = 0; t <= 2 * r; t++) {
-      const float w = kw[t];
-      const float4 p = colp[t * kB2X];
-      a.x = fmaf(p.x, w, a.x);
-      a.y = fmaf(p.y, w, a.y);
-      a.z = fmaf(p.z, w, a.z);
-      a.w = fmaf(p.w, w, a.w);
-    }
-    out[gy * W + gx] = quantf(a);
-  }
-}
 
-void* blur2d_kernel() { return (void*)k_blur2d; }
 
 void launch_blur(uint32_t* img, uint32_t* tmp, long long W, long long H, int r,
                  const uint16_t* kern, uint32_t oob, int nsm, size_t maxSmem, cudaStream_t st) {
-  // radius < 8: both passes fused in one kernel, reading a copy of the image
-  // (tiles read their neighbours' pixels, so the output cannot overwrite them)
-  if (r < 8 && blur2d_smem(r) <= maxSmem && (H + kB2Y - 1) / kB2Y <= 65535) {
-    cudaMemcpyAsync(tmp, img, (size_t)(W * H * 4), cudaMemcpyDeviceToDevice, st);
-    dim3 g((unsigned)((W + kB2X - 1) / kB2X), (unsigned)((H + kB2Y - 1) / kB2Y));
-    k_blur2d<<<g, kB2Threads, blur2d_smem(r), st>>>(tmp, img, W, H, r, kern, oob); note_launch();
-    return;
-  }
   // radius >= 8: register-blocked tiles; smaller radii stay on the one-output
   // float32 tiles, where the blocked kernel's 8-tap granularity and halo cost
   // more than they save.

@@ -36,7 +36,6 @@ void record_error(const char* msg);
 void launch_blur(uint32_t* img, uint32_t* tmp, long long W, long long H, int r,
                  const uint16_t* kern, uint32_t oob, int nsm, size_t maxSmem, cudaStream_t st);
 void* blurb_kernel(bool x);
-void* blur2d_kernel();
 __global__ void k_blur_x(const uint32_t*, uint32_t*, long long, long long, int, const uint16_t*, uint32_t);
 __global__ void k_blur_y(const uint32_t*, uint32_t*, long long, long long, int, const uint16_t*, uint32_t);
 __global__ void k_blurf_x(const uint32_t*, uint32_t*, long long, long long, int, const uint16_t*, uint32_t);
@@ -82,7 +81,7 @@ int setup_device(int dev, DeviceSetup& out) {
     return fail("pxg_image_blur_noalloc: cannot query the device");
   const void* kernels[] = {pxg::blurb_kernel(true), pxg::blurb_kernel(false), (const void*)pxg::k_blurf_x,
                            (const void*)pxg::k_blurf_y, (const void*)pxg::k_blur_x,
-                           (const void*)pxg::k_blur_y, pxg::blur2d_kernel()};
+                           (const void*)pxg::k_blur_y};
   size_t maxSmem = (size_t)optin;
   for (const void* k : kernels) {
     cudaFuncAttributes fa;

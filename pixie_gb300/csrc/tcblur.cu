@@ -517,8 +517,10 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
 }
 
 // The pipelined pass's tile width: 64 outputs for r <= 64, 32 up to 128
-// (two A tiles, B and the output stage fit 227 KB of shared memory).
-int tcp_blur_n(int r) { return r < 1 || r > 128 ? 0 : (r <= 64 ? 64 : 32); }
+// (the input slots, B and the output stages fit 227 KB of shared memory).
+// Below r = 8 the CUDA-core kernels are as fast or faster (the pass is not
+// compute-bound there), and they take those radii.
+int tcp_blur_n(int r) { return r < 8 || r > 128 ? 0 : (r <= 64 ? 64 : 32); }
 int tcp_blur_k(int r) {
   const int n = tcp_blur_n(r);
   return n ? (n + 2 * r + 15) / 16 * 16 : 0;
