@@ -177,7 +177,41 @@ __device__ __forceinline__ float softLight1(float cb, float cs) {
   float d = cb <= 0.25f ? ((16.0f * cb - 12.0f) * cb + 4.0f) * cb : sqrtf(cb);
   return cb + (2.0f * cs - 1.0f) * (d - cb);
 }
+// One float mode, inlined where the mode is a compile-time constant (draw).
+template <int MODE>
+__device__ __forceinline__ uint32_t blendFloatT(const uint8_t* tbl, uint32_t bp, uint32_t sp);
+
 static __device__ __noinline__ uint32_t blendFloat(const uint8_t* tbl, uint32_t bp, uint32_t sp, int mode) {
+  Px b8 = straight8(tbl, bp), s8 = straight8(tbl, sp);
+  const float* u = reinterpret_cast<const float*>(tbl + kTblUnitOff);  // u[v] = v / 255.0f
+  F3 cb{u[b8.r], u[b8.g], u[b8.b]};
+  F3 cs{u[s8.r], u[s8.g], u[s8.b]};
+  float ab = u[b8.a], as = u[s8.a];
+  F3 m;
+  switch (mode) {
+    case kSoftLight:
+      m = F3{softLight1(cb.r, cs.r), softLight1(cb.g, cs.g), softLight1(cb.b, cs.b)};
+      break;
+    case kHue: m = setLum(setSat(cs, sat3(cb)), lum3(cb)); break;
+    case kSaturation: m = setLum(setSat(cb, sat3(cs)), lum3(cb)); break;
+    case kColor: m = setLum(cs, lum3(cb)); break;
+    default: m = setLum(cb, lum3(cs)); break;
+  }
+  float ao = as + ab * (1.0f - as);
+  if (!(ao > 0.0f)) return 0u;
+  float k = (1.0f - as) * ab;
+  float csr = (1.0f - ab) * cs.r + ab * m.r;
+  float csg = (1.0f - ab) * cs.g + ab * m.g;
+  float csb = (1.0f - ab) * cs.b + ab * m.b;
+  float orr = (as * csr + k * cb.r) / ao;
+  float og = (as * csg + k * cb.g) / ao;
+  float ob = (as * csb + k * cb.b) / ao;
+  return premul8(pack(unit_to_u8(orr), unit_to_u8(og), unit_to_u8(ob), unit_to_u8(ao)));
+}
+
+template <int MODE>
+__device__ __forceinline__ uint32_t blendFloatT(const uint8_t* tbl, uint32_t bp, uint32_t sp) {
+  constexpr int mode = MODE;
   Px b8 = straight8(tbl, bp), s8 = straight8(tbl, sp);
   const float* u = reinterpret_cast<const float*>(tbl + kTblUnitOff);  // u[v] = v / 255.0f
   F3 cb{u[b8.r], u[b8.g], u[b8.b]};
