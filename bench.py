@@ -503,9 +503,11 @@ def run_scene(px, wl, seed=7, n_paths=2000, size=1024, reps=3):
                     "record_ms is the host command walk and stroke outlining of all paths"}
 
 
-# Per-launch DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) from
-# the ncu captures summarised in profiles/; None until captured.
-TRAFFIC = {}
+# DRAM traffic per operation (dram__bytes_read.sum + dram__bytes_write.sum,
+# summed over the operation's launches) from an ncu capture of the same
+# kernels: blur radius 64 of 4096x4096 = the two tensor-core passes
+# (python bench.py --case blur64).
+TRAFFIC = {"blur:64": 67153152 + 23181312 + 67162624 + 20830208}
 
 
 # -- CPU baseline / reference arm ----------------------------------------------------------

@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(kTX * kYThreadsY) k_blur_y(const uint32_t* __r
 // float4 (converted once per load) and each thread accumulates one output
 // with one 128-bit shared load and four FFMAs per tap.
 constexpr int kFX = 256;             // X pass: outputs per row per CTA
-constexpr int kFXRows = 8;           // X pass: rows per CTA
+constexpr int kFXRows = 2;           // X pass: rows per CTA
 constexpr int kFYT = 64;             // Y pass: output rows per CTA
 constexpr int kFYThreads = 8;        // Y pass: block is 32 x 8
 
@@ -111,13 +111,14 @@ __global__ void __launch_bounds__(kFX) k_blurf_x(const uint32_t* __restrict__ in
   float* kw = reinterpret_cast<float*>(px + kFXRows * span);  // 2r + 1
   const long long x0 = (long long)blockIdx.x * kFX, y0 = (long long)blockIdx.y * kFXRows;
   const float4 o = px4(oob);
-  // all rows' loads issued together (independent iterations, unrolled)
-  const int total = kFXRows * span;
-#pragma unroll 4
-  for (int i = threadIdx.x; i < total; i += kFX) {
-    const int rr = i / span, c = i - rr * span;
-    const long long y = y0 + rr, gx = x0 - r + c;
-    if (y < H) px[i] = (gx >= 0 && gx < W) ? px4(in[y * W + gx]) : o;
+  for (int rr = 0; rr < kFXRows; rr++) {
+    long long y = y0 + rr;
+    if (y >= H) break;
+    const uint32_t* row = in + y * W;
+    for (int i = threadIdx.x; i < span; i += kFX) {
+      long long gx = x0 - r + i;
+      px[rr * span + i] = (gx >= 0 && gx < W) ? px4(row[gx]) : o;
+    }
   }
   for (int i = threadIdx.x; i < 2 * r + 1; i += kFX) kw[i] = (float)kern[i];
   __syncthreads();
@@ -154,7 +155,6 @@ __global__ void __launch_bounds__(32 * kFYThreads) k_blurf_y(const uint32_t* __r
   const int tx = threadIdx.x, ty = threadIdx.y;
   const long long x = x0 + tx;
   const float4 o = px4(oob);
-#pragma unroll 4
   for (int i = ty; i < span; i += kFYThreads) {
     long long gy = y0 - r + i;
     float4 v = o;
