@@ -200,12 +200,14 @@ def run_gpu(args, ws, rank, local):
         t0 = torch.cuda.Event(enable_timing=True)
         t1 = torch.cuda.Event(enable_timing=True)
         t0.record(stream)
+        h0 = time.perf_counter()
         for s in range(args.steps):
             for i, op in enumerate(ops):
                 evs[s][i].record(stream)
                 run_op(op)
             evs[s][n_ops].record(stream)
         t1.record(stream)
+        host_ms = (time.perf_counter() - h0) * 1e3 / args.steps  # enqueue time per step on the host
         stream.synchronize()
         torch.cuda.synchronize()
         barrier(ws)
@@ -245,6 +247,7 @@ def run_gpu(args, ws, rank, local):
     e2e = run_e2e(px, A, B, BL, M, SH, a_host, b_host, blur_host, run_op, ops, args, ws)
 
     extra = {"per_op_ms": {f"{k}:{p}": round(float(t), 4) for (k, p), t in zip(ops, op_ms)},
+             "host_enqueue_ms_per_step": round(host_ms, 4),
              "draw_gbs_min_median_max": [round(min(draw_gbs), 1), round(statistics.median(draw_gbs), 1),
                                          round(max(draw_gbs), 1)],
              "blur_ms": blur_ms}
@@ -580,10 +583,11 @@ def run_case(case: str, slice_w: int = 0):
         img = px.Image(512, 512)
         for s in (1, 2, 3):
             img.fill_path(wl.plain_path(s), wl.PLAIN_COLOR)
-    elif case == "blur64":  # blur radius 64 of a 4096x4096 image
+    elif case.startswith("blur"):  # blur<r>: two blurs of radius r (default 64) of a 4096x4096 image
+        r = int(case[4:] or 64)
         img = px.Image.from_numpy(wl.premultiplied_image(9, 4096, 4096))
         for _ in range(2):
-            img.blur(64)
+            img.blur(r)
     elif case == "draw":  # NormalBlend draw of 4096x4096 onto 4096x4096 (inputs > L2)
         a = px.Image.from_numpy(wl.premultiplied_image(1, 4096, 4096))
         b = px.Image.from_numpy(wl.premultiplied_image(2, 4096, 4096))
@@ -639,7 +643,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--slice", type=int, default=0, help="scene row slice width for --case scene*")
     ap.add_argument("--case", default=None,
-                    help="run one small operation for profiling: fill512 | blur64 | draw | glyphs | scene | scene_small | masks")
+                    help="run one small operation for profiling: fill512 | blur<r> (blur64) | draw | glyphs | scene | scene_small | masks")
     args = ap.parse_args()
     if args.case:
         run_case(args.case, args.slice)

@@ -450,9 +450,17 @@ def scene_config(slice_width: int = 256, coverage_bytes: int = -1):
 
 
 def blur_config(mode):
-    """1/True (default): pipelined tensor-core blur (radii 8..128); 2: the
-    single-stage tensor-core kernel (radii 8..128); 0/False: CUDA cores."""
+    """3 (default): tensor-core blur with TMA-fed input rings (radii 1..128,
+    rows a multiple of 16 bytes); 1: the pipelined tensor-core kernel that
+    loads through registers (radii 8..128); 2: the single-stage tensor-core
+    kernel (radii 8..128); 0: CUDA cores.  Radii or images a mode does not
+    take run on the next family (3 -> 1 -> 0)."""
     _check(lib().pxg_blur_config(int(mode)))
+
+
+def last_blur_kernel() -> int:
+    """Kernel family the last blur ran on (3, 2, 1, 0; -1 before any)."""
+    return int(lib().pxg_last_blur_kernel())
 
 
 def autotune(enable: bool):

@@ -142,6 +142,10 @@ const void* tc_blur_kernel(bool x, int n);
 bool launch_blur_tcp(uint32_t* img, uint32_t* tmp, long long W, long long H, int r, const uint16_t* kern,
                      uint32_t oob, int nsm, size_t maxSmem, int* err, cudaStream_t st);
 const void* tcp_blur_kernel(bool x, int n);
+bool ring_blur_init(size_t* maxSmem);
+bool weights_exact_f16(const uint16_t* hostKern, int r);
+bool launch_blur_ring(uint32_t* img, uint32_t* tmp, long long W, long long H, int r, const uint16_t* kern,
+                      bool exactF16, uint32_t oob, int nsm, size_t maxSmem, int* err, cudaStream_t st);
 __global__ void k_blur_x(const uint32_t*, uint32_t*, long long, long long, int, const uint16_t*, uint32_t);
 __global__ void k_blur_y(const uint32_t*, uint32_t*, long long, long long, int, const uint16_t*, uint32_t);
 __global__ void k_blurf_x(const uint32_t*, uint32_t*, long long, long long, int, const uint16_t*, uint32_t);
@@ -231,8 +235,13 @@ struct Ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evr0 = nullptr, evr1 = nullptr;
   int* dev_err = nullptr;   // device-side error flag (a tensor-core wait that ran out)
   int* host_err = nullptr;  // its pinned mirror
-  int blur_tensor = 1;      // 1: pipelined tensor-core blur, 2: single-stage one, 0: CUDA cores
+  // blur kernels: 3 TMA-fed ring passes on the tensor cores (falling back to 1, then 0, where they do
+  // not apply), 1 pipelined tensor-core passes, 2 single-stage ones, 0 CUDA cores
+  int blur_tensor = 3;
   size_t tcSmemMax = 0;
+  bool ring_ok = false;  // the ring kernels and the driver's tensor-map encoder are available
+  int last_blur = -1;    // kernel family of the last blur
+  size_t ringSmemMax = 0;
   float last_ms = 0;
   long long stats[6] = {0, 0, 0, 0, 0, 0};  // last fill launch: paths, prims, segments, entries, blends, wide rows
   int rows_ctas_per_sm[2] = {1, 1};  // resident CTAs of each row-kernel variant
@@ -240,6 +249,7 @@ struct Ctx {
   int scene_slice = 256;              // pixels of a row one warp of the drawing pass owns (0: chosen per launch)
   bool blocking = true;  // image operations wait for their GPU work
   std::map<int64_t, uint16_t*> weights;  // gaussian weights per radius, on the device
+  std::map<int64_t, bool> weights_f16;   // every weight of the radius is an exact f16
 };
 Ctx g;
 
@@ -310,6 +320,7 @@ void init_locked(int device) {
   g.tcSmemMax = std::min(g.tcSmemMax, allow_max_smem(tcp_blur_kernel(false, 64)));
   g.tcSmemMax = std::min(g.tcSmemMax, allow_max_smem(tcp_blur_kernel(true, 32)));
   g.tcSmemMax = std::min(g.tcSmemMax, allow_max_smem(tcp_blur_kernel(false, 32)));
+  g.ring_ok = ring_blur_init(&g.ringSmemMax);
   g.ready = true;
 }
 void ensure_init() {
@@ -325,7 +336,31 @@ const uint16_t* weights_for(int64_t r) {
   CU(cudaMalloc((void**)&d, k.size() * 2));
   CU(cudaMemcpy(d, k.data(), k.size() * 2, cudaMemcpyHostToDevice));
   g.weights[r] = d;
+  g.weights_f16[r] = r <= (1 << 16) && weights_exact_f16(k.data(), (int)r);
   return d;
+}
+
+// Both blur passes of an RGBX image (img -> tmp -> img) with the configured
+// kernels; a kernel family that does not take this image or radius hands it
+// to the next one.
+void blur_dispatch(uint32_t* img, uint32_t* tmp, long long W, long long H, int64_t r, uint32_t oob) {
+  const uint16_t* kern = weights_for(r);
+  int used = -1;
+  if (g.blur_tensor == 3 && g.ring_ok &&
+      launch_blur_ring(img, tmp, W, H, (int)r, kern, g.weights_f16[r], oob, g.nsm, g.ringSmemMax, g.dev_err,
+                       g.stream))
+    used = 3;
+  if (used < 0 && g.blur_tensor == 2 &&
+      launch_blur_tc(img, tmp, W, H, (int)r, kern, oob, g.nsm, g.tcSmemMax, g.dev_err, g.stream))
+    used = 2;
+  if (used < 0 && (g.blur_tensor == 1 || g.blur_tensor == 3) &&
+      launch_blur_tcp(img, tmp, W, H, (int)r, kern, oob, g.nsm, g.tcSmemMax, g.dev_err, g.stream))
+    used = 1;
+  if (used < 0) {
+    launch_blur(img, tmp, W, H, (int)r, kern, oob, g.nsm, g.blurSmemMax, g.stream);
+    used = 0;
+  }
+  g.last_blur = used;
 }
 
 void* scratch(long long bytes) {
@@ -1041,9 +1076,7 @@ void srv_step(pxg_server* sv) {
     }
     if (j->next >= j->scene->jobs.size()) {
       if (j->blur > 0) {
-        const uint16_t* kern = weights_for(j->blur);
-        launch_blur((uint32_t*)j->canvas.data, (uint32_t*)j->tmp, j->W, j->H, (int)j->blur, kern, 0u, g.nsm,
-                    g.blurSmemMax, g.stream);
+        blur_dispatch((uint32_t*)j->canvas.data, (uint32_t*)j->tmp, j->W, j->H, j->blur, 0u);
         CU(cudaGetLastError());
       }
       done.push_back(j);
@@ -1779,9 +1812,14 @@ int pxg_scene_config(int slice_width, int64_t coverage_bytes) {
 
 int pxg_blur_config(int use_tensor_cores) {
   return guarded([&] {
-    if (use_tensor_cores < 0 || use_tensor_cores > 2) throw ApiError{"Invalid blur configuration"};
+    if (use_tensor_cores < 0 || use_tensor_cores > 3) throw ApiError{"Invalid blur configuration"};
     g.blur_tensor = use_tensor_cores;
   });
+}
+
+int pxg_last_blur_kernel(void) {
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  return g.last_blur;
 }
 
 int pxg_autotune(int enable) {
@@ -1844,17 +1882,10 @@ int pxg_image_blur(pxg_image* im, float radius, const float* oob) {
     if (r > (1 << 20)) throw ApiError{"Blur radius too large"};
     static const float zero[4] = {0, 0, 0, 0};
     uint32_t o = color_to_rgbx(oob ? oob : zero);
-    const uint16_t* kern = weights_for(r);
+    weights_for(r);
     uint32_t* tmp = (uint32_t*)scratch(im->width * im->height * 4);
     Timed t;
-    const bool tc = g.blur_tensor == 2 ? launch_blur_tc((uint32_t*)im->data, tmp, im->width, im->height, (int)r,
-                                                        kern, o, g.nsm, g.tcSmemMax, g.dev_err, g.stream)
-                    : g.blur_tensor == 1 && launch_blur_tcp((uint32_t*)im->data, tmp, im->width, im->height,
-                                                            (int)r, kern, o, g.nsm, g.tcSmemMax, g.dev_err,
-                                                            g.stream);
-    if (!tc)
-      launch_blur((uint32_t*)im->data, tmp, im->width, im->height, (int)r, kern, o, g.nsm,
-                  g.blurSmemMax, g.stream);
+    blur_dispatch((uint32_t*)im->data, tmp, im->width, im->height, r, o);
     CU(cudaGetLastError());
     t.done();
     if (g.blocking) check_device_error();

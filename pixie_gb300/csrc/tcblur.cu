@@ -32,6 +32,7 @@
 #include <cstdint>
 
 #include "pxg_device.cuh"
+#include "tc_ptx.cuh"
 
 namespace pxg {
 
@@ -39,93 +40,9 @@ void note_launch();
 
 namespace {
 
+using namespace tc;
+
 constexpr int kTcThreads = 256;          // two warpgroups: warps w and w + 4 share TMEM lanes 32 * (w % 4)
-constexpr long long kWaitCap = 1 << 22;  // mbarrier polls before giving up (far above a tile's MMA time)
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-// tcgen05 shared-memory matrix descriptor: K-major, no swizzle.
-__device__ __forceinline__ uint64_t mat_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
-         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
-}
-
-// Instruction descriptor of kind::f16: f16 A and B (K-major), f32 D, M x N.
-__host__ __device__ constexpr uint32_t instr_desc(int M, int N) {
-  return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-// Byte offset of element (row, k) in a K-major no-swizzle operand with K
-// columns.
-__device__ __forceinline__ uint32_t canon_off(int row, int k, int K) {
-  return (uint32_t)((row >> 3) * (K >> 3) * 128 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
-}
-
-__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                        uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
-}
-
-__device__ __forceinline__ void mma_commit(uint32_t mbar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
-               : "memory");
-}
-
-// Waits for the mbarrier to complete the phase with the given parity;
-// returns false if it did not within kWaitCap polls.
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
-  for (long long i = 0; i < kWaitCap; i++) {
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(done)
-        : "r"(mbar), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
-}
-
-// 32 lanes x 32 columns of f32 from TMEM (this warp's lane quarter).
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ uint16_t f16_bits(uint32_t v) {  // an integer 0..255 as f16
-  return __half_as_ushort(__uint2half_rn(v));
-}
-
-// Channel c of two RGBX pixels as an f16 pair (x's in the low half): the
-// bytes are placed under the f16 exponent of 1024 (0x64), where the mantissa
-// step is 1, giving 1024 + v exactly; subtracting 1024 leaves v.
-__device__ __forceinline__ uint32_t f16_pair(uint32_t x, uint32_t y, int c) {
-  const uint32_t p = __byte_perm(x, y, (uint32_t)c | ((uint32_t)(c + 4) << 4));  // [x_c, y_c, ., .]
-  const uint32_t q = __byte_perm(p, 0x64646464u, 0x5140u);                      // [x_c, 64, y_c, 64]
-  const __half2 h = __hsub2(*reinterpret_cast<const __half2*>(&q), __halves2half2(__ushort_as_half(0x6400),
-                                                                                  __ushort_as_half(0x6400)));
-  return *reinterpret_cast<const uint32_t*>(&h);
-}
-
 }  // namespace
 
 // One pass.  XPASS: rows of A are (image row, channel) pairs, 32 image rows
@@ -290,30 +207,6 @@ __global__ void __launch_bounds__(kTcThreads, 2)
 // stops, the others' waits then run out too, and the CTA frees its TMEM.
 constexpr int kPipeThreads = 544;  // 8 producer warps, 8 epilogue warps, 1 MMA warp
 constexpr int kProducers = 256, kEpilogue = 256;
-
-__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(mbar), "r"(count) : "memory");
-}
-// bar.red.or over the 128 threads of epilogue group g (named barrier 1 + g):
-// every thread gets the same answer, so the group leaves a loop together.
-__device__ __forceinline__ bool epi_bar_or(int g, bool v) {
-  uint32_t r;
-  asm volatile(
-      "{\n\t.reg .pred p, q;\n\t"
-      "setp.ne.u32 p, %1, 0;\n\t"
-      "bar.red.or.pred q, %2, 128, p;\n\t"
-      "selp.u32 %0, 1, 0, q;\n\t}\n"
-      : "=r"(r)
-      : "r"((uint32_t)v), "r"(1 + g)
-      : "memory");
-  return r != 0;
-}
-__device__ __forceinline__ void epi_bar(int g) {
-  asm volatile("bar.sync %0, 128;\n" ::"r"(1 + g) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(mbar) : "memory");
-}
 
 template <bool XPASS, int N>
 __global__ void __launch_bounds__(kPipeThreads, 1)
