@@ -91,17 +91,19 @@ int pxg_image_draw(pxg_image* a, const pxg_image* b, int64_t translate_x, int64_
  * (bindings/bindings.nim:133) */
 int pxg_image_blur(pxg_image* image, float radius, const float out_of_bounds[4]);
 
-/* Blur kernels: 3 (default) runs radii 1..128 on the tensor cores with
- * TMA-fed input rings (images whose rows are a multiple of 16 bytes; others
- * take mode 1's kernels); 1 runs radii 8..128 on the tensor cores with the
- * warp-specialised kernel that loads through registers; 2 uses the
- * single-stage tensor-core kernel (radii 8..128); 0 the CUDA-core kernels
- * (which every mode uses for the radii it does not take).  All write the same
- * bytes.  No counterpart in the reference. */
+/* Blur kernels: 3 (default) runs radii 1..8 on register-blocked CUDA-core
+ * passes and radii 9..128 on the tensor cores with TMA-fed input rings in
+ * tensor memory (images whose sides are multiples of 4; others take mode 1's
+ * kernels); 1 runs radii 8..128 on the tensor cores with the warp-specialised
+ * kernel that loads through registers; 2 uses the single-stage tensor-core
+ * kernel (radii 8..128); 0 the tiled CUDA-core kernels (which every mode uses
+ * for the radii it does not take).  All write the same bytes.  No
+ * counterpart in the reference. */
 int pxg_blur_config(int use_tensor_cores);
 
-/* The kernel family the last blur ran on: 3, 2, 1 or 0 as above (-1 before
- * any blur).  No counterpart in the reference. */
+/* The kernel family the last blur ran on: 4 (the small-radius passes of
+ * mode 3), 3 (the ring passes), 2, 1 or 0 as above (-1 before any blur).
+ * No counterpart in the reference. */
 int pxg_last_blur_kernel(void);
 
 /* spread(Image, float32)  src/pixie/images.nim:700-758 (private in the

@@ -146,6 +146,8 @@ bool ring_blur_init(size_t* maxSmem);
 bool weights_exact_f16(const uint16_t* hostKern, int r);
 bool launch_blur_ring(uint32_t* img, uint32_t* tmp, long long W, long long H, int r, const uint16_t* kern,
                       bool exactF16, uint32_t oob, int nsm, size_t maxSmem, int* err, cudaStream_t st);
+bool launch_blur_small(uint32_t* img, uint32_t* tmp, long long W, long long H, int r, const uint16_t* kern,
+                       uint32_t oob, int nsm, cudaStream_t st);
 __global__ void k_blur_x(const uint32_t*, uint32_t*, long long, long long, int, const uint16_t*, uint32_t);
 __global__ void k_blur_y(const uint32_t*, uint32_t*, long long, long long, int, const uint16_t*, uint32_t);
 __global__ void k_blurf_x(const uint32_t*, uint32_t*, long long, long long, int, const uint16_t*, uint32_t);
@@ -235,12 +237,13 @@ struct Ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evr0 = nullptr, evr1 = nullptr;
   int* dev_err = nullptr;   // device-side error flag (a tensor-core wait that ran out)
   int* host_err = nullptr;  // its pinned mirror
-  // blur kernels: 3 TMA-fed ring passes on the tensor cores (falling back to 1, then 0, where they do
-  // not apply), 1 pipelined tensor-core passes, 2 single-stage ones, 0 CUDA cores
+  // blur kernels: 3 register-blocked CUDA-core passes for radii up to 8, TMA-fed ring passes on the
+  // tensor cores above (falling back to 1, then 0, where they do not apply), 1 pipelined
+  // tensor-core passes, 2 single-stage ones, 0 the tiled CUDA-core passes
   int blur_tensor = 3;
   size_t tcSmemMax = 0;
   bool ring_ok = false;  // the ring kernels and the driver's tensor-map encoder are available
-  int last_blur = -1;    // kernel family of the last blur
+  int last_blur = -1;    // kernel family of the last blur (4: the small-radius passes)
   size_t ringSmemMax = 0;
   float last_ms = 0;
   long long stats[6] = {0, 0, 0, 0, 0, 0};  // last fill launch: paths, prims, segments, entries, blends, wide rows
@@ -346,7 +349,8 @@ const uint16_t* weights_for(int64_t r) {
 void blur_dispatch(uint32_t* img, uint32_t* tmp, long long W, long long H, int64_t r, uint32_t oob) {
   const uint16_t* kern = weights_for(r);
   int used = -1;
-  if (g.blur_tensor == 3 && g.ring_ok &&
+  if (g.blur_tensor == 3 && launch_blur_small(img, tmp, W, H, (int)r, kern, oob, g.nsm, g.stream)) used = 4;
+  if (used < 0 && g.blur_tensor == 3 && g.ring_ok &&
       launch_blur_ring(img, tmp, W, H, (int)r, kern, g.weights_f16[r], oob, g.nsm, g.ringSmemMax, g.dev_err,
                        g.stream))
     used = 3;

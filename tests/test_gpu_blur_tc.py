@@ -16,7 +16,7 @@ def _init():
     px.lib().pxg_init(0)
     pxo.set_golden_mode(False)
     yield
-    px.blur_config(1)
+    px.blur_config(3)
 
 
 def blur_gpu(img, r, oob=(0, 0, 0, 0), tensor=1):
