@@ -183,16 +183,25 @@ def run_gpu(args, ws, rank, local):
         else:
             M.shadow_into(SH, (8, 8), 4, 12, black)
 
-    # warm-up
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
-            for op in ops:
-                run_op(op)
-    stream.synchronize()
-
-    # timed region: K steps, events around every op on the library's stream
+    # warm-up; its last step is instrumented to find the dominant operation
     n_ops = len(ops)
-    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(n_ops + 1)] for _ in range(args.steps)]
+    wev = [torch.cuda.Event(enable_timing=True) for _ in range(n_ops + 1)]
+    with torch.cuda.stream(stream):
+        for w in range(args.warmup):
+            for i, op in enumerate(ops):
+                if w == args.warmup - 1:
+                    wev[i].record(stream)
+                run_op(op)
+            if w == args.warmup - 1:
+                wev[n_ops].record(stream)
+    stream.synchronize()
+    dom = int(np.argmax([wev[i].elapsed_time(wev[i + 1]) for i in range(n_ops)])) if args.warmup else 0
+
+    # timed region: K steps bracketed by two events on the library's stream;
+    # the dominant operation alone is bracketed by events inside it (its
+    # kernels' duration for the roofline)
+    dev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
     l0 = px.launch_count()
     barrier(ws)
     torch.cuda.synchronize()
@@ -203,9 +212,12 @@ def run_gpu(args, ws, rank, local):
         h0 = time.perf_counter()
         for s in range(args.steps):
             for i, op in enumerate(ops):
-                evs[s][i].record(stream)
-                run_op(op)
-            evs[s][n_ops].record(stream)
+                if i == dom:
+                    dev[s][0].record(stream)
+                    run_op(op)
+                    dev[s][1].record(stream)
+                else:
+                    run_op(op)
         t1.record(stream)
         host_ms = (time.perf_counter() - h0) * 1e3 / args.steps  # enqueue time per step on the host
         stream.synchronize()
@@ -214,14 +226,25 @@ def run_gpu(args, ws, rank, local):
     launches = (px.launch_count() - l0) // args.steps
     total_ms = max_over_ranks(ws, t0.elapsed_time(t1))
     ms_step = total_ms / args.steps
+
+    # per-operation breakdown, outside the timed region: events around every op
+    # over a few more steps (the events add small gaps between operations)
+    n_prof = max(1, min(args.steps, 5))
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(n_ops + 1)] for _ in range(n_prof)]
+    for s in range(n_prof):
+        for i, op in enumerate(ops):
+            evs[s][i].record(stream)
+            run_op(op)
+        evs[s][n_ops].record(stream)
+    stream.synchronize()
     op_ms = np.zeros(n_ops)
-    for s in range(args.steps):
+    for s in range(n_prof):
         for i in range(n_ops):
             op_ms[i] += evs[s][i].elapsed_time(evs[s][i + 1])
-    op_ms /= args.steps
+    op_ms /= n_prof
 
-    # roofline of the dominant operation
-    dom = int(np.argmax(op_ms))
+    # roofline of the dominant operation, timed inside the timed region
+    dom_ms = float(np.mean([a.elapsed_time(b) for a, b in dev]))
     kind, p = ops[dom]
     if kind == "draw":
         bpp = 8 if p == 17 else 12
@@ -234,7 +257,7 @@ def run_gpu(args, ws, rank, local):
         algo = 5 * SHADOW_W * SHADOW_W
         unit_desc = "shadow: 5 B/px x 1024^2 px"
     peak, peak_src = peaks()
-    achieved = algo / (op_ms[dom] * 1e-3) / 1e9
+    achieved = algo / (dom_ms * 1e-3) / 1e9
     roof = {"bound": "hbm", "kernel": f"{kind}:{p}", "unit_bytes": algo, "unit": "GB/s",
             "achieved": round(achieved, 1), "peak": peak, "peak_source": peak_src,
             "frac": round(achieved / peak, 4), "traffic": TRAFFIC.get(f"{kind}:{p}"),

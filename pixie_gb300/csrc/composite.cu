@@ -21,6 +21,8 @@ __device__ __forceinline__ uint32_t draw_px(const uint8_t* tbl, uint32_t a, uint
   if (MODE == kNormal) return blendNormal(a, b);
   if (MODE == kOverwrite) return b;
   if (MODE == kMask) return blendMaskPx(a, b);
+  if (MODE == kColorBurn) return blendBurnDodge<true>(tbl, a, b);
+  if (MODE == kColorDodge) return blendBurnDodge<false>(tbl, a, b);
   if (MODE == kSoftLight || MODE == kHue || MODE == kSaturation || MODE == kColor || MODE == kLuminosity)
     return blendFloatT<MODE>(tbl, a, b);  // the float modes inline, without the mode switch
   return blend_px(MODE, tbl, a, b);

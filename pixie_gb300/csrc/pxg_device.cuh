@@ -87,16 +87,6 @@ struct BlendTables {
   const uint8_t* straight;
 };
 
-__device__ __forceinline__ uint32_t alphaFix8(Px bd, Px src, Px mixed) {  // :18-39 -> straight RGBA
-  uint32_t sa = src.a, ba = bd.a;
-  uint32_t t0 = sa * (255 - ba), t1 = sa * ba, t2 = (255 - sa) * ba;
-  uint32_t r = t0 * src.r + t1 * mixed.r + t2 * bd.r;
-  uint32_t g = t0 * src.g + t1 * mixed.g + t2 * bd.g;
-  uint32_t b = t0 * src.b + t1 * mixed.b + t2 * bd.b;
-  uint32_t a = sa + ba * (255 - sa) / 255;
-  if (a == 0) return 0u;
-  return pack(r / a / 255, g / a / 255, b / a / 255, a);
-}
 __device__ __forceinline__ uint32_t premul8(uint32_t sv) {  // internal.nim:86-96
   Px s = unpack(sv);
   if (s.a == 255) return sv;
@@ -239,17 +229,59 @@ __device__ __forceinline__ uint32_t blendFloatT(const uint8_t* tbl, uint32_t bp,
   return premul8(pack(unit_to_u8(orr), unit_to_u8(og), unit_to_u8(ob), unit_to_u8(ao)));
 }
 
-__device__ __forceinline__ uint32_t colorBurn1(uint32_t b, uint32_t s) {  // :115-121
-  if (b == 255) return 255;
-  if (s == 0) return 0;
-  uint32_t v = (255 * (255 - b)) / s;
-  return (255 - (v < 255 ? v : 255)) & 255u;
+
+// floor(n / d) for integers held exactly in floats, 0 <= n, n + d < 2^24,
+// 1 <= d, n / d < 2^21.  rd is rcp.approx(d) (relative error below 2^-22), so
+// n * rd is within n/d * 2^-22 < 0.5 of n / d and its floor -- a round-down
+// FMA onto 1.5 * 2^23 -- is off by at most one; one exact remainder test
+// (n - q * d, an integer below 2^24 in magnitude) corrects it.
+__device__ __forceinline__ float rcp_approx(float d) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(d));
+  return r;
 }
-__device__ __forceinline__ uint32_t colorDodge1(uint32_t b, uint32_t s) {  // :162-168
-  if (b == 0) return 0;
-  if (s == 255) return 255;
-  uint32_t v = (255 * b) / (255 - s);
-  return v < 255 ? v : 255;
+__device__ __forceinline__ uint32_t fdiv_floor(float n, float d, float rd) {
+  const float t = __fmaf_rd(n, rd, 12582912.0f);
+  const float q = t - 12582912.0f;
+  const float rem = fmaf(-q, d, n);
+  uint32_t qi = __float_as_uint(t) - 0x4B400000u;
+  qi -= rem < 0.0f ? 1u : 0u;
+  qi += rem >= d ? 1u : 0u;
+  return qi;
+}
+__device__ __forceinline__ float small_to_f(uint32_t x) {  // exact for x < 2^23
+  return __uint_as_float(0x4B000000u | x) - 8388608.0f;
+}
+// ColorBurn / ColorDodge (blends.nim:111-126, :158-173) with the divisions
+// done as above: the same integers as the reference's integer divisions.
+template <bool BURN>
+__device__ __forceinline__ uint32_t blendBurnDodge(const uint8_t* tbl, uint32_t bv, uint32_t sv) {
+  const Px bd = straight8(tbl, bv), sr = straight8(tbl, sv);
+  auto mix = [](uint32_t b, uint32_t s) -> uint32_t {
+    if (BURN) {
+      if (b == 255) return 255u;
+      if (s == 0) return 0u;
+      const float sf = small_to_f(s);
+      const uint32_t v = fdiv_floor(small_to_f(255u * (255u - b)), sf, rcp_approx(sf));
+      return 255u - (v < 255u ? v : 255u);
+    }
+    if (b == 0) return 0u;
+    if (s == 255) return 255u;
+    const float df = small_to_f(255u - s);
+    const uint32_t v = fdiv_floor(small_to_f(255u * b), df, rcp_approx(df));
+    return v < 255u ? v : 255u;
+  };
+  const uint32_t mr = mix(bd.r, sr.r), mg = mix(bd.g, sr.g), mb = mix(bd.b, sr.b);
+  // alphaFix (blends.nim:18-39): (t0 src + t1 mixed + t2 backdrop) / a / 255 = ... / (255 a)
+  const uint32_t sa = sr.a, ba = bd.a;
+  const uint32_t a = sa + ba * (255 - sa) / 255;
+  if (a == 0) return 0u;
+  const float t0 = small_to_f(sa * (255 - ba)), t1 = small_to_f(sa * ba), t2 = small_to_f((255 - sa) * ba);
+  const float d = small_to_f(255u * a), rd = rcp_approx(d);
+  const float r = fmaf(t0, small_to_f(sr.r), fmaf(t1, small_to_f(mr), t2 * small_to_f(bd.r)));
+  const float g = fmaf(t0, small_to_f(sr.g), fmaf(t1, small_to_f(mg), t2 * small_to_f(bd.g)));
+  const float b = fmaf(t0, small_to_f(sr.b), fmaf(t1, small_to_f(mb), t2 * small_to_f(bd.b)));
+  return premul8(pack(fdiv_floor(r, d, rd), fdiv_floor(g, d, rd), fdiv_floor(b, d, rd), a));
 }
 
 // blender(mode)(backdrop, source)  blends.nim:275-299
@@ -305,16 +337,8 @@ __device__ __forceinline__ uint32_t blend_px(int mode, const uint8_t* tbl, uint3
       };
       return pack(f(b.r, s.r), f(b.g, s.g), f(b.b, s.b), blendAlpha(b.a, s.a));
     }
-    case kColorBurn:
-    case kColorDodge: {  // :111-126, :158-173
-      Px bd = straight8(tbl, bv), sr = straight8(tbl, sv), m;
-      if (mode == kColorBurn) {
-        m = Px{colorBurn1(bd.r, sr.r), colorBurn1(bd.g, sr.g), colorBurn1(bd.b, sr.b), 0};
-      } else {
-        m = Px{colorDodge1(bd.r, sr.r), colorDodge1(bd.g, sr.g), colorDodge1(bd.b, sr.b), 0};
-      }
-      return premul8(alphaFix8(bd, sr, m));
-    }
+    case kColorBurn: return blendBurnDodge<true>(tbl, bv, sv);
+    case kColorDodge: return blendBurnDodge<false>(tbl, bv, sv);
     case kSoftLight:
     case kHue:
     case kSaturation:
