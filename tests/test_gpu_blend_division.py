@@ -60,3 +60,27 @@ def test_burn_dodge_random_pixels(mode):
     A = px.Image.from_numpy(a)
     A.draw(px.Image.from_numpy(b), (0, 0), mode)
     assert np.array_equal(A.to_numpy(), ref)
+
+
+@pytest.mark.parametrize("mode", [3, 6, 8, 12, 13, 14, 15])
+def test_straight_alpha_every_pair(mode):
+    # every (alpha, channel) pair as the backdrop's straight-alpha input, over
+    # a few sources: the arithmetic straight alpha and v / 255 against the oracle
+    px.lib().pxg_init(0)
+    a, c = np.meshgrid(np.arange(256), np.arange(256), indexing="ij")
+    a, c = a.ravel(), c.ravel()
+    bd = np.stack([c, (c * 7) % 256, 255 - c, a], 1).astype(np.uint8)
+    for sv in ((200, 10, 90, 220), (3, 250, 128, 255), (0, 0, 0, 0), (255, 255, 255, 255), (60, 60, 60, 61)):
+        src = np.tile(np.array(sv, np.uint8), (65536, 1))
+        B = px.Image.from_numpy(bd.reshape(256, 256, 4))
+        S = px.Image.from_numpy(src.reshape(256, 256, 4))
+        O = px.Image(256, 256)
+        px.blend_pixels(mode, B.device_ptr, S.device_ptr, O.device_ptr, 65536)
+        ref = pxo.blend_pixels(mode, bd, src)
+        got = O.to_numpy().reshape(-1, 4)
+        bad = np.nonzero((got != ref).any(1))[0]
+        assert bad.size == 0, f"mode {mode} src {sv}: {bad.size} pixels differ, first a={a[bad[0]]} c={c[bad[0]]}"
+        # the same pairs as the source
+        px.blend_pixels(mode, S.device_ptr, B.device_ptr, O.device_ptr, 65536)
+        ref = pxo.blend_pixels(mode, src, bd)
+        assert np.array_equal(O.to_numpy().reshape(-1, 4), ref), f"mode {mode} backdrop {sv}"
