@@ -476,8 +476,10 @@ bool plan_pass(RingArgs& a, int alen, int clen, int r, int nsm, size_t maxSmem, 
   a.clen = clen;
   a.r = r;
   a.kspan = (kPos + 2 * r + 15) / 16 * 16;
-  a.nring = (a.kspan + kPos - 1) / kPos + 2;
-  if (a.nring > kMaxRing || kRingCol0 + 32 * a.nring > kTmemCols) return false;
+  // the ring takes every TMEM column above the accumulators: the converters run
+  // up to (nring - span) chunks ahead of the tile the MMAs read
+  a.nring = (kTmemCols - kRingCol0) / 32;
+  if (a.nring > kMaxRing || (a.kspan + kPos - 1) / kPos + 1 > a.nring) return false;
   a.delta = (4 - (r & 3)) & 3;  // (s0 - r) mod 4; every s0 is a multiple of 64
   a.rawStride = (kRawBytes + 1023) / 1024 * 1024;
   // as many raw stages as shared memory allows
