@@ -530,10 +530,11 @@ def run_scene(px, wl, seed=7, n_paths=2000, size=1024, reps=3):
 
 
 # DRAM traffic per operation (dram__bytes_read.sum + dram__bytes_write.sum,
-# summed over the operation's launches) from an ncu capture of the same
-# kernels: blur radius 64 of 4096x4096 = the two tensor-core passes
-# (python bench.py --case blur64).
-TRAFFIC = {"blur:64": 67153152 + 23181312 + 67162624 + 20830208}
+# summed over the operation's launches) from ncu captures of the same
+# kernels: a blur of 4096x4096 at radius 16 or 64 = the two tensor-core ring
+# passes (python bench.py --case blur16 / blur64).
+TRAFFIC = {"blur:16": 67246336 + 16806656 + 67213312 + 13801984,
+           "blur:64": 67231232 + 17640192 + 67214080 + 17206528}
 
 
 # -- CPU baseline / reference arm ----------------------------------------------------------
