@@ -555,21 +555,52 @@ __global__ void __launch_bounds__(256) k_setup(PathJob* jobs, Arena A, int maxBa
   (void)height;
 
   // Phase D: each segment's band range (partitionRange :1201-1213), each
-  // band's entry count and anti-aliasing flag (:1215-1234)
+  // band's entry count and anti-aliasing flag (:1215-1234).  With at most
+  // kBallotBands bands each warp owns a contiguous run of segments and counts
+  // its entries per band (the list build below places them); otherwise
+  // shared-memory atomics per band.
+  const bool ballot = numP <= (uint32_t)kBallotBands && maxBands <= kBallotBands;
+  const int NW = T >> 5;
+  int* wc = dsm + 2 * maxBands;  // [warp][band]: entries, then each warp's start
+  const long long per = ((nseg + NW - 1) / NW + 31) / 32 * 32;
+  const long long ws0 = min(nseg, (long long)warp * per), ws1 = min(nseg, ws0 + per);
+  int* mine = wc + warp * (int)numP;
   for (uint32_t k = tid; k < numP; k += T) {
     bandc[k] = 0;
     bandf[k] = 0;
   }
+  if (ballot)
+    for (int k = tid; k < 2 * NW * (int)numP; k += T) wc[k] = 0;  // counts and band masks
   __syncthreads();
-  for (long long i = tid; i < nseg; i += T) {
-    float4 s = A.segs[segbase + i];
-    uint32_t a, b;
-    bandRange(s, a, b);
-    A.segband[segbase + i] = make_uint2(a, b);
-    bool aa = segRequiresAA(s);
-    for (uint32_t k = a; k <= b; k++) {
-      atomicAdd(&bandc[k], 1);
-      if (aa) atomicOr(&bandf[k], kBandAA);
+  if (ballot) {
+    for (long long i = ws0 + lane; i < ws1; i += 32) {
+      const float4 sg = A.segs[segbase + i];
+      uint32_t a, b;
+      bandRange(sg, a, b);
+      A.segband[segbase + i] = make_uint2(a, b);
+      const bool aa = segRequiresAA(sg);
+      for (uint32_t k = a; k <= b; k++) {
+        atomicAdd(&mine[k], 1);
+        if (aa) atomicOr(&bandf[k], kBandAA);
+      }
+    }
+    __syncthreads();
+    for (uint32_t k = tid; k < numP; k += T) {
+      int c = 0;
+      for (int w = 0; w < NW; w++) c += wc[w * numP + k];
+      bandc[k] = c;
+    }
+  } else {
+    for (long long i = tid; i < nseg; i += T) {
+      float4 sg = A.segs[segbase + i];
+      uint32_t a, b;
+      bandRange(sg, a, b);
+      A.segband[segbase + i] = make_uint2(a, b);
+      bool aa = segRequiresAA(sg);
+      for (uint32_t k = a; k <= b; k++) {
+        atomicAdd(&bandc[k], 1);
+        if (aa) atomicOr(&bandf[k], kBandAA);
+      }
     }
   }
   __syncthreads();
@@ -585,7 +616,8 @@ __global__ void __launch_bounds__(256) k_setup(PathJob* jobs, Arena A, int maxBa
   }
   // Phase E: each band's entry list, segment indices ascending -- the order in
   // which partitionSegments appends them (:1215-1234).  Offsets by a scan of
-  // the counts; then every thread owns bands and walks the segments in order.
+  // the counts; then either each warp writes its run's entries (ballot build)
+  // or every thread owns bands and walks the segments in order.
   long long etotal = 0;
   for (uint32_t c0 = 0; c0 < numP; c0 += T) {
     const uint32_t k = c0 + tid;
@@ -613,57 +645,42 @@ __global__ void __launch_bounds__(256) k_setup(PathJob* jobs, Arena A, int maxBa
   }
   int* L = A.bandseg + s_listbase;
   for (uint32_t k = tid; k < numP; k += T) A.bands[s_bandbase + k].off += s_listbase;
-  if (numP <= (uint32_t)kBallotBands && maxBands <= kBallotBands) {
-    // Each warp owns a contiguous range of segments and walks it 32 at a
-    // time; for every band the 32 segments touch, a ballot orders them.  A
-    // first pass counts each warp's entries per band (giving every warp its
-    // start in every band), the second writes them: O(entries) work.
-    const int NW = T >> 5;
-    int* wc = dsm + 2 * maxBands;  // [warp][band]
-    for (int k = tid; k < NW * (int)numP; k += T) wc[k] = 0;
+  if (ballot) {
+    // each warp's start in every band: the band's offset plus the earlier
+    // warps' entries; then the warp writes its run's entries: O(entries) work
+    for (uint32_t k = tid; k < numP; k += T) {
+      int run = bandc[k];
+      for (int w = 0; w < NW; w++) {
+        const int t = wc[w * numP + k];
+        wc[w * numP + k] = run;
+        run += t;
+      }
+    }
     __syncthreads();
-    const long long per = ((nseg + NW - 1) / NW + 31) / 32 * 32;
-    const long long s0 = min(nseg, (long long)warp * per), s1 = min(nseg, s0 + per);
-    int* mine = wc + warp * (int)numP;
-    for (int pass = 0; pass < 2; pass++) {
-      if (pass == 1) {
-        __syncthreads();
-        for (uint32_t k = tid; k < numP; k += T) {
-          int run = bandc[k];
-          for (int w = 0; w < NW; w++) {
-            const int t = wc[w * numP + k];
-            wc[w * numP + k] = run;
-            run += t;
-          }
-        }
-        __syncthreads();
+    // per batch of 32 segments: every lane marks the bands its segment
+    // touches in the warp's band masks; a segment's place in band k is the
+    // warp's cursor plus the number of lower lanes in k's mask (the reference's
+    // append order); each band's lowest lane then advances the cursor and
+    // clears the mask
+    uint32_t* bm = reinterpret_cast<uint32_t*>(wc + NW * (int)numP) + warp * (int)numP;
+    for (long long c0 = ws0; c0 < ws1; c0 += 32) {
+      const long long i = c0 + lane;
+      const bool valid = i < ws1;
+      uint2 r = make_uint2(1u, 0u);  // empty range
+      if (valid) r = A.segband[segbase + i];
+      const uint32_t bit = 1u << lane;
+      for (uint32_t k = r.x; k <= r.y; k++) atomicOr(&bm[k], bit);
+      __syncwarp();
+      for (uint32_t k = r.x; k <= r.y; k++) L[mine[k] + __popc(bm[k] & lt32)] = (int)i;
+      __syncwarp();
+      for (uint32_t k = r.x; k <= r.y; k++) {
+        const uint32_t m = bm[k];
+        if (!(m & lt32)) mine[k] += __popc(m);
       }
-      for (long long c0 = s0; c0 < s1; c0 += 32) {
-        const long long i = c0 + lane;
-        const bool valid = i < s1;
-        uint2 r = make_uint2(UINT_MAX, 0u);
-        if (valid) r = A.segband[segbase + i];
-        uint32_t lo = r.x, hi = r.y;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-          hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-        }
-        for (uint32_t k = lo; k <= hi; k++) {
-          const bool in = valid && r.x <= k && k <= r.y;
-          const unsigned m = __ballot_sync(0xffffffffu, in);
-          if (!m) continue;
-          if (pass == 0) {
-            if (lane == 0) mine[k] += __popc(m);
-          } else {
-            const int base = mine[k];
-            if (in) L[base + __popc(m & lt32)] = (int)i;
-            __syncwarp();
-            if (lane == 0) mine[k] = base + __popc(m);
-          }
-          __syncwarp();
-        }
-      }
+      __syncwarp();
+      for (uint32_t k = r.x; k <= r.y; k++)
+        if (!(bm[k] & lt32)) bm[k] = 0u;
+      __syncwarp();
     }
     if (tid == 0) {
       J.band_off = s_bandbase;
@@ -1728,8 +1745,8 @@ void launch_scene(unsigned blocks, cudaStream_t st, PathJob* jobs, const SceneRu
 // Dynamic shared memory of k_setup for a launch whose images have at most
 // maxBands bands: per band a count and flags, plus per warp and band a cursor
 // for the ballot band-list build.
-size_t setup_smem(int maxBands) {
-  return (size_t)maxBands * 8 + (maxBands <= kBallotBands ? (size_t)(256 / 32) * maxBands * 4 : 0);
+size_t setup_smem(int maxBands) {  // counts and flags, then per warp: band counts/cursors and band masks
+  return (size_t)maxBands * 8 + (maxBands <= kBallotBands ? (size_t)2 * (256 / 32) * maxBands * 4 : 0);
 }
 
 size_t scene_wide_bytes() { return sizeof(RowScratch<kWideMaxH, kWideXT>); }
