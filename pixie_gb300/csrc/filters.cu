@@ -462,10 +462,114 @@ void launch_spread(uint32_t* img, uint8_t* a0, uint8_t* a1, long long W, long lo
   k_alpha_to_rgbx<<<grid_for(n, nsm), 256, 0, st>>>(a0, img, n); note_launch();
 }
 
+// shadow in one pass over 64 x 64 output tiles: the tile and a halo of
+// |spread| + radius (at most kShadowHalo) of the offset alpha plane are staged
+// in shared memory and the reference's stages run there in order -- spread
+// along x then y (a running max or min over the window clipped to the image:
+// positions outside the image hold the neutral value), blur along x then y
+// (taps outside the image read 0; integer sums and v div 256 div 255 as the
+// blur passes), then colour * alpha / 255 (the MaskBlend draw of the filled
+// result) written once.
+constexpr int kShadowTile = 64, kShadowHalo = 32;
+__global__ void __launch_bounds__(256) k_shadow_tile(const uint32_t* __restrict__ src, uint32_t* __restrict__ out,
+                                                     int W, int H, int ox, int oy, int m, int grow, int r,
+                                                     const uint16_t* __restrict__ kern, uint32_t color) {
+  extern __shared__ __align__(16) unsigned char sh[];
+  const int h = m + r, S = kShadowTile + 2 * h;  // staged side
+  unsigned char* b0 = sh;
+  unsigned char* b1 = sh + S * S;
+  uint32_t* wk = reinterpret_cast<uint32_t*>(sh + ((2 * S * S + 15) & ~15));
+  const int gx0 = blockIdx.x * kShadowTile - h, gy0 = blockIdx.y * kShadowTile - h;  // staged [0][0]
+  const int tid = threadIdx.x, T = blockDim.x;
+  if (r > 0)  // without a blur there is no weight table
+    for (int k = tid; k <= 2 * r; k += T) wk[k] = kern[k];
+  const unsigned char neutral = (m > 0 && !grow) ? 255 : 0;
+  auto inside = [&](int i, int j) {
+    const int gx = gx0 + j, gy = gy0 + i;
+    return gx >= 0 && gx < W && gy >= 0 && gy < H;
+  };
+  // the offset alpha plane (k_alpha_offset), neutral outside the image
+  for (int idx = tid; idx < S * S; idx += T) {
+    const int i = idx / S, j = idx - i * S;
+    const int gx = gx0 + j, gy = gy0 + i;
+    unsigned char v = neutral;
+    if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+      const int sx = gx - ox, sy = gy - oy;
+      v = (sx >= 0 && sx < W && sy >= 0 && sy < H) ? (unsigned char)(src[(long long)sy * W + sx] >> 24) : 0;
+    }
+    b0[idx] = v;
+  }
+  __syncthreads();
+  if (m > 0) {  // spread along x into b1, then along y back into b0 (rows and columns [m, S - m))
+    for (int idx = tid; idx < S * (S - 2 * m); idx += T) {
+      const int i = idx / (S - 2 * m), j = m + (idx - i * (S - 2 * m));
+      const unsigned char* p = b0 + i * S + j - m;
+      uint32_t v = neutral;
+      for (int t = 0; t <= 2 * m; t++) v = grow ? max(v, (uint32_t)p[t]) : min(v, (uint32_t)p[t]);
+      b1[i * S + j] = (unsigned char)v;
+    }
+    __syncthreads();
+    for (int idx = tid; idx < (S - 2 * m) * (S - 2 * m); idx += T) {
+      const int i = m + idx / (S - 2 * m), j = m + idx % (S - 2 * m);
+      const unsigned char* p = b1 + (i - m) * S + j;
+      uint32_t v = neutral;
+      for (int t = 0; t <= 2 * m; t++) v = grow ? max(v, (uint32_t)p[t * S]) : min(v, (uint32_t)p[t * S]);
+      b0[i * S + j] = inside(i, j) ? (unsigned char)v : 0;  // blur taps outside the image read 0
+    }
+    __syncthreads();
+  } else if (neutral != 0) {
+    for (int idx = tid; idx < S * S; idx += T)
+      if (!inside(idx / S, idx % S)) b0[idx] = 0;
+    __syncthreads();
+  }
+  const unsigned char* fin = b0;  // final alpha at [h + y][h + x]
+  if (r > 0) {
+    // blur along x: rows [m, S - m), the tile's columns, into b1 (0 outside the image)
+    for (int idx = tid; idx < (S - 2 * m) * kShadowTile; idx += T) {
+      const int i = m + idx / kShadowTile, j = h + (idx % kShadowTile);
+      const unsigned char* p = b0 + i * S + j - r;
+      uint32_t acc = 0;
+      for (int t = 0; t <= 2 * r; t++) acc += (uint32_t)p[t] * wk[t];
+      b1[i * S + j] = inside(i, j) ? (unsigned char)(acc / 256 / 255) : 0;
+    }
+    __syncthreads();
+    // blur along y: the tile, into b0
+    for (int idx = tid; idx < kShadowTile * kShadowTile; idx += T) {
+      const int i = h + idx / kShadowTile, j = h + (idx % kShadowTile);
+      const unsigned char* p = b1 + (i - r) * S + j;
+      uint32_t acc = 0;
+      for (int t = 0; t <= 2 * r; t++) acc += (uint32_t)p[t * S] * wk[t];
+      b0[i * S + j] = (unsigned char)(acc / 256 / 255);
+    }
+    __syncthreads();
+  }
+  const Px c = unpack(color);
+  for (int idx = tid; idx < kShadowTile * kShadowTile; idx += T) {
+    const int y = idx / kShadowTile, x = idx % kShadowTile;
+    const int gx = gx0 + h + x, gy = gy0 + h + y;
+    if (gx >= W || gy >= H) continue;
+    const uint32_t k = fin[(h + y) * S + h + x];
+    out[(long long)gy * W + gx] = pack((c.r * k) / 255, (c.g * k) / 255, (c.b * k) / 255, (c.a * k) / 255);
+  }
+}
+size_t shadow_tile_smem(int h) {
+  const int S = kShadowTile + 2 * h;
+  return (size_t)((2 * S * S + 15) & ~15) + (size_t)(2 * kShadowHalo + 1) * 4;
+}
+
 void launch_shadow(const uint32_t* src, uint32_t* out, uint8_t* a0, uint8_t* a1, long long W,
                    long long H, long long ox, long long oy, int s, int r, const uint16_t* kern,
                    uint32_t color, int nsm, cudaStream_t st) {
   long long n = W * H;
+  const int m = s > 0 ? s : -s;
+  if (m + r <= kShadowHalo && W <= (1 << 24) && H <= (1 << 24) && ox > -(1 << 24) && ox < (1 << 24) &&
+      oy > -(1 << 24) && oy < (1 << 24)) {
+    const dim3 g((unsigned)((W + kShadowTile - 1) / kShadowTile), (unsigned)((H + kShadowTile - 1) / kShadowTile));
+    k_shadow_tile<<<g, 256, shadow_tile_smem(m + r), st>>>(src, out, (int)W, (int)H, (int)ox, (int)oy, m, s > 0, r,
+                                                           kern, color);
+    note_launch();
+    return;
+  }
   k_alpha_offset<<<grid_for(n, nsm), 256, 0, st>>>(src, a0, W, H, ox, oy); note_launch();
   if (s != 0) {
     int grow = s > 0, m = s > 0 ? s : -s;
