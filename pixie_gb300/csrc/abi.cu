@@ -225,6 +225,8 @@ struct Ctx {
   long long ovf_cap = 0;
   long long* xcl = nullptr;
   long long xcl_cap = 0;
+  uint8_t* fsteps = nullptr;  // flattening step records (fill setup)
+  long long fsteps_cap = 0;
   // upload area: jobs | counters | prims (device and pinned mirror)
   unsigned char* d_up = nullptr;
   unsigned char* h_up = nullptr;
@@ -509,6 +511,12 @@ Staged stage(const std::vector<PathJob>& run, const void* extra, size_t extraByt
   A.ovf_cap = g.ovf_cap;
   A.xclears = g.xcl;
   A.xclear_cap = g.xcl_cap / 3;
+  if (!g.fsteps) {  // step records of the first 16 setup CTAs of a launch (512 steps x 256 groups each)
+    CU(cudaMalloc(&g.fsteps, (size_t)16 * 256 * 512));
+    g.fsteps_cap = (long long)16 * 256 * 512;
+  }
+  A.fsteps = g.fsteps;
+  A.fsteps_cap = g.fsteps_cap;
   return S;
 }
 

@@ -141,7 +141,8 @@ __device__ int flatten_curve_group(const Prim& p, float ems, int G, int gl, int 
 // none) and that curve's index in errp.
 template <class Emit, class Done>
 __device__ int flatten_curves_converged(const Prim* P, int np, float ems, int G, int gid, int NG, int gl, int leader,
-                                        int& errp, Emit&& emit, Done&& done) {
+                                        int& errp, Emit&& emit, Done&& done, uint8_t* rec = nullptr, int cap = 0,
+                                        int* nrec = nullptr) {
   const unsigned gbits = G == 32 ? 0xffffffffu : ((1u << G) - 1);
   auto next_curve = [&](int q) {
     while (q < np && P[q].kind == kPrimLine) q += NG;
@@ -222,6 +223,10 @@ __device__ int flatten_curves_converged(const Prim* P, int np, float ems, int G,
       continue;
     }
     const int kdec = base + __ffs(mine) - 1;
+    if (rec) {  // record the step's halving level for the replay
+      if (*nrec < cap && gl == 0) rec[*nrec] = (uint8_t)kdec;
+      ++*nrec;
+    }
     const float step = s0 * pow2neg(kdec);
     const V2 nxt{nxx, nxy};
     if (prev.x - nxt.x != 0.0f || prev.y - nxt.y != 0.0f) emit(p, prev, nxt);
@@ -238,6 +243,39 @@ __device__ int flatten_curves_converged(const Prim* P, int np, float ems, int G,
     base = 0;
   }
   return status;
+}
+
+// The group's curves again from the halving levels the search recorded: the
+// accepted point of a step is cubicAt/quadAt at t + s0 * 2^-level, the same
+// expression the search evaluated, so the same segments come out without
+// the search.  emit and done as for flatten_curves_converged.
+template <class Emit, class Done>
+__device__ void replay_curves(const Prim* P, int np, int gid, int NG, const uint8_t* rec, int nrec, Emit&& emit,
+                              Done&& done) {
+  int n = 0;
+  for (int p = gid; p < np; p += NG) {
+    const Prim& q = P[p];
+    if (q.kind == kPrimLine) continue;
+    const bool cubic = q.kind == kPrimCubic;
+    const V2 at{q.x[0], q.y[0]}, c1{q.x[1], q.y[1]}, c2{q.x[2], q.y[2]};
+    const V2 to{cubic ? q.x[3] : q.x[2], cubic ? q.y[3] : q.y[2]};
+    float t = 0, s0 = 1;
+    bool halfStepping = false;
+    V2 prev = at;
+    while (true) {
+      if (n >= nrec) return;  // a complete record ends with the last curve's t == 1
+      const int kdec = rec[n++];
+      const float step = s0 * pow2neg(kdec);
+      const V2 nxt = cubic ? cubicAt(at, c1, c2, to, t + step) : quadAt(at, c1, c2, t + step);
+      if (prev.x - nxt.x != 0.0f || prev.y - nxt.y != 0.0f) emit(p, prev, nxt);
+      t += step;
+      if (t == 1) break;
+      prev = nxt;
+      if (kdec > 0) halfStepping = true;
+      s0 = (!cubic && halfStepping) ? nmin(step, 1 - t) : nmin(step * 2, 1 - t);
+    }
+    done(p);
+  }
 }
 
 // transform + shapesToSegments for one emitted pair (paths.nim:1059-1096).
@@ -395,6 +433,12 @@ __global__ void __launch_bounds__(256) k_setup(PathJob* jobs, Arena A, int maxBa
     V2 a{P[p].x[0], P[p].y[0]}, b{P[p].x[1], P[p].y[1]};
     PC[p] = ((a.x - b.x != 0.0f || a.y - b.y != 0.0f) && make_seg(J, a, b, s, w)) ? 1 : 0;
   }
+  // each group's record of halving levels, for the emitting pass to replay
+  constexpr int kStepCap = 512;
+  uint8_t* rec = nullptr;
+  if (A.fsteps && ((long long)blockIdx.x + 1) * 256 * kStepCap <= A.fsteps_cap)
+    rec = A.fsteps + ((long long)blockIdx.x * 256 + gid) * kStepCap;
+  int nrec = 0;
   {
     int cnt = 0, errp = 0;
     const int st = flatten_curves_converged(
@@ -407,7 +451,8 @@ __global__ void __launch_bounds__(256) k_setup(PathJob* jobs, Arena A, int maxBa
         [&](int p) {
           if (gl == 0) PC[p] = cnt;
           cnt = 0;
-        });
+        },
+        rec, kStepCap, &nrec);
     if (st != kOk && gl == 0)  // the reference raises at the first failing primitive
       atomicMin(&s_err, ((long long)errp << 8) | st);
   }
@@ -456,17 +501,20 @@ __global__ void __launch_bounds__(256) k_setup(PathJob* jobs, Arena A, int maxBa
   }
   {
     int cnt = 0, errp = 0;
-    flatten_curves_converged(
-        P, np, J.ems, G, gid, NG, gl, leader, errp,
-        [&](int p, V2 a, V2 b) {
-          float4 s;
-          int w;
-          if (make_seg(J, a, b, s, w)) {
-            if (gl == 0) put(s_segbase + PC[p] + cnt, s, w);
-            cnt++;
-          }
-        },
-        [&](int) { cnt = 0; });
+    auto emitB = [&](int p, V2 a, V2 b) {
+      float4 s;
+      int w;
+      if (make_seg(J, a, b, s, w)) {
+        if (gl == 0) put(s_segbase + PC[p] + cnt, s, w);
+        cnt++;
+      }
+    };
+    auto doneB = [&](int) { cnt = 0; };
+    // replay where every group of the warp kept its whole record, else search again
+    if (__all_sync(0xffffffffu, rec != nullptr && nrec <= kStepCap))
+      replay_curves(P, np, gid, NG, rec, nrec, emitB, doneB);
+    else
+      flatten_curves_converged(P, np, J.ems, G, gid, NG, gl, leader, errp, emitB, doneB);
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {

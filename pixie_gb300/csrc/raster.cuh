@@ -114,6 +114,8 @@ struct Arena {
   long long ovf_cap;
   long long* xclears;   // (job, start, end) linear-pixel clears that reach into earlier rows
   long long xclear_cap;
+  uint8_t* fsteps;      // fill setup: the halving level of every accepted flattening step, per group
+  long long fsteps_cap; // (the second pass replays them); bytes
 };
 
 }  // namespace pxg
