@@ -612,11 +612,12 @@ def run_case(case: str, slice_w: int = 0):
         img = px.Image.from_numpy(wl.premultiplied_image(9, 4096, 4096))
         for _ in range(2):
             img.blur(r)
-    elif case == "draw":  # NormalBlend draw of 4096x4096 onto 4096x4096 (inputs > L2)
+    elif case.startswith("draw"):  # draw<mode>: a 4096x4096 draw onto 4096x4096 (inputs > L2), default Normal
+        mode = int(case[4:] or 0)
         a = px.Image.from_numpy(wl.premultiplied_image(1, 4096, 4096))
         b = px.Image.from_numpy(wl.premultiplied_image(2, 4096, 4096))
         for _ in range(2):
-            a.draw(b, (0, 0), 0)
+            a.draw(b, (0, 0), mode)
     elif case == "glyphs":  # batched fill of 512 glyph masks
         glyphs, _ = wl.glyph_batch(7, n=512)
         imgs = [px.Image(w, h) for (_, w, h, _) in glyphs]
@@ -667,7 +668,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--slice", type=int, default=0, help="scene row slice width for --case scene*")
     ap.add_argument("--case", default=None,
-                    help="run one small operation for profiling: fill512 | blur<r> (blur64) | draw | glyphs | scene | scene_small | masks")
+                    help="run one small operation for profiling: fill512 | blur<r> (blur64) | draw<mode> (draw13) | glyphs | scene | scene_small | masks")
     args = ap.parse_args()
     if args.case:
         run_case(args.case, args.slice)

@@ -36,38 +36,38 @@ __global__ void __launch_bounds__(256) k_draw(uint32_t* __restrict__ a, const ui
                                               long long bx, long long by, long long w, long long h,
                                               const uint8_t* tbl, int vec) {
   if (vec) {
-    // 4 independent 16-byte quads per thread per iteration, all loads issued
-    // before any blend, so each SM keeps enough bytes in flight to saturate HBM.
+    // One 16-byte quad (4 pixels) per thread per iteration: the blend is
+    // inlined four times, not sixteen, so the float modes keep their code in
+    // the instruction cache and their registers low enough for 5-8 resident
+    // CTAs, whose warps hide the table gathers and the HBM latency.  The
+    // quad's row and column advance by the grid stride without a division.
     const long long qpr = w >> 2;  // quads per row
     const long long nq = qpr * h;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long q0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; q0 < nq; q0 += 4 * stride) {
-      uint4* pa[4];
-      uint4 va[4], vb[4];
-#pragma unroll
-      for (int u = 0; u < 4; u++) {
-        long long q = q0 + u * stride;
-        pa[u] = nullptr;
-        if (q < nq) {
-          long long r = q / qpr, c = (q - r * qpr) << 2;
-          pa[u] = reinterpret_cast<uint4*>(a + (ay + r) * Wa + ax + c);
-          vb[u] = __ldcs(reinterpret_cast<const uint4*>(b + (by + r) * Wb + bx + c));
-          if (MODE != kOverwrite) va[u] = __ldcs(pa[u]);
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < 4; u++) {
-        if (!pa[u]) continue;
+    if (qpr > 0) {
+      const long long stride = (long long)gridDim.x * blockDim.x;
+      const long long sr = stride / qpr, sc = stride - sr * qpr;
+      long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+      long long r = q / qpr, c = q - r * qpr;
+      for (; q < nq; q += stride) {
+        uint4* pa = reinterpret_cast<uint4*>(a + (ay + r) * Wa + ax + (c << 2));
+        const uint4 vb = __ldcs(reinterpret_cast<const uint4*>(b + (by + r) * Wb + bx + (c << 2)));
         uint4 o;
         if (MODE == kOverwrite) {
-          o = vb[u];
+          o = vb;
         } else {
-          o.x = draw_px<MODE>(tbl, va[u].x, vb[u].x);
-          o.y = draw_px<MODE>(tbl, va[u].y, vb[u].y);
-          o.z = draw_px<MODE>(tbl, va[u].z, vb[u].z);
-          o.w = draw_px<MODE>(tbl, va[u].w, vb[u].w);
+          const uint4 va = __ldcs(pa);
+          o.x = draw_px<MODE>(tbl, va.x, vb.x);
+          o.y = draw_px<MODE>(tbl, va.y, vb.y);
+          o.z = draw_px<MODE>(tbl, va.z, vb.z);
+          o.w = draw_px<MODE>(tbl, va.w, vb.w);
         }
-        __stcs(pa[u], o);
+        __stcs(pa, o);
+        r += sr;
+        c += sc;
+        if (c >= qpr) {
+          c -= qpr;
+          r++;
+        }
       }
     }
     // leftover columns (w % 4)
@@ -145,6 +145,22 @@ DrawKernel draw_kernel(int mode) {
   return table[mode];
 }
 
+// Grid cap of a draw: whole waves of resident CTAs.  The modes with float
+// formulas or divisions (ColorBurn, ColorDodge, SoftLight, Hue, Saturation,
+// Color, Luminosity) run four waves, the rest two: the measured optimum of
+// 2048x2048 draws on 152 SMs, where one wave left SMs idle behind the slowest CTAs.
+static int draw_grid_cap(int mode, int nsm) {
+  static int resident[kNumBlends] = {0};
+  if (!resident[mode]) {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, draw_kernel(mode), 256, 0) != cudaSuccess || b < 1) b = 1;
+    resident[mode] = b;
+  }
+  const bool heavy = mode == kColorBurn || mode == kColorDodge || mode == kSoftLight || mode == kHue ||
+                     mode == kSaturation || mode == kColor || mode == kLuminosity;
+  return nsm * resident[mode] * (heavy ? 4 : 2);
+}
+
 void launch_draw(uint32_t* a, const uint32_t* b, long long Wa, long long Ha, long long Wb,
                  long long Hb, long long px, long long py, int mode, const uint8_t* tbl, int nsm,
                  cudaStream_t st) {
@@ -161,9 +177,9 @@ void launch_draw(uint32_t* a, const uint32_t* b, long long Wa, long long Ha, lon
   long long w = xEnd - xStart, h = yEnd - yStart;
   long long ax = xStart + px, ay = yStart + py;
   int vec = (Wa % 4 == 0) && (Wb % 4 == 0) && (ax % 4 == 0) && (xStart % 4 == 0);
-  long long work = vec ? ((w / 4) * h + 3) / 4 : w * h;
+  long long work = vec ? (w / 4) * h : w * h;
   long long blocks = (work + 255) / 256;
-  long long cap = (long long)nsm * 8;
+  long long cap = draw_grid_cap(mode, nsm);
   if (blocks > cap) blocks = cap;
   if (blocks < 1) blocks = 1;
   if (mode == kMask) {
