@@ -87,6 +87,21 @@ int pxg_image_stroke_path(pxg_image* image, const float* commands, int64_t n_com
 int pxg_image_draw(pxg_image* a, const pxg_image* b, int64_t translate_x, int64_t translate_y,
                    int blend_mode);
 
+/* draw(Image, Image, Mat3, BlendMode) with any transform
+ * src/pixie/images.nim:636-678 (bindings/bindings.nim:137): the minifyBy2 /
+ * magnifyBy2 pre-passes while the transform scales by 2 or more (or by 1/2 or
+ * less), then drawSmooth (:531-634, bilinear getRgbaSmooth :367-403) unless the
+ * transform is a whole-pixel translation, which takes blendRect as
+ * pxg_image_draw does.  transform is vmath's Mat3: 9 floats, column-major
+ * (translation in transform[6], transform[7]). */
+int pxg_image_draw_transform(pxg_image* a, const pxg_image* b, const float transform[9], int blend_mode);
+
+/* minifyBy2(Image, power) / magnifyBy2(Image, power)  src/pixie/images.nim:168-259:
+ * a new image (NULL on error: "Cannot minifyBy2 with negative power",
+ * "Cannot magnifyBy2 with negative power"); power 0 returns a copy. */
+pxg_image* pxg_image_minify_by2(const pxg_image* image, int power);
+pxg_image* pxg_image_magnify_by2(const pxg_image* image, int power);
+
 /* blur(Image, float32, Color)  src/pixie/images.nim:304-365
  * (bindings/bindings.nim:133) */
 int pxg_image_blur(pxg_image* image, float radius, const float out_of_bounds[4]);

@@ -1701,6 +1701,221 @@ static void blendRect(Image& a, const Image& b, int64_t px, int64_t py, int mode
   }
 }
 
+// ---------------------------------------------------------------------------
+// draw with a Mat3 transform  images.nim:636-678: the minify/magnify
+// pre-passes, then drawSmooth (:531-634) unless the transform is a whole-pixel
+// translation (blendRect).  vmath and bumpy are not vendored: Mat3 products,
+// the inverse and the line/segment intersection are restated from their
+// mathematical definitions (left-to-right sums), pinned by the reference's
+// smooth-draw masters.
+// ---------------------------------------------------------------------------
+static const float kHalf = 0.5f;  // images.nim:5  h
+
+// `mix`(ColorRGBX, ColorRGBX, float32)  common.nim:59-65
+static inline RGBX mix_c(RGBX a, RGBX b, float t) {
+  const uint32_t x = nim_u32(roundf(t * 255.0f));
+  return rgbx((a.r * (255 - x) + b.r * x + 127) / 255, (a.g * (255 - x) + b.g * x + 127) / 255,
+              (a.b * (255 - x) + b.b * x + 127) / 255, (a.a * (255 - x) + b.a * x + 127) / 255);
+}
+
+// vmath Mat3 * Mat3, column-major: (A B)[c][r] = A[0][r] B[c][0] + A[1][r] B[c][1] + A[2][r] B[c][2]
+static Mat3 matmul(const Mat3& A, const Mat3& B) {
+  Mat3 R;
+  for (int c = 0; c < 3; c++)
+    for (int r = 0; r < 3; r++)
+      R.m[c * 3 + r] = A.m[0 * 3 + r] * B.m[c * 3 + 0] + A.m[1 * 3 + r] * B.m[c * 3 + 1] +
+                       A.m[2 * 3 + r] * B.m[c * 3 + 2];
+  return R;
+}
+static Mat3 scale_m(float sx, float sy) { return Mat3{{sx, 0, 0, 0, sy, 0, 0, 0, 1}}; }
+
+// vmath Mat3 inverse: the adjugate over the determinant (cofactor expansion
+// along the first column of storage).  a(c, r) = m[c*3 + r].
+static Mat3 inverse_m(const Mat3& M) {
+  auto a = [&](int c, int r) { return M.m[c * 3 + r]; };
+  const float det = a(0, 0) * (a(1, 1) * a(2, 2) - a(2, 1) * a(1, 2)) -
+                    a(0, 1) * (a(1, 0) * a(2, 2) - a(1, 2) * a(2, 0)) +
+                    a(0, 2) * (a(1, 0) * a(2, 1) - a(1, 1) * a(2, 0));
+  const float invDet = 1.0f / det;
+  Mat3 R;
+  R.m[0] = (a(1, 1) * a(2, 2) - a(2, 1) * a(1, 2)) * invDet;
+  R.m[1] = (a(0, 2) * a(2, 1) - a(0, 1) * a(2, 2)) * invDet;
+  R.m[2] = (a(0, 1) * a(1, 2) - a(0, 2) * a(1, 1)) * invDet;
+  R.m[3] = (a(1, 2) * a(2, 0) - a(1, 0) * a(2, 2)) * invDet;
+  R.m[4] = (a(0, 0) * a(2, 2) - a(0, 2) * a(2, 0)) * invDet;
+  R.m[5] = (a(1, 0) * a(0, 2) - a(0, 0) * a(1, 2)) * invDet;
+  R.m[6] = (a(1, 0) * a(2, 1) - a(2, 0) * a(1, 1)) * invDet;
+  R.m[7] = (a(2, 0) * a(0, 1) - a(0, 0) * a(2, 1)) * invDet;
+  R.m[8] = (a(0, 0) * a(1, 1) - a(1, 0) * a(0, 1)) * invDet;
+  return R;
+}
+
+struct OwnedImage {
+  int64_t width = 0, height = 0;
+  std::vector<RGBX> px;
+  Image view() { return Image{width, height, px.data()}; }
+};
+static OwnedImage copy_image(const Image& b) {
+  OwnedImage o;
+  o.width = b.width;
+  o.height = b.height;
+  o.px.assign(b.data, b.data + b.len());
+  return o;
+}
+
+// minifyBy2 (power 1)  images.nim:168-232
+static OwnedImage minifyBy2(const Image& src) {
+  const bool oddW = (src.width % 2) != 0, oddH = (src.height % 2) != 0;
+  const int64_t ew = src.width / 2, eh = src.height / 2;
+  OwnedImage r;
+  r.width = oddW ? ew + 1 : ew;
+  r.height = oddH ? eh + 1 : eh;
+  r.px.assign((size_t)(r.width * r.height), RGBX{0, 0, 0, 0});
+  auto S = [&](int64_t x, int64_t y) { return src.data[src.idx(x, y)]; };
+  for (int64_t y = 0; y < eh; y++) {
+    for (int64_t x = 0; x < ew; x++) {
+      const RGBX a = S(2 * x, 2 * y), b = S(2 * x + 1, 2 * y), c = S(2 * x + 1, 2 * y + 1),
+                 d = S(2 * x, 2 * y + 1);
+      r.px[(size_t)(r.width * y + x)] =
+          rgbx(((uint32_t)a.r + b.r + c.r + d.r + 2) / 4, ((uint32_t)a.g + b.g + c.g + d.g + 2) / 4,
+               ((uint32_t)a.b + b.b + c.b + d.b + 2) / 4, ((uint32_t)a.a + b.a + c.a + d.a + 2) / 4);
+    }
+    if (oddW)
+      r.px[(size_t)(r.width * y + r.width - 1)] =
+          mul_f(mix_c(S(src.width - 1, 2 * y), S(src.width - 1, 2 * y + 1), 0.5f), 0.5f);
+  }
+  if (oddH) {
+    for (int64_t x = 0; x < ew; x++)
+      r.px[(size_t)(r.width * (r.height - 1) + x)] =
+          mul_f(mix_c(S(2 * x, src.height - 1), S(2 * x + 1, src.height - 1), 0.5f), 0.5f);
+    if (oddW) r.px[(size_t)(r.width * r.height - 1)] = mul_f(S(src.width - 1, src.height - 1), 0.25f);
+  }
+  return r;
+}
+
+// magnifyBy2 (power 1)  images.nim:234-259
+static OwnedImage magnifyBy2(const Image& src) {
+  OwnedImage r;
+  r.width = src.width * 2;
+  r.height = src.height * 2;
+  r.px.resize((size_t)(r.width * r.height));
+  for (int64_t y = 0; y < r.height; y++)
+    for (int64_t x = 0; x < r.width; x++) r.px[(size_t)(r.width * y + x)] = src.data[src.idx(x / 2, y / 2)];
+  return r;
+}
+
+// getRgbaSmooth (not wrapped)  images.nim:367-403; image[x, y] is transparent
+// outside the image (:37-40)
+static RGBX getRgbaSmooth(const Image& img, float x, float y) {
+  const float fx = floorf(x), fy = floorf(y);
+  const int64_t x0 = nim_int(fx), y0 = nim_int(fy);
+  const int64_t x1 = x0 == INT64_MAX ? x0 : x0 + 1, y1 = y0 == INT64_MAX ? y0 : y0 + 1;
+  const float xFractional = x - fx, yFractional = y - fy;
+  auto at = [&](int64_t px, int64_t py) {
+    return (px >= 0 && px < img.width && py >= 0 && py < img.height) ? img.data[img.idx(px, py)]
+                                                                      : RGBX{0, 0, 0, 0};
+  };
+  const RGBX x0y0 = at(x0, y0), x1y0 = at(x1, y0), x0y1 = at(x0, y1), x1y1 = at(x1, y1);
+  RGBX topMix = x0y0;
+  if (xFractional > 0 && !same(x0y0, x1y0)) topMix = mix_c(x0y0, x1y0, xFractional);
+  RGBX bottomMix = x0y1;
+  if (xFractional > 0 && !same(x0y1, x1y1)) bottomMix = mix_c(x0y1, x1y1, xFractional);
+  if (yFractional != 0 && !same(topMix, bottomMix)) return mix_c(topMix, bottomMix, yFractional);
+  return topMix;
+}
+
+// drawSmooth  images.nim:531-634
+static void drawSmooth(Image& a, const Image& b, const Mat3& transform, int mode) {
+  const Vec2 corners[4] = {mul(transform, v2(0, 0)), mul(transform, v2((float)b.width, 0)),
+                           mul(transform, v2((float)b.width, (float)b.height)),
+                           mul(transform, v2(0, (float)b.height))};
+  const Segment perimeter[4] = {{corners[0], corners[1]}, {corners[1], corners[2]},
+                                {corners[2], corners[3]}, {corners[3], corners[0]}};
+  const Mat3 inv = inverse_m(transform);
+  const Vec2 p = mul(inv, v2(0 + kHalf, 0 + kHalf));
+  const Vec2 dx = mul(inv, v2(1 + kHalf, 0 + kHalf)) - p;
+  const Vec2 dy = mul(inv, v2(0 + kHalf, 1 + kHalf)) - p;
+  int64_t yStart = a.height, yEnd = 0;
+  for (const Segment& sg : perimeter) {
+    yStart = std::min<int64_t>(yStart, nim_int(floorf(sg.at.y)));
+    yEnd = std::max<int64_t>(yEnd, nim_int(ceilf(sg.at.y)));
+  }
+  yStart = std::clamp<int64_t>(yStart, 0, a.height);
+  yEnd = std::clamp<int64_t>(yEnd, 0, a.height);
+  const RGBX zero{0, 0, 0, 0};
+  if (mode == MaskBlend && yStart > 0) fillUnsafe(a, zero, 0, yStart * a.width);
+  for (int64_t y = yStart; y < yEnd; y++) {
+    float xMin = (float)a.width, xMax = 0.0f;
+    for (float yOffset : {0.0f, 1.0f}) {
+      const Vec2 l0 = v2(-1000, (float)y + yOffset), l1 = v2(1000, (float)y + yOffset);
+      for (const Segment& sg : perimeter) {
+        Vec2 at;
+        if (intersectSegLine(sg, l0, l1, at) && sg.to != at) {
+          xMin = nmin(xMin, at.x);
+          xMax = nmax(xMax, at.x);
+        }
+      }
+    }
+    const int64_t xStart = std::clamp<int64_t>(nim_int(floorf(xMin)), 0, a.width);
+    const int64_t xEnd = std::clamp<int64_t>(nim_int(ceilf(xMax)), 0, a.width);
+    if (xEnd - xStart == 0) continue;
+    // a row the perimeter does not cross has xEnd < xStart: its sample loop is
+    // empty; MaskBlend still clears [0, xStart) and [xEnd, width), the whole
+    // row (OverwriteBlend's copyMem of a negative length, which fails in the
+    // reference, copies nothing here)
+    Vec2 srcPos = p + dx * (float)xStart + dy * (float)y;
+    srcPos = v2(srcPos.x - kHalf, srcPos.y - kHalf);
+    RGBX* line = a.data + a.idx(0, y);
+    if (mode == MaskBlend && xStart > 0) fillUnsafe(a, zero, a.idx(0, y), xStart);
+    for (int64_t x = xStart; x < xEnd; x++) {
+      const RGBX s = getRgbaSmooth(b, srcPos.x, srcPos.y);
+      srcPos = srcPos + dx;
+      line[x] = mode == OverwriteBlend ? s : blend_px(mode, line[x], s);
+    }
+    if (mode == MaskBlend && a.width - xEnd > 0) fillUnsafe(a, zero, a.idx(xEnd, y), a.width - xEnd);
+  }
+  if (mode == MaskBlend && a.height - yEnd > 0) fillUnsafe(a, zero, a.idx(0, yEnd), (a.height - yEnd) * a.width);
+}
+
+// draw(a, b, transform, blendMode)  images.nim:636-678
+static void drawTransform(Image& a, const Image& bIn, Mat3 transform, int mode) {
+  const Mat3 inv = inverse_m(transform);
+  Vec2 p = mul(inv, v2(0 + kHalf, 0 + kHalf));
+  Vec2 dx = mul(inv, v2(1 + kHalf, 0 + kHalf)) - p;
+  Vec2 dy = mul(inv, v2(0 + kHalf, 1 + kHalf)) - p;
+  float filterBy2 = nmax(length(dx), length(dy));
+  // an infinite filterBy2 (a singular transform) would halve forever in the
+  // reference's minify loop; raise instead
+  if (std::isinf(filterBy2)) throw PixieError("draw transform is not invertible");
+  OwnedImage cur = copy_image(bIn);
+  while (filterBy2 >= 2.0f) {
+    cur = minifyBy2(cur.view());
+    p = p / 2;
+    dx = dx / 2;
+    dy = dy / 2;
+    filterBy2 /= 2;
+    transform = matmul(transform, scale_m(2, 2));
+  }
+  while (filterBy2 <= 0.5f) {
+    if (cur.width * cur.height > ((int64_t)1 << 30))
+      throw PixieError("draw would magnify the source image beyond 2^32 bytes");
+    cur = magnifyBy2(cur.view());
+    p = p * 2;
+    dx = dx * 2;
+    dy = dy * 2;
+    filterBy2 *= 2;
+    transform = matmul(transform, scale_m(1.0f / 2, 1.0f / 2));
+  }
+  const bool hasRotationOrScaling = !(dx == v2(1, 0) && dy == v2(0, 1));
+  const bool smooth = !(length(dx) == 1.0f && length(dy) == 1.0f && fractional(transform.m[6]) == 0.0f &&
+                        fractional(transform.m[7]) == 0.0f);
+  Image b = cur.view();
+  if (hasRotationOrScaling || smooth)
+    drawSmooth(a, b, transform, mode);
+  else
+    blendRect(a, b, nim_i32(transform.m[6]), nim_i32(transform.m[7]), mode);
+}
+
 // gaussianKernel  internal.nim:17-34.  `s` and the exp() argument are float32;
 // `1 / sqrt(2 * PI * s^2) * exp(...)` meets the float64 constant PI and is
 // float64; `total` is a float64 variable and
@@ -1926,6 +2141,32 @@ int pxo_draw(uint8_t* a, int64_t aw, int64_t ah, const uint8_t* b, int64_t bw, i
   } catch (const std::exception& e) {
     return fail(e);
   }
+}
+
+int pxo_draw_transform(uint8_t* a, int64_t aw, int64_t ah, const uint8_t* b, int64_t bw, int64_t bh,
+                       const float* mat3, int blend) {
+  try {
+    Image A{aw, ah, (RGBX*)a};
+    Image B{bw, bh, (RGBX*)b};
+    Mat3 M;
+    memcpy(M.m, mat3, sizeof(M.m));
+    drawTransform(A, B, M, blend);
+    return 0;
+  } catch (const std::exception& e) {
+    return fail(e);
+  }
+}
+
+// minifyBy2 / magnifyBy2 with power 1 into a caller buffer of the result size
+int pxo_minify_by2(const uint8_t* src, int64_t w, int64_t h, uint8_t* out) {
+  OwnedImage r = minifyBy2(Image{w, h, (RGBX*)src});
+  memcpy(out, r.px.data(), r.px.size() * 4);
+  return 0;
+}
+int pxo_magnify_by2(const uint8_t* src, int64_t w, int64_t h, uint8_t* out) {
+  OwnedImage r = magnifyBy2(Image{w, h, (RGBX*)src});
+  memcpy(out, r.px.data(), r.px.size() * 4);
+  return 0;
 }
 
 int pxo_blend_pixels(int blend, const uint8_t* backdrop, const uint8_t* source, uint8_t* out,

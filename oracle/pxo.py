@@ -49,6 +49,9 @@ def lib():
         L.pxo_stroke_shapes.restype = I64
         L.pxo_draw.argtypes = [P, I64, I64, P, I64, I64, I64, I64, I]
         L.pxo_blend_pixels.argtypes = [I, P, P, P, I64]
+        L.pxo_draw_transform.argtypes = [P, I64, I64, P, I64, I64, P, I]
+        L.pxo_minify_by2.argtypes = [P, I64, I64, P]
+        L.pxo_magnify_by2.argtypes = [P, I64, I64, P]
         L.pxo_fill.argtypes = [P, I64, I64, P]
         L.pxo_color_to_rgbx.argtypes = [P, P]
         L.pxo_blur.argtypes = [P, I64, I64, F, P]
@@ -139,6 +142,28 @@ def stroke_shapes(cmds, mat=None, width=1.0, cap=0, join=0, miter_limit=4.0, das
 def draw(a, b, tx=0, ty=0, blend=0):
     _check(lib().pxo_draw(_p(a), a.shape[1], a.shape[0], _p(b), b.shape[1], b.shape[0],
                           int(tx), int(ty), int(blend)))
+
+
+def draw_transform(a, b, mat, blend=0):
+    """draw(a, b, transform, blendMode); mat is vmath's Mat3 as 9 floats,
+    column-major (translation in mat[6], mat[7]), as fill_path takes it."""
+    m = _f32(mat, 9)
+    _check(lib().pxo_draw_transform(_p(a), a.shape[1], a.shape[0], _p(b), b.shape[1], b.shape[0],
+                                    _p(m), int(blend)))
+
+
+def minify_by2(img):
+    h, w = img.shape[:2]
+    out = np.zeros(((h + 1) // 2, (w + 1) // 2, 4), np.uint8)
+    lib().pxo_minify_by2(_p(np.ascontiguousarray(img)), w, h, _p(out))
+    return out
+
+
+def magnify_by2(img):
+    h, w = img.shape[:2]
+    out = np.zeros((2 * h, 2 * w, 4), np.uint8)
+    lib().pxo_magnify_by2(_p(np.ascontiguousarray(img)), w, h, _p(out))
+    return out
 
 
 def blend_pixels(blend, backdrop, source):

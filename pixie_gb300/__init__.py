@@ -95,6 +95,11 @@ def lib():
         L.pxg_image_fill_path.argtypes = [P, P, I64, P, F, I, P, I]
         L.pxg_image_stroke_path.argtypes = [P, P, I64, P, F, I, P, F, I, I, F, P, I64]
         L.pxg_image_draw.argtypes = [P, P, I64, I64, I]
+        L.pxg_image_draw_transform.argtypes = [P, P, P, I]
+        L.pxg_image_minify_by2.argtypes = [P, I]
+        L.pxg_image_minify_by2.restype = P
+        L.pxg_image_magnify_by2.argtypes = [P, I]
+        L.pxg_image_magnify_by2.restype = P
         L.pxg_image_blur.argtypes = [P, F, P]
         L.pxg_image_spread.argtypes = [P, F]
         L.pxg_image_shadow.argtypes = [P, F, F, F, F, P]
@@ -265,10 +270,31 @@ class Image:
                                            _ptr(d), len(dashes)))
 
     def draw(self, b: "Image", translate_xy=(0, 0), blend_mode=BlendMode.NormalBlend):
+        """draw(a, b, translate(x, y), mode): whole-pixel offsets take blendRect,
+        fractional ones drawSmooth (images.nim:636-678)."""
         tx, ty = translate_xy
         if tx != int(tx) or ty != int(ty):
-            raise PixieError("only integer translations take draw's blendRect path")
+            self.draw_transform(b, [1, 0, 0, 0, 1, 0, tx, ty, 1], blend_mode)
+            return
         _check(lib().pxg_image_draw(self._h, b._h, int(tx), int(ty), int(blend_mode)))
+
+    def draw_transform(self, b: "Image", transform, blend_mode=BlendMode.NormalBlend):
+        """draw(a, b, transform: Mat3, mode); transform is 9 floats, column-major
+        like vmath's Mat3 (translation in [6], [7])."""
+        m = np.ascontiguousarray(np.asarray(transform, dtype=np.float32).reshape(9))
+        _check(lib().pxg_image_draw_transform(self._h, b._h, _ptr(m), int(blend_mode)))
+
+    def minify_by2(self, power: int = 1) -> "Image":
+        h = lib().pxg_image_minify_by2(self._h, int(power))
+        if not h:
+            raise PixieError(lib().pxg_take_error().decode())
+        return Image(0, 0, _handle=h)
+
+    def magnify_by2(self, power: int = 1) -> "Image":
+        h = lib().pxg_image_magnify_by2(self._h, int(power))
+        if not h:
+            raise PixieError(lib().pxg_take_error().decode())
+        return Image(0, 0, _handle=h)
 
     def blur(self, radius: float, out_of_bounds=(0, 0, 0, 0)):
         _check(lib().pxg_image_blur(self._h, float(radius), _ptr(_color(out_of_bounds))))

@@ -118,6 +118,15 @@ void launch_draw_masks(int tile, uint32_t* page, long long W, long long H, const
 size_t rows_smem_fast();
 size_t rows_smem_wide();
 int rows_warps_fast();
+struct SmoothArgs {
+  float px, py, dxx, dxy, dyx, dyy;
+  float seg[4][4];
+  long long yStart, yEnd;
+};
+void launch_minify2(const uint32_t* src, long long w, long long h, uint32_t* out, int nsm, cudaStream_t st);
+void launch_magnify2(const uint32_t* src, long long w, long long h, uint32_t* out, int nsm, cudaStream_t st);
+void launch_draw_smooth(uint32_t* a, long long W, long long H, const uint32_t* b, long long bw, long long bh,
+                        const SmoothArgs& g, int mode, const uint8_t* tbl, int nsm, cudaStream_t st);
 void launch_draw(uint32_t* a, const uint32_t* b, long long Wa, long long Ha, long long Wb,
                  long long Hb, long long px, long long py, int mode, const uint8_t* tbl, int nsm,
                  cudaStream_t st);
@@ -225,6 +234,8 @@ struct Ctx {
   long long ovf_cap = 0;
   long long* xcl = nullptr;
   long long xcl_cap = 0;
+  uint32_t* sm_buf[2] = {nullptr, nullptr};  // minify/magnify pre-pass images (ping-pong)
+  long long sm_cap[2] = {0, 0};
   uint8_t* fsteps = nullptr;  // flattening step records (fill setup)
   long long fsteps_cap = 0;
   // upload area: jobs | counters | prims (device and pinned mirror)
@@ -1884,6 +1895,208 @@ int pxg_image_draw(pxg_image* a, const pxg_image* b, int64_t tx, int64_t ty, int
   });
 }
 
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// draw with a Mat3 (images.nim:636-678).  The host does the reference's float32
+// geometry (inverse, movement vectors, the minify/magnify decisions, the
+// perimeter and row range of drawSmooth) in the same operations and order;
+// the device resamples.  vmath's Mat3 is column-major: m[c * 3 + r], the
+// translation in m[6], m[7].
+// ---------------------------------------------------------------------------
+namespace {
+struct M3 {
+  float m[9];
+};
+struct V {
+  float x, y;
+};
+inline V m3v(const M3& M, float x, float y) {  // Mat3 * Vec2
+  return V{M.m[0] * x + M.m[3] * y + M.m[6], M.m[1] * x + M.m[4] * y + M.m[7]};
+}
+inline V vsub(V a, V b) { return V{a.x - b.x, a.y - b.y}; }
+inline float vlen(V v) { return sqrtf(v.x * v.x + v.y * v.y); }
+inline float fnmax(float x, float y) { return y <= x ? x : y; }
+inline float frac_abs(float v) {  // vmath fractional
+  const float a = fabsf(v);
+  return a - floorf(a);
+}
+inline int64_t h_nim_int(float f) {
+  if (!(f >= -9223372036854775808.0f && f < 9223372036854775808.0f)) return INT64_MIN;
+  return (int64_t)f;
+}
+inline int32_t h_nim_i32(float f) {
+  if (!(f >= -2147483648.0f && f < 2147483648.0f)) return INT32_MIN;
+  return (int32_t)f;
+}
+M3 m3mul(const M3& A, const M3& B) {
+  M3 R;
+  for (int c = 0; c < 3; c++)
+    for (int r = 0; r < 3; r++)
+      R.m[c * 3 + r] = A.m[r] * B.m[c * 3] + A.m[3 + r] * B.m[c * 3 + 1] + A.m[6 + r] * B.m[c * 3 + 2];
+  return R;
+}
+M3 m3inv(const M3& M) {  // the adjugate over the determinant
+  auto a = [&](int c, int r) { return M.m[c * 3 + r]; };
+  const float det = a(0, 0) * (a(1, 1) * a(2, 2) - a(2, 1) * a(1, 2)) -
+                    a(0, 1) * (a(1, 0) * a(2, 2) - a(1, 2) * a(2, 0)) +
+                    a(0, 2) * (a(1, 0) * a(2, 1) - a(1, 1) * a(2, 0));
+  const float id = 1.0f / det;
+  return M3{{(a(1, 1) * a(2, 2) - a(2, 1) * a(1, 2)) * id, (a(0, 2) * a(2, 1) - a(0, 1) * a(2, 2)) * id,
+             (a(0, 1) * a(1, 2) - a(0, 2) * a(1, 1)) * id, (a(1, 2) * a(2, 0) - a(1, 0) * a(2, 2)) * id,
+             (a(0, 0) * a(2, 2) - a(0, 2) * a(2, 0)) * id, (a(1, 0) * a(0, 2) - a(0, 0) * a(1, 2)) * id,
+             (a(1, 0) * a(2, 1) - a(2, 0) * a(1, 1)) * id, (a(2, 0) * a(0, 1) - a(0, 0) * a(2, 1)) * id,
+             (a(0, 0) * a(1, 1) - a(1, 0) * a(0, 1)) * id}};
+}
+constexpr float kH = 0.5f;  // images.nim:5
+
+// One level of minifyBy2 / magnifyBy2 from src into pre-pass buffer k.
+const uint32_t* resample_level(const uint32_t* src, int64_t& w, int64_t& h, bool minify, int k) {
+  const int64_t nw = minify ? (w + 1) / 2 : w * 2, nh = minify ? (h + 1) / 2 : h * 2;
+  dev_grow(g.sm_buf[k], g.sm_cap[k], nw * nh);
+  if (minify)
+    launch_minify2(src, w, h, g.sm_buf[k], g.nsm, g.stream);
+  else
+    launch_magnify2(src, w, h, g.sm_buf[k], g.nsm, g.stream);
+  w = nw;
+  h = nh;
+  return g.sm_buf[k];
+}
+
+void draw_transform(pxg_image* a, const pxg_image* b, M3 T, int blend) {
+  const M3 inv0 = m3inv(T);
+  V p = m3v(inv0, 0 + kH, 0 + kH);
+  V dx = vsub(m3v(inv0, 1 + kH, 0 + kH), p);
+  V dy = vsub(m3v(inv0, 0 + kH, 1 + kH), p);
+  float filterBy2 = fnmax(vlen(dx), vlen(dy));
+  // an infinite filterBy2 (a singular transform) would halve forever in the
+  // reference's minify loop; raise instead
+  if (std::isinf(filterBy2)) throw ApiError{"draw transform is not invertible"};
+  const uint32_t* src = (const uint32_t*)b->data;
+  int64_t bw = b->width, bh = b->height;
+  int k = 0;
+  while (filterBy2 >= 2.0f) {
+    src = resample_level(src, bw, bh, true, k);
+    k ^= 1;
+    p = V{p.x / 2, p.y / 2};
+    dx = V{dx.x / 2, dx.y / 2};
+    dy = V{dy.x / 2, dy.y / 2};
+    filterBy2 /= 2;
+    T = m3mul(T, M3{{2, 0, 0, 0, 2, 0, 0, 0, 1}});
+  }
+  while (filterBy2 <= 0.5f) {
+    if (bw * bh > ((int64_t)1 << 30)) throw ApiError{"draw would magnify the source image beyond 2^32 bytes"};
+    src = resample_level(src, bw, bh, false, k);
+    k ^= 1;
+    p = V{p.x * 2, p.y * 2};
+    dx = V{dx.x * 2, dx.y * 2};
+    dy = V{dy.x * 2, dy.y * 2};
+    filterBy2 *= 2;
+    T = m3mul(T, M3{{1.0f / 2, 0, 0, 0, 1.0f / 2, 0, 0, 0, 1}});
+  }
+  const bool hasRotationOrScaling = !(dx.x == 1 && dx.y == 0 && dy.x == 0 && dy.y == 1);
+  const bool smooth = !(vlen(dx) == 1.0f && vlen(dy) == 1.0f && frac_abs(T.m[6]) == 0.0f && frac_abs(T.m[7]) == 0.0f);
+  if (!hasRotationOrScaling && !smooth) {
+    launch_draw((uint32_t*)a->data, src, a->width, a->height, bw, bh, h_nim_i32(T.m[6]), h_nim_i32(T.m[7]), blend,
+                g.tbl, g.nsm, g.stream);
+    return;
+  }
+  // drawSmooth  images.nim:531-561
+  const V c[4] = {m3v(T, 0, 0), m3v(T, (float)bw, 0), m3v(T, (float)bw, (float)bh), m3v(T, 0, (float)bh)};
+  SmoothArgs G;
+  for (int i = 0; i < 4; i++) {
+    G.seg[i][0] = c[i].x;
+    G.seg[i][1] = c[i].y;
+    G.seg[i][2] = c[(i + 1) & 3].x;
+    G.seg[i][3] = c[(i + 1) & 3].y;
+  }
+  const M3 inv = m3inv(T);
+  const V sp = m3v(inv, 0 + kH, 0 + kH);
+  const V sdx = vsub(m3v(inv, 1 + kH, 0 + kH), sp);
+  const V sdy = vsub(m3v(inv, 0 + kH, 1 + kH), sp);
+  G.px = sp.x;
+  G.py = sp.y;
+  G.dxx = sdx.x;
+  G.dxy = sdx.y;
+  G.dyx = sdy.x;
+  G.dyy = sdy.y;
+  int64_t yStart = a->height, yEnd = 0;
+  for (int i = 0; i < 4; i++) {
+    yStart = std::min<int64_t>(yStart, h_nim_int(floorf(c[i].y)));
+    yEnd = std::max<int64_t>(yEnd, h_nim_int(ceilf(c[i].y)));
+  }
+  G.yStart = std::clamp<int64_t>(yStart, 0, a->height);
+  G.yEnd = std::clamp<int64_t>(yEnd, 0, a->height);
+  launch_draw_smooth((uint32_t*)a->data, a->width, a->height, src, bw, bh, G, blend, g.tbl, g.nsm, g.stream);
+}
+
+pxg_image* resampled_copy(const pxg_image* im, int power, bool minify) {
+  if (power < 0)
+    throw ApiError{minify ? "Cannot minifyBy2 with negative power" : "Cannot magnifyBy2 with negative power"};
+  int64_t w = im->width, h = im->height;
+  for (int i = 0; i < power; i++) {
+    w = minify ? (w + 1) / 2 : w * 2;
+    h = minify ? (h + 1) / 2 : h * 2;
+    if (w * h > ((int64_t)1 << 31)) throw ApiError{"Image too large"};
+  }
+  pxg_image* res = pxg_new_image(w, h);
+  if (!res) throw ApiError{std::string(t_err)};
+  const uint32_t* src = (const uint32_t*)im->data;
+  w = im->width;
+  h = im->height;
+  int k = 0;
+  for (int i = 0; i < power; i++) {
+    if (i == power - 1) {  // the last level straight into the result
+      if (minify)
+        launch_minify2(src, w, h, (uint32_t*)res->data, g.nsm, g.stream);
+      else
+        launch_magnify2(src, w, h, (uint32_t*)res->data, g.nsm, g.stream);
+    } else {
+      src = resample_level(src, w, h, minify, k);
+      k ^= 1;
+    }
+  }
+  if (power == 0)
+    CU(cudaMemcpyAsync(res->data, im->data, (size_t)(w * h * 4), cudaMemcpyDeviceToDevice, g.stream));
+  return res;
+}
+}  // namespace
+
+extern "C" {
+
+int pxg_image_draw_transform(pxg_image* a, const pxg_image* b, const float* mat3, int blend) {
+  return guarded([&] {
+    check_image(a);
+    check_image(b);
+    check_blend(blend);
+    if (!mat3) throw ApiError{"transform is null"};
+    M3 T;
+    memcpy(T.m, mat3, sizeof(T.m));
+    Timed t;
+    draw_transform(a, b, T, blend);
+    CU(cudaGetLastError());
+    t.done();
+  });
+}
+
+static pxg_image* resampled(const pxg_image* im, int power, bool minify) {
+  pxg_image* out = nullptr;
+  guarded([&] {
+    check_image(im);
+    Timed t;
+    pxg_image* res = resampled_copy(im, power, minify);
+    if (cudaGetLastError() != cudaSuccess) {
+      pxg_image_free(res);
+      throw ApiError{"CUDA error in minifyBy2/magnifyBy2"};
+    }
+    t.done();
+    out = res;
+  });
+  return out;
+}
+pxg_image* pxg_image_minify_by2(const pxg_image* im, int power) { return resampled(im, power, true); }
+pxg_image* pxg_image_magnify_by2(const pxg_image* im, int power) { return resampled(im, power, false); }
 
 int pxg_image_blur(pxg_image* im, float radius, const float* oob) {
   return guarded([&] {

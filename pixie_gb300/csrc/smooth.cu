@@ -1,0 +1,265 @@
+// draw with a Mat3 transform (src/pixie/images.nim:636-678): the minifyBy2 /
+// magnifyBy2 pre-passes (:168-259) and drawSmooth (:531-634) with bilinear
+// sampling by getRgbaSmooth (:367-403) and `mix` (common.nim:59-65).
+//
+// k_minify2 / k_magnify2 are HBM-bound: one output pixel per thread (minify,
+// four 4-byte loads of the 2x2 block), one source pixel per thread (magnify,
+// two 8-byte stores of its 2x2 block: both rows start at an even pixel offset,
+// 2y * 2w and (2y + 1) * 2w).
+//
+// k_draw_smooth: a warp owns one destination row.  Eight lanes intersect the
+// row's two scanlines with the four perimeter segments; lane 0 folds the hits
+// into the row's x range in the reference's order (so even NaN geometry gives
+// the same range).  The reference walks the sample position along the row by
+// repeated addition (srcPos += dx); that sum is sequential in float32, so every
+// lane of the warp runs the same chain and lane k keeps the k-th position of
+// each 32-pixel chunk: the positions are the reference's floats exactly.  Each
+// lane then samples its pixel (four gathers, two or three byte-wise mixes) and
+// blends it into the destination with the mode's blender.
+#include <cstdint>
+
+#include "pxg_device.cuh"
+
+namespace pxg {
+
+void note_launch();
+
+namespace {
+
+// `mix`(ColorRGBX, ColorRGBX, float32)  common.nim:59-65
+__device__ __forceinline__ uint32_t mix_px(uint32_t a, uint32_t b, float t) {
+  const uint32_t x = nim_u32(roundf(t * 255.0f));
+  const Px p = unpack(a), q = unpack(b);
+  return pack((p.r * (255 - x) + q.r * x + 127) / 255, (p.g * (255 - x) + q.g * x + 127) / 255,
+              (p.b * (255 - x) + q.b * x + 127) / 255, (p.a * (255 - x) + q.a * x + 127) / 255);
+}
+// mix(a, b, 0.5): round(0.5 * 255) = round(127.5) = 128 (half away from zero)
+__device__ __forceinline__ uint32_t mix_half(uint32_t a, uint32_t b) {
+  const Px p = unpack(a), q = unpack(b);
+  return pack((p.r * 127 + q.r * 128 + 127) / 255, (p.g * 127 + q.g * 128 + 127) / 255,
+              (p.b * 127 + q.b * 128 + 127) / 255, (p.a * 127 + q.a * 128 + 127) / 255);
+}
+// c * opacity for opacity 0.5 (x = 128) and 0.25 (x = round(63.75) = 64)
+__device__ __forceinline__ uint32_t mul_x(uint32_t c, uint32_t x) {
+  const Px p = unpack(c);
+  return pack((p.r * x + 127) / 255, (p.g * x + 127) / 255, (p.b * x + 127) / 255, (p.a * x + 127) / 255);
+}
+
+// minifyBy2 with power 1: out is ((w + 1) / 2) x ((h + 1) / 2)
+__global__ void __launch_bounds__(256) k_minify2(const uint32_t* __restrict__ src, long long w, long long h,
+                                                 uint32_t* __restrict__ out) {
+  const long long ew = w / 2, eh = h / 2, rw = (w + 1) / 2, rh = (h + 1) / 2;
+  const long long n = rw * rh;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long y = i / rw, x = i - y * rw;
+    uint32_t v;
+    if (x < ew && y < eh) {  // 4-byte loads: an odd width leaves the bottom row's pairs 4-byte aligned only
+      const uint32_t* t = src + 2 * y * w + 2 * x;
+      const uint32_t* u = t + w;
+      const Px a = unpack(t[0]), bb = unpack(t[1]), c = unpack(u[1]), d = unpack(u[0]);
+      v = pack((a.r + bb.r + c.r + d.r + 2) / 4, (a.g + bb.g + c.g + d.g + 2) / 4,
+               (a.b + bb.b + c.b + d.b + 2) / 4, (a.a + bb.a + c.a + d.a + 2) / 4);
+    } else if (y < eh) {  // odd width: the last column  images.nim:201-207
+      v = mul_x(mix_half(src[2 * y * w + w - 1], src[(2 * y + 1) * w + w - 1]), 128);
+    } else if (x < ew) {  // odd height: the last row  :209-216
+      v = mul_x(mix_half(src[(h - 1) * w + 2 * x], src[(h - 1) * w + 2 * x + 1]), 128);
+    } else {              // both odd: the corner  :218-220
+      v = mul_x(src[(h - 1) * w + w - 1], 64);
+    }
+    out[i] = v;
+  }
+}
+
+// magnifyBy2 with power 1: out is 2w x 2h
+__global__ void __launch_bounds__(256) k_magnify2(const uint32_t* __restrict__ src, long long w, long long h,
+                                                  uint32_t* __restrict__ out) {
+  const long long n = w * h;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long y = i / w, x = i - y * w;
+    const uint32_t v = src[i];
+    const uint2 vv = make_uint2(v, v);
+    *reinterpret_cast<uint2*>(out + 2 * y * (2 * w) + 2 * x) = vv;
+    *reinterpret_cast<uint2*>(out + (2 * y + 1) * (2 * w) + 2 * x) = vv;
+  }
+}
+
+}  // namespace
+
+// Geometry of one drawSmooth: p, dx, dy of the inverse transform, the four
+// perimeter segments (at.x, at.y, to.x, to.y) and the row range.
+struct SmoothArgs {
+  float px, py, dxx, dxy, dyx, dyy;
+  float seg[4][4];
+  long long yStart, yEnd;
+};
+
+namespace {
+
+// bumpy intersects(Line, Segment): the segment's parameter t in [0, 1], the
+// point taken on the segment (the same form as the band clipping's)
+__device__ __forceinline__ bool scan_hit(const float* s, float ly, float& ax, float& ay) {
+  const float s1x = s[2] - s[0], s1y = s[3] - s[1];
+  const float s2x = 1000.0f - -1000.0f, s2y = ly - ly;
+  const float den = (-s2x * s1y + s1x * s2y);
+  const float t = (s2x * (s[1] - ly) - s2y * (s[0] - -1000.0f)) / den;
+  if (t >= 0 && t <= 1) {
+    ax = s[0] + s1x * t;
+    ay = s[1] + s1y * t;
+    return true;
+  }
+  return false;
+}
+
+// image[x, y]: transparent outside  images.nim:37-40
+__device__ __forceinline__ uint32_t px_at(const uint32_t* __restrict__ b, long long bw, long long bh, long long x,
+                                          long long y) {
+  return (x >= 0 && x < bw && y >= 0 && y < bh) ? __ldg(b + y * bw + x) : 0u;
+}
+
+// getRgbaSmooth (not wrapped)  images.nim:367-403
+__device__ __forceinline__ uint32_t sample_smooth(const uint32_t* __restrict__ b, long long bw, long long bh, float x,
+                                                  float y) {
+  const float fx = floorf(x), fy = floorf(y);
+  const long long x0 = nim_int(fx), y0 = nim_int(fy);
+  const long long x1 = x0 == 9223372036854775807LL ? x0 : x0 + 1, y1 = y0 == 9223372036854775807LL ? y0 : y0 + 1;
+  const float xf = x - fx, yf = y - fy;
+  const uint32_t x0y0 = px_at(b, bw, bh, x0, y0), x1y0 = px_at(b, bw, bh, x1, y0);
+  const uint32_t x0y1 = px_at(b, bw, bh, x0, y1), x1y1 = px_at(b, bw, bh, x1, y1);
+  uint32_t top = x0y0;
+  if (xf > 0 && x0y0 != x1y0) top = mix_px(x0y0, x1y0, xf);
+  uint32_t bottom = x0y1;
+  if (xf > 0 && x0y1 != x1y1) bottom = mix_px(x0y1, x1y1, xf);
+  if (yf != 0 && top != bottom) return mix_px(top, bottom, yf);
+  return top;
+}
+
+template <int MODE>
+__device__ __forceinline__ uint32_t smooth_blend(const uint8_t* tbl, uint32_t a, uint32_t s) {
+  if (MODE == kNormal) return blendNormal(a, s);
+  if (MODE == kOverwrite) return s;
+  if (MODE == kMask) return blendMaskPx(a, s);
+  if (MODE == kColorBurn) return blendBurnDodge<true>(tbl, a, s);
+  if (MODE == kColorDodge) return blendBurnDodge<false>(tbl, a, s);
+  if (MODE == kSoftLight || MODE == kHue || MODE == kSaturation || MODE == kColor || MODE == kLuminosity)
+    return blendFloatT<MODE>(tbl, a, s);
+  return blend_px(MODE, tbl, a, s);
+}
+
+// Rows [rowLo, rowHi) of the destination, one warp per row.  MaskBlend runs
+// over every row (the rows outside [yStart, yEnd) are cleared); the others
+// over [yStart, yEnd) only.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_draw_smooth(uint32_t* __restrict__ a, long long W, long long H,
+                                                     const uint32_t* __restrict__ b, long long bw, long long bh,
+                                                     SmoothArgs g, long long rowLo, long long rowHi,
+                                                     const uint8_t* tbl) {
+  const int lane = threadIdx.x & 31;
+  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long y = rowLo + (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); y < rowHi; y += warps) {
+    uint32_t* line = a + y * W;
+    if (y < g.yStart || y >= g.yEnd) {  // MaskBlend only: rows the image does not reach
+      for (long long x = lane; x < W; x += 32) line[x] = 0u;
+      continue;
+    }
+    // the row's x range  images.nim:567-582
+    float hx = 0.0f;
+    bool hit = false;
+    if (lane < 8) {
+      const float ly = (float)y + (float)(lane >> 2);
+      const float* s = g.seg[lane & 3];
+      float ax = 0.0f, ay = 0.0f;
+      hit = scan_hit(s, ly, ax, ay) && !(s[2] == ax && s[3] == ay);
+      hx = ax;
+    }
+    const unsigned hits = __ballot_sync(0xffffffffu, hit);
+    float xMin = (float)W, xMax = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      const float v = __shfl_sync(0xffffffffu, hx, k);
+      if (hits >> k & 1u) {
+        xMin = nmin(xMin, v);
+        xMax = nmax(xMax, v);
+      }
+    }
+    long long xStart = nim_int(floorf(xMin)), xEnd = nim_int(ceilf(xMax));
+    xStart = xStart < 0 ? 0 : (xStart > W ? W : xStart);
+    xEnd = xEnd < 0 ? 0 : (xEnd > W ? W : xEnd);
+    if (xEnd - xStart == 0) continue;
+    if (MODE == kMask) {  // :612-620: clear [0, xStart) and [xEnd, W)
+      for (long long x = lane; x < xStart; x += 32) line[x] = 0u;
+      for (long long x = (xEnd > 0 ? xEnd : 0) + lane; x < W; x += 32) line[x] = 0u;
+    }
+    if (xEnd <= xStart) continue;
+    // srcPos = p + dx * xStart + dy * y, less h; then srcPos += dx per pixel
+    float cx = (g.px + g.dxx * (float)xStart) + g.dyx * (float)y;
+    float cy = (g.py + g.dxy * (float)xStart) + g.dyy * (float)y;
+    cx = cx - 0.5f;
+    cy = cy - 0.5f;
+    for (long long x0 = xStart; x0 < xEnd; x0 += 32) {
+      float mx = 0.0f, my = 0.0f;
+#pragma unroll
+      for (int k = 0; k < 32; k++) {
+        if (lane == k) {
+          mx = cx;
+          my = cy;
+        }
+        cx = cx + g.dxx;
+        cy = cy + g.dxy;
+      }
+      const long long x = x0 + lane;
+      if (x < xEnd) {
+        const uint32_t s = sample_smooth(b, bw, bh, mx, my);
+        line[x] = smooth_blend<MODE>(tbl, line[x], s);
+      }
+    }
+  }
+}
+
+typedef void (*SmoothKernel)(uint32_t*, long long, long long, const uint32_t*, long long, long long, SmoothArgs,
+                             long long, long long, const uint8_t*);
+template <int M>
+struct SmoothTable {
+  static void fill(SmoothKernel* t) {
+    t[M] = k_draw_smooth<M>;
+    SmoothTable<M + 1>::fill(t);
+  }
+};
+template <>
+struct SmoothTable<kNumBlends> {
+  static void fill(SmoothKernel*) {}
+};
+
+unsigned grid_for(long long items, long long per_block, int nsm) {
+  long long blocks = (items + per_block - 1) / per_block;
+  const long long cap = (long long)nsm * 8;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  return (unsigned)blocks;
+}
+
+}  // namespace
+
+void launch_minify2(const uint32_t* src, long long w, long long h, uint32_t* out, int nsm, cudaStream_t st) {
+  const long long n = ((w + 1) / 2) * ((h + 1) / 2);
+  k_minify2<<<grid_for(n, 256, nsm), 256, 0, st>>>(src, w, h, out);
+  note_launch();
+}
+
+void launch_magnify2(const uint32_t* src, long long w, long long h, uint32_t* out, int nsm, cudaStream_t st) {
+  k_magnify2<<<grid_for(w * h, 256, nsm), 256, 0, st>>>(src, w, h, out);
+  note_launch();
+}
+
+void launch_draw_smooth(uint32_t* a, long long W, long long H, const uint32_t* b, long long bw, long long bh,
+                        const SmoothArgs& g, int mode, const uint8_t* tbl, int nsm, cudaStream_t st) {
+  static SmoothKernel table[kNumBlends] = {nullptr};
+  if (!table[0]) SmoothTable<0>::fill(table);
+  const long long lo = mode == kMask ? 0 : g.yStart, hi = mode == kMask ? H : g.yEnd;
+  if (hi <= lo) return;
+  table[mode]<<<grid_for(hi - lo, 8, nsm), 256, 0, st>>>(a, W, H, b, bw, bh, g, lo, hi, tbl);
+  note_launch();
+}
+
+}  // namespace pxg

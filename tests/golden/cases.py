@@ -11,6 +11,8 @@ Backend interface (all images premultiplied RGBX):
   fill_path(img, cmds, color4f, opacity, blend, mat9, winding)
   stroke_path(img, cmds, color4f, opacity, blend, mat9, width, cap, join, miter, dashes)
   draw(a, b, tx, ty, blend)     blur(img, radius, oob_rgbx)     pixels(img) -> (h,w,4) uint8
+  draw_transform(a, b, mat9, blend)   load(premultiplied rgbx array) -> img
+  minify(img, power) -> img
 """
 from __future__ import annotations
 
@@ -459,6 +461,136 @@ for _i, (_tx, _ty) in enumerate([(0, 0), (50, -50), (50, 50), (-50, 50), (-50, -
             return a
         return fn
     CASES[f"images/maskClearsOnDraw{_i}"] = (_mk(_tx, _ty), "tests/test_images_draw.nim:311-331")
+
+
+# ---- tests/test_images_draw.nim: draw with a Mat3 (drawSmooth) -------------
+# vmath is not vendored: Mat3 helpers restated from their definitions
+# (column-major, float32, left-to-right sums), rotate from sinf/cosf.
+def mat_mul(A, Bm):
+    R = [0.0] * 9
+    for c in range(3):
+        for r in range(3):
+            R[c * 3 + r] = F.add(F.add(F.mul(A[r], Bm[c * 3]), F.mul(A[3 + r], Bm[c * 3 + 1])),
+                                 F.mul(A[6 + r], Bm[c * 3 + 2]))
+    return R
+
+
+def rotate(angle):
+    """vmath rotate(angle: float32): Mat3"""
+    sn, cs = F.sin(angle), F.cos(angle)
+    return [cs, sn, 0.0, -sn, cs, 0.0, 0.0, 0.0, 1.0]
+
+
+def to_radians(deg):
+    """vmath toRadians(deg: float32) = PI * deg / 180 in float32"""
+    return F.div(F.mul(F.PI, F.f32(deg)), 180.0)
+
+
+_INPUTS = {}
+
+
+def premultiplied(rgba8):
+    """toPremultipliedAlpha (internal.nim:86-96) of a straight RGBA uint8 array"""
+    px8 = rgba8.astype(np.uint32)
+    a = px8[..., 3:4]
+    out = np.where(a == 255, px8, (px8 * a + 127) // 255)
+    out[..., 3:4] = a
+    return np.ascontiguousarray(out.astype(np.uint8))
+
+
+def _load(B, name):
+    """readImage of one of the reference's test inputs (inputs.npz), premultiplied"""
+    if not _INPUTS:
+        import os
+        with np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "inputs.npz")) as z:
+            _INPUTS.update({k: z[k] for k in z.files})
+    return B.load(premultiplied(_INPUTS[name]))
+
+
+def _rot(deg):
+    def fn(B):
+        a, b = B.new_image(1000, 1000), B.new_image(500, 500)
+        B.fill(a, rgba(255, 0, 0, 255))
+        B.fill(b, rgba(0, 255, 0, 255))
+        m = translate(250, 250)
+        if deg:
+            m = mat_mul(m, rotate(F.div(F.mul(F.f32(-deg), F.PI), 180.0)))
+        B.draw_transform(a, b, m, NORMAL)
+        return a
+    return fn
+
+
+for _deg in (0, 90, 180, 270, 360):
+    CASES[f"images/rotate{_deg}"] = (_rot(_deg), f"tests/test_images_draw.nim:{3 + 10 * (_deg // 90)}-"
+                                                 f"{11 + 10 * (_deg // 90)}")
+
+
+@case("images/scaleHalf", "tests/test_images_draw.nim:121-129")
+def _c(B):
+    a, b = B.new_image(1000, 1000), B.new_image(500, 500)
+    B.fill(a, rgba(255, 0, 0, 255))
+    B.fill(b, rgba(0, 255, 0, 255))
+    B.draw_transform(a, b, mat_mul(translate(250, 250), scale(0.5, 0.5)), NORMAL)
+    return a
+
+
+def _smooth(w, h, bw, bh, bcol, m):
+    def fn(B):
+        a = B.new_image(w, h)
+        B.fill(a, rgba(255, 255, 255, 255))
+        if isinstance(bw, str):
+            b = _load(B, bw)
+        else:
+            b = B.new_image(bw, bh)
+            B.fill(b, bcol)
+        for mm in (m if isinstance(m[0], list) else [m]):
+            B.draw_transform(a, b, mm, NORMAL)
+        return a
+    return fn
+
+
+_R30 = mat_mul(translate(50, 50), rotate(to_radians(-30)))
+_R5 = mat_mul(translate(50, 50), rotate(to_radians(5)))
+_SMOOTH = {
+    1: ("131-138", 99, 99, color(0, 0, 0, 1), translate(0.5, 0.5)),
+    2: ("140-147", 50, 50, color(0, 0, 0, 1), mat_mul(translate(0, 50), rotate(to_radians(-45)))),
+    3: ("149-156", 50, 50, rgba(0, 0, 0, 255), translate(25.2, 25)),
+    4: ("158-165", 50, 50, rgba(0, 0, 0, 255), translate(25.2, 25.6)),
+    5: ("167-175", 10, 10, color(1, 0, 0, 1), _R30),
+    6: ("177-184", "turtle", None, None, _R30),
+    7: ("186-193", "turtle10x", None, None, mat_mul(_R30, scale(0.1, 0.1))),
+    8: ("195-202", "turtle", None, None, scale(2, 2)),
+    9: ("204-211", "turtle", None, None, mat_mul(translate(1, 1), scale(2, 2))),
+    10: ("213-220", "turtle", None, None, mat_mul(translate(0.5, 0.5), scale(2, 2))),
+    11: ("222-231", "turtle", None, None,
+         mat_mul(mat_mul(translate(-43.29, -103.87), rotate(to_radians(15))),
+                 scale(263.86 / 40, 263.86 / 40))),
+    12: ("233-243", "turtle", None, None,
+         [mat_mul(_R5, translate(0, 0)), mat_mul(_R5, translate(-40, 0)),
+          mat_mul(_R5, translate(-40, -40)), mat_mul(_R5, translate(0, -40))]),
+}
+for _k, (_lines, _bw, _bh, _bc, _m) in _SMOOTH.items():
+    CASES[f"images/masters/smooth{_k}"] = (_smooth(100, 100, _bw, _bh, _bc, _m),
+                                           f"tests/test_images_draw.nim:{_lines}")
+
+
+@case("images/masters/minify_odd", "tests/test_images_draw.nim:245-252")
+def _c(B):
+    a, b = B.new_image(100, 100), B.new_image(99, 99)
+    B.fill(a, rgba(255, 255, 255, 255))
+    B.fill(b, rgba(0, 0, 0, 255))
+    B.draw_transform(a, b, scale(0.5, 0.5), NORMAL)
+    return a
+
+
+@case("images/masters/rock_minified", "tests/test_images_draw.nim:254-258")
+def _c(B):
+    return B.minify(_load(B, "rock"), 1)
+
+
+@case("images/masters/rock_minified2", "tests/test_images_draw.nim:260-264")
+def _c(B):
+    return B.minify(_load(B, "rock"), 2)
 
 
 # ---- tests/test_contexts.nim ----------------------------------------------

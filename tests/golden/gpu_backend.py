@@ -23,6 +23,15 @@ class GpuBackend:
     def draw(self, a, b, tx, ty, blend):
         a.draw(b, (tx, ty), blend)
 
+    def draw_transform(self, a, b, mat, blend):
+        a.draw_transform(b, mat, blend)
+
+    def load(self, rgbx):
+        return px.Image.from_numpy(rgbx)
+
+    def minify(self, img, power):
+        return img.minify_by2(power)
+
     def blur(self, img, radius, oob):
         img.blur(radius, [np.float32(v) / np.float32(255) for v in oob])
 

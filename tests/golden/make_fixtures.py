@@ -5,7 +5,8 @@ Run once in a checkout that has the pixie reference next to it:
 Each entry is the straight-alpha RGBA uint8 pixel array of one master PNG that
 the reference's own tests write (tests/paths, tests/images, tests/contexts),
 keyed like "paths/pathHeart".  Only the masters used by tests/golden/cases.py
-are stored.
+are stored.  inputs.npz holds the images those tests read (readImage), also
+straight-alpha RGBA.
 """
 import os
 import sys
@@ -20,6 +21,11 @@ from png import read_png  # noqa: E402
 from cases import CASES  # noqa: E402
 
 
+# Input images the reference's tests read with readImage (straight-alpha RGBA),
+# keyed by the name cases.py loads them under.
+INPUTS = {"turtle": "images/turtle.png", "turtle10x": "images/turtle@10x.png", "rock": "images/rock.png"}
+
+
 def main(ref_root: str) -> None:
     out = {}
     for name in sorted(CASES):
@@ -27,6 +33,9 @@ def main(ref_root: str) -> None:
         out[name.replace("/", "__")] = read_png(path)
     np.savez_compressed(os.path.join(HERE, "goldens.npz"), **out)
     print(f"wrote {len(out)} goldens")
+    inputs = {k: read_png(os.path.join(ref_root, "tests", v)) for k, v in INPUTS.items()}
+    np.savez_compressed(os.path.join(HERE, "inputs.npz"), **inputs)
+    print(f"wrote {len(inputs)} input images")
 
 
 if __name__ == "__main__":

@@ -23,6 +23,17 @@ class OracleBackend:
     def draw(self, a, b, tx, ty, blend):
         pxo.draw(a, b, tx, ty, blend)
 
+    def draw_transform(self, a, b, mat, blend):
+        pxo.draw_transform(a, b, mat, blend)
+
+    def load(self, rgbx):
+        return np.ascontiguousarray(rgbx.copy())
+
+    def minify(self, img, power):
+        for _ in range(power):
+            img = pxo.minify_by2(img)
+        return img
+
     def blur(self, img, radius, oob):
         pxo.blur(img, radius, oob)
 
