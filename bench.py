@@ -275,7 +275,7 @@ def run_gpu(args, ws, rank, local):
                                          round(max(draw_gbs), 1)],
              "blur_ms": blur_ms}
     if rank == 0 and not args.no_fill:
-        extra.update(run_fill_extras(px, wl, args))
+        extra.update(run_fill_extras(px, wl, args, stream))
     return ms_step, launches, roof, e2e, extra, clk.summary()
 
 
@@ -323,7 +323,7 @@ def run_e2e(px, A, B, BL, M, SH, a_host, b_host, blur_host, run_op, ops, args, w
             "steps": steps, "ms_per_step": round(dt / steps * 1e3, 3)}
 
 
-def run_fill_extras(px, wl, args):
+def run_fill_extras(px, wl, args, stream):
     """Plain per-call fillPath and the batched glyph fill (paths/s)."""
     out = {}
     img = px.Image(512, 512)
@@ -343,11 +343,63 @@ def run_fill_extras(px, wl, args):
     out["plain_fill_512_64cubics"] = {"paths_per_s": round(n / dt, 1),
                                       "gpu_ms_per_path": round(gpu_ms / n, 4),
                                       "note": "one blocking C-ABI call per path, host pre-pass included"}
+    out["draw_transform_2048"] = run_draw_transform(px, wl, stream, cpu=not args.no_cpu_baseline)
     out["glyph_batch"] = run_glyphs(px, wl, args.glyphs)
     out["dense_scene_1024_2000"] = run_scene(px, wl)
     if args.serve_jobs > 0:
         out["serving"] = run_serving(px, wl, args.serve_jobs, args.serve_pool)
     px.set_blocking(False)
+    return out
+
+
+SMOOTH_CASES = {  # name: (column-major Mat3 of translate * rotate * scale, what it exercises)
+    "rotate30_scale1.1": ((30.0, 1.1, 1.1, 1024.0, -300.0), "drawSmooth only"),
+    "rotate10_scale0.3": ((10.0, 0.3, 0.3, 500.25, 400.5), "one minifyBy2 pre-pass + drawSmooth"),
+    "translate_0.5": ((0.0, 1.0, 1.0, 0.5, 0.5), "fractional translation: drawSmooth"),
+}
+
+
+def smooth_mat(angle, sx, sy, tx, ty):
+    import math
+    import numpy as np
+    a = math.radians(angle)
+    c, s = math.cos(a), math.sin(a)
+    return [float(np.float32(v)) for v in (c * sx, s * sx, 0, -s * sy, c * sy, 0, tx, ty, 1)]
+
+
+def run_draw_transform(px, wl, stream, cpu=True, reps=20):
+    """draw(a, b, Mat3, NormalBlend) of a 2048^2 source onto a 2048^2 canvas
+    (GPU ms per draw, CUDA events) beside the CPU baseline: the oracle on a
+    512^2 sample, scaled per pixel."""
+    import torch
+    out = {}
+    srcs = [px.Image.from_numpy(wl.premultiplied_image(40 + i, 2048, 2048)) for i in range(2)]
+    dsts = [px.Image.from_numpy(wl.premultiplied_image(50 + i, 2048, 2048)) for i in range(8)]
+    px.set_blocking(False)
+    for name, (geo, what) in SMOOTH_CASES.items():
+        m = smooth_mat(*geo)
+        for i in range(3):
+            dsts[i % 8].draw_transform(srcs[i % 2], m, 0)
+        px.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(reps):
+            dsts[i % 8].draw_transform(srcs[i % 2], m, 0)
+        e1.record(stream)
+        px.synchronize()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        out[name] = {"gpu_ms": round(ms, 4), "what": what,
+                     "canvas_gpix_per_s": round(2048 * 2048 / ms / 1e6, 2)}
+        if cpu:  # CPU baseline: the oracle, one thread, a 512^2 source onto a 512^2 canvas
+            from oracle import pxo
+            small = smooth_mat(geo[0], geo[1], geo[2], geo[3] / 4, geo[4] / 4)
+            a = wl.premultiplied_image(60, 512, 512)
+            b = wl.premultiplied_image(61, 512, 512)
+            t = time.perf_counter()
+            pxo.draw_transform(a, b, small, 0)
+            out[name]["cpu_oracle_ms_scaled_to_2048"] = round((time.perf_counter() - t) * 1000 * 16, 1)
+    px.set_blocking(True)
     return out
 
 
@@ -618,6 +670,11 @@ def run_case(case: str, slice_w: int = 0):
         b = px.Image.from_numpy(wl.premultiplied_image(2, 4096, 4096))
         for _ in range(2):
             a.draw(b, (0, 0), mode)
+    elif case == "smooth":  # draw of a 2048^2 source rotated 30 degrees, scaled 1.1, onto 2048^2
+        a = px.Image.from_numpy(wl.premultiplied_image(1, 2048, 2048))
+        b = px.Image.from_numpy(wl.premultiplied_image(2, 2048, 2048))
+        for _ in range(2):
+            a.draw_transform(b, smooth_mat(*SMOOTH_CASES["rotate30_scale1.1"][0]), 0)
     elif case == "glyphs":  # batched fill of 512 glyph masks
         glyphs, _ = wl.glyph_batch(7, n=512)
         imgs = [px.Image(w, h) for (_, w, h, _) in glyphs]
@@ -668,7 +725,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--slice", type=int, default=0, help="scene row slice width for --case scene*")
     ap.add_argument("--case", default=None,
-                    help="run one small operation for profiling: fill512 | blur<r> (blur64) | draw<mode> (draw13) | glyphs | scene | scene_small | masks")
+                    help="run one small operation for profiling: fill512 | blur<r> (blur64) | draw<mode> (draw13) | smooth | glyphs | scene | scene_small | masks")
     args = ap.parse_args()
     if args.case:
         run_case(args.case, args.slice)

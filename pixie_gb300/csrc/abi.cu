@@ -125,8 +125,10 @@ struct SmoothArgs {
 };
 void launch_minify2(const uint32_t* src, long long w, long long h, uint32_t* out, int nsm, cudaStream_t st);
 void launch_magnify2(const uint32_t* src, long long w, long long h, uint32_t* out, int nsm, cudaStream_t st);
+long long smooth_scratch_bytes(long long W, long long rows);
 void launch_draw_smooth(uint32_t* a, long long W, long long H, const uint32_t* b, long long bw, long long bh,
-                        const SmoothArgs& g, int mode, const uint8_t* tbl, int nsm, cudaStream_t st);
+                        const SmoothArgs& g, int mode, const uint8_t* tbl, void* scratch, int nsm,
+                        cudaStream_t st);
 void launch_draw(uint32_t* a, const uint32_t* b, long long Wa, long long Ha, long long Wb,
                  long long Hb, long long px, long long py, int mode, const uint8_t* tbl, int nsm,
                  cudaStream_t st);
@@ -2028,7 +2030,9 @@ void draw_transform(pxg_image* a, const pxg_image* b, M3 T, int blend) {
   }
   G.yStart = std::clamp<int64_t>(yStart, 0, a->height);
   G.yEnd = std::clamp<int64_t>(yEnd, 0, a->height);
-  launch_draw_smooth((uint32_t*)a->data, a->width, a->height, src, bw, bh, G, blend, g.tbl, g.nsm, g.stream);
+  if (a->width > INT32_MAX) throw ApiError{"Image too wide for draw with a transform"};
+  void* sc = scratch(smooth_scratch_bytes(a->width, G.yEnd - G.yStart));
+  launch_draw_smooth((uint32_t*)a->data, a->width, a->height, src, bw, bh, G, blend, g.tbl, sc, g.nsm, g.stream);
 }
 
 pxg_image* resampled_copy(const pxg_image* im, int power, bool minify) {

@@ -7,15 +7,17 @@
 // two 8-byte stores of its 2x2 block: both rows start at an even pixel offset,
 // 2y * 2w and (2y + 1) * 2w).
 //
-// k_draw_smooth: a warp owns one destination row.  Eight lanes intersect the
-// row's two scanlines with the four perimeter segments; lane 0 folds the hits
-// into the row's x range in the reference's order (so even NaN geometry gives
-// the same range).  The reference walks the sample position along the row by
-// repeated addition (srcPos += dx); that sum is sequential in float32, so every
-// lane of the warp runs the same chain and lane k keeps the k-th position of
-// each 32-pixel chunk: the positions are the reference's floats exactly.  Each
-// lane then samples its pixel (four gathers, two or three byte-wise mixes) and
-// blends it into the destination with the mode's blender.
+// drawSmooth in two passes.  The reference walks the sample position along a
+// row by repeated addition (srcPos += dx), a sum that is sequential in
+// float32.  k_smooth_rows gives each row one thread: it intersects the row's
+// two scanlines with the four perimeter segments in the reference's order
+// (the row's x span) and runs the row's walk with packed f32x2 adds (IEEE,
+// both coordinates at once), storing every 8th position, so a warp
+// instruction advances 32 rows.  k_draw_smooth then gives each warp 256 pixels
+// of a row; a lane resumes the walk from its stored position for 8 pixels,
+// samples each (four gathers, two or three byte-wise mixes) and blends it into
+// the destination with the mode's blender.  The positions are the reference's
+// floats exactly.
 #include <cstdint>
 
 #include "pxg_device.cuh"
@@ -147,78 +149,115 @@ __device__ __forceinline__ uint32_t smooth_blend(const uint8_t* tbl, uint32_t a,
   return blend_px(MODE, tbl, a, s);
 }
 
-// Rows [rowLo, rowHi) of the destination, one warp per row.  MaskBlend runs
-// over every row (the rows outside [yStart, yEnd) are cleared); the others
-// over [yStart, yEnd) only.
+__device__ __forceinline__ uint64_t f2(float x, float y) {
+  return ((uint64_t)__float_as_uint(y) << 32) | __float_as_uint(x);
+}
+// both coordinates of srcPos += dx in one packed add (IEEE round-to-nearest per lane)
+__device__ __forceinline__ uint64_t f2_add(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ float f2_x(uint64_t v) { return __uint_as_float((uint32_t)v); }
+__device__ __forceinline__ float f2_y(uint64_t v) { return __uint_as_float((uint32_t)(v >> 32)); }
+
+constexpr int kPosStep = 8;   // the row pass keeps every 8th sample position
+constexpr int kSegPx = 256;   // pixels per warp of the draw pass (32 lanes x 8)
+
+// Pass 1, one thread per row of [yStart, yEnd): the row's x range
+// (images.nim:567-582, the hits folded in the reference's order) and the
+// sample positions srcPos at xStart, xStart + 8, ... of the sequential walk
+// srcPos += dx (:585-589), stored as pos[k * R + row] (R = rows) so that the
+// 32 rows of a warp store 256 contiguous bytes.
+__global__ void __launch_bounds__(128) k_smooth_rows(SmoothArgs g, long long W, long long R, int2* __restrict__ rng,
+                                                     uint64_t* __restrict__ pos) {
+  const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long y = g.yStart + r;
+  if (y >= g.yEnd) return;
+  float xMin = (float)W, xMax = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    float ax = 0.0f, ay = 0.0f;
+    const float* s = g.seg[k & 3];
+    if (scan_hit(s, (float)y + (float)(k >> 2), ax, ay) && !(s[2] == ax && s[3] == ay)) {
+      xMin = nmin(xMin, ax);
+      xMax = nmax(xMax, ax);
+    }
+  }
+  long long xStart = nim_int(floorf(xMin)), xEnd = nim_int(ceilf(xMax));
+  xStart = xStart < 0 ? 0 : (xStart > W ? W : xStart);
+  xEnd = xEnd < 0 ? 0 : (xEnd > W ? W : xEnd);
+  rng[r] = make_int2((int)xStart, (int)xEnd);
+  float cx = (g.px + g.dxx * (float)xStart) + g.dyx * (float)y;
+  float cy = (g.py + g.dxy * (float)xStart) + g.dyy * (float)y;
+  uint64_t c = f2(cx - 0.5f, cy - 0.5f);
+  const uint64_t d = f2(g.dxx, g.dxy);
+  uint64_t* out = pos + r;
+  for (long long i = 0; i < xEnd - xStart; i += kPosStep, out += R) {
+    *out = c;
+#pragma unroll
+    for (int u = 0; u < kPosStep; u++) c = f2_add(c, d);
+  }
+}
+
+// Pass 2: warp (row, segment) handles pixels [256 s, 256 s + 256) of the
+// row's span [xStart, xEnd).  Lane j resumes the walk srcPos += dx from the
+// stored position of span pixel 256 s + 8 j for 8 pixels, into shared
+// memory; the warp then samples and blends 32 consecutive pixels at a time.
+// MaskBlend: the warp also clears the part of pixels [256 s, 256 s + 256) of
+// the row outside the span (the whole row when the span is empty or the row
+// lies outside [yStart, yEnd)).
 template <int MODE>
 __global__ void __launch_bounds__(256) k_draw_smooth(uint32_t* __restrict__ a, long long W, long long H,
                                                      const uint32_t* __restrict__ b, long long bw, long long bh,
-                                                     SmoothArgs g, long long rowLo, long long rowHi,
-                                                     const uint8_t* tbl) {
-  const int lane = threadIdx.x & 31;
+                                                     SmoothArgs g, const int2* __restrict__ rng,
+                                                     const uint64_t* __restrict__ pos, long long R, long long rowLo,
+                                                     long long rowHi, long long segs, const uint8_t* tbl) {
+  __shared__ uint64_t s_pos[8][kSegPx];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  uint64_t* sp = s_pos[wib];
+  const long long items = (rowHi - rowLo) * segs;
   const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
-  for (long long y = rowLo + (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); y < rowHi; y += warps) {
+  const uint64_t d = f2(g.dxx, g.dxy);
+  for (long long it = (long long)blockIdx.x * (blockDim.x >> 5) + wib; it < items; it += warps) {
+    const long long y = rowLo + it / segs, sg = it - (it / segs) * segs;
     uint32_t* line = a + y * W;
+    const long long s0 = sg * kSegPx;
     if (y < g.yStart || y >= g.yEnd) {  // MaskBlend only: rows the image does not reach
-      for (long long x = lane; x < W; x += 32) line[x] = 0u;
+      for (long long x = s0 + lane; x < s0 + kSegPx && x < W; x += 32) line[x] = 0u;
       continue;
     }
-    // the row's x range  images.nim:567-582
-    float hx = 0.0f;
-    bool hit = false;
-    if (lane < 8) {
-      const float ly = (float)y + (float)(lane >> 2);
-      const float* s = g.seg[lane & 3];
-      float ax = 0.0f, ay = 0.0f;
-      hit = scan_hit(s, ly, ax, ay) && !(s[2] == ax && s[3] == ay);
-      hx = ax;
-    }
-    const unsigned hits = __ballot_sync(0xffffffffu, hit);
-    float xMin = (float)W, xMax = 0.0f;
+    const int2 rr = rng[y - g.yStart];
+    const long long xStart = rr.x, xEnd = rr.y, len = xEnd - xStart;
+    if (len == 0) continue;  // :583-584
+    if (MODE == kMask)       // :612-620: clear [0, xStart) and [xEnd, W)
+      for (long long x = s0 + lane; x < s0 + kSegPx && x < W; x += 32)
+        if (x < xStart || x >= xEnd) line[x] = 0u;
+    if (s0 >= len) continue;
+    const long long i0 = s0 + (long long)lane * kPosStep;  // span offset of this lane's 8 positions
+    __syncwarp();
+    if (i0 < len) {
+      uint64_t c = pos[(i0 / kPosStep) * R + (y - g.yStart)];
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-      const float v = __shfl_sync(0xffffffffu, hx, k);
-      if (hits >> k & 1u) {
-        xMin = nmin(xMin, v);
-        xMax = nmax(xMax, v);
+      for (int u = 0; u < kPosStep; u++) {
+        sp[lane * kPosStep + u] = c;
+        c = f2_add(c, d);
       }
     }
-    long long xStart = nim_int(floorf(xMin)), xEnd = nim_int(ceilf(xMax));
-    xStart = xStart < 0 ? 0 : (xStart > W ? W : xStart);
-    xEnd = xEnd < 0 ? 0 : (xEnd > W ? W : xEnd);
-    if (xEnd - xStart == 0) continue;
-    if (MODE == kMask) {  // :612-620: clear [0, xStart) and [xEnd, W)
-      for (long long x = lane; x < xStart; x += 32) line[x] = 0u;
-      for (long long x = (xEnd > 0 ? xEnd : 0) + lane; x < W; x += 32) line[x] = 0u;
-    }
-    if (xEnd <= xStart) continue;
-    // srcPos = p + dx * xStart + dy * y, less h; then srcPos += dx per pixel
-    float cx = (g.px + g.dxx * (float)xStart) + g.dyx * (float)y;
-    float cy = (g.py + g.dxy * (float)xStart) + g.dyy * (float)y;
-    cx = cx - 0.5f;
-    cy = cy - 0.5f;
-    for (long long x0 = xStart; x0 < xEnd; x0 += 32) {
-      float mx = 0.0f, my = 0.0f;
-#pragma unroll
-      for (int k = 0; k < 32; k++) {
-        if (lane == k) {
-          mx = cx;
-          my = cy;
-        }
-        cx = cx + g.dxx;
-        cy = cy + g.dxy;
-      }
-      const long long x = x0 + lane;
-      if (x < xEnd) {
-        const uint32_t s = sample_smooth(b, bw, bh, mx, my);
-        line[x] = smooth_blend<MODE>(tbl, line[x], s);
-      }
+    __syncwarp();
+    const long long n = len - s0 < kSegPx ? len - s0 : kSegPx;
+    for (int k = lane; k < n; k += 32) {
+      const uint64_t c = sp[k];
+      const long long x = xStart + s0 + k;
+      const uint32_t sv = sample_smooth(b, bw, bh, f2_x(c), f2_y(c));
+      line[x] = smooth_blend<MODE>(tbl, line[x], sv);
     }
   }
 }
 
 typedef void (*SmoothKernel)(uint32_t*, long long, long long, const uint32_t*, long long, long long, SmoothArgs,
-                             long long, long long, const uint8_t*);
+                             const int2*, const uint64_t*, long long, long long, long long, long long,
+                             const uint8_t*);
 template <int M>
 struct SmoothTable {
   static void fill(SmoothKernel* t) {
@@ -252,13 +291,32 @@ void launch_magnify2(const uint32_t* src, long long w, long long h, uint32_t* ou
   note_launch();
 }
 
+// Scratch of one drawSmooth: per row of [yStart, yEnd) its span (int2) and
+// the sample position of every 8th pixel of the span.
+long long smooth_scratch_bytes(long long W, long long rows) {
+  const long long P = (W + kPosStep - 1) / kPosStep + 1;
+  return rows * 8 + rows * P * 8;
+}
+
 void launch_draw_smooth(uint32_t* a, long long W, long long H, const uint32_t* b, long long bw, long long bh,
-                        const SmoothArgs& g, int mode, const uint8_t* tbl, int nsm, cudaStream_t st) {
+                        const SmoothArgs& g, int mode, const uint8_t* tbl, void* scratch, int nsm,
+                        cudaStream_t st) {
   static SmoothKernel table[kNumBlends] = {nullptr};
   if (!table[0]) SmoothTable<0>::fill(table);
+  const long long rows = g.yEnd - g.yStart;
+  int2* rng = reinterpret_cast<int2*>(scratch);
+  uint64_t* pos = reinterpret_cast<uint64_t*>(reinterpret_cast<char*>(scratch) + rows * 8);
+  if (rows > 0) {
+    k_smooth_rows<<<(unsigned)((rows + 127) / 128), 128, 0, st>>>(g, W, rows, rng, pos);
+    note_launch();
+  }
   const long long lo = mode == kMask ? 0 : g.yStart, hi = mode == kMask ? H : g.yEnd;
   if (hi <= lo) return;
-  table[mode]<<<grid_for(hi - lo, 8, nsm), 256, 0, st>>>(a, W, H, b, bw, bh, g, lo, hi, tbl);
+  const long long segs = (W + kSegPx - 1) / kSegPx;
+  long long blocks = ((hi - lo) * segs + 7) / 8;
+  const long long cap = (long long)nsm * 64;
+  if (blocks > cap) blocks = cap;
+  table[mode]<<<(unsigned)blocks, 256, 0, st>>>(a, W, H, b, bw, bh, g, rng, pos, rows, lo, hi, segs, tbl);
   note_launch();
 }
 
