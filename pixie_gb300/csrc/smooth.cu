@@ -28,12 +28,19 @@ void note_launch();
 
 namespace {
 
-// `mix`(ColorRGBX, ColorRGBX, float32)  common.nim:59-65
+// floor(v / 255) of both 16-bit lanes, each v <= 65152: (v + 1 + (v >> 8)) >> 8
+// (exact for every v < 65536, checked exhaustively; no carry crosses lanes)
+__device__ __forceinline__ uint32_t div255x2(uint32_t w) {
+  return ((w + 0x00010001u + ((w >> 8) & 0x00FF00FFu)) >> 8) & 0x00FF00FFu;
+}
+// `mix`(ColorRGBX, ColorRGBX, float32)  common.nim:59-65: per channel
+// (a (255 - x) + b x + 127) div 255 with x = round(t * 255) <= 255, two
+// channels per 32-bit word (each lane <= 255 * 255 + 127 = 65152)
 __device__ __forceinline__ uint32_t mix_px(uint32_t a, uint32_t b, float t) {
   const uint32_t x = nim_u32(roundf(t * 255.0f));
-  const Px p = unpack(a), q = unpack(b);
-  return pack((p.r * (255 - x) + q.r * x + 127) / 255, (p.g * (255 - x) + q.g * x + 127) / 255,
-              (p.b * (255 - x) + q.b * x + 127) / 255, (p.a * (255 - x) + q.a * x + 127) / 255);
+  const uint32_t lo = (a & 0x00FF00FFu) * (255 - x) + (b & 0x00FF00FFu) * x + 0x007F007Fu;
+  const uint32_t hi = ((a >> 8) & 0x00FF00FFu) * (255 - x) + ((b >> 8) & 0x00FF00FFu) * x + 0x007F007Fu;
+  return div255x2(lo) | (div255x2(hi) << 8);
 }
 // mix(a, b, 0.5): round(0.5 * 255) = round(127.5) = 128 (half away from zero)
 __device__ __forceinline__ uint32_t mix_half(uint32_t a, uint32_t b) {
@@ -127,6 +134,7 @@ __device__ __forceinline__ uint32_t sample_smooth(const uint32_t* __restrict__ b
   const long long x0 = nim_int(fx), y0 = nim_int(fy);
   const long long x1 = x0 == 9223372036854775807LL ? x0 : x0 + 1, y1 = y0 == 9223372036854775807LL ? y0 : y0 + 1;
   const float xf = x - fx, yf = y - fy;
+  if (x0 < -1 || x0 >= bw || y0 < -1 || y0 >= bh) return 0u;  // all four taps outside: transparent
   const uint32_t x0y0 = px_at(b, bw, bh, x0, y0), x1y0 = px_at(b, bw, bh, x1, y0);
   const uint32_t x0y1 = px_at(b, bw, bh, x0, y1), x1y1 = px_at(b, bw, bh, x1, y1);
   uint32_t top = x0y0;
@@ -213,7 +221,9 @@ __global__ void __launch_bounds__(256) k_draw_smooth(uint32_t* __restrict__ a, l
                                                      SmoothArgs g, const int2* __restrict__ rng,
                                                      const uint64_t* __restrict__ pos, long long R, long long rowLo,
                                                      long long rowHi, long long segs, const uint8_t* tbl) {
-  __shared__ uint64_t s_pos[8][kSegPx];
+  // lane j's 8 positions at [9 j, 9 j + 8): the stride of 9 entries keeps the
+  // 8-byte stores of each half-warp on distinct bank pairs
+  __shared__ uint64_t s_pos[8][32 * 9];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   uint64_t* sp = s_pos[wib];
   const long long items = (rowHi - rowLo) * segs;
@@ -240,14 +250,14 @@ __global__ void __launch_bounds__(256) k_draw_smooth(uint32_t* __restrict__ a, l
       uint64_t c = pos[(i0 / kPosStep) * R + (y - g.yStart)];
 #pragma unroll
       for (int u = 0; u < kPosStep; u++) {
-        sp[lane * kPosStep + u] = c;
+        sp[lane * 9 + u] = c;
         c = f2_add(c, d);
       }
     }
     __syncwarp();
     const long long n = len - s0 < kSegPx ? len - s0 : kSegPx;
     for (int k = lane; k < n; k += 32) {
-      const uint64_t c = sp[k];
+      const uint64_t c = sp[(k >> 3) * 9 + (k & 7)];
       const long long x = xStart + s0 + k;
       const uint32_t sv = sample_smooth(b, bw, bh, f2_x(c), f2_y(c));
       line[x] = smooth_blend<MODE>(tbl, line[x], sv);
