@@ -1916,6 +1916,320 @@ static void drawTransform(Image& a, const Image& bIn, Mat3 transform, int mode) 
     blendRect(a, b, nim_i32(transform.m[6]), nim_i32(transform.m[7]), mode);
 }
 
+// ---------------------------------------------------------------------------
+// Paints  paints.nim, pixie.nim:120-131 (fill with a paint) and fillPath /
+// strokePath with a non-solid paint (paths.nim:2115-2142, :2178-2210)
+// ---------------------------------------------------------------------------
+enum PaintKind {
+  SolidPaint = 0, ImagePaint, TiledImagePaint, LinearGradientPaint, RadialGradientPaint, AngularGradientPaint
+};
+struct ColorStop {
+  float color[4];
+  float position;
+};
+struct PaintDesc {
+  int kind = SolidPaint;
+  int blend = 0;
+  float opacity = 1;
+  float color[4] = {0, 0, 0, 0};
+  Image image{0, 0, nullptr};
+  Mat3 imageMat{{1, 0, 0, 0, 1, 0, 0, 0, 1}};
+  std::vector<Vec2> handles;
+  std::vector<ColorStop> stops;
+};
+
+// atan2 for float32 arguments, correctly rounded to float32 (but for inputs
+// whose true value lies within ~1e-16 of a rounding boundary): evaluated in
+// float64 from the mathematics alone -- atan(x) = pi/2 - atan(1/x) above 1,
+// two halvings atan(x) = 2 atan(x / (1 + sqrt(1 + x^2))) to |x| < 0.2, and
+// 14 terms of the Taylor series -- so the CUDA path, which runs the same
+// IEEE float64 operations, gets the same floats.  (pixie calls the C
+// library's atan2f, which is not reproduced here bit for bit.)
+static double atan_unit(double x) {  // x >= 0
+  const bool inv = x > 1;
+  if (inv) x = 1 / x;
+  x = x / (1 + sqrt(1 + x * x));
+  x = x / (1 + sqrt(1 + x * x));
+  const double x2 = x * x;
+  double term = x, sum = x;
+  for (int n = 1; n <= 13; n++) {
+    term = term * -x2;
+    sum = sum + term / (double)(2 * n + 1);
+  }
+  sum = sum * 4;
+  return inv ? 1.5707963267948966 - sum : sum;
+}
+static float atan2_cr(float y, float x) {
+  if (std::isnan(x) || std::isnan(y)) return NAN;
+  const double pi = 3.141592653589793;
+  double r;
+  if (y == 0) {
+    r = (std::signbit(x)) ? pi : 0.0;
+  } else if (x == 0) {
+    r = pi / 2;
+  } else if (std::isinf(x) || std::isinf(y)) {
+    if (std::isinf(x) && std::isinf(y))
+      r = x > 0 ? pi / 4 : 3 * pi / 4;
+    else if (std::isinf(x))
+      r = x > 0 ? 0.0 : pi;
+    else
+      r = pi / 2;
+  } else {
+    const double a = atan_unit(fabs((double)y / (double)x));
+    r = x > 0 ? a : pi - a;
+  }
+  return (float)(std::signbit(y) ? -r : r);
+}
+
+// chroma mix(Color, Color, t): componentwise lerp a + (b - a) * t
+static inline float lerp_f(float a, float b, float t) { return a + (b - a) * t; }
+
+// gradientColor  paints.nim:68-93
+static RGBX gradientColor(const PaintDesc& p, float t) {
+  int index = -1;
+  for (size_t i = 0; i < p.stops.size(); i++) {
+    if (p.stops[i].position < t) index = (int)i;
+    if (p.stops[i].position > t) break;
+  }
+  float c[4];
+  if (index == -1) {
+    memcpy(c, p.stops[0].color, sizeof c);
+  } else if (index + 1 >= (int)p.stops.size()) {
+    memcpy(c, p.stops[(size_t)index].color, sizeof c);
+  } else {
+    const ColorStop& a = p.stops[(size_t)index];
+    const ColorStop& b = p.stops[(size_t)index + 1];
+    const float u = (t - a.position) / (b.position - a.position);
+    for (int k = 0; k < 4; k++) c[k] = lerp_f(a.color[k], b.color[k], u);
+  }
+  c[3] *= p.opacity;
+  return color_to_rgbx(c);
+}
+
+static bool gradientPrologue(PaintDesc& p, size_t handles, const char* msg) {
+  if (p.handles.size() != handles) throw PixieError(msg);
+  if (p.stops.empty()) throw PixieError("Gradient must have at least 1 color stop");
+  p.opacity = p.opacity < 0 ? 0 : (p.opacity > 1 ? 1 : p.opacity);
+  return p.opacity != 0;
+}
+
+// fillGradientLinear  paints.nim:95-176.  The horizontal and vertical
+// branches fill each column / row with the general formula's value at y = 0
+// / x = 0, which equals its value at every y / x (the zero term adds +-0).
+static void fillGradientLinear(Image& img, PaintDesc& p) {
+  if (!gradientPrologue(p, 2, "Linear gradient requires 2 handles")) return;
+  const Vec2 at = p.handles[0], to = p.handles[1];
+  const Vec2 d = to - at;
+  const float det = d.x * d.x + d.y * d.y;
+  for (int64_t y = 0; y < img.height; y++)
+    for (int64_t x = 0; x < img.width; x++) {
+      const float t = (d.y * ((float)y - at.y) + d.x * ((float)x - at.x)) / det;
+      img.data[img.idx(x, y)] = gradientColor(p, t);
+    }
+}
+
+// vmath rotate(angle): column-major [cos, sin, 0, -sin, cos, 0, 0, 0, 1]
+static Mat3 rotate_m(float a) {
+  const float sn = sinf(a), cs = cosf(a);
+  return Mat3{{cs, sn, 0, -sn, cs, 0, 0, 0, 1}};
+}
+static Mat3 translate_m(Vec2 v) { return Mat3{{1, 0, 0, 0, 1, 0, v.x, v.y, 1}}; }
+
+// fillGradientRadial  paints.nim:178-205
+static void fillGradientRadial(Image& img, PaintDesc& p) {
+  if (!gradientPrologue(p, 3, "Radial gradient requires 3 handles")) return;
+  const Vec2 center = p.handles[0], edge = p.handles[1], skew = p.handles[2];
+  const float distanceX = length(center - edge), distanceY = length(center - skew);
+  const float gradientAngle = fixAngle(angleOf(normalize(center - edge)));
+  const Mat3 mat = inverse_m(matmul(matmul(translate_m(center), rotate_m(gradientAngle)),
+                                    scale_m(distanceX, distanceY)));
+  for (int64_t y = 0; y < img.height; y++)
+    for (int64_t x = 0; x < img.width; x++) {
+      const float t = length(mul(mat, v2((float)x, (float)y)));
+      img.data[img.idx(x, y)] = gradientColor(p, t);
+    }
+}
+
+// fillGradientAngular  paints.nim:207-229 (its error text says "2 handles")
+static void fillGradientAngular(Image& img, PaintDesc& p) {
+  if (!gradientPrologue(p, 3, "Angular gradient requires 2 handles")) return;
+  const Vec2 center = p.handles[0], edge = p.handles[1];
+  const float f32PI = (float)kPI;
+  const float gradientAngle = fixAngle(angleOf(normalize(edge - center)));
+  for (int64_t y = 0; y < img.height; y++)
+    for (int64_t x = 0; x < img.width; x++) {
+      const Vec2 v = normalize(v2((float)x, (float)y) - center);
+      const float angle = atan2_cr(v.y, v.x);
+      const float t = fixAngle(angle + gradientAngle + f32PI / 2) / 2 / f32PI + 0.5f;
+      img.data[img.idx(x, y)] = gradientColor(p, t);
+    }
+}
+
+static void fillGradient(Image& img, PaintDesc p) {  // paints.nim:231-241
+  switch (p.kind) {
+    case LinearGradientPaint: fillGradientLinear(img, p); break;
+    case RadialGradientPaint: fillGradientRadial(img, p); break;
+    case AngularGradientPaint: fillGradientAngular(img, p); break;
+    default: throw PixieError("Paint must be a gradient");
+  }
+}
+
+// applyOpacity  images.nim:261-277
+static void applyOpacity(Image& img, float opacity) {
+  const uint32_t o = (uint16_t)nim_i32(roundf(255 * opacity));
+  if (o == 255) return;
+  if (o == 0) {
+    fillUnsafe(img, RGBX{0, 0, 0, 0}, 0, img.len());
+    return;
+  }
+  for (int64_t i = 0; i < img.len(); i++) {
+    RGBX& c = img.data[i];
+    c = rgbx((c.r * o) / 255, (c.g * o) / 255, (c.b * o) / 255, (c.a * o) / 255);
+  }
+}
+
+// getRgbaSmooth with wrapped = true (images.nim:381-385): the taps are
+// image.unsafe[x mod w, y mod h] with Nim's truncating mod, so a negative
+// coordinate addresses data[w * (y mod h) + (x mod w)] linearly (the previous
+// row's last pixel for x = -1); an address outside the buffer, which reads
+// foreign memory in the reference, reads transparent here.
+static RGBX getRgbaSmoothWrapped(const Image& img, float x, float y) {
+  const float fx = floorf(x), fy = floorf(y);
+  const int64_t x0 = nim_int(fx), y0 = nim_int(fy);
+  const int64_t x1 = x0 == INT64_MAX ? x0 : x0 + 1, y1 = y0 == INT64_MAX ? y0 : y0 + 1;
+  const float xFractional = x - fx, yFractional = y - fy;
+  auto at = [&](int64_t px, int64_t py) {
+    const int64_t i = img.width * (py % img.height) + (px % img.width);
+    return (i >= 0 && i < img.len()) ? img.data[i] : RGBX{0, 0, 0, 0};
+  };
+  const RGBX x0y0 = at(x0, y0), x1y0 = at(x1, y0), x0y1 = at(x0, y1), x1y1 = at(x1, y1);
+  RGBX topMix = x0y0;
+  if (xFractional > 0 && !same(x0y0, x1y0)) topMix = mix_c(x0y0, x1y0, xFractional);
+  RGBX bottomMix = x0y1;
+  if (xFractional > 0 && !same(x0y1, x1y1)) bottomMix = mix_c(x0y1, x1y1, xFractional);
+  if (yFractional != 0 && !same(topMix, bottomMix)) return mix_c(topMix, bottomMix, yFractional);
+  return topMix;
+}
+
+// drawCorrect  images.nim:405-445 (drawTiled :680-683 is tiled = true): every
+// destination pixel samples inverseTransform * (x + h, y + h) - h
+static void drawCorrect(Image& a, const Image& bIn, const Mat3& transform, int mode, bool tiled) {
+  Mat3 inv = inverse_m(transform);
+  Vec2 p = mul(inv, v2(0 + kHalf, 0 + kHalf));
+  Vec2 dx = mul(inv, v2(1 + kHalf, 0 + kHalf)) - p;
+  Vec2 dy = mul(inv, v2(0 + kHalf, 1 + kHalf)) - p;
+  float filterBy2 = nmax(length(dx), length(dy));
+  if (std::isinf(filterBy2)) throw PixieError("draw transform is not invertible");
+  OwnedImage cur = copy_image(bIn);
+  while (filterBy2 >= 2.0f) {
+    cur = minifyBy2(cur.view());
+    p = p / 2;
+    dx = dx / 2;
+    dy = dy / 2;
+    filterBy2 /= 2;
+    inv = matmul(scale_m(0.5f, 0.5f), inv);
+  }
+  while (filterBy2 <= 0.5f) {
+    if (cur.width * cur.height > ((int64_t)1 << 30))
+      throw PixieError("draw would magnify the source image beyond 2^32 bytes");
+    cur = magnifyBy2(cur.view());
+    p = p * 2;
+    dx = dx * 2;
+    dy = dy * 2;
+    filterBy2 *= 2;
+    inv = matmul(scale_m(2, 2), inv);
+  }
+  const Image b = cur.view();
+  for (int64_t y = 0; y < a.height; y++)
+    for (int64_t x = 0; x < a.width; x++) {
+      const Vec2 sp = mul(inv, v2((float)x + kHalf, (float)y + kHalf));
+      const float xf = sp.x - kHalf, yf = sp.y - kHalf;
+      const RGBX s = tiled ? getRgbaSmoothWrapped(b, xf, yf) : getRgbaSmooth(b, xf, yf);
+      RGBX& d = a.data[a.idx(x, y)];
+      d = blend_px(mode, d, s);
+    }
+}
+
+// the paint image of a non-solid paint (paths.nim:2121-2134): the image
+// paint drawn, tiled, or the gradient, with the paint at opacity 1
+static void paintImage(Image& fill, const PaintDesc& paint) {
+  PaintDesc p = paint;
+  p.opacity = 1;
+  switch (p.kind) {
+    case ImagePaint: drawTransform(fill, p.image, p.imageMat, NormalBlend); break;
+    case TiledImagePaint: drawCorrect(fill, p.image, p.imageMat, NormalBlend, true); break;
+    default: fillGradient(fill, p); break;
+  }
+}
+// mask -> fill -> MaskBlend -> draw  paths.nim:2115-2142
+static void compositePaint(Image& img, Image& mask, const PaintDesc& paint) {
+  OwnedImage fill;
+  fill.width = img.width;
+  fill.height = img.height;
+  fill.px.assign((size_t)img.len(), RGBX{0, 0, 0, 0});
+  Image F = fill.view();
+  paintImage(F, paint);
+  const float op = paint.opacity < 0 ? 0 : (paint.opacity > 1 ? 1 : paint.opacity);
+  if (op != 1) applyOpacity(mask, op);
+  blendRect(F, mask, 0, 0, MaskBlend);
+  blendRect(img, F, 0, 0, paint.blend);
+}
+
+static void fillPathPaint(Image& img, const float* cmds, int64_t n, const PaintDesc& paint, const Mat3& M,
+                          int rule) {
+  const float op = paint.opacity < 0 ? 0 : (paint.opacity > 1 ? 1 : paint.opacity);
+  if (op == 0) return;
+  if (paint.kind == SolidPaint) {
+    fillPath(img, cmds, n, paint.color, op, paint.blend, M, rule);
+    return;
+  }
+  validateCommands(cmds, n);
+  OwnedImage mask;
+  mask.width = img.width;
+  mask.height = img.height;
+  mask.px.assign((size_t)img.len(), RGBX{0, 0, 0, 0});
+  Image Mk = mask.view();
+  const float white[4] = {1, 1, 1, 1};
+  fillPath(Mk, cmds, n, white, 1, NormalBlend, M, rule);
+  compositePaint(img, Mk, paint);
+}
+
+static void strokePathPaint(Image& img, const float* cmds, int64_t n, const PaintDesc& paint, const Mat3& M,
+                            float width, int cap, int join, float miter, const float* dashes, int nd) {
+  const float op = paint.opacity < 0 ? 0 : (paint.opacity > 1 ? 1 : paint.opacity);
+  if (op == 0) return;
+  if (paint.kind == SolidPaint) {
+    strokePath(img, cmds, n, paint.color, op, paint.blend, M, width, cap, join, miter, dashes, nd);
+    return;
+  }
+  validateCommands(cmds, n);
+  OwnedImage mask;
+  mask.width = img.width;
+  mask.height = img.height;
+  mask.px.assign((size_t)img.len(), RGBX{0, 0, 0, 0});
+  Image Mk = mask.view();
+  const float white[4] = {1, 1, 1, 1};
+  strokePath(Mk, cmds, n, white, 1, NormalBlend, M, width, cap, join, miter, dashes, nd);
+  compositePaint(img, Mk, paint);
+}
+
+// fill(image, paint)  pixie.nim:120-131
+static void fillWithPaint(Image& img, const PaintDesc& paint) {
+  switch (paint.kind) {
+    case SolidPaint: fillUnsafe(img, color_to_rgbx(paint.color), 0, img.len()); break;
+    case ImagePaint:
+    case TiledImagePaint: {
+      fillUnsafe(img, RGBX{0, 0, 0, 0}, 0, img.len());
+      const float rect[] = {Move, 0, 0, Line, (float)img.width, 0, Line, (float)img.width, (float)img.height,
+                            Line, 0, (float)img.height, Close};
+      fillPathPaint(img, rect, (int64_t)(sizeof rect / sizeof rect[0]), paint, Mat3{{1, 0, 0, 0, 1, 0, 0, 0, 1}},
+                    0);
+      break;
+    }
+    default: fillGradient(img, paint); break;
+  }
+}
+
 // gaussianKernel  internal.nim:17-34.  `s` and the exp() argument are float32;
 // `1 / sqrt(2 * PI * s^2) * exp(...)` meets the float64 constant PI and is
 // float64; `total` is a float64 variable and
@@ -2142,6 +2456,74 @@ int pxo_draw(uint8_t* a, int64_t aw, int64_t ah, const uint8_t* b, int64_t bw, i
     return fail(e);
   }
 }
+
+// A paint as floats: [kind, blend, opacity, r, g, b, a, imageMat[9],
+// nHandles, x, y, ..., nStops, r, g, b, a, position, ...]; the image of an
+// image paint is passed beside it.
+static PaintDesc paint_from(const float* f, int64_t nf, const uint8_t* img, int64_t iw, int64_t ih) {
+  PaintDesc p;
+  if (nf < 18) throw PixieError("bad paint encoding");
+  p.kind = (int)f[0];
+  p.blend = (int)f[1];
+  p.opacity = f[2];
+  memcpy(p.color, f + 3, sizeof p.color);
+  memcpy(p.imageMat.m, f + 7, sizeof p.imageMat.m);
+  int64_t k = 16;
+  const int64_t nh = (int64_t)f[k++];
+  if (k + 2 * nh + 1 > nf) throw PixieError("bad paint encoding");
+  for (int64_t i = 0; i < nh; i++, k += 2) p.handles.push_back(v2(f[k], f[k + 1]));
+  const int64_t ns = (int64_t)f[k++];
+  if (k + 5 * ns > nf) throw PixieError("bad paint encoding");
+  for (int64_t i = 0; i < ns; i++, k += 5) {
+    ColorStop c;
+    memcpy(c.color, f + k, sizeof c.color);
+    c.position = f[k + 4];
+    p.stops.push_back(c);
+  }
+  p.image = Image{iw, ih, (RGBX*)img};
+  if ((p.kind == ImagePaint || p.kind == TiledImagePaint) && (!img || iw <= 0 || ih <= 0))
+    throw PixieError("Image paint needs an image");
+  return p;
+}
+
+int pxo_fill_path_paint(uint8_t* rgbx_data, int64_t w, int64_t h, const float* cmds, int64_t n,
+                        const float* paint, int64_t np, const uint8_t* pimg, int64_t pw, int64_t ph,
+                        const float* mat, int rule) {
+  try {
+    Image img{w, h, (RGBX*)rgbx_data};
+    fillPathPaint(img, cmds, n, paint_from(paint, np, pimg, pw, ph), mat_from(mat), rule);
+    return 0;
+  } catch (const std::exception& e) {
+    return fail(e);
+  }
+}
+
+int pxo_stroke_path_paint(uint8_t* rgbx_data, int64_t w, int64_t h, const float* cmds, int64_t n,
+                          const float* paint, int64_t np, const uint8_t* pimg, int64_t pw, int64_t ph,
+                          const float* mat, float width, int cap, int join, float miter, const float* dashes,
+                          int nd) {
+  try {
+    Image img{w, h, (RGBX*)rgbx_data};
+    strokePathPaint(img, cmds, n, paint_from(paint, np, pimg, pw, ph), mat_from(mat), width, cap, join, miter,
+                    dashes, nd);
+    return 0;
+  } catch (const std::exception& e) {
+    return fail(e);
+  }
+}
+
+int pxo_fill_paint(uint8_t* rgbx_data, int64_t w, int64_t h, const float* paint, int64_t np, const uint8_t* pimg,
+                   int64_t pw, int64_t ph) {
+  try {
+    Image img{w, h, (RGBX*)rgbx_data};
+    fillWithPaint(img, paint_from(paint, np, pimg, pw, ph));
+    return 0;
+  } catch (const std::exception& e) {
+    return fail(e);
+  }
+}
+
+float pxo_atan2(float y, float x) { return atan2_cr(y, x); }
 
 int pxo_draw_transform(uint8_t* a, int64_t aw, int64_t ah, const uint8_t* b, int64_t bw, int64_t bh,
                        const float* mat3, int blend) {

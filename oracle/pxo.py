@@ -50,6 +50,11 @@ def lib():
         L.pxo_draw.argtypes = [P, I64, I64, P, I64, I64, I64, I64, I]
         L.pxo_blend_pixels.argtypes = [I, P, P, P, I64]
         L.pxo_draw_transform.argtypes = [P, I64, I64, P, I64, I64, P, I]
+        L.pxo_fill_path_paint.argtypes = [P, I64, I64, P, I64, P, I64, P, I64, I64, P, I]
+        L.pxo_stroke_path_paint.argtypes = [P, I64, I64, P, I64, P, I64, P, I64, I64, P, F, I, I, F, P, I]
+        L.pxo_fill_paint.argtypes = [P, I64, I64, P, I64, P, I64, I64]
+        L.pxo_atan2.argtypes = [F, F]
+        L.pxo_atan2.restype = F
         L.pxo_minify_by2.argtypes = [P, I64, I64, P]
         L.pxo_magnify_by2.argtypes = [P, I64, I64, P]
         L.pxo_fill.argtypes = [P, I64, I64, P]
@@ -150,6 +155,60 @@ def draw_transform(a, b, mat, blend=0):
     m = _f32(mat, 9)
     _check(lib().pxo_draw_transform(_p(a), a.shape[1], a.shape[0], _p(b), b.shape[1], b.shape[0],
                                     _p(m), int(blend)))
+
+
+def encode_paint(paint):
+    """paint: dict(kind, blend=0, opacity=1, color=(r,g,b,a), image=None,
+    image_mat=9 floats column-major, handles=[(x, y)], stops=[((r,g,b,a), pos)]).
+    Returns (float32 array, image array or None)."""
+    f = [paint["kind"], paint.get("blend", 0), paint.get("opacity", 1.0)]
+    f += list(paint.get("color", (0, 0, 0, 0)))
+    f += list(paint.get("image_mat", (1, 0, 0, 0, 1, 0, 0, 0, 1)))
+    hs = paint.get("handles", [])
+    f.append(len(hs))
+    for x, y in hs:
+        f += [x, y]
+    st = paint.get("stops", [])
+    f.append(len(st))
+    for col, pos in st:
+        f += list(col) + [pos]
+    img = paint.get("image")
+    return np.asarray(f, np.float32), (None if img is None else np.ascontiguousarray(img))
+
+
+def _paint_args(paint):
+    f, img = encode_paint(paint)
+    if img is None:
+        return f, None, 0, 0
+    return f, img, img.shape[1], img.shape[0]
+
+
+def fill_path_paint(img, cmds, paint, mat=None, winding=0):
+    cmds = _f32(cmds)
+    f, pimg, pw, ph = _paint_args(paint)
+    m = _IDENT if mat is None else _f32(mat, 9)
+    _check(lib().pxo_fill_path_paint(_p(img), img.shape[1], img.shape[0], _p(cmds), cmds.size, _p(f), f.size,
+                                     _p(pimg) if pimg is not None else None, pw, ph, _p(m), int(winding)))
+
+
+def stroke_path_paint(img, cmds, paint, mat=None, width=1.0, cap=0, join=0, miter=4.0, dashes=()):
+    cmds = _f32(cmds)
+    f, pimg, pw, ph = _paint_args(paint)
+    m = _IDENT if mat is None else _f32(mat, 9)
+    d = _f32(list(dashes) or [0.0])
+    _check(lib().pxo_stroke_path_paint(_p(img), img.shape[1], img.shape[0], _p(cmds), cmds.size, _p(f), f.size,
+                                       _p(pimg) if pimg is not None else None, pw, ph, _p(m), float(width),
+                                       int(cap), int(join), float(miter), _p(d), len(dashes)))
+
+
+def fill_paint(img, paint):
+    f, pimg, pw, ph = _paint_args(paint)
+    _check(lib().pxo_fill_paint(_p(img), img.shape[1], img.shape[0], _p(f), f.size,
+                                _p(pimg) if pimg is not None else None, pw, ph))
+
+
+def atan2(y, x):
+    return lib().pxo_atan2(float(y), float(x))
 
 
 def minify_by2(img):

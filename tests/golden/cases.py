@@ -13,6 +13,8 @@ Backend interface (all images premultiplied RGBX):
   draw(a, b, tx, ty, blend)     blur(img, radius, oob_rgbx)     pixels(img) -> (h,w,4) uint8
   draw_transform(a, b, mat9, blend)   load(premultiplied rgbx array) -> img
   minify(img, power) -> img
+  fill_path_paint(img, cmds, paint)   fill_paint(img, paint)   (paint: a dict, see
+  oracle/pxo.py encode_paint; its "image" is a backend image)
 """
 from __future__ import annotations
 
@@ -591,6 +593,61 @@ def _c(B):
 @case("images/masters/rock_minified2", "tests/test_images_draw.nim:260-264")
 def _c(B):
     return B.minify(_load(B, "rock"), 2)
+
+
+# ---- tests/test_paints.nim: non-solid paints -------------------------------
+SOLID, IMAGE_PAINT, TILED_PAINT, LINEAR, RADIAL, ANGULAR = range(6)
+_STOPS = [((F.f32(1), 0.0, 0.0, F.f32(1)), 0.0), ((F.f32(1), 0.0, 0.0, F.f32(0.15625)), F.f32(1.0))]
+
+
+def _heart_paint(paint_fn, w=100, h=100):
+    def fn(B):
+        img = B.new_image(w, h)
+        B.fill_path_paint(img, parse_path(HEART).array(), paint_fn(B))
+        return img
+    return fn
+
+
+def _image_paint(kind, s, opacity=1.0):
+    def fn(B):
+        return dict(kind=kind, image=_load(B, "mandrill"), image_mat=scale(s, s), opacity=F.f32(opacity))
+    return fn
+
+
+def _gradient(kind, handles, opacity=1.0):
+    def fn(B):
+        return dict(kind=kind, handles=[(F.f32(x), F.f32(y)) for x, y in handles], stops=_STOPS,
+                    opacity=F.f32(opacity))
+    return fn
+
+
+_PAINT_CASES = {
+    "paths/paintImage": ("21-27", _image_paint(IMAGE_PAINT, 0.2)),
+    "paths/paintImageOpacity": ("29-36", _image_paint(IMAGE_PAINT, 0.2, 0.5)),
+    "paths/paintImageTiled": ("38-44", _image_paint(TILED_PAINT, 0.02)),
+    "paths/paintImageTiledOpacity": ("46-53", _image_paint(TILED_PAINT, 0.02, 0.5)),
+    "paths/gradientLinear": ("55-68", _gradient(LINEAR, [(0, 50), (100, 50)])),
+    "paths/gradientLinear2": ("70-83", _gradient(LINEAR, [(50, 0), (50, 100)])),
+    "paths/gradientRadial": ("85-99", _gradient(RADIAL, [(50, 50), (100, 50), (50, 100)])),
+    "paths/gradientAngular": ("101-115", _gradient(ANGULAR, [(50, 50), (100, 50), (50, 100)])),
+    "paths/gradientAngularOpacity": ("117-132", _gradient(ANGULAR, [(50, 50), (100, 50), (50, 100)], 0.5)),
+}
+for _name, (_lines, _pf) in _PAINT_CASES.items():
+    CASES[_name] = (_heart_paint(_pf), f"tests/test_paints.nim:{_lines}")
+
+
+def _fill_image_paint(kind, s):
+    def fn(B):
+        img = B.new_image(128, 128)
+        B.fill(img, color(0, 1, 0, 1))
+        B.fill_paint(img, dict(kind=kind, image=_load(B, "mandrill"), image_mat=scale(s, s),
+                               opacity=F.f32(0.5)))
+        return img
+    return fn
+
+
+CASES["paths/fillImagePaint"] = (_fill_image_paint(IMAGE_PAINT, 0.2), "tests/test_paints.nim:134-143")
+CASES["paths/fillTiledImagePaint"] = (_fill_image_paint(TILED_PAINT, 0.1), "tests/test_paints.nim:145-154")
 
 
 # ---- tests/test_contexts.nim ----------------------------------------------

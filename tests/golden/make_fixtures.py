@@ -23,7 +23,8 @@ from cases import CASES  # noqa: E402
 
 # Input images the reference's tests read with readImage (straight-alpha RGBA),
 # keyed by the name cases.py loads them under.
-INPUTS = {"turtle": "images/turtle.png", "turtle10x": "images/turtle@10x.png", "rock": "images/rock.png"}
+INPUTS = {"turtle": "images/turtle.png", "turtle10x": "images/turtle@10x.png", "rock": "images/rock.png",
+          "mandrill": "fileformats/png/mandrill.png"}
 
 
 def main(ref_root: str) -> None:

@@ -34,6 +34,12 @@ class OracleBackend:
             img = pxo.minify_by2(img)
         return img
 
+    def fill_path_paint(self, img, cmds, paint, mat=None, winding=0):
+        pxo.fill_path_paint(img, cmds, paint, mat, winding)
+
+    def fill_paint(self, img, paint):
+        pxo.fill_paint(img, paint)
+
     def blur(self, img, radius, oob):
         pxo.blur(img, radius, oob)
 
