@@ -102,6 +102,50 @@ int pxg_image_draw_transform(pxg_image* a, const pxg_image* b, const float trans
 pxg_image* pxg_image_minify_by2(const pxg_image* image, int power);
 pxg_image* pxg_image_magnify_by2(const pxg_image* image, int power);
 
+/* drawTiled(Image, Image, Mat3, BlendMode)  src/pixie/images.nim:680-683 (drawCorrect
+ * :405-445 with wrapped sampling): every destination pixel samples the source,
+ * repeated, through the inverse transform. */
+int pxg_image_draw_tiled(pxg_image* a, const pxg_image* b, const float transform[9], int blend_mode);
+
+/* A paint (src/pixie/paints.nim:12-26, bindings/bindings.nim Paint):
+ * kind is PaintKind (0 solid, 1 image, 2 tiled image, 3 linear gradient,
+ * 4 radial gradient, 5 angular gradient); color is chroma's straight float
+ * Color (solid); image / image_mat the image paint's image and vmath Mat3
+ * (column-major); handles n_handles (x, y) pairs and stops n_stops
+ * (r, g, b, a, position) records (gradients). */
+typedef struct pxg_paint {
+  int32_t kind;
+  int32_t blend_mode;
+  float opacity;
+  float color[4];
+  const pxg_image* image;
+  float image_mat[9];
+  int32_t n_handles;
+  const float* handles;
+  int32_t n_stops;
+  const float* stops;
+} pxg_paint;
+
+/* fillPath / strokePath with any paint  src/pixie/paths.nim:2093-2142,
+ * :2144-2210 (bindings/bindings.nim:143-144): a solid paint takes
+ * pxg_image_fill_path / pxg_image_stroke_path; the others fill a mask with
+ * the path, fill an image with the paint (image, tiled image or gradient),
+ * apply the paint's opacity to the mask, MaskBlend the mask onto it and draw
+ * it onto the image with the paint's blend mode.  Errors as the reference:
+ * "Linear gradient requires 2 handles", "Radial gradient requires 3 handles",
+ * "Angular gradient requires 2 handles" (sic, for 3),
+ * "Gradient must have at least 1 color stop". */
+int pxg_image_fill_path_paint(pxg_image* image, const float* commands, int64_t n_commands,
+                              const pxg_paint* paint, const float transform[9], int winding_rule);
+int pxg_image_stroke_path_paint(pxg_image* image, const float* commands, int64_t n_commands,
+                                const pxg_paint* paint, const float transform[9], float stroke_width,
+                                int line_cap, int line_join, float miter_limit, const float* dashes,
+                                int64_t n_dashes);
+
+/* fill(Image, Paint)  src/pixie.nim:120-131: the colour, the image paint
+ * through a full-image rectangle, or the gradient written in place. */
+int pxg_image_fill_paint(pxg_image* image, const pxg_paint* paint);
+
 /* blur(Image, float32, Color)  src/pixie/images.nim:304-365
  * (bindings/bindings.nim:133) */
 int pxg_image_blur(pxg_image* image, float radius, const float out_of_bounds[4]);

@@ -2525,6 +2525,20 @@ int pxo_fill_paint(uint8_t* rgbx_data, int64_t w, int64_t h, const float* paint,
 
 float pxo_atan2(float y, float x) { return atan2_cr(y, x); }
 
+int pxo_draw_tiled(uint8_t* a, int64_t aw, int64_t ah, const uint8_t* b, int64_t bw, int64_t bh,
+                   const float* mat3, int blend) {
+  try {
+    Image A{aw, ah, (RGBX*)a};
+    Image B{bw, bh, (RGBX*)b};
+    Mat3 M;
+    memcpy(M.m, mat3, sizeof(M.m));
+    drawCorrect(A, B, M, blend, true);
+    return 0;
+  } catch (const std::exception& e) {
+    return fail(e);
+  }
+}
+
 int pxo_draw_transform(uint8_t* a, int64_t aw, int64_t ah, const uint8_t* b, int64_t bw, int64_t bh,
                        const float* mat3, int blend) {
   try {

@@ -53,6 +53,7 @@ def lib():
         L.pxo_fill_path_paint.argtypes = [P, I64, I64, P, I64, P, I64, P, I64, I64, P, I]
         L.pxo_stroke_path_paint.argtypes = [P, I64, I64, P, I64, P, I64, P, I64, I64, P, F, I, I, F, P, I]
         L.pxo_fill_paint.argtypes = [P, I64, I64, P, I64, P, I64, I64]
+        L.pxo_draw_tiled.argtypes = [P, I64, I64, P, I64, I64, P, I]
         L.pxo_atan2.argtypes = [F, F]
         L.pxo_atan2.restype = F
         L.pxo_minify_by2.argtypes = [P, I64, I64, P]
@@ -205,6 +206,12 @@ def fill_paint(img, paint):
     f, pimg, pw, ph = _paint_args(paint)
     _check(lib().pxo_fill_paint(_p(img), img.shape[1], img.shape[0], _p(f), f.size,
                                 _p(pimg) if pimg is not None else None, pw, ph))
+
+
+def draw_tiled(a, b, mat, blend=0):
+    """drawTiled(a, b, transform, blendMode); mat is a column-major Mat3"""
+    _check(lib().pxo_draw_tiled(_p(a), a.shape[1], a.shape[0], _p(b), b.shape[1], b.shape[0], _p(_f32(mat, 9)),
+                                int(blend)))
 
 
 def atan2(y, x):

@@ -96,6 +96,10 @@ def lib():
         L.pxg_image_stroke_path.argtypes = [P, P, I64, P, F, I, P, F, I, I, F, P, I64]
         L.pxg_image_draw.argtypes = [P, P, I64, I64, I]
         L.pxg_image_draw_transform.argtypes = [P, P, P, I]
+        L.pxg_image_draw_tiled.argtypes = [P, P, P, I]
+        L.pxg_image_fill_path_paint.argtypes = [P, P, I64, P, P, I]
+        L.pxg_image_stroke_path_paint.argtypes = [P, P, I64, P, P, F, I, I, F, P, I64]
+        L.pxg_image_fill_paint.argtypes = [P, P]
         L.pxg_image_minify_by2.argtypes = [P, I]
         L.pxg_image_minify_by2.restype = P
         L.pxg_image_magnify_by2.argtypes = [P, I]
@@ -186,13 +190,51 @@ def scale(x, y):
     return np.array([x, 0, 0, 0, y, 0, 0, 0, 1], dtype=np.float32)
 
 
-class Paint:
-    """A solid paint (paints.nim:12-26): colour, opacity and blend mode."""
+class PaintKind(enum.IntEnum):  # paints.nim:4-10
+    SolidPaint = 0
+    ImagePaint = 1
+    TiledImagePaint = 2
+    LinearGradientPaint = 3
+    RadialGradientPaint = 4
+    AngularGradientPaint = 5
 
-    def __init__(self, color=(0, 0, 0, 1), opacity=1.0, blend_mode=BlendMode.NormalBlend):
+
+class _CPaint(C.Structure):  # pxg_paint (include/pxg.h)
+    _fields_ = [("kind", C.c_int32), ("blend_mode", C.c_int32), ("opacity", C.c_float),
+                ("color", C.c_float * 4), ("image", C.c_void_p), ("image_mat", C.c_float * 9),
+                ("n_handles", C.c_int32), ("handles", C.c_void_p), ("n_stops", C.c_int32),
+                ("stops", C.c_void_p)]
+
+
+class Paint:
+    """A paint (paints.nim:12-26): a solid colour, an image (imageMat places it,
+    tiled or not) or a linear / radial / angular gradient (handle positions in
+    image space, colour stops (color, position)); opacity and blend mode."""
+
+    def __init__(self, color=(0, 0, 0, 1), opacity=1.0, blend_mode=BlendMode.NormalBlend,
+                 kind=PaintKind.SolidPaint, image=None, image_mat=None, handles=(), stops=()):
+        self.kind = kind
         self.color = color
         self.opacity = opacity
         self.blend_mode = blend_mode
+        self.image = image
+        self.image_mat = image_mat
+        self.handles = list(handles)
+        self.stops = list(stops)
+
+    def _c(self):
+        """(the pxg_paint struct, arrays it points into, kept alive by the caller)"""
+        cp = _CPaint()
+        cp.kind, cp.blend_mode, cp.opacity = int(self.kind), int(self.blend_mode), float(self.opacity)
+        cp.color[:] = [float(v) for v in _color(self.color)]
+        cp.image = self.image._h if self.image is not None else None
+        cp.image_mat[:] = [float(v) for v in (_mat(self.image_mat) if self.image_mat is not None
+                                              else np.array([1, 0, 0, 0, 1, 0, 0, 0, 1], np.float32))]
+        h = np.ascontiguousarray(np.asarray(self.handles, np.float32).reshape(-1))
+        st = np.ascontiguousarray(np.asarray([list(c) + [pos] for c, pos in self.stops], np.float32).reshape(-1))
+        cp.n_handles, cp.handles = len(self.handles), (h.ctypes.data if h.size else None)
+        cp.n_stops, cp.stops = len(self.stops), (st.ctypes.data if st.size else None)
+        return cp, (h, st)
 
 
 def _paint(p):
@@ -248,12 +290,22 @@ class Image:
 
     # -- pixie's Image procs -------------------------------------------------
     def fill(self, color):
+        """fill with a colour (images.nim:55-57) or a Paint (pixie.nim:120-131)"""
+        if isinstance(color, Paint):
+            cp, keep = color._c()
+            _check(lib().pxg_image_fill_paint(self._h, C.byref(cp)))
+            return
         _check(lib().pxg_image_fill(self._h, _ptr(_color(color))))
 
     def fill_path(self, path, paint, transform=None, winding_rule=WindingRule.NonZero):
         cmds = as_commands(path)
-        col, op, blend = _paint(paint)
         m = _mat(transform)
+        if isinstance(paint, Paint) and paint.kind != PaintKind.SolidPaint:
+            cp, keep = paint._c()
+            _check(lib().pxg_image_fill_path_paint(self._h, _ptr(cmds), cmds.size, C.byref(cp),
+                                                   None if m is None else _ptr(m), int(winding_rule)))
+            return
+        col, op, blend = _paint(paint)
         _check(lib().pxg_image_fill_path(self._h, _ptr(cmds), cmds.size, _ptr(col), op, blend,
                                          None if m is None else _ptr(m), int(winding_rule)))
 
@@ -261,9 +313,16 @@ class Image:
                     line_cap=LineCap.ButtCap, line_join=LineJoin.MiterJoin,
                     miter_limit=DEFAULT_MITER_LIMIT, dashes=()):
         cmds = as_commands(path)
-        col, op, blend = _paint(paint)
         m = _mat(transform)
         d = np.ascontiguousarray(list(dashes) if len(dashes) else [0.0], dtype=np.float32)
+        if isinstance(paint, Paint) and paint.kind != PaintKind.SolidPaint:
+            cp, keep = paint._c()
+            _check(lib().pxg_image_stroke_path_paint(self._h, _ptr(cmds), cmds.size, C.byref(cp),
+                                                     None if m is None else _ptr(m), float(stroke_width),
+                                                     int(line_cap), int(line_join), float(miter_limit),
+                                                     _ptr(d), len(dashes)))
+            return
+        col, op, blend = _paint(paint)
         _check(lib().pxg_image_stroke_path(self._h, _ptr(cmds), cmds.size, _ptr(col), op, blend,
                                            None if m is None else _ptr(m), float(stroke_width),
                                            int(line_cap), int(line_join), float(miter_limit),
@@ -283,6 +342,11 @@ class Image:
         like vmath's Mat3 (translation in [6], [7])."""
         m = np.ascontiguousarray(np.asarray(transform, dtype=np.float32).reshape(9))
         _check(lib().pxg_image_draw_transform(self._h, b._h, _ptr(m), int(blend_mode)))
+
+    def draw_tiled(self, b: "Image", transform, blend_mode=BlendMode.NormalBlend):
+        """drawTiled(a, b, transform, mode) (images.nim:680-683)"""
+        m = np.ascontiguousarray(np.asarray(transform, dtype=np.float32).reshape(9))
+        _check(lib().pxg_image_draw_tiled(self._h, b._h, _ptr(m), int(blend_mode)))
 
     def minify_by2(self, power: int = 1) -> "Image":
         h = lib().pxg_image_minify_by2(self._h, int(power))

@@ -16,6 +16,7 @@
 
 #include "../../include/pxg.h"
 #include "host_geom.h"
+#include "paint.cuh"
 #include "pxg_device.cuh"
 #include "raster.cuh"
 
@@ -236,6 +237,10 @@ struct Ctx {
   long long ovf_cap = 0;
   long long* xcl = nullptr;
   long long xcl_cap = 0;
+  uint32_t* pt_buf[2] = {nullptr, nullptr};  // the mask and the fill image of a non-solid paint
+  long long pt_cap[2] = {0, 0};
+  float* pt_stops = nullptr;  // gradient stops on the device
+  long long pt_stops_cap = 0;
   uint32_t* sm_buf[2] = {nullptr, nullptr};  // minify/magnify pre-pass images (ping-pong)
   long long sm_cap[2] = {0, 0};
   uint8_t* fsteps = nullptr;  // flattening step records (fill setup)
@@ -2065,6 +2070,154 @@ pxg_image* resampled_copy(const pxg_image* im, int power, bool minify) {
     CU(cudaMemcpyAsync(res->data, im->data, (size_t)(w * h * 4), cudaMemcpyDeviceToDevice, g.stream));
   return res;
 }
+
+// drawCorrect / drawTiled  images.nim:405-445, :680-683: every destination
+// pixel samples the (pre-passed) source at inverseTransform * (x + h, y + h) - h
+void draw_correct(pxg_image* a, const pxg_image* b, const M3& T, int blend, bool tiled) {
+  M3 inv = m3inv(T);
+  V p = m3v(inv, 0 + kH, 0 + kH);
+  V dx = vsub(m3v(inv, 1 + kH, 0 + kH), p);
+  V dy = vsub(m3v(inv, 0 + kH, 1 + kH), p);
+  float filterBy2 = fnmax(vlen(dx), vlen(dy));
+  if (std::isinf(filterBy2)) throw ApiError{"draw transform is not invertible"};
+  const uint32_t* src = (const uint32_t*)b->data;
+  int64_t bw = b->width, bh = b->height;
+  int k = 0;
+  while (filterBy2 >= 2.0f) {
+    src = resample_level(src, bw, bh, true, k);
+    k ^= 1;
+    p = V{p.x / 2, p.y / 2};
+    dx = V{dx.x / 2, dx.y / 2};
+    dy = V{dy.x / 2, dy.y / 2};
+    filterBy2 /= 2;
+    inv = m3mul(M3{{0.5f, 0, 0, 0, 0.5f, 0, 0, 0, 1}}, inv);
+  }
+  while (filterBy2 <= 0.5f) {
+    if (bw * bh > ((int64_t)1 << 30)) throw ApiError{"draw would magnify the source image beyond 2^32 bytes"};
+    src = resample_level(src, bw, bh, false, k);
+    k ^= 1;
+    p = V{p.x * 2, p.y * 2};
+    dx = V{dx.x * 2, dx.y * 2};
+    dy = V{dy.x * 2, dy.y * 2};
+    filterBy2 *= 2;
+    inv = m3mul(M3{{2, 0, 0, 0, 2, 0, 0, 0, 1}}, inv);
+  }
+  Mat9 I;
+  memcpy(I.m, inv.m, sizeof I.m);
+  launch_draw_correct((uint32_t*)a->data, a->width, a->height, src, bw, bh, I, blend, tiled, g.tbl, g.nsm, g.stream);
+}
+
+// ---------------------------------------------------------------------------
+// Non-solid paints: gradient fills (paints.nim:95-241) and the
+// mask -> fill -> MaskBlend -> draw chain of fillPath / strokePath
+// (paths.nim:2115-2142).  The per-paint geometry (the radial gradient's
+// matrix, the edge angles) is float32 host arithmetic with the C library's
+// atan2f / sinf / cosf, as the reference computes it once per paint.
+// ---------------------------------------------------------------------------
+inline float fix_angle_h(float a) {  // a float32 compared with the float64 PI
+  const double pi = 3.141592653589793;
+  const float tau = (float)(pi * 2);
+  while ((double)a > pi) a -= tau;
+  while ((double)a < -pi) a += tau;
+  return a;
+}
+inline V vnorm(V v) {
+  const float l = vlen(v);
+  return V{v.x / l, v.y / l};
+}
+
+pxg_image temp_image(int i, int64_t w, int64_t h) {  // a zeroed non-owning scratch image
+  dev_grow(g.pt_buf[i], g.pt_cap[i], w * h);
+  CU(cudaMemsetAsync(g.pt_buf[i], 0, (size_t)(w * h * 4), g.stream));
+  return pxg_image{(uint8_t*)g.pt_buf[i], w, h, 0};
+}
+
+void fill_gradient(pxg_image* im, const pxg_paint& p, float opacity) {
+  const int nh = p.n_handles, ns = p.n_stops;
+  if (nh < 0 || ns < 0 || (nh > 0 && !p.handles) || (ns > 0 && !p.stops)) throw ApiError{"Invalid gradient"};
+  if (p.kind == 3 && nh != 2) throw ApiError{"Linear gradient requires 2 handles"};
+  if (p.kind == 4 && nh != 3) throw ApiError{"Radial gradient requires 3 handles"};
+  if (p.kind == 5 && nh != 3) throw ApiError{"Angular gradient requires 2 handles"};
+  if (ns == 0) throw ApiError{"Gradient must have at least 1 color stop"};
+  opacity = opacity < 0 ? 0 : (opacity > 1 ? 1 : opacity);
+  if (opacity == 0) return;
+  GradientArgs G{};
+  G.kind = p.kind;
+  G.nstops = ns;
+  G.opacity = opacity;
+  const V h0{p.handles[0], p.handles[1]}, h1{p.handles[2], p.handles[3]};
+  if (p.kind == 3) {
+    const V d = vsub(h1, h0);
+    G.atx = h0.x;
+    G.aty = h0.y;
+    G.dx = d.x;
+    G.dy = d.y;
+    G.det = d.x * d.x + d.y * d.y;
+  } else if (p.kind == 4) {
+    const V skew{p.handles[4], p.handles[5]};
+    const float distanceX = vlen(vsub(h0, h1)), distanceY = vlen(vsub(h0, skew));
+    const V n = vnorm(vsub(h0, h1));
+    const float ang = fix_angle_h(atan2f(n.y, n.x));
+    const float sn = sinf(ang), cs = cosf(ang);
+    const M3 T{{1, 0, 0, 0, 1, 0, h0.x, h0.y, 1}}, R{{cs, sn, 0, -sn, cs, 0, 0, 0, 1}};
+    const M3 S{{distanceX, 0, 0, 0, distanceY, 0, 0, 0, 1}};
+    const M3 inv = m3inv(m3mul(m3mul(T, R), S));
+    memcpy(G.m, inv.m, sizeof G.m);
+  } else {
+    const V n = vnorm(vsub(h1, h0));
+    G.cx = h0.x;
+    G.cy = h0.y;
+    G.gradientAngle = fix_angle_h(atan2f(n.y, n.x));
+  }
+  dev_grow(g.pt_stops, g.pt_stops_cap, 5 * (long long)ns);
+  CU(cudaMemcpyAsync(g.pt_stops, p.stops, sizeof(float) * 5 * (size_t)ns, cudaMemcpyHostToDevice, g.stream));
+  launch_gradient((uint32_t*)im->data, im->width, im->height, G, g.pt_stops, g.nsm, g.stream);
+}
+
+void check_paint(const pxg_paint* p) {
+  if (!p) throw ApiError{"paint is null"};
+  if (p->kind < 0 || p->kind > 5) throw ApiError{"Invalid paint kind"};
+  check_blend(p->blend_mode);
+  if ((p->kind == 1 || p->kind == 2)) {
+    if (!p->image) throw ApiError{"Image paint needs an image"};
+    check_image(p->image);
+  }
+}
+
+// the paint's own image at opacity 1  paths.nim:2121-2134
+void paint_fill_image(pxg_image* fill, const pxg_paint& p) {
+  M3 m;
+  memcpy(m.m, p.image_mat, sizeof m.m);
+  if (p.kind == 1)
+    draw_transform(fill, p.image, m, 0);
+  else if (p.kind == 2)
+    draw_correct(fill, p.image, m, 0, true);
+  else
+    fill_gradient(fill, p, 1.0f);
+}
+
+// images.nim:261-277
+void apply_opacity(pxg_image* im, float opacity) {
+  const uint32_t o = (uint16_t)h_nim_i32(roundf(255 * opacity));
+  if (o == 255) return;
+  if (o == 0) {
+    CU(cudaMemsetAsync(im->data, 0, (size_t)(im->width * im->height * 4), g.stream));
+    return;
+  }
+  launch_apply_opacity((uint32_t*)im->data, im->width * im->height, o, g.nsm, g.stream);
+}
+
+// fill.draw(mask, MaskBlend); image.draw(fill, blendMode)  paths.nim:2136-2142
+void composite_paint(pxg_image* im, pxg_image* mask, const pxg_paint& p) {
+  pxg_image fill = temp_image(1, im->width, im->height);
+  paint_fill_image(&fill, p);
+  const float op = p.opacity < 0 ? 0 : (p.opacity > 1 ? 1 : p.opacity);
+  if (op != 1) apply_opacity(mask, op);
+  const int64_t W = im->width, H = im->height;
+  launch_draw((uint32_t*)fill.data, (const uint32_t*)mask->data, W, H, W, H, 0, 0, kMask, g.tbl, g.nsm, g.stream);
+  launch_draw((uint32_t*)im->data, (const uint32_t*)fill.data, W, H, W, H, 0, 0, p.blend_mode, g.tbl, g.nsm,
+              g.stream);
+}
 }  // namespace
 
 extern "C" {
@@ -2101,6 +2254,91 @@ static pxg_image* resampled(const pxg_image* im, int power, bool minify) {
 }
 pxg_image* pxg_image_minify_by2(const pxg_image* im, int power) { return resampled(im, power, true); }
 pxg_image* pxg_image_magnify_by2(const pxg_image* im, int power) { return resampled(im, power, false); }
+
+int pxg_image_draw_tiled(pxg_image* a, const pxg_image* b, const float* mat3, int blend) {
+  return guarded([&] {
+    check_image(a);
+    check_image(b);
+    check_blend(blend);
+    if (!mat3) throw ApiError{"transform is null"};
+    M3 T;
+    memcpy(T.m, mat3, sizeof(T.m));
+    Timed t;
+    draw_correct(a, b, T, blend, true);
+    CU(cudaGetLastError());
+    t.done();
+  });
+}
+
+int pxg_image_fill_path_paint(pxg_image* im, const float* cmds, int64_t n, const pxg_paint* paint,
+                              const float* transform, int winding) {
+  return guarded([&] {
+    check_image(im);
+    check_paint(paint);
+    const float op = paint->opacity < 0 ? 0 : (paint->opacity > 1 ? 1 : paint->opacity);
+    if (op == 0) return;  // paths.nim:2101-2104
+    if (paint->kind == 0) {
+      if (pxg_image_fill_path(im, cmds, n, paint->color, paint->opacity, paint->blend_mode, transform, winding) != 0)
+        throw ApiError{std::string(t_err)};
+      return;
+    }
+    pxg_image mask = temp_image(0, im->width, im->height);
+    static const float white[4] = {1, 1, 1, 1};
+    if (pxg_image_fill_path(&mask, cmds, n, white, 1, 0, transform, winding) != 0) throw ApiError{std::string(t_err)};
+    Timed t;
+    composite_paint(im, &mask, *paint);
+    CU(cudaGetLastError());
+    t.done();
+  });
+}
+
+int pxg_image_stroke_path_paint(pxg_image* im, const float* cmds, int64_t n, const pxg_paint* paint,
+                                const float* transform, float width, int cap, int join, float miterLimit,
+                                const float* dashes, int64_t nd) {
+  return guarded([&] {
+    check_image(im);
+    check_paint(paint);
+    const float op = paint->opacity < 0 ? 0 : (paint->opacity > 1 ? 1 : paint->opacity);
+    if (op == 0) return;
+    if (paint->kind == 0) {
+      if (pxg_image_stroke_path(im, cmds, n, paint->color, paint->opacity, paint->blend_mode, transform, width, cap,
+                                join, miterLimit, dashes, nd) != 0)
+        throw ApiError{std::string(t_err)};
+      return;
+    }
+    pxg_image mask = temp_image(0, im->width, im->height);
+    static const float white[4] = {1, 1, 1, 1};
+    if (pxg_image_stroke_path(&mask, cmds, n, white, 1, 0, transform, width, cap, join, miterLimit, dashes, nd) != 0)
+      throw ApiError{std::string(t_err)};
+    Timed t;
+    composite_paint(im, &mask, *paint);
+    CU(cudaGetLastError());
+    t.done();
+  });
+}
+
+// fill(image, paint)  pixie.nim:120-131
+int pxg_image_fill_paint(pxg_image* im, const pxg_paint* paint) {
+  return guarded([&] {
+    check_image(im);
+    check_paint(paint);
+    if (paint->kind == 0) {
+      if (pxg_image_fill(im, paint->color) != 0) throw ApiError{std::string(t_err)};
+      return;
+    }
+    if (paint->kind == 1 || paint->kind == 2) {
+      CU(cudaMemsetAsync(im->data, 0, (size_t)(im->width * im->height * 4), g.stream));
+      const float w = (float)im->width, h = (float)im->height;
+      const float rect[] = {1, 0, 0, 2, w, 0, 2, w, h, 2, 0, h, 0};  // Move, Line x3, Close
+      if (pxg_image_fill_path_paint(im, rect, 13, paint, nullptr, 0) != 0) throw ApiError{std::string(t_err)};
+      return;
+    }
+    Timed t;
+    fill_gradient(im, *paint, paint->opacity);
+    CU(cudaGetLastError());
+    t.done();
+  });
+}
 
 int pxg_image_blur(pxg_image* im, float radius, const float* oob) {
   return guarded([&] {

@@ -1,0 +1,239 @@
+// Non-solid paints (src/pixie/paints.nim): gradient fills, applyOpacity
+// (images.nim:261-277) and drawTiled / drawCorrect (images.nim:405-445,
+// :680-683), the device parts of fillPath / strokePath with a paint
+// (paths.nim:2115-2142, :2178-2210).
+//
+// All three are one pixel per thread, HBM-bound apart from the angular
+// gradient's float64 arctangent.  Every float32 expression keeps the
+// reference's operation order (the file is built with -fmad=false).
+#include <cfloat>
+#include <cstdint>
+
+#include "paint.cuh"
+#include "pxg_device.cuh"
+
+namespace pxg {
+
+void note_launch();
+
+namespace {
+
+constexpr double kPI64 = 3.141592653589793;
+
+// atan for x >= 0 in float64: pi/2 - atan(1/x) above 1, two halvings
+// atan(x) = 2 atan(x / (1 + sqrt(1 + x^2))) to |x| < 0.2, 14 Taylor terms
+__device__ double atan_unit(double x) {
+  const bool inv = x > 1;
+  if (inv) x = 1 / x;
+  x = x / (1 + sqrt(1 + x * x));
+  x = x / (1 + sqrt(1 + x * x));
+  const double x2 = x * x;
+  double term = x, sum = x;
+#pragma unroll 1
+  for (int n = 1; n <= 13; n++) {
+    term = term * -x2;
+    sum = sum + term / (double)(2 * n + 1);
+  }
+  sum = sum * 4;
+  return inv ? 1.5707963267948966 - sum : sum;
+}
+// atan2 of float32 arguments rounded once to float32 (correctly rounded but
+// for true values within ~1e-16 of a rounding boundary)
+__device__ float atan2_cr(float y, float x) {
+  if (isnan(x) || isnan(y)) return __int_as_float(0x7fc00000);
+  double r;
+  if (y == 0) {
+    r = signbit(x) ? kPI64 : 0.0;
+  } else if (x == 0) {
+    r = kPI64 / 2;
+  } else if (isinf(x) || isinf(y)) {
+    if (isinf(x) && isinf(y))
+      r = x > 0 ? kPI64 / 4 : 3 * kPI64 / 4;
+    else if (isinf(x))
+      r = x > 0 ? 0.0 : kPI64;
+    else
+      r = kPI64 / 2;
+  } else {
+    const double a = atan_unit(fabs((double)y / (double)x));
+    r = x > 0 ? a : kPI64 - a;
+  }
+  return (float)(signbit(y) ? -r : r);
+}
+// fixAngle: a float32 compared with the float64 PI, stepped by float32 tau
+__device__ __forceinline__ float fix_angle(float a) {
+  const float tau = (float)(kPI64 * 2);
+  while ((double)a > kPI64) a -= tau;
+  while ((double)a < -kPI64) a += tau;
+  return a;
+}
+__device__ __forceinline__ uint32_t color_rgbx(float r, float g, float b, float a) {  // chroma asRgbx
+  return premul8(pack(unit_to_u8(r), unit_to_u8(g), unit_to_u8(b), unit_to_u8(a)));
+}
+
+// gradientColor  paints.nim:68-93 (chroma mix: a + (b - a) * t per component)
+__device__ uint32_t gradient_color(const float* __restrict__ st, int n, float opacity, float t) {
+  int index = -1;
+  for (int i = 0; i < n; i++) {
+    const float pos = st[5 * i + 4];
+    if (pos < t) index = i;
+    if (pos > t) break;
+  }
+  float c[4];
+  if (index == -1) {
+    for (int k = 0; k < 4; k++) c[k] = st[k];
+  } else if (index + 1 >= n) {
+    for (int k = 0; k < 4; k++) c[k] = st[5 * index + k];
+  } else {
+    const float* a = st + 5 * index;
+    const float* b = a + 5;
+    const float u = (t - a[4]) / (b[4] - a[4]);
+    for (int k = 0; k < 4; k++) c[k] = a[k] + (b[k] - a[k]) * u;
+  }
+  c[3] *= opacity;
+  return color_rgbx(c[0], c[1], c[2], c[3]);
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(256) k_gradient(uint32_t* __restrict__ img, long long W, long long H, GradientArgs g,
+                                                  const float* __restrict__ stops) {
+  const long long n = W * H;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long y = i / W, x = i - y * W;
+    const float fx = (float)x, fy = (float)y;
+    float t;
+    if (KIND == 3) {  // toLineSpace  paints.nim:111-116
+      t = (g.dy * (fy - g.aty) + g.dx * (fx - g.atx)) / g.det;
+    } else if (KIND == 4) {  // (mat * xy).length()  :201-203
+      const float vx = g.m[0] * fx + g.m[3] * fy + g.m[6], vy = g.m[1] * fx + g.m[4] * fy + g.m[7];
+      t = sqrtf(vx * vx + vy * vy);
+    } else {  // :222-227
+      const float vx = fx - g.cx, vy = fy - g.cy;
+      const float len = sqrtf(vx * vx + vy * vy);
+      const float angle = atan2_cr(vy / len, vx / len);
+      const float f32PI = (float)kPI64;
+      t = fix_angle(angle + g.gradientAngle + f32PI / 2) / 2 / f32PI + 0.5f;
+    }
+    img[i] = gradient_color(stops, g.nstops, g.opacity, t);
+  }
+}
+
+// applyOpacity with o = round(255 * opacity) in 1..254: (c * o) div 255
+__global__ void __launch_bounds__(256) k_apply_opacity(uint32_t* __restrict__ img, long long n, uint32_t o) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const Px p = unpack(img[i]);
+    img[i] = pack((p.r * o) / 255, (p.g * o) / 255, (p.b * o) / 255, (p.a * o) / 255);
+  }
+}
+
+__device__ __forceinline__ uint32_t mix_rgbx(uint32_t a, uint32_t b, float t) {  // common.nim:59-65
+  const uint32_t x = nim_u32(roundf(t * 255.0f));
+  const Px p = unpack(a), q = unpack(b);
+  return pack((p.r * (255 - x) + q.r * x + 127) / 255, (p.g * (255 - x) + q.g * x + 127) / 255,
+              (p.b * (255 - x) + q.b * x + 127) / 255, (p.a * (255 - x) + q.a * x + 127) / 255);
+}
+
+// getRgbaSmooth, wrapped (images.nim:381-385) when TILED: the taps are
+// data[w * (y mod h) + (x mod w)] with Nim's truncating mod, read linearly;
+// an address outside the buffer reads transparent.  Not wrapped: image[x, y],
+// transparent outside.
+template <bool TILED>
+__device__ __forceinline__ uint32_t tap(const uint32_t* __restrict__ b, long long bw, long long bh, long long x,
+                                        long long y) {
+  if (TILED) {
+    const long long i = bw * (y % bh) + (x % bw);
+    return (i >= 0 && i < bw * bh) ? __ldg(b + i) : 0u;
+  }
+  return (x >= 0 && x < bw && y >= 0 && y < bh) ? __ldg(b + y * bw + x) : 0u;
+}
+template <bool TILED>
+__device__ uint32_t sample(const uint32_t* __restrict__ b, long long bw, long long bh, float x, float y) {
+  const float fx = floorf(x), fy = floorf(y);
+  const long long x0 = nim_int(fx), y0 = nim_int(fy);
+  const long long x1 = x0 == 9223372036854775807LL ? x0 : x0 + 1, y1 = y0 == 9223372036854775807LL ? y0 : y0 + 1;
+  const float xf = x - fx, yf = y - fy;
+  const uint32_t x0y0 = tap<TILED>(b, bw, bh, x0, y0), x1y0 = tap<TILED>(b, bw, bh, x1, y0);
+  const uint32_t x0y1 = tap<TILED>(b, bw, bh, x0, y1), x1y1 = tap<TILED>(b, bw, bh, x1, y1);
+  uint32_t top = x0y0;
+  if (xf > 0 && x0y0 != x1y0) top = mix_rgbx(x0y0, x1y0, xf);
+  uint32_t bottom = x0y1;
+  if (xf > 0 && x0y1 != x1y1) bottom = mix_rgbx(x0y1, x1y1, xf);
+  if (yf != 0 && top != bottom) return mix_rgbx(top, bottom, yf);
+  return top;
+}
+
+template <int MODE>
+__device__ __forceinline__ uint32_t blend_mode_px(const uint8_t* tbl, uint32_t a, uint32_t s) {
+  if (MODE == kNormal) return blendNormal(a, s);
+  if (MODE == kOverwrite) return s;
+  if (MODE == kMask) return blendMaskPx(a, s);
+  return blend_px(MODE, tbl, a, s);
+}
+
+// drawCorrect's per-pixel loop: every destination pixel samples
+// inverseTransform * (x + h, y + h) - h and blends
+template <int MODE, bool TILED>
+__global__ void __launch_bounds__(256) k_draw_correct(uint32_t* __restrict__ a, long long W, long long H,
+                                                      const uint32_t* __restrict__ b, long long bw, long long bh,
+                                                      Mat9 inv, const uint8_t* tbl) {
+  const long long n = W * H;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long y = i / W, x = i - y * W;
+    const float px = (float)x + 0.5f, py = (float)y + 0.5f;
+    const float sx = inv.m[0] * px + inv.m[3] * py + inv.m[6], sy = inv.m[1] * px + inv.m[4] * py + inv.m[7];
+    const uint32_t s = sample<TILED>(b, bw, bh, sx - 0.5f, sy - 0.5f);
+    a[i] = blend_mode_px<MODE>(tbl, a[i], s);
+  }
+}
+
+unsigned grid(long long n, int nsm) {
+  long long blocks = (n + 255) / 256;
+  if (blocks > (long long)nsm * 8) blocks = (long long)nsm * 8;
+  return (unsigned)(blocks < 1 ? 1 : blocks);
+}
+
+typedef void (*CorrectKernel)(uint32_t*, long long, long long, const uint32_t*, long long, long long, Mat9,
+                              const uint8_t*);
+template <int M>
+struct CorrectTable {
+  static void fill(CorrectKernel* t, CorrectKernel* u) {
+    t[M] = k_draw_correct<M, true>;
+    u[M] = k_draw_correct<M, false>;
+    CorrectTable<M + 1>::fill(t, u);
+  }
+};
+template <>
+struct CorrectTable<kNumBlends> {
+  static void fill(CorrectKernel*, CorrectKernel*) {}
+};
+
+}  // namespace
+
+void launch_gradient(uint32_t* img, long long W, long long H, const GradientArgs& g, const float* stops, int nsm,
+                     cudaStream_t st) {
+  const long long n = W * H;
+  if (g.kind == 3)
+    k_gradient<3><<<grid(n, nsm), 256, 0, st>>>(img, W, H, g, stops);
+  else if (g.kind == 4)
+    k_gradient<4><<<grid(n, nsm), 256, 0, st>>>(img, W, H, g, stops);
+  else
+    k_gradient<5><<<grid(n, nsm), 256, 0, st>>>(img, W, H, g, stops);
+  note_launch();
+}
+
+void launch_apply_opacity(uint32_t* img, long long n, uint32_t o, int nsm, cudaStream_t st) {
+  k_apply_opacity<<<grid(n, nsm), 256, 0, st>>>(img, n, o);
+  note_launch();
+}
+
+void launch_draw_correct(uint32_t* a, long long W, long long H, const uint32_t* b, long long bw, long long bh,
+                         const Mat9& inv, int mode, bool tiled, const uint8_t* tbl, int nsm, cudaStream_t st) {
+  static CorrectKernel tiledK[kNumBlends] = {nullptr}, plainK[kNumBlends] = {nullptr};
+  if (!tiledK[0]) CorrectTable<0>::fill(tiledK, plainK);
+  (tiled ? tiledK : plainK)[mode]<<<grid(W * H, nsm), 256, 0, st>>>(a, W, H, b, bw, bh, inv, tbl);
+  note_launch();
+}
+
+}  // namespace pxg

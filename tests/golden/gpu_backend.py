@@ -32,6 +32,18 @@ class GpuBackend:
     def minify(self, img, power):
         return img.minify_by2(power)
 
+    @staticmethod
+    def _paint(paint):
+        return px.Paint(paint.get("color", (0, 0, 0, 0)), paint.get("opacity", 1.0), paint.get("blend", 0),
+                        kind=paint["kind"], image=paint.get("image"), image_mat=paint.get("image_mat"),
+                        handles=paint.get("handles", ()), stops=paint.get("stops", ()))
+
+    def fill_path_paint(self, img, cmds, paint, mat=None, winding=0):
+        img.fill_path(cmds, self._paint(paint), mat, winding)
+
+    def fill_paint(self, img, paint):
+        img.fill(self._paint(paint))
+
     def blur(self, img, radius, oob):
         img.blur(radius, [np.float32(v) / np.float32(255) for v in oob])
 
