@@ -344,6 +344,7 @@ def run_fill_extras(px, wl, args, stream):
                                       "gpu_ms_per_path": round(gpu_ms / n, 4),
                                       "note": "one blocking C-ABI call per path, host pre-pass included"}
     out["draw_transform_2048"] = run_draw_transform(px, wl, stream, cpu=not args.no_cpu_baseline)
+    out["paints_2048"] = run_paints(px, wl, stream, cpu=not args.no_cpu_baseline)
     out["glyph_batch"] = run_glyphs(px, wl, args.glyphs)
     out["dense_scene_1024_2000"] = run_scene(px, wl)
     if args.serve_jobs > 0:
@@ -399,6 +400,57 @@ def run_draw_transform(px, wl, stream, cpu=True, reps=20):
             t = time.perf_counter()
             pxo.draw_transform(a, b, small, 0)
             out[name]["cpu_oracle_ms_scaled_to_2048"] = round((time.perf_counter() - t) * 1000 * 16, 1)
+    px.set_blocking(True)
+    return out
+
+
+PAINT_STOPS = [((1.0, 0.0, 0.0, 1.0), 0.0), ((0.2, 0.6, 1.0, 0.75), 0.4), ((0.0, 0.0, 0.5, 0.15625), 1.0)]
+PAINT_HANDLES = {3: [(0.0, 1024.0), (2048.0, 1024.0)], 4: [(1024.0, 1024.0), (2048.0, 1024.0), (1024.0, 2048.0)],
+                 5: [(1024.0, 1024.0), (2048.0, 1024.0), (1024.0, 2048.0)]}
+
+
+def run_paints(px, wl, stream, cpu=True, reps=10):
+    """Gradient fills of a 2048^2 image (fill(image, paint)) and fillPath of a
+    2048^2-scaled heart with a linear gradient paint (the mask / gradient /
+    MaskBlend / draw chain), GPU ms (CUDA events) beside the oracle."""
+    import torch
+    out = {}
+    img = px.Image(2048, 2048)
+    names = {3: "linear", 4: "radial", 5: "angular"}
+    for kind, hs in PAINT_HANDLES.items():
+        paint = px.Paint(kind=kind, handles=hs, stops=PAINT_STOPS)
+        px.set_blocking(False)
+        for _ in range(2):
+            img.fill(paint)
+        px.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            img.fill(paint)
+        e1.record(stream)
+        px.synchronize()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        row = {"gpu_ms": round(ms, 4), "gpix_per_s": round(2048 * 2048 / ms / 1e6, 2)}
+        if cpu:  # the oracle, one thread, on a 512^2 image with the handles scaled by 1/4
+            from oracle import pxo
+            small = pxo.new_image(512, 512)
+            t = time.perf_counter()
+            pxo.fill_paint(small, dict(kind=kind, handles=[(x / 4, y / 4) for x, y in hs], stops=PAINT_STOPS))
+            row["cpu_oracle_ms_scaled_to_2048"] = round((time.perf_counter() - t) * 1000 * 16, 1)
+        out[f"fill_{names[kind]}_gradient"] = row
+    heart = wl.heart_commands(20.48)
+    paint = px.Paint(kind=3, handles=PAINT_HANDLES[3], stops=PAINT_STOPS, opacity=0.8)
+    px.set_blocking(True)
+    for _ in range(2):
+        img.fill_path(heart, paint)
+    t = time.perf_counter()
+    for _ in range(reps):
+        img.fill_path(heart, paint)
+    dt = (time.perf_counter() - t) / reps * 1000
+    out["fill_path_linear_gradient_heart"] = {"call_ms": round(dt, 3),
+                                              "note": "one blocking call, 2048^2: mask fill + gradient + "
+                                                      "MaskBlend + draw"}
     px.set_blocking(True)
     return out
 

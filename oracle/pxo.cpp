@@ -1942,7 +1942,7 @@ struct PaintDesc {
 // whose true value lies within ~1e-16 of a rounding boundary): evaluated in
 // float64 from the mathematics alone -- atan(x) = pi/2 - atan(1/x) above 1,
 // two halvings atan(x) = 2 atan(x / (1 + sqrt(1 + x^2))) to |x| < 0.2, and
-// 14 terms of the Taylor series -- so the CUDA path, which runs the same
+// 14 terms of the Taylor series (Horner form) -- so the CUDA path, which runs the same
 // IEEE float64 operations, gets the same floats.  (pixie calls the C
 // library's atan2f, which is not reproduced here bit for bit.)
 static double atan_unit(double x) {  // x >= 0
@@ -1950,13 +1950,23 @@ static double atan_unit(double x) {  // x >= 0
   if (inv) x = 1 / x;
   x = x / (1 + sqrt(1 + x * x));
   x = x / (1 + sqrt(1 + x * x));
+  // x (1 - x^2/3 + x^4/5 - ... - x^26/27) in Horner form, 1/(2n+1) as float64 constants
   const double x2 = x * x;
-  double term = x, sum = x;
-  for (int n = 1; n <= 13; n++) {
-    term = term * -x2;
-    sum = sum + term / (double)(2 * n + 1);
-  }
-  sum = sum * 4;
+  double poly = -1.0 / 27;
+  poly = poly * x2 + 1.0 / 25;
+  poly = poly * x2 - 1.0 / 23;
+  poly = poly * x2 + 1.0 / 21;
+  poly = poly * x2 - 1.0 / 19;
+  poly = poly * x2 + 1.0 / 17;
+  poly = poly * x2 - 1.0 / 15;
+  poly = poly * x2 + 1.0 / 13;
+  poly = poly * x2 - 1.0 / 11;
+  poly = poly * x2 + 1.0 / 9;
+  poly = poly * x2 - 1.0 / 7;
+  poly = poly * x2 + 1.0 / 5;
+  poly = poly * x2 - 1.0 / 3;
+  poly = poly * x2 + 1.0;
+  const double sum = x * poly * 4;
   return inv ? 1.5707963267948966 - sum : sum;
 }
 static float atan2_cr(float y, float x) {

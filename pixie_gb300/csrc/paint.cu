@@ -21,20 +21,29 @@ namespace {
 constexpr double kPI64 = 3.141592653589793;
 
 // atan for x >= 0 in float64: pi/2 - atan(1/x) above 1, two halvings
-// atan(x) = 2 atan(x / (1 + sqrt(1 + x^2))) to |x| < 0.2, 14 Taylor terms
+// atan(x) = 2 atan(x / (1 + sqrt(1 + x^2))) to |x| < 0.2, 14 Taylor terms (Horner)
 __device__ double atan_unit(double x) {
   const bool inv = x > 1;
   if (inv) x = 1 / x;
   x = x / (1 + sqrt(1 + x * x));
   x = x / (1 + sqrt(1 + x * x));
+  // x (1 - x^2/3 + x^4/5 - ... - x^26/27) in Horner form, 1/(2n+1) as float64 constants
   const double x2 = x * x;
-  double term = x, sum = x;
-#pragma unroll 1
-  for (int n = 1; n <= 13; n++) {
-    term = term * -x2;
-    sum = sum + term / (double)(2 * n + 1);
-  }
-  sum = sum * 4;
+  double poly = -1.0 / 27;
+  poly = poly * x2 + 1.0 / 25;
+  poly = poly * x2 - 1.0 / 23;
+  poly = poly * x2 + 1.0 / 21;
+  poly = poly * x2 - 1.0 / 19;
+  poly = poly * x2 + 1.0 / 17;
+  poly = poly * x2 - 1.0 / 15;
+  poly = poly * x2 + 1.0 / 13;
+  poly = poly * x2 - 1.0 / 11;
+  poly = poly * x2 + 1.0 / 9;
+  poly = poly * x2 - 1.0 / 7;
+  poly = poly * x2 + 1.0 / 5;
+  poly = poly * x2 - 1.0 / 3;
+  poly = poly * x2 + 1.0;
+  const double sum = x * poly * 4;
   return inv ? 1.5707963267948966 - sum : sum;
 }
 // atan2 of float32 arguments rounded once to float32 (correctly rounded but

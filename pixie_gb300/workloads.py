@@ -191,3 +191,16 @@ def poisson_arrivals(seed: int, rate: float, n: int) -> np.ndarray:
     """n arrival times (seconds from 0) of a Poisson process of `rate` jobs/s."""
     u = uniform01(seed * 7 + 3, n).astype(np.float64)
     return np.cumsum(-np.log1p(-u) / rate)
+
+
+def heart_commands(scale: float = 1.0):
+    """pixie's test heart (tests/test_paints.nim:3-9, a 100x100 design) scaled by `scale`."""
+    from .paths import parse_path
+    k = float(scale)
+    return parse_path(f"""
+        M {10 * k},{30 * k}
+        A {20 * k},{20 * k} 0,0,1 {50 * k},{30 * k}
+        A {20 * k},{20 * k} 0,0,1 {90 * k},{30 * k}
+        Q {90 * k},{60 * k} {50 * k},{90 * k}
+        Q {10 * k},{60 * k} {10 * k},{30 * k} z
+    """).array()
