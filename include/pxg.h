@@ -221,6 +221,21 @@ int pxg_scene_stroke_path(pxg_scene* scene, const float* commands, int64_t n_com
                           const float color[4], float opacity, int blend_mode,
                           const float transform[9], float stroke_width, int line_cap,
                           int line_join, float miter_limit, const float* dashes, int64_t n_dashes);
+
+/* n recordings in one call, as n calls of pxg_scene_fill_path (kinds[i] 0)
+ * or pxg_scene_stroke_path (kinds[i] 1, no dashes) would make them: path i's
+ * commands are cmds[offs[i] .. offs[i + 1]), its paint colors[4 i ..],
+ * opacities[i], blends[i], its transform transforms[9 i ..] (NULL:
+ * identity), windings[i] (fills), widths / caps / joins / miters[i]
+ * (strokes).  The geometry is built on `threads` host threads (0: all) and the
+ * paths are appended in submission order.  status[i] (may be NULL) is 1 where
+ * path i failed -- it is skipped, as a failed call records nothing, and the
+ * first failure's message is left for pxg_take_error -- else 0. */
+int pxg_scene_record_batch(pxg_scene* scene, int64_t n, const int32_t* kinds, const float* cmds,
+                           const int64_t* offs, const float* colors, const float* opacities,
+                           const int32_t* blends, const float* transforms, const int32_t* windings,
+                           const float* widths, const int32_t* caps, const int32_t* joins,
+                           const float* miters, int32_t* status, int threads);
 int pxg_image_draw_scene(pxg_image* image, const pxg_scene* scene);
 /* Scene drawing configuration (every choice writes the same bytes):
  * slice_width is the part of a canvas row one warp of the drawing pass owns

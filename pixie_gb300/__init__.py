@@ -122,6 +122,7 @@ def lib():
         L.pxg_scene_len.restype = I64
         L.pxg_scene_fill_path.argtypes = [P, P, I64, P, F, I, P, I]
         L.pxg_scene_stroke_path.argtypes = [P, P, I64, P, F, I, P, F, I, I, F, P, I64]
+        L.pxg_scene_record_batch.argtypes = [P, I64, P, P, P, P, P, P, P, P, P, P, P, P, P, I]
         L.pxg_image_draw_scene.argtypes = [P, P]
         L.pxg_scene_config.argtypes = [I, I64]
         L.pxg_last_fill_stats.argtypes = [P]
@@ -401,6 +402,37 @@ class Scene:
         h, self._h = getattr(self, "_h", None), None
         if h and _lib is not None:
             _lib.pxg_scene_free(h)
+
+    def record_batch(self, paths, threads: int = 0) -> np.ndarray:
+        """Records many fill_path / stroke_path calls at once, their geometry
+        built on host threads and appended in order.  Each path is a dict:
+        kind ("fill" or "stroke"), cmds, color, opacity (1), blend (0),
+        transform (None), winding (fills), width / cap / join / miter (strokes).
+        Returns the per-path status (1 where the path failed and was skipped)."""
+        n = len(paths)
+        cm = [as_commands(p["cmds"]) for p in paths]
+        offs = np.zeros(n + 1, np.int64)
+        offs[1:] = np.cumsum([c.size for c in cm])
+        cmds = np.ascontiguousarray(np.concatenate(cm) if n else np.zeros(1, np.float32), dtype=np.float32)
+        kinds = np.array([0 if p["kind"] == "fill" else 1 for p in paths], np.int32)
+        colors = np.ascontiguousarray(np.array([_color(p["color"]) for p in paths], np.float32).reshape(-1))
+        ops = np.array([p.get("opacity", 1.0) for p in paths], np.float32)
+        blends = np.array([int(p.get("blend", 0)) for p in paths], np.int32)
+        has_t = any(p.get("transform") is not None for p in paths)
+        mats = (np.ascontiguousarray(np.array([_mat(p.get("transform")) if p.get("transform") is not None
+                                               else np.array([1, 0, 0, 0, 1, 0, 0, 0, 1], np.float32)
+                                               for p in paths], np.float32).reshape(-1)) if has_t else None)
+        wind = np.array([int(p.get("winding", 0)) for p in paths], np.int32)
+        widths = np.array([p.get("width", 1.0) for p in paths], np.float32)
+        caps = np.array([int(p.get("cap", 0)) for p in paths], np.int32)
+        joins = np.array([int(p.get("join", 0)) for p in paths], np.int32)
+        miters = np.array([p.get("miter", DEFAULT_MITER_LIMIT) for p in paths], np.float32)
+        status = np.zeros(max(n, 1), np.int32)
+        _check(lib().pxg_scene_record_batch(self._h, n, _ptr(kinds), _ptr(cmds), _ptr(offs), _ptr(colors),
+                                            _ptr(ops), _ptr(blends), None if mats is None else _ptr(mats),
+                                            _ptr(wind), _ptr(widths), _ptr(caps), _ptr(joins), _ptr(miters),
+                                            _ptr(status), int(threads)))
+        return status[:n]
 
     def __len__(self):
         return int(lib().pxg_scene_len(self._h))

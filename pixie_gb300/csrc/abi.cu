@@ -12,6 +12,8 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
+#include <atomic>
 #include <vector>
 
 #include "../../include/pxg.h"
@@ -1558,6 +1560,92 @@ int pxg_scene_stroke_path(pxg_scene* sc, const float* cmds, int64_t n, const flo
     sc->prims.insert(sc->prims.end(), prims.begin(), prims.end());
     sc->jobs.push_back(j);
     sc->dirty = true;
+  });
+}
+
+// n recordings at once: each path's geometry (the command walk, arcs, stroke
+// outlines) is built on a pool of host threads, independently, and the paths
+// are appended in submission order -- the scene n calls of
+// pxg_scene_fill_path / pxg_scene_stroke_path would build.
+int pxg_scene_record_batch(pxg_scene* sc, int64_t n, const int32_t* kinds, const float* cmds, const int64_t* offs,
+                           const float* colors, const float* opacities, const int32_t* blends,
+                           const float* transforms, const int32_t* windings, const float* widths,
+                           const int32_t* caps, const int32_t* joins, const float* miters, int32_t* status,
+                           int threads) {
+  return guarded_host([&] {
+    if (!sc) throw ApiError{"Invalid scene handle"};
+    if (n < 0 || (n > 0 && (!kinds || !cmds || !offs || !colors || !opacities || !blends)))
+      throw ApiError{"Invalid batch"};
+    struct Rec {
+      std::vector<Prim> prims;
+      PathJob job;
+      int state = 0;  // 0 nothing to draw, 1 recorded, 2 failed
+      std::string err;
+    };
+    std::vector<Rec> rec((size_t)n);
+    auto build = [&](int64_t i) {
+      Rec& r = rec[(size_t)i];
+      try {
+        const int blend = blends[i];
+        check_blend(blend);
+        const int64_t a = offs[i], b = offs[i + 1];
+        if (a < 0 || b < a) throw ApiError{"Invalid path commands"};
+        validate_commands(cmds + a, b - a);
+        uint32_t rgbx;
+        float op = opacities[i];
+        if (!paint_color(colors + 4 * i, op, blend, rgbx)) return;
+        const float* mat = transforms ? transforms + 9 * i : kIdent;
+        const float ps = pixel_scale(mat);
+        int winding = 0;
+        if (kinds[i] == 0) {
+          winding = windings ? windings[i] : 0;
+          if (winding != 0 && winding != 1) throw ApiError{"Invalid winding rule"};
+          build_fill_prims(cmds + a, b - a, ps, r.prims);
+        } else {
+          if (!widths || !caps || !joins || !miters) throw ApiError{"Invalid batch"};
+          build_stroke_prims(cmds + a, b - a, ps, widths[i], caps[i], joins[i], miters[i], nullptr, 0, r.prims);
+        }
+        r.job = make_job(nullptr, rgbx, blend, mat, ps, winding);
+        r.state = 1;
+      } catch (const ApiError& e) {
+        r.state = 2;
+        r.err = e.msg;
+      } catch (const GeomError& e) {
+        r.state = 2;
+        r.err = e.msg;
+      } catch (const std::exception& e) {
+        r.state = 2;
+        r.err = e.what();
+      }
+    };
+    int nt = threads > 0 ? threads : (int)std::thread::hardware_concurrency();
+    nt = std::max(1, std::min<int>(nt, (int)std::min<int64_t>(n / 4 + 1, 256)));
+    std::atomic<int64_t> next{0};
+    auto worker = [&] {
+      for (int64_t i = next.fetch_add(1); i < n; i = next.fetch_add(1)) build(i);
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; t++) pool.emplace_back(worker);
+    worker();
+    for (auto& t : pool) t.join();
+    size_t total = sc->prims.size();
+    for (const Rec& r : rec) total += r.state == 1 ? r.prims.size() : 0;
+    sc->prims.reserve(total);  // one allocation: no regrowth copies of the scene's primitives
+    sc->jobs.reserve(sc->jobs.size() + (size_t)n);
+    std::string firstErr;
+    for (int64_t i = 0; i < n; i++) {  // append in submission order
+      Rec& r = rec[(size_t)i];
+      if (status) status[i] = r.state == 2 ? 1 : 0;
+      if (r.state == 2 && firstErr.empty()) firstErr = r.err;
+      if (r.state != 1) continue;
+      r.job.prim_off = (long long)sc->prims.size();
+      r.job.nprims = (int)r.prims.size();
+      r.job.group = curve_group(r.prims, 0, r.job.nprims);
+      sc->prims.insert(sc->prims.end(), r.prims.begin(), r.prims.end());
+      sc->jobs.push_back(r.job);
+      sc->dirty = true;
+    }
+    if (!firstErr.empty()) set_err(firstErr.c_str());  // reported, not raised: the other paths are recorded
   });
 }
 

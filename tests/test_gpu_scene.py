@@ -92,6 +92,41 @@ def test_dense_scene_full_size_1024_2000_paths():
     assert_same(img.to_numpy(), ref, "scene 1024^2 x 2000")
 
 
+@pytest.mark.parametrize("threads", [1, 3, 0])
+def test_batched_recording_equals_per_call_recording(threads):
+    """record_batch builds the paths' geometry on host threads and appends
+    them in order: the same scene, the same failures, the same bytes (with
+    transforms and every blend mode)"""
+    items = wl.dense_scene(5, n_paths=600, size=512.0)
+    for k, it in enumerate(items):
+        if k % 3 == 0:
+            it["transform"] = [1.05, 0.02, 0, -0.03, 0.97, 0, 3.5, -2.25, 1]
+        it["blend"] = k % 20
+    f_one = []
+    sc1 = px.Scene()
+    for k, it in enumerate(items):
+        paint = px.Paint(it["color"], 1.0, it["blend"])
+        try:
+            if it["kind"] == "fill":
+                sc1.fill_path(it["cmds"], paint, it.get("transform"), it["winding"])
+            else:
+                sc1.stroke_path(it["cmds"], paint, it.get("transform"), it["width"], it["cap"], it["join"],
+                                it["miter"])
+            f_one.append(0)
+        except px.PixieError:
+            f_one.append(1)
+    sc2 = px.Scene()
+    status = sc2.record_batch(items, threads)
+    assert list(status) == f_one
+    assert len(sc1) == len(sc2)
+    bg = wl.premultiplied_image(9, 512, 512)
+    a = px.Image.from_numpy(bg)
+    a.draw_scene(sc1)
+    b = px.Image.from_numpy(bg)
+    b.draw_scene(sc2)
+    assert_same(b.to_numpy(), a.to_numpy(), f"batched recording, {threads} threads")
+
+
 def test_scene_equals_one_call_per_path():
     items = wl.dense_scene(11, n_paths=150, size=300.0)
     a = px.Image(300, 300)
