@@ -268,6 +268,15 @@ void pxg_masks_free(pxg_masks* masks);
 int64_t pxg_masks_len(const pxg_masks* masks);
 int pxg_masks_add_path(pxg_masks* masks, const float* commands, int64_t n_commands, int64_t width,
                        int64_t height, const float transform[9], int winding_rule);
+
+/* n glyphs in one call, as n calls of pxg_masks_add_path would add them
+ * (path i: cmds[offs[i] .. offs[i + 1]), widths[i] x heights[i],
+ * transforms[9 i ..] or NULL, windings[i] or NULL for NonZero); the geometry
+ * is built on `threads` host threads (0: all).  All or nothing: if a path
+ * fails, no glyph is added and its error is returned. */
+int pxg_masks_add_paths(pxg_masks* masks, int64_t n, const float* cmds, const int64_t* offs,
+                        const int64_t* widths, const int64_t* heights, const float* transforms,
+                        const int32_t* windings, int threads);
 int pxg_masks_render(pxg_masks* masks);
 /* Renders with a given row-kernel configuration instead of the tuned one
  * (variant 0: 256-crossing scratch, 1: 32-crossing scratch; rows per work

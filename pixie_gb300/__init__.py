@@ -123,6 +123,7 @@ def lib():
         L.pxg_scene_fill_path.argtypes = [P, P, I64, P, F, I, P, I]
         L.pxg_scene_stroke_path.argtypes = [P, P, I64, P, F, I, P, F, I, I, F, P, I64]
         L.pxg_scene_record_batch.argtypes = [P, I64, P, P, P, P, P, P, P, P, P, P, P, P, P, I]
+        L.pxg_masks_add_paths.argtypes = [P, I64, P, P, P, P, P, P, I]
         L.pxg_image_draw_scene.argtypes = [P, P]
         L.pxg_scene_config.argtypes = [I, I64]
         L.pxg_last_fill_stats.argtypes = [P]
@@ -487,6 +488,22 @@ class Masks:
         _check(lib().pxg_masks_add_path(self._h, _ptr(cmds), cmds.size, int(width), int(height),
                                         None if m is None else _ptr(m), int(winding_rule)))
         self._sizes.append((int(width), int(height)))
+
+    def add_paths(self, paths, threads: int = 0):
+        """add_path for many glyphs at once: (path, width, height, winding_rule)
+        tuples, geometry built on host threads, masks appended in order (all
+        or nothing)."""
+        n = len(paths)
+        cm = [as_commands(p[0]) for p in paths]
+        offs = np.zeros(n + 1, np.int64)
+        offs[1:] = np.cumsum([c.size for c in cm])
+        cmds = np.ascontiguousarray(np.concatenate(cm) if n else np.zeros(1, np.float32), dtype=np.float32)
+        ws = np.array([int(p[1]) for p in paths], np.int64)
+        hs = np.array([int(p[2]) for p in paths], np.int64)
+        wind = np.array([int(p[3]) if len(p) > 3 else 0 for p in paths], np.int32)
+        _check(lib().pxg_masks_add_paths(self._h, n, _ptr(cmds), _ptr(offs), _ptr(ws), _ptr(hs), None,
+                                         _ptr(wind), int(threads)))
+        self._sizes.extend(zip(ws.tolist(), hs.tolist()))
 
     def render(self):
         _check(lib().pxg_masks_render(self._h))

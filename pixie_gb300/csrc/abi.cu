@@ -1732,6 +1732,85 @@ int pxg_masks_add_path(pxg_masks* m, const float* cmds, int64_t n, int64_t width
   });
 }
 
+// n glyphs at once, as n calls of pxg_masks_add_path would add them: the
+// geometry is built on host threads and the masks are appended in order.
+// All or nothing: if any path fails, none is added and the first failure is
+// raised (a skipped glyph would shift the masks' indices).
+int pxg_masks_add_paths(pxg_masks* m, int64_t n, const float* cmds, const int64_t* offs, const int64_t* widths,
+                        const int64_t* heights, const float* transforms, const int32_t* windings, int threads) {
+  return guarded_host([&] {
+    if (!m) throw ApiError{"Invalid mask batch handle"};
+    if (n < 0 || (n > 0 && (!cmds || !offs || !widths || !heights))) throw ApiError{"Invalid batch"};
+    struct Rec {
+      std::vector<Prim> prims;
+      PathJob job;
+      std::string err;
+    };
+    std::vector<Rec> rec((size_t)n);
+    std::atomic<int> failed{0};
+    auto build = [&](int64_t i) {
+      Rec& r = rec[(size_t)i];
+      try {
+        const int64_t w = widths[i], h = heights[i];
+        if (w <= 0 || h <= 0) throw ApiError{"Image width and height must be > 0"};
+        if (w > (1 << 20) || h > (1 << 20)) throw ApiError{"Mask too large"};
+        const int winding = windings ? windings[i] : 0;
+        if (winding != 0 && winding != 1) throw ApiError{"Invalid winding rule"};
+        const int64_t a = offs[i], b = offs[i + 1];
+        if (a < 0 || b < a) throw ApiError{"Invalid path commands"};
+        validate_commands(cmds + a, b - a);
+        const float* mat = transforms ? transforms + 9 * i : kIdent;
+        const float ps = pixel_scale(mat);
+        build_fill_prims(cmds + a, b - a, ps, r.prims);
+        static const float white[4] = {1, 1, 1, 1};
+        r.job = make_job(nullptr, color_to_rgbx(white), kNormal, mat, ps, winding);
+        r.job.a8 = 1;
+        r.job.W = w;
+        r.job.H = h;
+      } catch (const ApiError& e) {
+        r.err = e.msg;
+        failed = 1;
+      } catch (const GeomError& e) {
+        r.err = e.msg;
+        failed = 1;
+      } catch (const std::exception& e) {
+        r.err = e.what();
+        failed = 1;
+      }
+    };
+    int nt = threads > 0 ? threads : (int)std::thread::hardware_concurrency();
+    nt = std::max(1, std::min<int>(nt, (int)std::min<int64_t>(n / 16 + 1, 256)));
+    std::atomic<int64_t> next{0};
+    auto worker = [&] {
+      for (int64_t i = next.fetch_add(1); i < n; i = next.fetch_add(1)) build(i);
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; t++) pool.emplace_back(worker);
+    worker();
+    for (auto& t : pool) t.join();
+    if (failed)
+      for (const Rec& r : rec)
+        if (!r.err.empty()) throw ApiError{r.err};
+    size_t total = m->prims.size();
+    for (const Rec& r : rec) total += r.prims.size();
+    m->prims.reserve(total);
+    for (int64_t i = 0; i < n; i++) {
+      Rec& r = rec[(size_t)i];
+      r.job.prim_off = (long long)m->prims.size();
+      r.job.nprims = (int)r.prims.size();
+      r.job.group = curve_group(r.prims, 0, r.job.nprims);
+      m->prims.insert(m->prims.end(), r.prims.begin(), r.prims.end());
+      m->jobs.push_back(r.job);
+      m->offs.push_back(m->bytes);
+      m->bytes += (r.job.W * r.job.H + 15) / 16 * 16;
+    }
+    if (n > 0) {
+      m->dirty = true;
+      m->rendered = false;
+    }
+  });
+}
+
 int pxg_masks_render(pxg_masks* m) {
   return guarded([&] {
     if (!m) throw ApiError{"Invalid mask batch handle"};

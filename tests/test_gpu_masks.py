@@ -53,6 +53,26 @@ def test_masks_match_oracle_alpha():
         assert_same(m.mask(i), ref[..., 3], f"mask {i}")
 
 
+@pytest.mark.parametrize("threads", [1, 5, 0])
+def test_batched_glyph_recording_equals_per_call(threads):
+    """add_paths builds the glyphs' geometry on host threads and appends
+    them in order: the same masks as one add_path per glyph, and a failing
+    glyph adds none"""
+    glyphs, _ = wl.glyph_batch(4, n=300)
+    a = make_batch(glyphs)
+    b = px.Masks()
+    b.add_paths(glyphs, threads)
+    a.render()
+    b.render()
+    for i in range(len(glyphs)):
+        assert_same(b.mask(i), a.mask(i), f"mask {i}")
+    c = px.Masks()
+    bad = list(glyphs[:5]) + [(glyphs[5][0], 0, 10, 0)] + list(glyphs[6:10])
+    with pytest.raises(px.PixieError, match="Image width and height must be > 0"):
+        c.add_paths(bad, threads)
+    assert len(c._sizes) == 0
+
+
 @pytest.mark.parametrize("variant,rpi", [(0, 1), (1, 1), (1, 2), (1, 4), (0, 3)])
 def test_every_row_configuration_writes_the_same_masks(variant, rpi):
     glyphs, _ = wl.glyph_batch(5, n=120)
