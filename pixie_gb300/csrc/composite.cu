@@ -91,15 +91,25 @@ __global__ void __launch_bounds__(256) k_draw(uint32_t* __restrict__ a, const ui
   }
 }
 
-// MaskBlend zeroes the destination outside the overlap (images.nim:473-520).
+// MaskBlend zeroes the destination outside the overlap (images.nim:473-520):
+// the rows above y0 and from y1 down (whole rows, contiguous), then the
+// columns left of x0 and from x1 on in rows [y0, y1).  Only those pixels are
+// visited.
 __global__ void __launch_bounds__(256) k_clear_outside(uint32_t* a, long long Wa, long long Ha,
                                                        long long x0, long long y0, long long x1,
                                                        long long y1) {
-  const long long n = Wa * Ha;
+  const long long top = y0 * Wa, bottom = (Ha - y1) * Wa, side = x0 + (Wa - x1), mid = (y1 - y0) * side;
+  const long long n = top + bottom + mid;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    long long y = i / Wa, x = i - y * Wa;
-    if (y < y0 || y >= y1 || x < x0 || x >= x1) a[i] = 0u;
+    if (i < top) {
+      a[i] = 0u;
+    } else if (i < top + bottom) {
+      a[y1 * Wa + (i - top)] = 0u;
+    } else {
+      const long long k = i - top - bottom, r = k / side, c = k - r * side;
+      a[(y0 + r) * Wa + (c < x0 ? c : x1 + (c - x0))] = 0u;
+    }
   }
 }
 
@@ -183,8 +193,13 @@ void launch_draw(uint32_t* a, const uint32_t* b, long long Wa, long long Ha, lon
   if (blocks > cap) blocks = cap;
   if (blocks < 1) blocks = 1;
   if (mode == kMask) {
-    k_clear_outside<<<nsm * 4, 256, 0, st>>>(a, Wa, Ha, ax, ay, ax + w, ay + h);
-    note_launch();
+    const long long outside = Wa * Ha - w * h;  // pixels outside the overlap
+    if (outside > 0) {
+      long long cb = (outside + 255) / 256;
+      if (cb > (long long)nsm * 4) cb = (long long)nsm * 4;
+      k_clear_outside<<<(unsigned)cb, 256, 0, st>>>(a, Wa, Ha, ax, ay, ax + w, ay + h);
+      note_launch();
+    }
   }
   if (w > 0 && h > 0) {
     draw_kernel(mode)<<<(unsigned)blocks, 256, 0, st>>>(a, b, Wa, Wb, ax, ay, xStart, yStart, w, h,

@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(256) k_blur_sx(const uint32_t* __restrict__ in
     if (vec && xa >= 0 && xa + 4 * NC <= W) {
 #pragma unroll
       for (int c = 0; c < NC; c++) {
-        const uint4 v = __ldg(reinterpret_cast<const uint4*>(row + xa) + c);
+        const uint4 v = __ldcs(reinterpret_cast<const uint4*>(row + xa) + c);
         px[4 * c] = v.x;
         px[4 * c + 1] = v.y;
         px[4 * c + 2] = v.z;
@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(256) k_blur_sx(const uint32_t* __restrict__ in
 #pragma unroll
       for (int i = 0; i < 4 * NC; i++) {
         const int x = xa + i;
-        px[i] = (x >= 0 && x < W) ? __ldg(row + x) : oob;
+        px[i] = (x >= 0 && x < W) ? __ldcs(row + x) : oob;
       }
     }
     uint64_t arg[kOut], aba[kOut];
@@ -157,12 +157,12 @@ __global__ void __launch_bounds__(256) k_blur_sy(const uint32_t* __restrict__ in
     if (y0 - R >= 0 && y0 + kOut + R <= H) {
       const uint32_t* p = in + (long long)(y0 - R) * W + x;
 #pragma unroll
-      for (int t = 0; t < NI; t++, p += W) px[t] = __ldg(p);
+      for (int t = 0; t < NI; t++, p += W) px[t] = __ldcs(p);
     } else {
 #pragma unroll
       for (int t = 0; t < NI; t++) {
         const int y = y0 - R + t;
-        px[t] = (y >= 0 && y < H) ? __ldg(in + (long long)y * W + x) : oob;
+        px[t] = (y >= 0 && y < H) ? __ldcs(in + (long long)y * W + x) : oob;
       }
     }
     uint64_t arg[kOut], aba[kOut];
@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(256) k_blur_sy(const uint32_t* __restrict__ in
     uint32_t* q = out + (long long)y0 * W + x;
 #pragma unroll
     for (int o = 0; o < kOut; o++, q += W)
-      if (y0 + o < H) *q = quot_px(arg[o], aba[o], kq, km);
+      if (y0 + o < H) __stcs(q, quot_px(arg[o], aba[o], kq, km));
   }
 }
 
