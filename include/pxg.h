@@ -170,8 +170,10 @@ int pxg_last_blur_kernel(void);
 int pxg_image_spread(pxg_image* image, float spread);
 
 /* shadow(Image, Vec2, spread, blur, Color) -> new Image
- * src/pixie/images.nim:760-776 (bindings/bindings.nim:135).  Offsets must be
- * integral (the blendRect branch of draw); the result is a new image. */
+ * src/pixie/images.nim:760-776 (bindings/bindings.nim:135).  A whole-pixel
+ * offset moves the mask as draw's blendRect branch does; a fractional one
+ * resamples it with drawSmooth (OverwriteBlend) first.  The result is a new
+ * image. */
 pxg_image* pxg_image_shadow(const pxg_image* image, float offset_x, float offset_y, float spread,
                             float blur, const float color[4]);
 /* The same shadow written into `out` (an image of the same size), with no

@@ -2646,6 +2646,29 @@ int pxo_shadow(const uint8_t* src, int64_t w, int64_t h, int64_t ox, int64_t oy,
   }
 }
 
+// shadow with any offset: draw(image, translate(offset), OverwriteBlend) takes
+// drawSmooth for a fractional offset (images.nim:760-769, :636-678)
+int pxo_shadow_f(const uint8_t* src, int64_t w, int64_t h, float ox, float oy, float sp, float blurR,
+                 const float* color, uint8_t* out) {
+  try {
+    std::vector<RGBX> mask((size_t)(w * h), RGBX{0, 0, 0, 0});
+    Image M{w, h, mask.data()};
+    Image S{w, h, (RGBX*)src};
+    if (ox == 0 && oy == 0)
+      memcpy(mask.data(), src, (size_t)(w * h * 4));
+    else
+      drawTransform(M, S, translate_m(v2(ox, oy)), OverwriteBlend);
+    spread(M, sp);
+    blur(M, blurR, RGBX{0, 0, 0, 0});
+    Image R{w, h, (RGBX*)out};
+    fillUnsafe(R, color_to_rgbx(color), 0, R.len());
+    blendRect(R, M, 0, 0, MaskBlend);
+    return 0;
+  } catch (const std::exception& e) {
+    return fail(e);
+  }
+}
+
 // toStraightAlpha over a buffer (internal.nim:76-84), for comparing with the
 // straight-alpha golden PNGs.
 int pxo_to_straight(uint8_t* rgbx_data, int64_t npx) {

@@ -64,6 +64,7 @@ def lib():
         L.pxo_gaussian_kernel.argtypes = [I64, P]
         L.pxo_spread.argtypes = [P, I64, I64, F]
         L.pxo_shadow.argtypes = [P, I64, I64, I64, I64, F, F, P, P]
+        L.pxo_shadow_f.argtypes = [P, I64, I64, F, F, F, F, P, P]
         L.pxo_to_straight.argtypes = [P, I64]
         L.pxo_set_golden_mode.argtypes = [I]
         _lib = L
@@ -272,6 +273,15 @@ def shadow(src, ox, oy, sp, blur_r, color):
     col = _f32(color, 4)
     _check(lib().pxo_shadow(_p(src), src.shape[1], src.shape[0], int(ox), int(oy), float(sp),
                             float(blur_r), _p(col), _p(out)))
+    return out
+
+
+def shadow_f(src, ox, oy, sp, blur_r, color):
+    """shadow with a float offset (a fractional one takes drawSmooth)"""
+    out = np.zeros_like(src)
+    col = _f32(color, 4)
+    _check(lib().pxo_shadow_f(_p(src), src.shape[1], src.shape[0], float(ox), float(oy), float(sp),
+                              float(blur_r), _p(col), _p(out)))
     return out
 
 

@@ -2548,18 +2548,25 @@ int pxg_image_shadow_into(const pxg_image* im, pxg_image* res, float ox, float o
     check_image(res);
     if (res->width != im->width || res->height != im->height)
       throw ApiError{"Shadow output must have the size of the image"};
-    if (ox != floorf(ox) || oy != floorf(oy))
-      throw ApiError{"Shadow offsets must be whole pixels (the smooth draw path is not provided)"};
     int64_t s = nim_round_int(spread), r = nim_round_int(blur);
     if (r < 0) throw ApiError{"Cannot apply negative blur"};
     if (r > (1 << 20) || s > (1 << 24) || s < -(1 << 24)) throw ApiError{"Shadow parameters too large"};
     long long n = im->width * im->height;
-    uint8_t* a = (uint8_t*)scratch(2 * n);
     const uint16_t* kern = r > 0 ? weights_for(r) : nullptr;
     Timed t;
-    launch_shadow((const uint32_t*)im->data, (uint32_t*)res->data, a, a + n, im->width, im->height,
-                  (long long)ox, (long long)oy, (int)s, (int)r, kern, color_to_rgbx(color), g.nsm,
-                  g.stream);
+    const uint32_t* src = (const uint32_t*)im->data;
+    if (ox != floorf(ox) || oy != floorf(oy)) {
+      // mask.draw(image, translate(offset), OverwriteBlend) takes drawSmooth
+      // (images.nim:768-769); the shadow then runs on that mask at offset 0
+      pxg_image mask = temp_image(0, im->width, im->height);
+      draw_transform(&mask, im, M3{{1, 0, 0, 0, 1, 0, ox, oy, 1}}, kOverwrite);
+      src = (const uint32_t*)mask.data;
+      ox = 0;
+      oy = 0;
+    }
+    uint8_t* a = (uint8_t*)scratch(2 * n);  // after the smooth draw, which uses the scratch too
+    launch_shadow(src, (uint32_t*)res->data, a, a + n, im->width, im->height, (long long)ox, (long long)oy, (int)s,
+                  (int)r, kern, color_to_rgbx(color), g.nsm, g.stream);
     CU(cudaGetLastError());
     t.done();
   });

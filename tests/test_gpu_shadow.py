@@ -38,3 +38,16 @@ def test_shadow_random_alpha_large():
         ref = pxo.shadow(img, off[0], off[1], sp, bl, [0, 0, 0, 1])
         out = px.Image.from_numpy(img).shadow(off, sp, bl, [0, 0, 0, 1])
         assert np.array_equal(out.to_numpy(), ref), f"shadow {off} {sp} {bl}"
+
+
+@pytest.mark.parametrize("off", [(0.5, 0.5), (8.25, -3.75), (-0.1, 12.0), (3.0, 0.5), (100.5, 7.5)])
+@pytest.mark.parametrize("sp,bl", [(4, 12), (-2, 3), (0, 0), (6, 40)])
+def test_shadow_fractional_offset_takes_draw_smooth(off, sp, bl):
+    """a fractional offset draws the mask with drawSmooth (OverwriteBlend)
+    before spread and blur (images.nim:760-776)"""
+    px.lib().pxg_init(0)
+    mask = _mask(180, 140, 13)
+    col = [0.1, 0.2, 0.7, 0.9]
+    ref = pxo.shadow_f(mask, off[0], off[1], sp, bl, col)
+    out = px.Image.from_numpy(mask).shadow(off, sp, bl, col)
+    assert np.array_equal(out.to_numpy(), ref), f"shadow {off} {sp} {bl}"
