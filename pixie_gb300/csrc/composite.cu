@@ -35,6 +35,8 @@ __global__ void __launch_bounds__(256) k_draw(uint32_t* __restrict__ a, const ui
                                               long long Wa, long long Wb, long long ax, long long ay,
                                               long long bx, long long by, long long w, long long h,
                                               const uint8_t* tbl, int vec) {
+  pdl_trigger();
+  pdl_wait();
   if (vec) {
     // One 16-byte quad (4 pixels) per thread per iteration: the blend is
     // inlined four times, not sixteen, so the float modes keep their code in
@@ -98,6 +100,8 @@ __global__ void __launch_bounds__(256) k_draw(uint32_t* __restrict__ a, const ui
 __global__ void __launch_bounds__(256) k_clear_outside(uint32_t* a, long long Wa, long long Ha,
                                                        long long x0, long long y0, long long x1,
                                                        long long y1) {
+  pdl_trigger();
+  pdl_wait();
   const long long top = y0 * Wa, bottom = (Ha - y1) * Wa, side = x0 + (Wa - x1), mid = (y1 - y0) * side;
   const long long n = top + bottom + mid;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -197,13 +201,13 @@ void launch_draw(uint32_t* a, const uint32_t* b, long long Wa, long long Ha, lon
     if (outside > 0) {
       long long cb = (outside + 255) / 256;
       if (cb > (long long)nsm * 4) cb = (long long)nsm * 4;
-      k_clear_outside<<<(unsigned)cb, 256, 0, st>>>(a, Wa, Ha, ax, ay, ax + w, ay + h);
+      launch_pdl(k_clear_outside, dim3((unsigned)cb), dim3(256), 0, st, a, Wa, Ha, ax, ay, ax + w, ay + h);
       note_launch();
     }
   }
   if (w > 0 && h > 0) {
-    draw_kernel(mode)<<<(unsigned)blocks, 256, 0, st>>>(a, b, Wa, Wb, ax, ay, xStart, yStart, w, h,
-                                                        tbl, vec);
+    launch_pdl(draw_kernel(mode), dim3((unsigned)blocks), dim3(256), 0, st, a, b, Wa, Wb, ax, ay, xStart, yStart, w,
+               h, tbl, vec);
     note_launch();
   }
 }

@@ -5,6 +5,9 @@
 // operation order and rounding.
 #pragma once
 #include <cstdint>
+#include <utility>
+
+#include <cuda_runtime.h>
 
 namespace pxg {
 
@@ -22,6 +25,29 @@ __device__ __forceinline__ Px unpack(uint32_t v) {
 }
 __device__ __forceinline__ uint32_t pack(uint32_t r, uint32_t g, uint32_t b, uint32_t a) {
   return (r & 255u) | ((g & 255u) << 8) | ((b & 255u) << 16) | ((a & 255u) << 24);
+}
+
+// Programmatic dependent launch: a kernel launched with launch_pdl lets the
+// next PDL kernel on its stream be set up while its own blocks finish
+// (pdl_trigger), and waits before touching memory until the kernel before
+// it has completed with its writes visible (pdl_wait).  Both are no-ops for
+// an ordinary launch.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+template <class... KArgs, class... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                              Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
 // Nim float32 -> int conversions as the reference's x86-64 builds perform them

@@ -78,6 +78,8 @@ __global__ void __launch_bounds__(256) k_blur_sx(const uint32_t* __restrict__ in
   constexpr int NI = kOut + 2 * R;      // inputs per thread
   constexpr int D = (4 - (R & 3)) & 3;  // (x0 - R) mod 4, x0 a multiple of 8
   constexpr int NC = (D + NI + 3) / 4;  // 16-byte chunks covering them
+  pdl_trigger();
+  pdl_wait();
   uint64_t w2[2 * R + 1];
 #pragma unroll
   for (int t = 0; t <= 2 * R; t++) {
@@ -142,6 +144,8 @@ template <int R>
 __global__ void __launch_bounds__(256) k_blur_sy(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
                                                  int W, int H, const uint16_t* __restrict__ kern, uint32_t oob) {
   constexpr int NI = kOut + 2 * R;
+  pdl_trigger();
+  pdl_wait();
   uint64_t w2[2 * R + 1];
 #pragma unroll
   for (int t = 0; t <= 2 * R; t++) {
@@ -195,9 +199,9 @@ void launch_small(uint32_t* img, uint32_t* tmp, int W, int H, const uint16_t* ke
   // kernels loop over the rest)
   const unsigned gxx = (unsigned)(((W + kOut - 1) / kOut + 255) / 256), gxy = (unsigned)std::min(H, 65535);
   const unsigned gyx = (unsigned)((W + 255) / 256), gyy = (unsigned)std::min((H + kOut - 1) / kOut, 65535);
-  k_blur_sx<R><<<dim3(gxx, gxy), 256, 0, st>>>(img, tmp, W, H, kern, oob, vec);
+  launch_pdl(k_blur_sx<R>, dim3(gxx, gxy), dim3(256), 0, st, img, tmp, W, H, kern, oob, vec);
   note_launch();
-  k_blur_sy<R><<<dim3(gyx, gyy), 256, 0, st>>>(tmp, img, W, H, kern, oob);
+  launch_pdl(k_blur_sy<R>, dim3(gyx, gyy), dim3(256), 0, st, tmp, img, W, H, kern, oob);
   note_launch();
 }
 
