@@ -481,6 +481,8 @@ __global__ void __launch_bounds__(256) k_shadow_tile(const uint32_t* __restrict_
   uint32_t* wk = reinterpret_cast<uint32_t*>(sh + ((2 * S * S + 15) & ~15));
   const int gx0 = blockIdx.x * kShadowTile - h, gy0 = blockIdx.y * kShadowTile - h;  // staged [0][0]
   const int tid = threadIdx.x, T = blockDim.x;
+  pdl_trigger();
+  pdl_wait();
   if (r > 0)  // without a blur there is no weight table
     for (int k = tid; k <= 2 * r; k += T) wk[k] = kern[k];
   const unsigned char neutral = (m > 0 && !grow) ? 255 : 0;
@@ -565,8 +567,8 @@ void launch_shadow(const uint32_t* src, uint32_t* out, uint8_t* a0, uint8_t* a1,
   if (m + r <= kShadowHalo && W <= (1 << 24) && H <= (1 << 24) && ox > -(1 << 24) && ox < (1 << 24) &&
       oy > -(1 << 24) && oy < (1 << 24)) {
     const dim3 g((unsigned)((W + kShadowTile - 1) / kShadowTile), (unsigned)((H + kShadowTile - 1) / kShadowTile));
-    k_shadow_tile<<<g, 256, shadow_tile_smem(m + r), st>>>(src, out, (int)W, (int)H, (int)ox, (int)oy, m, s > 0, r,
-                                                           kern, color);
+    launch_pdl(k_shadow_tile, g, dim3(256), shadow_tile_smem(m + r), st, src, out, (int)W, (int)H, (int)ox, (int)oy,
+               m, (int)(s > 0), r, kern, color);
     note_launch();
     return;
   }

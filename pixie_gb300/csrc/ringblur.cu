@@ -167,6 +167,7 @@ __global__ void __launch_bounds__(kRingThreads, 1)
   uint32_t* taddr_s =
       reinterpret_cast<uint32_t*>(sm + L.bars + (2 * kMaxRaw + 2 * kMaxRing + 2 * kMaxAcc + 1) * 8);
   const int r = a.r;
+  pdl_trigger();  // the next pass may be set up while this one runs
 
   // The Toeplitz weights, once per CTA (K padded with zeros to whole blocks).
   const int kpad = (a.kspan + 63) / 64 * 64;
@@ -207,6 +208,9 @@ __global__ void __launch_bounds__(kRingThreads, 1)
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  // the weights and barriers above read only constant data; the input
+  // (written by the previous kernel) and the output are touched only after it
+  pdl_wait();
   const uint32_t tmem = *taddr_s;
 
   if (warp == 0) {
@@ -513,7 +517,7 @@ void launch_ring_pass(const RingArgs& a, int grid, const CUtensorMap& tin, uint3
                       const uint16_t* kern, int* err, cudaStream_t st) {
   // at least 120 KB, so that no second CTA (and tensor-memory allocation) shares an SM
   const size_t smem = std::max<size_t>(ring_smem(a, SPLIT).total + 1024, 120 * 1024);
-  k_blur_ring<SPLIT><<<grid, kRingThreads, smem, st>>>(tin, out, a, kern, err);
+  launch_pdl(k_blur_ring<SPLIT>, dim3(grid), dim3(kRingThreads), smem, st, tin, out, a, kern, err);
   note_launch();
 }
 
