@@ -356,8 +356,13 @@ float pxg_last_gpu_ms(void);
 /* blocking = 1 (default): every call returns after its GPU work finished,
  * like the reference's synchronous procs.  blocking = 0: draw, fill, blur,
  * spread and shadow only enqueue their kernels on the library's stream and
- * report launch errors; pxg_synchronize() waits.  fillPath/strokePath always
- * wait (their errors come from the GPU).  No counterpart in the reference. */
+ * report launch errors; pxg_image_upload / pxg_image_download run on their
+ * own copy streams, ordered after the calls before them and before the calls
+ * after them (an upload's host buffer must stay unchanged, and a download's
+ * holds the image, only after pxg_synchronize), so copies overlap other
+ * images' work; pxg_synchronize() waits for everything.  fillPath/strokePath
+ * always wait (their errors come from the GPU).  No counterpart in the
+ * reference. */
 int pxg_set_blocking(int blocking);
 
 /* Number of kernels this library has launched since it was loaded. */

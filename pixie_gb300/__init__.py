@@ -284,6 +284,8 @@ class Image:
     def to_numpy(self) -> np.ndarray:
         out = np.empty((self.height, self.width, 4), dtype=np.uint8)
         _check(lib().pxg_image_download(self._h, _ptr(out), out.nbytes))
+        if not _blocking:  # an asynchronous download: wait for it before handing the array out
+            _check(lib().pxg_synchronize())
         return out
 
     def upload(self, arr: np.ndarray):
@@ -653,10 +655,16 @@ def last_fill_stats() -> dict:
             "pixel_blends": int(v[4]), "wide_rows": int(v[5])}
 
 
+_blocking = True
+
+
 def set_blocking(blocking: bool):
     """True (default): calls wait for their GPU work; False: image operations
-    only enqueue their kernels (see pxg_set_blocking in include/pxg.h)."""
+    only enqueue their kernels, and uploads / downloads run asynchronously on
+    their own streams (see pxg_set_blocking in include/pxg.h)."""
+    global _blocking
     _check(lib().pxg_set_blocking(1 if blocking else 0))
+    _blocking = bool(blocking)
 
 
 def synchronize():

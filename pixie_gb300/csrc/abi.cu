@@ -26,6 +26,7 @@ struct pxg_image {
   uint8_t* data;
   int64_t width, height;
   int owned;
+  cudaEvent_t copy_ev = nullptr;  // the last asynchronous upload or download of the image
 };
 
 struct GraphCacheHolder;
@@ -212,6 +213,15 @@ struct Ctx {
   size_t smemOptin = 48 * 1024;
   size_t setupSmemMax = 0, blurSmemMax = 0;
   cudaStream_t own = nullptr, stream = nullptr;
+  // Non-blocking mode: uploads and downloads run on their own streams.  Each
+  // call's compute waits for the copies issued before it (copies_pending); a
+  // copy waits for the compute issued before it (compute_ev, recorded at the
+  // end of every call once copies went asynchronous) and for the image's own
+  // previous copy (pxg_image::copy_ev).
+  cudaStream_t h2d = nullptr, d2h = nullptr;
+  cudaEvent_t compute_ev = nullptr;
+  bool async_copies = false;
+  std::vector<cudaEvent_t> copies_pending, ev_pool;
   uint8_t* tbl = nullptr;
   // fill arena
   float4* segs = nullptr;
@@ -298,6 +308,9 @@ void init_locked(int device) {
   g.smemOptin = prop.sharedMemPerBlockOptin;
   CU(cudaStreamCreateWithFlags(&g.own, cudaStreamNonBlocking));
   g.stream = g.own;
+  CU(cudaStreamCreateWithFlags(&g.h2d, cudaStreamNonBlocking));
+  CU(cudaStreamCreateWithFlags(&g.d2h, cudaStreamNonBlocking));
+  CU(cudaEventCreateWithFlags(&g.compute_ev, cudaEventDisableTiming));
   // the straight-alpha table (256 x 256 bytes), then v / 255.0f for v = 0..255
   std::vector<uint8_t> t(kTblBytes);
   straight_alpha_table(t.data());
@@ -951,12 +964,56 @@ int guarded_host(F&& f) {
   return 1;
 }
 
-template <class F>
+// Compute issued from here on waits for the asynchronous copies issued so far.
+void copy_fence() {
+  for (cudaEvent_t e : g.copies_pending) {
+    CU(cudaStreamWaitEvent(g.stream, e, 0));
+    g.ev_pool.push_back(e);
+  }
+  g.copies_pending.clear();
+}
+cudaEvent_t pooled_event() {
+  cudaEvent_t e = nullptr;
+  if (!g.ev_pool.empty()) {
+    e = g.ev_pool.back();
+    g.ev_pool.pop_back();
+  } else {
+    CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  return e;
+}
+// An asynchronous copy on stream cs of image im: after the compute issued
+// before it and the image's previous copy; compute issued after it waits.
+template <class Copy>
+void async_copy(pxg_image* im, cudaStream_t cs, Copy&& copy) {
+  if (!g.async_copies) {  // the first one: the compute stream's position now
+    g.async_copies = true;
+    CU(cudaEventRecord(g.compute_ev, g.stream));
+  }
+  CU(cudaStreamWaitEvent(cs, g.compute_ev, 0));
+  if (im->copy_ev)
+    CU(cudaStreamWaitEvent(cs, im->copy_ev, 0));
+  else
+    CU(cudaEventCreateWithFlags(&im->copy_ev, cudaEventDisableTiming));
+  copy();
+  CU(cudaEventRecord(im->copy_ev, cs));
+  cudaEvent_t e = pooled_event();
+  CU(cudaEventRecord(e, cs));
+  g.copies_pending.push_back(e);
+}
+
+// Every entry point runs through guarded.  A compute call first waits for
+// the asynchronous copies issued before it and afterwards records the compute
+// stream's position for later copies; a copy call (COPY) does neither -- it
+// waits for that recorded position, so it is not ordered after other copies.
+template <bool COPY = false, class F>
 int guarded(F&& f) {
   std::lock_guard<std::recursive_mutex> lk(g.mu);
   try {
     ensure_init();
+    if (!COPY && !g.copies_pending.empty()) copy_fence();
     f();
+    if (!COPY && g.async_copies) CU(cudaEventRecord(g.compute_ev, g.stream));
     return 0;
   } catch (const ApiError& e) {
     set_err(e.msg);
@@ -1317,13 +1374,25 @@ int pxg_set_stream(void* s) {
 }
 
 int pxg_synchronize(void) {
-  return guarded([&] { CU(cudaStreamSynchronize(g.stream)); });
+  return guarded([&] {
+    CU(cudaStreamSynchronize(g.stream));
+    if (g.async_copies) {
+      CU(cudaStreamSynchronize(g.h2d));
+      CU(cudaStreamSynchronize(g.d2h));
+    }
+  });
 }
 
 float pxg_last_gpu_ms(void) { return g.last_ms; }
 
 int pxg_set_blocking(int blocking) {
-  return guarded([&] { g.blocking = blocking != 0; });
+  return guarded([&] {
+    if (blocking && !g.blocking && g.async_copies) {  // back to blocking: finish the asynchronous copies
+      CU(cudaStreamSynchronize(g.h2d));
+      CU(cudaStreamSynchronize(g.d2h));
+    }
+    g.blocking = blocking != 0;
+  });
 }
 
 int64_t pxg_launch_count(void) { return (int64_t)launch_count(); }
@@ -1363,6 +1432,10 @@ pxg_image* pxg_image_wrap(void* ptr, int64_t width, int64_t height) {
 void pxg_image_free(pxg_image* im) {
   if (!im) return;
   std::lock_guard<std::recursive_mutex> lk(g.mu);
+  if (im->copy_ev) {  // a copy may still be in flight on the image's memory
+    cudaEventSynchronize(im->copy_ev);
+    cudaEventDestroy(im->copy_ev);
+  }
   if (im->owned && im->data) cudaFree(im->data);
   delete im;
 }
@@ -1372,6 +1445,14 @@ int64_t pxg_image_height(const pxg_image* im) { return im ? im->height : 0; }
 void* pxg_image_device_ptr(pxg_image* im) { return im ? im->data : nullptr; }
 
 int pxg_image_upload(pxg_image* im, const void* host, int64_t nbytes) {
+  if (!g.blocking)
+    return guarded<true>([&] {  // on the upload stream; the host buffer must stay as it is until pxg_synchronize
+      check_image(im);
+      if (nbytes != im->width * im->height * 4) throw ApiError{"Byte count does not match the image"};
+      async_copy(im, g.h2d, [&] {
+        CU(cudaMemcpyAsync(im->data, host, (size_t)nbytes, cudaMemcpyHostToDevice, g.h2d));
+      });
+    });
   return guarded([&] {
     check_image(im);
     if (nbytes != im->width * im->height * 4) throw ApiError{"Byte count does not match the image"};
@@ -1381,6 +1462,15 @@ int pxg_image_upload(pxg_image* im, const void* host, int64_t nbytes) {
 }
 
 int pxg_image_download(const pxg_image* im, void* host, int64_t nbytes) {
+  if (!g.blocking)
+    return guarded<true>([&] {  // on the download stream; the host buffer holds the image after pxg_synchronize
+      check_image(im);
+      if (nbytes != im->width * im->height * 4) throw ApiError{"Byte count does not match the image"};
+      pxg_image* m = const_cast<pxg_image*>(im);
+      async_copy(m, g.d2h, [&] {
+        CU(cudaMemcpyAsync(host, im->data, (size_t)nbytes, cudaMemcpyDeviceToHost, g.d2h));
+      });
+    });
   return guarded([&] {
     check_image(im);
     if (nbytes != im->width * im->height * 4) throw ApiError{"Byte count does not match the image"};
