@@ -27,6 +27,7 @@ struct pxg_image {
   int64_t width, height;
   int owned;
   cudaEvent_t copy_ev = nullptr;  // the last asynchronous upload or download of the image
+  bool copy_pending = false;      // ... which no compute on the image has waited for yet
 };
 
 struct GraphCacheHolder;
@@ -997,6 +998,7 @@ void async_copy(pxg_image* im, cudaStream_t cs, Copy&& copy) {
     CU(cudaEventCreateWithFlags(&im->copy_ev, cudaEventDisableTiming));
   copy();
   CU(cudaEventRecord(im->copy_ev, cs));
+  im->copy_pending = true;
   cudaEvent_t e = pooled_event();
   CU(cudaEventRecord(e, cs));
   g.copies_pending.push_back(e);
@@ -1014,6 +1016,34 @@ int guarded(F&& f) {
     if (!COPY && !g.copies_pending.empty()) copy_fence();
     f();
     if (!COPY && g.async_copies) CU(cudaEventRecord(g.compute_ev, g.stream));
+    return 0;
+  } catch (const ApiError& e) {
+    set_err(e.msg);
+  } catch (const GeomError& e) {
+    set_err(e.msg);
+  } catch (const std::exception& e) {
+    set_err(e.what());
+  }
+  return 1;
+}
+
+// A compute call that names the images it reads and writes: it waits only for
+// those images' asynchronous copies, so it can start while copies of other
+// images are still running.
+template <class F>
+int guarded_images(std::initializer_list<const pxg_image*> ims, F&& f) {
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  try {
+    ensure_init();
+    for (const pxg_image* c : ims) {
+      pxg_image* im = const_cast<pxg_image*>(c);
+      if (im && im->copy_pending) {
+        CU(cudaStreamWaitEvent(g.stream, im->copy_ev, 0));
+        im->copy_pending = false;
+      }
+    }
+    f();
+    if (g.async_copies) CU(cudaEventRecord(g.compute_ev, g.stream));
     return 0;
   } catch (const ApiError& e) {
     set_err(e.msg);
@@ -1480,7 +1510,7 @@ int pxg_image_download(const pxg_image* im, void* host, int64_t nbytes) {
 }
 
 int pxg_image_fill(pxg_image* im, const float* color) {
-  return guarded([&] {
+  return guarded_images({im}, [&] {
     check_image(im);
     Timed t;
     launch_fill((uint32_t*)im->data, im->width * im->height, color_to_rgbx(color), g.nsm, g.stream);
@@ -2147,7 +2177,7 @@ int64_t pxg_autotune_report(char* buf, int64_t cap) {
 }
 
 int pxg_image_draw(pxg_image* a, const pxg_image* b, int64_t tx, int64_t ty, int blend) {
-  return guarded([&] {
+  return guarded_images({a, b}, [&] {
     check_image(a);
     check_image(b);
     check_blend(blend);
@@ -2480,7 +2510,7 @@ void composite_paint(pxg_image* im, pxg_image* mask, const pxg_paint& p) {
 extern "C" {
 
 int pxg_image_draw_transform(pxg_image* a, const pxg_image* b, const float* mat3, int blend) {
-  return guarded([&] {
+  return guarded_images({a, b}, [&] {
     check_image(a);
     check_image(b);
     check_blend(blend);
@@ -2598,7 +2628,7 @@ int pxg_image_fill_paint(pxg_image* im, const pxg_paint* paint) {
 }
 
 int pxg_image_blur(pxg_image* im, float radius, const float* oob) {
-  return guarded([&] {
+  return guarded_images({im}, [&] {
     check_image(im);
     int64_t r = nim_round_int(radius);  // images.nim:308-312
     if (r == 0) return;
@@ -2633,7 +2663,7 @@ int pxg_image_spread(pxg_image* im, float spread) {
 
 int pxg_image_shadow_into(const pxg_image* im, pxg_image* res, float ox, float oy, float spread,
                           float blur, const float* color) {
-  return guarded([&] {
+  return guarded_images({im, res}, [&] {
     check_image(im);
     check_image(res);
     if (res->width != im->width || res->height != im->height)
