@@ -28,6 +28,8 @@ struct pxg_image {
   int owned;
   cudaEvent_t copy_ev = nullptr;  // the last asynchronous upload or download of the image
   bool copy_pending = false;      // ... which no compute on the image has waited for yet
+  cudaEvent_t compute_ev = nullptr;  // after the last compute call that named the image
+  bool compute_set = false;
 };
 
 struct GraphCacheHolder;
@@ -992,6 +994,7 @@ void async_copy(pxg_image* im, cudaStream_t cs, Copy&& copy) {
     CU(cudaEventRecord(g.compute_ev, g.stream));
   }
   CU(cudaStreamWaitEvent(cs, g.compute_ev, 0));
+  if (im->compute_set) CU(cudaStreamWaitEvent(cs, im->compute_ev, 0));
   if (im->copy_ev)
     CU(cudaStreamWaitEvent(cs, im->copy_ev, 0));
   else
@@ -1029,7 +1032,10 @@ int guarded(F&& f) {
 
 // A compute call that names the images it reads and writes: it waits only for
 // those images' asynchronous copies, so it can start while copies of other
-// images are still running.
+// images are still running, and records an event on each of them, so later
+// copies of those images wait for it and not for unrelated compute.  (The
+// global position g.compute_ev moves only with calls that do not name their
+// images.)
 template <class F>
 int guarded_images(std::initializer_list<const pxg_image*> ims, F&& f) {
   std::lock_guard<std::recursive_mutex> lk(g.mu);
@@ -1043,7 +1049,14 @@ int guarded_images(std::initializer_list<const pxg_image*> ims, F&& f) {
       }
     }
     f();
-    if (g.async_copies) CU(cudaEventRecord(g.compute_ev, g.stream));
+    if (g.async_copies)  // later copies of these images wait for this call only
+      for (const pxg_image* c : ims) {
+        pxg_image* im = const_cast<pxg_image*>(c);
+        if (!im) continue;
+        if (!im->compute_ev) CU(cudaEventCreateWithFlags(&im->compute_ev, cudaEventDisableTiming));
+        CU(cudaEventRecord(im->compute_ev, g.stream));
+        im->compute_set = true;
+      }
     return 0;
   } catch (const ApiError& e) {
     set_err(e.msg);
@@ -1466,6 +1479,7 @@ void pxg_image_free(pxg_image* im) {
     cudaEventSynchronize(im->copy_ev);
     cudaEventDestroy(im->copy_ev);
   }
+  if (im->compute_ev) cudaEventDestroy(im->compute_ev);
   if (im->owned && im->data) cudaFree(im->data);
   delete im;
 }
