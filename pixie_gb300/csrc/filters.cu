@@ -471,7 +471,7 @@ void launch_spread(uint32_t* img, uint8_t* a0, uint8_t* a1, long long W, long lo
 // blur passes), then colour * alpha / 255 (the MaskBlend draw of the filled
 // result) written once.
 constexpr int kShadowTile = 64, kShadowHalo = 32;
-__global__ void __launch_bounds__(256) k_shadow_tile(const uint32_t* __restrict__ src, uint32_t* __restrict__ out,
+__global__ void __launch_bounds__(1024) k_shadow_tile(const uint32_t* __restrict__ src, uint32_t* __restrict__ out,
                                                      int W, int H, int ox, int oy, int m, int grow, int r,
                                                      const uint16_t* __restrict__ kern, uint32_t color) {
   extern __shared__ __align__(16) unsigned char sh[];
@@ -567,7 +567,7 @@ void launch_shadow(const uint32_t* src, uint32_t* out, uint8_t* a0, uint8_t* a1,
   if (m + r <= kShadowHalo && W <= (1 << 24) && H <= (1 << 24) && ox > -(1 << 24) && ox < (1 << 24) &&
       oy > -(1 << 24) && oy < (1 << 24)) {
     const dim3 g((unsigned)((W + kShadowTile - 1) / kShadowTile), (unsigned)((H + kShadowTile - 1) / kShadowTile));
-    launch_pdl(k_shadow_tile, g, dim3(256), shadow_tile_smem(m + r), st, src, out, (int)W, (int)H, (int)ox, (int)oy,
+    launch_pdl(k_shadow_tile, g, dim3(1024), shadow_tile_smem(m + r), st, src, out, (int)W, (int)H, (int)ox, (int)oy,
                m, (int)(s > 0), r, kern, color);
     note_launch();
     return;
