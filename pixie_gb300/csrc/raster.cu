@@ -1646,7 +1646,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_scene_rec(PathJob* jobs, const S
 }
 
 template <int XT, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32, 3) k_scene(PathJob* jobs, const SceneRun* runs, int nruns,
+__global__ void __launch_bounds__(WARPS * 32, 4) k_scene(PathJob* jobs, const SceneRun* runs, int nruns,
                                                       long long totalItems, Arena A, const uint8_t* tbl,
                                                       int sliceW) {
   __shared__ int accs[WARPS][XT + 1];
