@@ -396,6 +396,8 @@ __device__ long long block_excl_scan(long long v, long long* s_warp, long long& 
 // k_setup: flatten -> segments -> bounds -> partitions (one CTA per job)
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_setup(PathJob* jobs, Arena A, int maxBands) {
+  pdl_trigger();  // the row kernel may be set up while this runs; it waits for the segments
+  pdl_wait();
   extern __shared__ int dsm[];
   int* bandc = dsm;             // per band: entry count
   int* bandf = dsm + maxBands;  // per band: flags
@@ -1508,6 +1510,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_rows(PathJob* jobs, const long l
   using Scratch = RowScratch<MAXH, XT>;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   Scratch& S = reinterpret_cast<Scratch*>(rsm)[warp];
+  pdl_trigger();
+  pdl_wait();  // the setup's segments, bands and queue counters
   while (true) {
     unsigned long long q = 0;
     if (lane == 0) q = atomicAdd(&A.counters[kCtrQueue], 1ull);
@@ -1611,6 +1615,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_scene_rec(PathJob* jobs, const S
   using Scratch = RowScratch<MAXH, kRecXT>;
   using Wide = RowScratch<kWideMaxH, kWideXT>;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  pdl_trigger();
+  pdl_wait();
   Scratch& S = reinterpret_cast<Scratch*>(rsm)[warp];
   const long long gw = (long long)blockIdx.x * WARPS + warp;
   while (true) {
@@ -1652,6 +1658,8 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_scene(PathJob* jobs, const Sc
   __shared__ int accs[WARPS][XT + 1];
   __shared__ uint32_t pix[WARPS][XT];  // the warp's row slice while its paths are applied
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  pdl_trigger();
+  pdl_wait();
   int* acc = accs[warp];
   const bool staged = sliceW <= XT;
   if (A.counters[kCtrProgFull]) return;  // programs incomplete: the host reruns the launch
@@ -1782,12 +1790,13 @@ int scene_warps() { return kSceneWarps; }
 int scene_tile() { return kSceneXT; }
 void launch_scene_rec(unsigned blocks, cudaStream_t st, PathJob* jobs, const SceneRun* runs, int nruns,
                       long long items, const Arena& A, unsigned char* wide, long long slots) {
-  k_scene_rec<kRecMaxH, kRecWarps><<<blocks, kRecWarps * 32, scene_rec_smem(), st>>>(jobs, runs, nruns, items, A,
-                                                                                    wide, slots);
+  launch_pdl(k_scene_rec<kRecMaxH, kRecWarps>, dim3(blocks), dim3(kRecWarps * 32), scene_rec_smem(), st, jobs, runs,
+             nruns, items, A, wide, slots);
 }
 void launch_scene(unsigned blocks, cudaStream_t st, PathJob* jobs, const SceneRun* runs, int nruns, long long items,
                   const Arena& A, const uint8_t* tbl, int sliceW) {
-  k_scene<kSceneXT, kSceneWarps><<<blocks, kSceneWarps * 32, 0, st>>>(jobs, runs, nruns, items, A, tbl, sliceW);
+  launch_pdl(k_scene<kSceneXT, kSceneWarps>, dim3(blocks), dim3(kSceneWarps * 32), 0, st, jobs, runs, nruns, items,
+             A, tbl, sliceW);
 }
 
 // Dynamic shared memory of k_setup for a launch whose images have at most
@@ -1817,11 +1826,11 @@ int rows_warps(int v) { return v == 1 ? kSmallWarps : kFastWarps; }
 void launch_rows(int v, unsigned blocks, cudaStream_t st, PathJob* jobs, const long long* offs, int njobs,
                  const Arena& A, const uint8_t* tbl, long long items, int rpi) {
   if (v == 1)
-    k_rows<kSmallMaxH, kSmallXT, kSmallWarps><<<blocks, kSmallWarps * 32, rows_smem(1), st>>>(jobs, offs, njobs, A,
-                                                                                              tbl, items, rpi);
+    launch_pdl(k_rows<kSmallMaxH, kSmallXT, kSmallWarps>, dim3(blocks), dim3(kSmallWarps * 32), rows_smem(1), st, jobs,
+               offs, njobs, A, tbl, items, rpi);
   else
-    k_rows<kFastMaxH, kFastXT, kFastWarps><<<blocks, kFastWarps * 32, rows_smem(0), st>>>(jobs, offs, njobs, A, tbl,
-                                                                                          items, rpi);
+    launch_pdl(k_rows<kFastMaxH, kFastXT, kFastWarps>, dim3(blocks), dim3(kFastWarps * 32), rows_smem(0), st, jobs,
+               offs, njobs, A, tbl, items, rpi);
 }
 
 }  // namespace pxg
