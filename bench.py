@@ -291,32 +291,33 @@ def run_e2e(px, A, B, BL, M, SH, a_host, b_host, blur_host, run_op, ops, args, w
     pinned_mask = torch.from_numpy(mask_host).pin_memory().numpy()
     steps = max(1, min(args.steps, args.e2e_steps))
     h2d = d2h = 0
-    barrier(ws)
-    px.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        h2d = d2h = 0
-        for k in range(N_MODES):  # inputs host -> device
-            A[k].upload(pinned_a[k % 2])
-            B[k].upload(pinned_b[k % 2])
-            h2d += 2 * DRAW_W * DRAW_W * 4
-        for im in BL:
-            im.upload(pinned_blur)
-            h2d += BLUR_W * BLUR_W * 4
-        M.upload(pinned_mask)
-        h2d += SHADOW_W * SHADOW_W * 4
-        for op in ops:
-            run_op(op)
-        for k in range(N_MODES):  # results device -> host
-            px.lib().pxg_image_download(A[k]._h, px._ptr(out_draw), out_draw.nbytes)
-            d2h += out_draw.nbytes
-        for im in BL:
-            px.lib().pxg_image_download(im._h, px._ptr(out_blur), out_blur.nbytes)
-            d2h += out_blur.nbytes
-        px.lib().pxg_image_download(SH._h, px._ptr(out_sh), out_sh.nbytes)
-        d2h += out_sh.nbytes
-    px.synchronize()
-    dt = time.perf_counter() - t0
+    for warm in (True, False):  # one untimed step, then the timed ones
+        barrier(ws)
+        px.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(1 if warm else steps):
+            h2d = d2h = 0
+            for k in range(N_MODES):  # inputs host -> device
+                A[k].upload(pinned_a[k % 2])
+                B[k].upload(pinned_b[k % 2])
+                h2d += 2 * DRAW_W * DRAW_W * 4
+            for im in BL:
+                im.upload(pinned_blur)
+                h2d += BLUR_W * BLUR_W * 4
+            M.upload(pinned_mask)
+            h2d += SHADOW_W * SHADOW_W * 4
+            for op in ops:
+                run_op(op)
+            for k in range(N_MODES):  # results device -> host
+                px.lib().pxg_image_download(A[k]._h, px._ptr(out_draw), out_draw.nbytes)
+                d2h += out_draw.nbytes
+            for im in BL:
+                px.lib().pxg_image_download(im._h, px._ptr(out_blur), out_blur.nbytes)
+                d2h += out_blur.nbytes
+            px.lib().pxg_image_download(SH._h, px._ptr(out_sh), out_sh.nbytes)
+            d2h += out_sh.nbytes
+        px.synchronize()
+        dt = time.perf_counter() - t0
     dt = max_over_ranks(ws, dt)
     return {"value": round(STEP_PIXELS * steps * int(os.environ.get("WORLD_SIZE", "1")) / dt / 1e9, 3),
             "unit": "Gpix/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -774,7 +775,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="pxg", choices=["pxg", "reference"])
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--glyphs", type=int, default=4096)
     ap.add_argument("--serve-jobs", type=int, default=40, help="jobs per arrival rate (0: skip serving)")
     ap.add_argument("--serve-pool", type=int, default=12, help="distinct recorded jobs the arrivals draw from")
