@@ -184,3 +184,38 @@ def test_gradient_errors(paint, msg):
         pxo.fill_paint(pxo.new_image(8, 8), paint)
     with pytest.raises(px.PixieError, match=msg):
         px.Image(8, 8).fill(gpu_paint(paint))
+
+
+@pytest.mark.parametrize("kind", [LINEAR, RADIAL, ANGULAR])
+@pytest.mark.parametrize("stops,handles,opacity", [
+    # two stops at the same position, a t that lands exactly on a stop (x = 50 of a 0..100 gradient)
+    ([((1.0, 0.0, 0.0, 1.0), 0.0), ((0.0, 1.0, 0.0, 1.0), 0.5), ((0.0, 0.0, 1.0, 1.0), 0.5),
+      ((1.0, 1.0, 0.0, 0.5), 1.0)], [(0.0, 50.0), (100.0, 50.0), (0.0, 100.0)], 1.0),
+    # stops outside 0..1 and out of order
+    ([((0.2, 0.4, 0.6, 0.8), -0.5), ((0.9, 0.1, 0.3, 0.7), 1.5), ((0.5, 0.5, 0.5, 1.0), 0.25)],
+     [(10.0, 10.0), (90.0, 70.0), (10.0, 90.0)], 0.75),
+    # coincident handles: t is NaN (linear) or the matrix is singular (radial)
+    ([((1.0, 0.0, 0.0, 1.0), 0.0), ((0.0, 0.0, 1.0, 1.0), 1.0)], [(50.0, 50.0), (50.0, 50.0), (50.0, 50.0)], 1.0),
+    # a single stop, opacity above 1 (clamped)
+    ([((0.3, 0.6, 0.9, 0.4), 0.7)], [(0.0, 0.0), (100.0, 100.0), (0.0, 100.0)], 1.7),
+    # opacity 0 draws nothing
+    ([((0.3, 0.6, 0.9, 0.4), 0.0), ((0.1, 0.2, 0.3, 1.0), 1.0)], [(0.0, 0.0), (100.0, 0.0), (0.0, 100.0)], 0.0),
+])
+def test_gradient_edges(kind, stops, handles, opacity):
+    st = [(tuple(f32(c) for c in col), f32(p)) for col, p in stops]
+    hs = [(f32(x), f32(y)) for x, y in handles[:2 if kind == LINEAR else 3]]
+    paint = dict(kind=kind, handles=hs, stops=st, opacity=f32(opacity))
+    dst = wl.premultiplied_image(5, 100, 100)
+    ref = dst.copy()
+    try:
+        pxo.fill_paint(ref, paint)
+    except pxo.OracleError as e:
+        with pytest.raises(px.PixieError, match=str(e)):
+            px.Image.from_numpy(dst).fill(gpu_paint(paint))
+        return
+    img = px.Image.from_numpy(dst)
+    img.fill(gpu_paint(paint))
+    assert_same(img.to_numpy(), ref, f"kind {kind}")
+    # and through fillPath's paint chain
+    gpu, ref2 = both_fill_path(dst, heart(), paint)
+    assert_same(gpu, ref2, f"fillPath kind {kind}")
