@@ -1489,6 +1489,7 @@ int64_t pxg_image_height(const pxg_image* im) { return im ? im->height : 0; }
 void* pxg_image_device_ptr(pxg_image* im) { return im ? im->data : nullptr; }
 
 int pxg_image_upload(pxg_image* im, const void* host, int64_t nbytes) {
+  std::lock_guard<std::recursive_mutex> lk(g.mu);  // the mode is read and used under the library's lock
   if (!g.blocking)
     return guarded<true>([&] {  // on the upload stream; the host buffer must stay as it is until pxg_synchronize
       check_image(im);
@@ -1506,6 +1507,7 @@ int pxg_image_upload(pxg_image* im, const void* host, int64_t nbytes) {
 }
 
 int pxg_image_download(const pxg_image* im, void* host, int64_t nbytes) {
+  std::lock_guard<std::recursive_mutex> lk(g.mu);  // the mode is read and used under the library's lock
   if (!g.blocking)
     return guarded<true>([&] {  // on the download stream; the host buffer holds the image after pxg_synchronize
       check_image(im);
