@@ -1005,6 +1005,9 @@ void async_copy(pxg_image* im, cudaStream_t cs, Copy&& copy) {
   cudaEvent_t e = pooled_event();
   CU(cudaEventRecord(e, cs));
   g.copies_pending.push_back(e);
+  // calls that name their images never drain the list; keep it bounded (the
+  // compute stream then waits for all of them: conservative, still correct)
+  if (g.copies_pending.size() > 1024) copy_fence();
 }
 
 // Every entry point runs through guarded.  A compute call first waits for
