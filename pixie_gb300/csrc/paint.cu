@@ -8,6 +8,7 @@
 // reference's operation order (the file is built with -fmad=false).
 #include <cfloat>
 #include <cstdint>
+#include <stdexcept>
 
 #include "paint.cuh"
 #include "pxg_device.cuh"
@@ -104,7 +105,10 @@ __device__ uint32_t gradient_color(const float* __restrict__ st, int n, float op
 
 template <int KIND>
 __global__ void __launch_bounds__(256) k_gradient(uint32_t* __restrict__ img, long long W, long long H, GradientArgs g,
-                                                  const float* __restrict__ stops) {
+                                                  const float* __restrict__ gstops) {
+  extern __shared__ float stops[];  // the stops, staged once per CTA
+  for (int i = threadIdx.x; i < 5 * g.nstops; i += blockDim.x) stops[i] = gstops[i];
+  __syncthreads();
   const long long n = W * H;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
@@ -223,12 +227,17 @@ struct CorrectTable<kNumBlends> {
 void launch_gradient(uint32_t* img, long long W, long long H, const GradientArgs& g, const float* stops, int nsm,
                      cudaStream_t st) {
   const long long n = W * H;
+  const size_t smem = sizeof(float) * 5 * (size_t)g.nstops;
+  if (smem > 48 * 1024) throw std::runtime_error("Too many gradient stops");
+  long long blocks = (n + 255) / 256;  // four waves of eight CTAs per SM at most
+  if (blocks > (long long)nsm * 32) blocks = (long long)nsm * 32;
+  const unsigned gb = (unsigned)(blocks < 1 ? 1 : blocks);
   if (g.kind == 3)
-    k_gradient<3><<<grid(n, nsm), 256, 0, st>>>(img, W, H, g, stops);
+    k_gradient<3><<<gb, 256, smem, st>>>(img, W, H, g, stops);
   else if (g.kind == 4)
-    k_gradient<4><<<grid(n, nsm), 256, 0, st>>>(img, W, H, g, stops);
+    k_gradient<4><<<gb, 256, smem, st>>>(img, W, H, g, stops);
   else
-    k_gradient<5><<<grid(n, nsm), 256, 0, st>>>(img, W, H, g, stops);
+    k_gradient<5><<<gb, 256, smem, st>>>(img, W, H, g, stops);
   note_launch();
 }
 
