@@ -1939,56 +1939,108 @@ struct PaintDesc {
 };
 
 // atan2 for float32 arguments, correctly rounded to float32 (but for inputs
-// whose true value lies within ~1e-16 of a rounding boundary): evaluated in
-// float64 from the mathematics alone -- atan(x) = pi/2 - atan(1/x) above 1,
-// two halvings atan(x) = 2 atan(x / (1 + sqrt(1 + x^2))) to |x| < 0.2, and
-// 14 terms of the Taylor series (Horner form) -- so the CUDA path, which runs the same
-// IEEE float64 operations, gets the same floats.  (pixie calls the C
-// library's atan2f, which is not reproduced here bit for bit.)
-static double atan_unit(double x) {  // x >= 0
-  const bool inv = x > 1;
-  if (inv) x = 1 / x;
-  x = x / (1 + sqrt(1 + x * x));
-  x = x / (1 + sqrt(1 + x * x));
-  // x (1 - x^2/3 + x^4/5 - ... - x^26/27) in Horner form, 1/(2n+1) as float64 constants
-  const double x2 = x * x;
-  double poly = -1.0 / 27;
-  poly = poly * x2 + 1.0 / 25;
-  poly = poly * x2 - 1.0 / 23;
-  poly = poly * x2 + 1.0 / 21;
-  poly = poly * x2 - 1.0 / 19;
-  poly = poly * x2 + 1.0 / 17;
-  poly = poly * x2 - 1.0 / 15;
-  poly = poly * x2 + 1.0 / 13;
-  poly = poly * x2 - 1.0 / 11;
-  poly = poly * x2 + 1.0 / 9;
-  poly = poly * x2 - 1.0 / 7;
-  poly = poly * x2 + 1.0 / 5;
-  poly = poly * x2 - 1.0 / 3;
-  poly = poly * x2 + 1.0;
-  const double sum = x * poly * 4;
-  return inv ? 1.5707963267948966 - sum : sum;
+// whose true value lies within ~2^-40 of a rounding boundary): evaluated in
+// float-float arithmetic from the mathematics alone, so the CUDA path, which
+// runs the same IEEE float32 operations, gets the same floats.  (pixie calls
+// the C library's atan2f, which is not reproduced here bit for bit.)
+
+// float-float ("double-float") arithmetic: a value is hi + lo with |lo| <=
+// ulp(hi) / 2; two_sum and the fused-multiply-add two_prod give exact error
+// terms (Dekker, Knuth), so every operation is a fixed sequence of IEEE
+// float32 operations.
+struct DF {
+  float hi, lo;
+};
+static inline DF two_sum(float a, float b) {
+  const float s = a + b, bb = s - a;
+  return DF{s, (a - (s - bb)) + (b - bb)};
 }
-static float atan2_cr(float y, float x) {
+static inline DF quick_two_sum(float a, float b) {
+  const float s = a + b;
+  return DF{s, b - (s - a)};
+}
+static inline DF two_prod(float a, float b) {
+  const float p = a * b;
+  return DF{p, std::fma(a, b, -p)};
+}
+static inline DF df_add(DF x, DF y) {
+  DF s = two_sum(x.hi, y.hi);
+  const DF t = two_sum(x.lo, y.lo);
+  s.lo = s.lo + t.hi;
+  s = quick_two_sum(s.hi, s.lo);
+  s.lo = s.lo + t.lo;
+  return quick_two_sum(s.hi, s.lo);
+}
+static inline DF df_neg(DF x) { return DF{-x.hi, -x.lo}; }
+static inline DF df_mul(DF x, DF y) {
+  DF p = two_prod(x.hi, y.hi);
+  p.lo = p.lo + (x.hi * y.lo + x.lo * y.hi);
+  return quick_two_sum(p.hi, p.lo);
+}
+static inline DF df_div(DF x, DF y) {
+  const float q1 = x.hi / y.hi;
+  DF r = df_add(x, df_neg(df_mul(y, DF{q1, 0.0f})));
+  const float q2 = r.hi / y.hi;
+  r = df_add(r, df_neg(df_mul(y, DF{q2, 0.0f})));
+  const float q3 = r.hi / y.hi;
+  return df_add(quick_two_sum(q1, q2), DF{q3, 0.0f});
+}
+static inline DF df_sqrt(DF a) {  // a > 0
+  const float s = std::sqrt(a.hi);
+  const DF e = df_add(a, df_neg(two_prod(s, s)));
+  return quick_two_sum(s, e.hi / (2.0f * s));
+}
+#define DF_CONST(v) DF{(float)(v), (float)((v) - (double)(float)(v))}
+// atan(x) for x >= 0: pi/2 - atan(1/x) above 1, two halvings
+// atan(x) = 2 atan(x / (1 + sqrt(1 + x^2))) to x < 0.2, then 14 Taylor
+// terms in Horner form
+static inline DF df_atan_unit(DF x) {
+  const DF one{1.0f, 0.0f};
+  const bool inv = x.hi > 1.0f || (x.hi == 1.0f && x.lo > 0.0f);
+  if (inv) x = df_div(one, x);
+  x = df_div(x, df_add(one, df_sqrt(df_add(one, df_mul(x, x)))));
+  x = df_div(x, df_add(one, df_sqrt(df_add(one, df_mul(x, x)))));
+  const DF x2 = df_mul(x, x);
+  DF poly = DF_CONST(-1.0 / 27);
+  poly = df_add(df_mul(poly, x2), DF_CONST(1.0 / 25));
+  poly = df_add(df_mul(poly, x2), DF_CONST(-1.0 / 23));
+  poly = df_add(df_mul(poly, x2), DF_CONST(1.0 / 21));
+  poly = df_add(df_mul(poly, x2), DF_CONST(-1.0 / 19));
+  poly = df_add(df_mul(poly, x2), DF_CONST(1.0 / 17));
+  poly = df_add(df_mul(poly, x2), DF_CONST(-1.0 / 15));
+  poly = df_add(df_mul(poly, x2), DF_CONST(1.0 / 13));
+  poly = df_add(df_mul(poly, x2), DF_CONST(-1.0 / 11));
+  poly = df_add(df_mul(poly, x2), DF_CONST(1.0 / 9));
+  poly = df_add(df_mul(poly, x2), DF_CONST(-1.0 / 7));
+  poly = df_add(df_mul(poly, x2), DF_CONST(1.0 / 5));
+  poly = df_add(df_mul(poly, x2), DF_CONST(-1.0 / 3));
+  poly = df_add(df_mul(poly, x2), one);
+  const DF sum = df_mul(df_mul(x, poly), DF{4.0f, 0.0f});
+  return inv ? df_add(DF_CONST(1.5707963267948966), df_neg(sum)) : sum;
+}
+// atan2 of float32 arguments rounded to float32 (correctly rounded but for
+// true values within ~2^-40 of a rounding boundary)
+static inline float atan2_cr(float y, float x) {
   if (std::isnan(x) || std::isnan(y)) return NAN;
-  const double pi = 3.141592653589793;
-  double r;
+  DF r;
   if (y == 0) {
-    r = (std::signbit(x)) ? pi : 0.0;
+    r = std::signbit(x) ? DF_CONST(3.141592653589793) : DF{0.0f, 0.0f};
   } else if (x == 0) {
-    r = pi / 2;
+    r = DF_CONST(1.5707963267948966);
   } else if (std::isinf(x) || std::isinf(y)) {
     if (std::isinf(x) && std::isinf(y))
-      r = x > 0 ? pi / 4 : 3 * pi / 4;
+      r = x > 0 ? DF_CONST(0.7853981633974483) : DF_CONST(2.356194490192345);
     else if (std::isinf(x))
-      r = x > 0 ? 0.0 : pi;
+      r = x > 0 ? DF{0.0f, 0.0f} : DF_CONST(3.141592653589793);
     else
-      r = pi / 2;
+      r = DF_CONST(1.5707963267948966);
   } else {
-    const double a = atan_unit(fabs((double)y / (double)x));
-    r = x > 0 ? a : pi - a;
+    const DF q = df_div(DF{std::fabs(y), 0.0f}, DF{std::fabs(x), 0.0f});
+    const DF a = df_atan_unit(q);
+    r = x > 0 ? a : df_add(DF_CONST(3.141592653589793), df_neg(a));
   }
-  return (float)(std::signbit(y) ? -r : r);
+  const float v = r.hi + r.lo;
+  return std::signbit(y) ? -v : v;
 }
 
 // chroma mix(Color, Color, t): componentwise lerp a + (b - a) * t
