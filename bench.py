@@ -728,6 +728,12 @@ def run_case(case: str, slice_w: int = 0):
         b = px.Image.from_numpy(wl.premultiplied_image(2, 4096, 4096))
         for _ in range(2):
             a.draw(b, (0, 0), mode)
+    elif case == "paint":  # 2048^2: a fill with each gradient kind, then fillPath of a heart with a linear gradient
+        img = px.Image(2048, 2048)
+        for kind, hs in PAINT_HANDLES.items():
+            img.fill(px.Paint(kind=kind, handles=hs, stops=PAINT_STOPS))
+        img.fill_path(wl.heart_commands(20.48), px.Paint(kind=3, handles=PAINT_HANDLES[3], stops=PAINT_STOPS,
+                                                         opacity=0.8))
     elif case == "smooth":  # draw of a 2048^2 source rotated 30 degrees, scaled 1.1, onto 2048^2
         a = px.Image.from_numpy(wl.premultiplied_image(1, 2048, 2048))
         b = px.Image.from_numpy(wl.premultiplied_image(2, 2048, 2048))
@@ -783,7 +789,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--slice", type=int, default=0, help="scene row slice width for --case scene*")
     ap.add_argument("--case", default=None,
-                    help="run one small operation for profiling: fill512 | blur<r> (blur64) | draw<mode> (draw13) | smooth | glyphs | scene | scene_small | masks")
+                    help="run one small operation for profiling: fill512 | blur<r> (blur64) | draw<mode> (draw13) | smooth | paint | glyphs | scene | scene_small | masks")
     args = ap.parse_args()
     if args.case:
         run_case(args.case, args.slice)
