@@ -274,9 +274,70 @@ def run_gpu(args, ws, rank, local):
              "draw_gbs_min_median_max": [round(min(draw_gbs), 1), round(statistics.median(draw_gbs), 1),
                                          round(max(draw_gbs), 1)],
              "blur_ms": blur_ms}
+    parity = None
+    if rank == 0 and not args.no_parity:
+        parity = check_parity(px, A, B, BL, M, SH, a_host, b_host, blur_host, seed)
     if rank == 0 and not args.no_fill:
         extra.update(run_fill_extras(px, wl, args, stream))
-    return ms_step, launches, roof, e2e, extra, clk.summary()
+    return ms_step, launches, roof, e2e, extra, clk.summary(), parity
+
+
+def check_parity(px, A, B, BL, M, SH, a_host, b_host, blur_host, seed):
+    """Outside the timed region: every operation of the step once more on
+    fresh copies of its seeded inputs, compared byte for byte with the
+    oracle's render of the same inputs (the oracle's calls run in threads)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import pxo
+    from pixie_gb300 import workloads as wl
+    pxo.set_golden_mode(False)
+
+    def ref_draw(mode):
+        r = a_host[mode % 2].copy()
+        pxo.draw(r, b_host[mode % 2], 0, 0, mode)
+        return r
+
+    def ref_blur(r):
+        x = blur_host.copy()
+        pxo.blur(x, r)
+        return x
+
+    def ref_shadow():
+        m = pxo.new_image(SHADOW_W, SHADOW_W)
+        pxo.fill_path(m, wl.disc_mask_path(seed), [1, 1, 1, 1])
+        return pxo.shadow(m, 8, 8, 4, 12, [0, 0, 0, 1])
+
+    t = time.perf_counter()
+    with ThreadPoolExecutor(min(16, os.cpu_count() or 1)) as ex:
+        f_draw = {m: ex.submit(ref_draw, m) for m in range(N_MODES)}
+        f_blur = {r: ex.submit(ref_blur, r) for r in RADII}
+        f_sh = ex.submit(ref_shadow)
+        got = {}
+        for m in range(N_MODES):  # the GPU side meanwhile
+            A[m].upload(a_host[m % 2])
+            B[m].upload(b_host[m % 2])
+            A[m].draw(B[m], (0, 0), m)
+            got[f"draw:{m}"] = A[m].to_numpy()
+        for i, r in enumerate(RADII):
+            BL[i].upload(blur_host)
+            BL[i].blur(r)
+            got[f"blur:{r}"] = BL[i].to_numpy()
+        M.shadow_into(SH, (8, 8), 4, 12, [0, 0, 0, 1])
+        got["shadow:0"] = SH.to_numpy()
+        want = {f"draw:{m}": f.result() for m, f in f_draw.items()}
+        want.update({f"blur:{r}": f.result() for r, f in f_blur.items()})
+        want["shadow:0"] = f_sh.result()
+    worst, differing, bad = 0, 0, {}
+    for k, g in got.items():
+        d = np.abs(g.astype(np.int16) - want[k].astype(np.int16))
+        mx, n = int(d.max()), int((d.reshape(-1, 4).max(axis=1) > 0).sum())
+        worst, differing = max(worst, mx), differing + n
+        if n:
+            bad[k] = {"max_abs_delta": mx, "differing_px": n}
+    return {"max_abs_delta": worst, "differing_px": differing, "ops_checked": len(got),
+            "against": "oracle (scalar restatement of pixie), same seeded inputs, one fresh run of each "
+                       "operation of the step at full size", "failing_ops": bad,
+            "oracle_s": round(time.perf_counter() - t, 1)}
 
 
 def run_e2e(px, A, B, BL, M, SH, a_host, b_host, blur_host, run_op, ops, args, ws):
@@ -341,17 +402,75 @@ def run_fill_extras(px, wl, args, stream):
             gpu_ms += px.last_gpu_ms()
             n += 1
     dt = time.perf_counter() - t
+    segs = 0
+    for c in paths:  # flattened segments (edges) per path, from the library's counters
+        img.fill_path(c, wl.PLAIN_COLOR)
+        segs += px.last_fill_stats()["segments"]
+    edges_per_path = segs / len(paths)
     out["plain_fill_512_64cubics"] = {"paths_per_s": round(n / dt, 1),
+                                      "edges_per_s": round(n / dt * edges_per_path, 1),
+                                      "edges_per_path": round(edges_per_path, 1),
                                       "gpu_ms_per_path": round(gpu_ms / n, 4),
                                       "note": "one blocking C-ABI call per path, host pre-pass included"}
-    out["draw_transform_2048"] = run_draw_transform(px, wl, stream, cpu=not args.no_cpu_baseline)
-    out["paints_2048"] = run_paints(px, wl, stream, cpu=not args.no_cpu_baseline)
+    cpu = not args.no_cpu_baseline
+    out["draw_transform_2048"] = run_draw_transform(px, wl, stream, cpu=cpu)
+    out["paints_2048"] = run_paints(px, wl, stream, cpu=cpu)
     out["glyph_batch"] = run_glyphs(px, wl, args.glyphs)
     out["dense_scene_1024_2000"] = run_scene(px, wl)
     if args.serve_jobs > 0:
-        out["serving"] = run_serving(px, wl, args.serve_jobs, args.serve_pool)
+        rates = tuple(float(r) for r in args.serve_rates.split(",") if r)
+        out["serving"] = run_serving(px, wl, args.serve_jobs, args.serve_pool, rates=rates)
+    if cpu:
+        add_cpu_baselines(out)
     px.set_blocking(False)
     return out
+
+
+def add_cpu_baselines(out):
+    """The oracle (C++ restatement of pixie's scalar path) on bounded samples
+    of the fill, scene, glyph and serving workloads: one thread, and one
+    independent sample per host core in spawned processes."""
+    from oracle import cpu_baselines as cb
+    cores = os.cpu_count() or 1
+    host = cb.host()
+
+    def both(name, kw, per_core_kw=None):
+        t1, n1 = cb.SAMPLES[name](**kw)
+        wall, n_all, _ = cb.all_cores(name, per_core_kw or [kw] * cores)
+        return t1, n1, wall, n_all
+
+    t1, n1, wall, n_all = both("plain_fill", {"n_paths": 200})
+    pf = out["plain_fill_512_64cubics"]
+    pf["cpu_oracle"] = {"paths_per_s_1core": round(n1 / t1, 1), "paths_per_s_all_cores": round(n_all / wall, 1),
+                        "edges_per_s_1core": round(n1 / t1 * pf["edges_per_path"], 1),
+                        "cores": cores, **host, "sample": "200 plain paths per process"}
+    pf["gpu_over_cpu_1core"] = round(pf["paths_per_s"] / (n1 / t1), 1)
+    t1, n1, wall, n_all = both("dense_scene", {"n_paths": 150})
+    sc = out["dense_scene_1024_2000"]
+    per_path = t1 / n1
+    sc["cpu_oracle"] = {"paths_per_s_1core": round(1 / per_path, 2), "paths_per_s_all_cores": round(n_all / wall, 1),
+                        "ms_per_scene_1core_est": round(per_path * 2000 * 1e3, 0),
+                        "edges_per_s_1core": round(sc["segments"] / sc["paths_recorded"] / per_path, 1),
+                        "cores": cores, **host,
+                        "sample": "the scene's first 150 paths on its 1024^2 canvas per process, scaled per path"}
+    sc["gpu_over_cpu_1core"] = round(sc["paths_per_s_gpu"] * per_path, 1)
+    t1, n1, wall, n_all = both("glyphs", {"n": 1024})
+    gb = out["glyph_batch"]
+    gb["cpu_oracle"] = {"paths_per_s_1core": round(n1 / t1, 1), "paths_per_s_all_cores": round(n_all / wall, 1),
+                        "cores": cores, **host,
+                        "sample": "fillPath of the first 1024 glyphs into their own images + draw onto a "
+                                  "4096^2 page, per process"}
+    gb["batched_gpu_over_cpu_1core"] = round(gb["batched_paths_per_s"] / (n1 / t1), 1)
+    if "serving" in out:
+        seeds = out["serving"]["pool_seeds"][:4]
+        per_job = [cb.serving_job(sd, 60)[0] for sd in seeds]
+        mean_job = sum(per_job) / len(per_job)
+        out["serving"]["cpu_oracle"] = {
+            "s_per_job_1core_est": round(mean_job, 2), "jobs_per_s_1core_est": round(1 / mean_job, 3),
+            "jobs_per_s_all_cores_est": round(cores / mean_job, 2), "cores": cores, **host,
+            "sample": "4 pool jobs: their first 60 paths drawn and scaled per path to the whole job, plus the "
+                      "job's blur; all cores = cores / time per job (independent jobs, as the other "
+                      "workloads' all-core samples measure)"}
 
 
 SMOOTH_CASES = {  # name: (column-major Mat3 of translate * rotate * scale, what it exercises)
@@ -464,35 +583,50 @@ def record_scene(px, items, threads=0):
     return sc, int(status.sum())
 
 
-def run_serving(px, wl, n_jobs, pool, rates=(100, 300, 1000, 3000, 10000, 20000), seed=11):
+def run_serving(px, wl, n_jobs, pool, rates=(5, 10, 100, 20000), seed=11):
     """Open-loop serving sweep: Poisson arrivals at each rate, n_jobs jobs per
     rate drawn from a pool of recorded jobs (canvas side log-U[256, 4096],
     10..5000 dense-scene paths, blur r in 2..32 on 20% of jobs), admitted
     against a 40 GB budget.  Latency = arrival -> canvas copied back to the
-    host.  Every served canvas is compared with the same job rendered alone."""
+    host.  Every served canvas is compared with the same job rendered alone.
+    Rates below the service capacity measure service latency; rates above it
+    measure the drain of the queue.  Occupancy = device bytes the admitted
+    jobs hold (sampled after every step) over the budget."""
+    budget = 40 << 30
     t = time.perf_counter()
-    jobs = [wl.serving_job(seed * 100 + k) for k in range(pool)]
+    seeds = [seed * 100 + k for k in range(pool)]
+    jobs = [wl.serving_job(sd) for sd in seeds]
     scenes = [record_scene(px, j["items"])[0] for j in jobs]
     prep_s = time.perf_counter() - t
     alone = []
+    alone_ms = []
     for j, sc in zip(jobs, scenes):
         img = px.Image(j["side"], j["side"])
+        t = time.perf_counter()
         img.draw_scene(sc)
         if j["blur"]:
             img.blur(j["blur"])
         alone.append(img.to_numpy())
-    res = {"pool_jobs": pool, "jobs_per_rate": n_jobs, "budget_gb": 40,
-           "pool_sides": [j["side"] for j in jobs], "pool_paths": [len(s) for s in scenes],
-           "pool_blur": [j["blur"] for j in jobs], "prep_s": round(prep_s, 1), "rates": []}
+        alone_ms.append((time.perf_counter() - t) * 1e3)
+    res = {"pool_jobs": pool, "jobs_per_rate": n_jobs, "budget_gb": 40, "pool_seeds": seeds,
+           "pool_side_min_median_max": [min(j["side"] for j in jobs), int(np.median([j["side"] for j in jobs])),
+                                        max(j["side"] for j in jobs)],
+           "pool_paths_min_median_max": [min(len(s) for s in scenes), int(np.median([len(s) for s in scenes])),
+                                         max(len(s) for s in scenes)],
+           "pool_blurred": sum(1 for j in jobs if j["blur"]), "prep_s": round(prep_s, 1),
+           "alone_ms_mean": round(float(np.mean(alone_ms)), 2),
+           "service_capacity_jobs_per_s_est": round(1e3 / float(np.mean(alone_ms)), 2), "rates": []}
     all_exact = True
     for ri, rate in enumerate(rates):
-        sv = px.Server(40 << 30, 512, 16384)
+        sv = px.Server(budget, 512, 16384)
         arr = wl.poisson_arrivals(seed + ri, float(rate), n_jobs)
         which = {}
         lat = []
         exact = True
         i = 0
         done = 0
+        occ, adm = [], []
+        step_host_s = 0.0
         t0 = time.perf_counter()
         while done < n_jobs:
             now = time.perf_counter() - t0
@@ -502,7 +636,12 @@ def run_serving(px, wl, n_jobs, pool, rates=(100, 300, 1000, 3000, 10000, 20000)
                 which[jid] = (k, arr[i])
                 i += 1
             if sv.pending() > 0:
+                ts = time.perf_counter()
                 sv.step()
+                step_host_s += time.perf_counter() - ts
+                st = sv.stats()
+                occ.append(st["bytes_used"])
+                adm.append(st["admitted"])
             elif i < n_jobs:
                 time.sleep(max(0.0, min(arr[i] - (time.perf_counter() - t0), 0.002)))
             for jid in sv.poll():
@@ -516,10 +655,15 @@ def run_serving(px, wl, n_jobs, pool, rates=(100, 300, 1000, 3000, 10000, 20000)
         lat_ms = np.sort(np.asarray(lat)) * 1e3
         res["rates"].append({"rate_jobs_per_s": rate, "jobs": n_jobs,
                              "jobs_per_s": round(n_jobs / wall, 2),
+                             "saturated": bool(n_jobs / wall < 0.9 * rate),
                              "p50_ms": round(float(np.percentile(lat_ms, 50)), 2),
                              "p99_ms": round(float(np.percentile(lat_ms, 99)), 2),
                              "steps": st["steps"], "peak_admitted": st["peak_admitted"],
-                             "peak_gb": round(st["peak_bytes"] / 2**30, 2),
+                             "mean_admitted": round(float(np.mean(adm)), 2) if adm else 0.0,
+                             "peak_gb": round(st["peak_bytes"] / 2**30, 3),
+                             "budget_occupancy_mean": round(float(np.mean(occ)) / budget, 5) if occ else 0.0,
+                             "budget_occupancy_peak": round(st["peak_bytes"] / budget, 5),
+                             "step_call_share_of_wall": round(step_host_s / wall, 3),
                              "bitexact_vs_alone": bool(exact)})
         all_exact = all_exact and exact
         del sv
@@ -783,10 +927,13 @@ def main():
     ap.add_argument("--impl", default="pxg", choices=["pxg", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--glyphs", type=int, default=4096)
-    ap.add_argument("--serve-jobs", type=int, default=40, help="jobs per arrival rate (0: skip serving)")
-    ap.add_argument("--serve-pool", type=int, default=12, help="distinct recorded jobs the arrivals draw from")
+    ap.add_argument("--serve-jobs", type=int, default=200, help="jobs per arrival rate (0: skip serving)")
+    ap.add_argument("--serve-pool", type=int, default=100, help="distinct recorded jobs the arrivals draw from")
     ap.add_argument("--no-fill", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the oracle comparison of the step's outputs")
+    ap.add_argument("--serve-rates", default="5,10,100,20000",
+                    help="comma-separated Poisson arrival rates (jobs/s) of the serving sweep")
     ap.add_argument("--slice", type=int, default=0, help="scene row slice width for --case scene*")
     ap.add_argument("--case", default=None,
                     help="run one small operation for profiling: fill512 | blur<r> (blur64) | draw<mode> (draw13) | smooth | paint | glyphs | scene | scene_small | masks")
@@ -815,21 +962,22 @@ def main():
             print(json.dumps(line), flush=True)
         return
 
-    ms_step, launches, roof, e2e, extra, clocks = run_gpu(args, ws, rank, local)
+    ms_step, launches, roof, e2e, extra, clocks, parity = run_gpu(args, ws, rank, local)
     if rank != 0:
         return
     value = STEP_PIXELS * ws / (ms_step * 1e-3) / 1e9
     cpu = None
     if not args.no_cpu_baseline:
         est, sample = cpu_sample_rates(1)
+        from oracle import cpu_baselines
         cpu = {"value": round(STEP_PIXELS / est / 1e9, 5), "unit": "Gpix/s", "cores": 1,
-               "kind": "port", "sample": sample}
+               "kind": "port", "sample": sample, **cpu_baselines.host()}
     line = {"metric": METRIC, "value": round(value, 3), "unit": "Gpix/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
             "data": "synthetic (seeded splitmix64; shapes/distributions of the configuration)",
             "config": WORKLOAD, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
-            "gpu_launches": int(launches), "clocks": clocks, "extra": extra}
+            "gpu_launches": int(launches), "clocks": clocks, "parity": parity, "extra": extra}
     print(json.dumps(line), flush=True)
 
 

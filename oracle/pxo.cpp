@@ -1432,6 +1432,13 @@ static void fillHits(Image& img, RGBX c, int64_t startX, int64_t y, const std::v
   }
 }
 
+// Row window of this thread (test infrastructure, not in the reference):
+// fillShapes computes every row's geometry as usual but writes only rows in
+// [g_row_lo, g_row_hi).  Rows are independent in the reference's row loop, so
+// threads that each own a window and draw every path of a scene in order
+// produce, together, the bytes of one thread drawing the whole canvas.
+static thread_local int64_t g_row_lo = INT64_MIN, g_row_hi = INT64_MAX;
+
 static void fillShapes(Image& img, const std::vector<Polygon>& shapes, RGBX c, int rule,
                        int mode) {  // :1593-1912
   std::vector<WSeg> segs = shapesToSegments(shapes);
@@ -1471,11 +1478,15 @@ static void fillShapes(Image& img, const std::vector<Polygon>& shapes, RGBX c, i
       int64_t maxX = std::min<int64_t>(std::max<int64_t>(right, 0), img.width);
       bool skipBlending = mode == OverwriteBlend || (mode == NormalBlend && c.a == 255);
       if (skipBlending && minX == 0 && maxX == img.width) {
-        int64_t start = img.idx(0, y);
-        int64_t len = img.idx(0, y + pHeight) - start;
-        fillUnsafe(img, c, start, len);
+        const int64_t r0 = std::max(y, g_row_lo), r1 = std::min(y + pHeight, g_row_hi);
+        if (r1 > r0) {
+          int64_t start = img.idx(0, r0);
+          int64_t len = img.idx(0, r1) - start;
+          fillUnsafe(img, c, start, len);
+        }
       } else {
         for (int64_t r = 0; r < pHeight; r++) {
+          if (y + r < g_row_lo || y + r >= g_row_hi) continue;
           hits[0] = Hit{(Fixed32)(uint32_t)(minX * 256), 1};
           hits[1] = Hit{(Fixed32)(uint32_t)(maxX * 256), -1};
           fillHits(img, c, 0, y + r, hits, 2, 0, mode, true, spans);
@@ -1485,6 +1496,10 @@ static void fillShapes(Image& img, const std::vector<Polygon>& shapes, RGBX c, i
       continue;
     }
 
+    if (y < g_row_lo || y >= g_row_hi) {  // another thread's row
+      y++;
+      continue;
+    }
     float scanTop = (float)y, scanBottom = (float)(y + 1);
     bool allSpan = true;
     int numEntryIdx = 0;
@@ -1633,10 +1648,17 @@ static void fillShapes(Image& img, const std::vector<Polygon>& shapes, RGBX c, i
   }
   (void)W;
   if (mode == MaskBlend) {
-    clearUnsafe(img, 0, 0, 0, startY);
-    // rows [pathHeight, height); a negative pathHeight (path above the image)
-    // is clamped to 0 where the reference writes before its buffer.
-    clearUnsafe(img, 0, std::max<int64_t>(pathHeight, 0), 0, img.height);
+    const int64_t lo = std::max<int64_t>(g_row_lo, 0), hi = std::min<int64_t>(g_row_hi, img.height);
+    if (lo == 0 && hi == img.height) {
+      clearUnsafe(img, 0, 0, 0, startY);
+      // rows [pathHeight, height); a negative pathHeight (path above the image)
+      // is clamped to 0 where the reference writes before its buffer.
+      clearUnsafe(img, 0, std::max<int64_t>(pathHeight, 0), 0, img.height);
+    } else {  // the same rows, within the window
+      if (std::min(startY, hi) > lo) clearUnsafe(img, 0, lo, 0, std::min(startY, hi));
+      const int64_t b0 = std::max<int64_t>(std::max<int64_t>(pathHeight, 0), lo);
+      if (hi > b0) clearUnsafe(img, 0, b0, 0, hi);
+    }
   }
 }
 
@@ -2424,6 +2446,12 @@ const char* pxo_last_error(void) { return g_err.c_str(); }
 
 // Golden-pinning mode switch (see g_golden_mode); 0 = scalar oracle.
 void pxo_set_golden_mode(int on) { g_golden_mode = on; }
+
+// This thread's row window for fills and strokes (see g_row_lo).
+void pxo_set_row_window(int64_t lo, int64_t hi) {
+  g_row_lo = lo;
+  g_row_hi = hi;
+}
 
 int pxo_fill_path(uint8_t* rgbx_data, int64_t w, int64_t h, const float* cmds, int64_t n,
                   const float* color, float opacity, int blend, const float* mat, int rule) {

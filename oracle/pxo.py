@@ -67,6 +67,7 @@ def lib():
         L.pxo_shadow_f.argtypes = [P, I64, I64, F, F, F, F, P, P]
         L.pxo_to_straight.argtypes = [P, I64]
         L.pxo_set_golden_mode.argtypes = [I]
+        L.pxo_set_row_window.argtypes = [I64, I64]
         _lib = L
     return _lib
 
@@ -295,3 +296,41 @@ def set_golden_mode(on: bool):
     """Golden-pinning only: reproduce the build that wrote the reference's
     master PNGs (floored coverage multiply, SSE2 sliver rounding)."""
     lib().pxo_set_golden_mode(1 if on else 0)
+
+
+def draw_items(img, items, threads: int = 1):
+    """Draws a scene's items (dicts of workloads.dense_scene: fill or stroke,
+    solid colour, blend mode) onto img in order, as a caller of the reference's
+    fillPath/strokePath does, skipping the paths the reference raises for.
+    threads > 1 splits the canvas into row windows, one per thread; every
+    thread draws every path within its rows (the reference's rows are
+    independent), so the bytes equal the one-thread render.  Returns the
+    number of skipped paths."""
+    h = img.shape[0]
+    threads = max(1, min(int(threads), h))
+
+    def run(lo, hi):
+        lib().pxo_set_row_window(lo, hi)
+        failed = 0
+        try:
+            for it in items:
+                try:
+                    if it["kind"] == "fill":
+                        fill_path(img, it["cmds"], it["color"], 1.0, it["blend"], None, it["winding"])
+                    else:
+                        stroke_path(img, it["cmds"], it["color"], 1.0, it["blend"], None, it["width"],
+                                    it["cap"], it["join"], it["miter"])
+                except OracleError:
+                    failed += 1
+        finally:
+            lib().pxo_set_row_window(-(1 << 62), 1 << 62)
+        return failed
+
+    if threads == 1:
+        return run(-(1 << 62), 1 << 62)
+    from concurrent.futures import ThreadPoolExecutor
+    bounds = [h * k // threads for k in range(threads + 1)]
+    bounds[0], bounds[-1] = -(1 << 62), 1 << 62
+    with ThreadPoolExecutor(threads) as ex:
+        res = list(ex.map(run, bounds[:-1], bounds[1:]))
+    return res[0]

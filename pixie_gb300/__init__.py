@@ -265,9 +265,8 @@ class Image:
 
     @classmethod
     def from_numpy(cls, arr: np.ndarray) -> "Image":
-        arr = np.ascontiguousarray(arr, dtype=np.uint8)
         img = cls(arr.shape[1], arr.shape[0])
-        _check(lib().pxg_image_upload(img._h, _ptr(arr), arr.nbytes))
+        img.upload(arr)
         return img
 
     @classmethod
@@ -291,6 +290,8 @@ class Image:
     def upload(self, arr: np.ndarray):
         arr = np.ascontiguousarray(arr, dtype=np.uint8)
         _check(lib().pxg_image_upload(self._h, _ptr(arr), arr.nbytes))
+        if not _blocking:  # an asynchronous upload reads the host bytes until pxg_synchronize
+            _pending_uploads.append(arr)
 
     # -- pixie's Image procs -------------------------------------------------
     def fill(self, color):
@@ -656,6 +657,9 @@ def last_fill_stats() -> dict:
 
 
 _blocking = True
+# host arrays of asynchronous uploads, kept alive until the next synchronize
+# (np.ascontiguousarray may have made a temporary copy the caller does not hold)
+_pending_uploads: list = []
 
 
 def set_blocking(blocking: bool):
@@ -665,10 +669,13 @@ def set_blocking(blocking: bool):
     global _blocking
     _check(lib().pxg_set_blocking(1 if blocking else 0))
     _blocking = bool(blocking)
+    if _blocking:
+        synchronize()
 
 
 def synchronize():
     _check(lib().pxg_synchronize())
+    _pending_uploads.clear()
 
 
 def set_stream(cuda_stream: int):

@@ -8,7 +8,9 @@
 // caller's image buffer and stream and takes its work space from a
 // fixed-size array in the library's own device image instead of allocating:
 //   - the blur's intermediate image and the gaussian weights live in
-//     g_noalloc_scratch below, a file-scope static __device__ array of
+//     g_noalloc_scratch below (the weights are passed by value to a small
+//     kernel that stores them there, so the call never copies from host
+//     memory), a file-scope static __device__ array of
 //     kWeightsBytes + 4 * kNoAllocMaxPixels bytes (8 MiB + 16 KiB).  Every GPU
 //     that loads the library holds it until the process exits;
 //   - images larger than kNoAllocMaxPixels pixels, or radii above
@@ -20,6 +22,10 @@
 //   - the first call on a device looks up the array's device address
 //     (cudaGetSymbolAddress) and sets the blur kernels' shared-memory limits;
 //     make that first call before any stream capture.
+//   - the blur runs the CUDA-core passes (k_blurf_x/k_blurf_y below radius 8,
+//     the register-blocked k_blurb passes from radius 8), not the default
+//     small-radius or tensor-core passes of pxg_image_blur; the bytes are the
+//     same.
 // No cudaMalloc, cudaFree or other allocating routine is called, on the GPU
 // or on the host (errors go to fixed per-thread buffers).
 #include <cuda_runtime.h>
@@ -50,6 +56,19 @@ constexpr size_t kWeightsBytes = 16 * 1024;             // >= (2 * 2048 + 1) * 2
 constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kWeightsBytes + kNoAllocMaxPixels * 4];
+
+// Gaussian weights passed by value: (2 * 2048 + 1) uint16 = 8194 bytes, inside
+// the 32764-byte kernel-parameter limit of sm_70 and later.
+struct WeightsParam {
+  uint16_t w[2 * kNoAllocMaxRadius + 2];
+  int n;
+};
+static_assert(sizeof(WeightsParam) <= 32764, "kernel parameter too large");
+
+__global__ void k_store_weights(const WeightsParam p, uint16_t* __restrict__ dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < p.n) dst[i] = p.w[i];
+}
 
 struct DeviceSetup {
   bool ready;
@@ -119,13 +138,15 @@ extern "C" int pxg_image_blur_noalloc(void* rgbx, int64_t width, int64_t height,
   DeviceSetup s;
   if (setup_device(dev, s) != 0) return 1;
 
-  // weights on the host stack, copied into the head of the scratch array
-  uint16_t w[2 * kNoAllocMaxRadius + 1];
+  // The weights travel by value, as a kernel parameter, and one small kernel
+  // writes them into the head of the scratch array: no host buffer has to
+  // outlive the call and the stream never waits for a pageable copy.
+  WeightsParam wp;
   float work[2 * kNoAllocMaxRadius + 1];
-  pxg::gaussian_kernel_into(r, work, w);
+  pxg::gaussian_kernel_into(r, work, wp.w);
+  wp.n = (int)(2 * r + 1);
   cudaStream_t st = (cudaStream_t)cuda_stream;
-  if (cudaMemcpyAsync(s.scratch, w, (size_t)(2 * r + 1) * 2, cudaMemcpyHostToDevice, st) != cudaSuccess)
-    return fail("pxg_image_blur_noalloc: weight upload failed");
+  k_store_weights<<<(wp.n + 255) / 256, 256, 0, st>>>(wp, (uint16_t*)s.scratch);
   static const float zero[4] = {0, 0, 0, 0};
   const uint32_t oob = pxg::color_to_rgbx(out_of_bounds ? out_of_bounds : zero);
   pxg::launch_blur((uint32_t*)rgbx, (uint32_t*)(s.scratch + kWeightsBytes), width, height, (int)r,

@@ -155,12 +155,19 @@ __device__ uint32_t gradient_color(const float* __restrict__ st, int n, float op
   return color_rgbx(c[0], c[1], c[2], c[3]);
 }
 
-template <int KIND>
+// STAGED: the stops are copied into shared memory once per CTA; otherwise
+// (more stops than 48 KB of shared memory holds) they are read from global
+// memory, through the read-only cache.
+template <int KIND, bool STAGED>
 __global__ void __launch_bounds__(256) k_gradient(uint32_t* __restrict__ img, long long W, long long H, GradientArgs g,
                                                   const float* __restrict__ gstops) {
-  extern __shared__ float stops[];  // the stops, staged once per CTA
-  for (int i = threadIdx.x; i < 5 * g.nstops; i += blockDim.x) stops[i] = gstops[i];
-  __syncthreads();
+  extern __shared__ float staged[];
+  const float* stops = gstops;
+  if (STAGED) {
+    for (int i = threadIdx.x; i < 5 * g.nstops; i += blockDim.x) staged[i] = gstops[i];
+    __syncthreads();
+    stops = staged;
+  }
   const long long n = W * H;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
@@ -279,17 +286,18 @@ struct CorrectTable<kNumBlends> {
 void launch_gradient(uint32_t* img, long long W, long long H, const GradientArgs& g, const float* stops, int nsm,
                      cudaStream_t st) {
   const long long n = W * H;
-  const size_t smem = sizeof(float) * 5 * (size_t)g.nstops;
-  if (smem > 48 * 1024) throw std::runtime_error("Too many gradient stops");
+  const size_t need = sizeof(float) * 5 * (size_t)g.nstops;
+  const bool staged = need <= 48 * 1024;
+  const size_t smem = staged ? need : 0;
   long long blocks = (n + 255) / 256;  // four waves of eight CTAs per SM at most
   if (blocks > (long long)nsm * 32) blocks = (long long)nsm * 32;
   const unsigned gb = (unsigned)(blocks < 1 ? 1 : blocks);
   if (g.kind == 3)
-    k_gradient<3><<<gb, 256, smem, st>>>(img, W, H, g, stops);
+    (staged ? k_gradient<3, true> : k_gradient<3, false>)<<<gb, 256, smem, st>>>(img, W, H, g, stops);
   else if (g.kind == 4)
-    k_gradient<4><<<gb, 256, smem, st>>>(img, W, H, g, stops);
+    (staged ? k_gradient<4, true> : k_gradient<4, false>)<<<gb, 256, smem, st>>>(img, W, H, g, stops);
   else
-    k_gradient<5><<<gb, 256, smem, st>>>(img, W, H, g, stops);
+    (staged ? k_gradient<5, true> : k_gradient<5, false>)<<<gb, 256, smem, st>>>(img, W, H, g, stops);
   note_launch();
 }
 

@@ -12,7 +12,7 @@ Backend interface (all images premultiplied RGBX):
   stroke_path(img, cmds, color4f, opacity, blend, mat9, width, cap, join, miter, dashes)
   draw(a, b, tx, ty, blend)     blur(img, radius, oob_rgbx)     pixels(img) -> (h,w,4) uint8
   draw_transform(a, b, mat9, blend)   load(premultiplied rgbx array) -> img
-  minify(img, power) -> img
+  minify(img, power) -> img     magnify(img, power) -> img
   fill_path_paint(img, cmds, paint)   fill_paint(img, paint)   (paint: a dict, see
   oracle/pxo.py encode_paint; its "image" is a backend image)
 """
@@ -593,6 +593,34 @@ def _c(B):
 @case("images/masters/rock_minified2", "tests/test_images_draw.nim:260-264")
 def _c(B):
     return B.minify(_load(B, "rock"), 2)
+
+
+# ---- tests/test_images.nim: minifyBy2 / magnifyBy2 -------------------------
+# The magnify blocks read back the masters the minify blocks wrote
+# (readImage("tests/images/minifiedBy2.png")), so those PNGs are inputs too.
+@case("images/minifiedBy2", "tests/test_images.nim:90-94")
+def _c(B):
+    return B.minify(_load(B, "flipped1"), 1)
+
+
+@case("images/magnifiedBy2", "tests/test_images.nim:96-100")
+def _c(B):
+    return B.magnify(_load(B, "minifiedBy2"), 1)
+
+
+@case("images/minifiedBy4", "tests/test_images.nim:102-106")
+def _c(B):
+    return B.minify(_load(B, "flipped1"), 2)
+
+
+@case("images/magnifiedBy4", "tests/test_images.nim:108-112")
+def _c(B):
+    return B.magnify(_load(B, "minifiedBy4"), 2)
+
+
+@case("images/minifiedMandrill", "tests/test_images.nim:114-118")
+def _c(B):
+    return B.minify(_load(B, "mandrill"), 1)
 
 
 # ---- tests/test_paints.nim: non-solid paints -------------------------------

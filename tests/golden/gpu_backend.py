@@ -32,6 +32,9 @@ class GpuBackend:
     def minify(self, img, power):
         return img.minify_by2(power)
 
+    def magnify(self, img, power):
+        return img.magnify_by2(power)
+
     @staticmethod
     def _paint(paint):
         return px.Paint(paint.get("color", (0, 0, 0, 0)), paint.get("opacity", 1.0), paint.get("blend", 0),

@@ -1,7 +1,8 @@
 """Regenerates tests/golden/goldens.npz from the reference's golden PNGs.
 
-Run once in a checkout that has the pixie reference next to it:
+Run once with a checkout of the pixie reference (6.0.0):
     python tests/golden/make_fixtures.py /path/to/pixie
+or with the checkout's path in the PIXIE_REFERENCE environment variable.
 Each entry is the straight-alpha RGBA uint8 pixel array of one master PNG that
 the reference's own tests write (tests/paths, tests/images, tests/contexts),
 keyed like "paths/pathHeart".  Only the masters used by tests/golden/cases.py
@@ -24,7 +25,8 @@ from cases import CASES  # noqa: E402
 # Input images the reference's tests read with readImage (straight-alpha RGBA),
 # keyed by the name cases.py loads them under.
 INPUTS = {"turtle": "images/turtle.png", "turtle10x": "images/turtle@10x.png", "rock": "images/rock.png",
-          "mandrill": "fileformats/png/mandrill.png"}
+          "mandrill": "fileformats/png/mandrill.png", "flipped1": "images/flipped1.png",
+          "minifiedBy2": "images/minifiedBy2.png", "minifiedBy4": "images/minifiedBy4.png"}
 
 
 def main(ref_root: str) -> None:
@@ -40,4 +42,7 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PIXIE_REFERENCE")
+    if not root:
+        sys.exit("usage: make_fixtures.py <pixie checkout>  (or set PIXIE_REFERENCE)")
+    main(root)

@@ -34,6 +34,11 @@ class OracleBackend:
             img = pxo.minify_by2(img)
         return img
 
+    def magnify(self, img, power):
+        for _ in range(power):
+            img = pxo.magnify_by2(img)
+        return img
+
     def fill_path_paint(self, img, cmds, paint, mat=None, winding=0):
         pxo.fill_path_paint(img, cmds, paint, mat, winding)
 

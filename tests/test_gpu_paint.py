@@ -96,7 +96,7 @@ def test_gradient_fill_paint_large(kind):
 
 
 def test_angular_gradient_atan2_matches():
-    """the shared float64 arctangent: every pixel of a 1500x1500 angular
+    """the shared float-float arctangent: every pixel of a 1500x1500 angular
     gradient whose stops turn each ulp of t into a colour step"""
     stops = [((0.0, 0.0, 0.0, 1.0), 0.0), ((1.0, 1.0, 1.0, 1.0), 1.0)]
     paint = dict(kind=ANGULAR, handles=[(f32(749.5), f32(750.25)), (f32(1400.0), f32(700.0)), (0.0, 0.0)],
@@ -106,6 +106,21 @@ def test_angular_gradient_atan2_matches():
     img = px.Image(1500, 1500)
     img.fill(gpu_paint(paint))
     assert_same(img.to_numpy(), ref, "angular 1500^2")
+
+
+@pytest.mark.parametrize("kind", [LINEAR, RADIAL, ANGULAR])
+@pytest.mark.parametrize("nstops", [2457, 2458, 3000])
+def test_gradient_many_stops(kind, nstops):
+    """gradientColor takes any number of stops: up to 2457 (48 KB) the kernel
+    stages them in shared memory, beyond that it reads them from global memory"""
+    rng = np.random.default_rng(nstops + kind)
+    paint = rand_gradient(rng, kind, 300, 200)
+    paint["stops"] = rand_stops(rng, nstops)
+    ref = pxo.new_image(300, 200)
+    pxo.fill_paint(ref, paint)
+    img = px.Image(300, 200)
+    img.fill(gpu_paint(paint))
+    assert_same(img.to_numpy(), ref, f"kind {kind}, {nstops} stops")
 
 
 @pytest.mark.parametrize("tiled", [False, True])

@@ -34,7 +34,9 @@ ROUNDING_SENSITIVE = {"paths/arcTo2", "paths/opacityFill", "paths/opacityStroke"
 #   of the inverse and of Mat3 * Vec2 gives the same position);
 # - rock_minified(2): (a + b + c + d + 1) div 4 fits 99.99 % of the master's
 #   pixels, the source's minifyBy2 has + 2 (images.nim:193-198, and the same
-#   in simd/sse2.nim:420-423).
+#   in simd/sse2.nim:420-423).  The minifiedBy2/By4 and minifiedMandrill
+#   masters of tests/test_images.nim:90-118 match + 2 exactly, so the rock
+#   masters are the stale ones.
 # The oracle follows the source; test_gpu_parity compares these scenes GPU vs
 # oracle, and test_stale_masters_differ_only_where_stated checks the claim.
 STALE_MASTERS = {f"images/masters/smooth{k}" for k in (1, 2, 3, 4, 5, 6, 7, 10, 11, 12)} | {
@@ -141,3 +143,31 @@ def test_rock_minified_master_rounds_plus_one():
     s = rock[:2 * h, :2 * w].reshape(h, 2, w, 2, 4).sum(axis=(1, 3))[..., 3]
     assert ((s + 1) // 4 == gold[:h, :w, 3]).mean() > 0.9999
     assert ((s + 2) // 4 == gold[:h, :w, 3]).mean() < 0.995
+
+
+def test_minified_mandrill_master_rounds_plus_two():
+    """minifiedMandrill (tests/test_images.nim:114-118): every byte of the
+    master is (sum + 2) div 4 of its 2x2 block, the source's rounding; the
+    + 1 of the stale rock masters fits only ~81 % of it."""
+    import cases
+    from oracle_backend import OracleBackend
+    cases._load(OracleBackend(), "mandrill")
+    m = cases.premultiplied(cases._INPUTS["mandrill"]).astype(int)
+    gold = GOLDENS["images__minifiedMandrill"].astype(int)
+    s = m.reshape(256, 2, 256, 2, 4).sum(axis=(1, 3))
+    assert np.array_equal((s + 2) // 4, gold)
+    assert ((s + 1) // 4 == gold).mean() < 0.9
+
+
+def test_row_windows_equal_one_thread():
+    """The oracle's threaded scene render (row windows) gives the bytes of
+    the one-thread render, MaskBlend's clears outside the path included."""
+    from pixie_gb300 import workloads as wl
+    items = wl.dense_scene(21, n_paths=80, size=256.0)
+    for k, it in enumerate(items):
+        if k % 9 == 0 and it["kind"] == "fill":
+            it["blend"] = 16  # MaskBlend
+    one = wl.premultiplied_image(4, 256, 256)
+    many = one.copy()
+    assert pxo.draw_items(one, items, 1) == pxo.draw_items(many, items, 5)
+    assert np.array_equal(one, many)
