@@ -792,11 +792,22 @@ TRAFFIC = {"blur:16": 67246336 + 16806656 + 67213312 + 13801984,
 
 
 # -- CPU baseline / reference arm ----------------------------------------------------------
-def cpu_sample_rates(seed=1):
+def cpu_sample_rates(seed=1, simd=True):
     """Single-thread oracle throughput per operation on a bounded sample.
+    simd: the Normal/Mask/Overwrite lines run the oracle's restatement of the
+    reference's NEON kernels (what a pixie build on this host runs: the
+    reference's blur and other blend modes are scalar on every ISA).
     Returns (estimated seconds for one full step, description)."""
     from oracle import pxo
     from pixie_gb300 import workloads as wl
+    pxo.set_simd_variant(simd)
+    try:
+        return _cpu_sample(seed, simd, pxo, wl)
+    finally:
+        pxo.set_simd_variant(False)
+
+
+def _cpu_sample(seed, simd, pxo, wl):
     S = 1024
     a = wl.premultiplied_image(seed * 10, S, S)
     b = wl.premultiplied_image(seed * 10 + 5, S, S)
@@ -819,15 +830,22 @@ def cpu_sample_rates(seed=1):
     t = time.perf_counter()
     pxo.shadow(mask, 8, 8, 4, 12, [0, 0, 0, 1])
     est += time.perf_counter() - t
-    return est, ("oracle (C++ restatement of pixie's scalar path), 1 thread: draw 20 modes on "
-                 "1024^2, blur r in {1,4,16,64} on 1024x384, shadow on 1024^2; scaled per pixel "
-                 "to the full step")
+    what = ("C++ restatement of pixie's SIMD build (its NEON line kernels for Normal/Mask lines, "
+            "scalar elsewhere as in pixie)" if simd else "C++ restatement of pixie's scalar path")
+    return est, (what + ", 1 thread: draw 20 modes on 1024^2, blur r in {1,4,16,64} on 1024x384, "
+                 "shadow on 1024^2; scaled per pixel to the full step")
 
 
-def _ref_worker(seed):
+def _ref_worker(args):
+    seed, simd = args
     sys.path.insert(0, ROOT)
-    est, _ = cpu_sample_rates(seed)
+    est, _ = cpu_sample_rates(seed, simd)
     return est
+
+
+def host_info():
+    import platform
+    return {"uname_m": platform.machine(), "nproc": os.cpu_count()}
 
 
 def run_reference(args, ws, rank):
@@ -838,17 +856,19 @@ def run_reference(args, ws, rank):
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
         for _ in range(args.warmup):
-            pool.map(_ref_worker, range(1, cores + 1))
+            pool.map(_ref_worker, [(k, True) for k in range(1, cores + 1)])
         t = time.perf_counter()
         est_total = 0.0
         for _ in range(args.steps):
-            ests = pool.map(_ref_worker, range(1, cores + 1))
+            ests = pool.map(_ref_worker, [(k, True) for k in range(1, cores + 1)])
             est_total += statistics.mean(ests)
         wall = time.perf_counter() - t
+        scalar = statistics.mean(pool.map(_ref_worker, [(k, False) for k in range(1, cores + 1)]))
     per_step_single = est_total / args.steps
     value = STEP_PIXELS * cores / per_step_single / 1e9  # cores run independent steps
     return {"value": value, "cores": cores, "wall_s": wall,
-            "ms_per_step": per_step_single * 1e3 / cores}
+            "ms_per_step": per_step_single * 1e3 / cores,
+            "scalar_value": STEP_PIXELS * cores / scalar / 1e9}
 
 
 def run_case(case: str, slice_w: int = 0):
@@ -953,10 +973,13 @@ def main():
                     "config": WORKLOAD, "impl": "reference",
                     "cpu_baseline": {"value": round(r["value"], 4), "unit": "Gpix/s",
                                      "cores": r["cores"], "kind": "port",
+                                     "scalar_value": round(r["scalar_value"], 4),
                                      "sample": "per core: draw 20 modes on 1024^2, blur r in "
                                                "{1,4,16,64} on 1024x384, shadow 1024^2, scaled "
                                                "per pixel; pixie (Nim) cannot be built here, so "
-                                               "this is the oracle's C++ restatement"},
+                                               "this is the oracle's C++ restatement of pixie's SIMD "
+                                               "build (NEON line kernels on aarch64; scalar_value: "
+                                               "the scalar build)", **host_info()},
                     "e2e": {"value": round(r["value"], 4), "unit": "Gpix/s",
                             "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
             print(json.dumps(line), flush=True)
@@ -969,9 +992,10 @@ def main():
     cpu = None
     if not args.no_cpu_baseline:
         est, sample = cpu_sample_rates(1)
-        from oracle import cpu_baselines
+        est_scalar, _ = cpu_sample_rates(1, simd=False)
         cpu = {"value": round(STEP_PIXELS / est / 1e9, 5), "unit": "Gpix/s", "cores": 1,
-               "kind": "port", "sample": sample, **cpu_baselines.host()}
+               "kind": "port", "sample": sample, "scalar_value": round(STEP_PIXELS / est_scalar / 1e9, 5),
+               **host_info()}
     line = {"metric": METRIC, "value": round(value, 3), "unit": "Gpix/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",

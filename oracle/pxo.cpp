@@ -38,6 +38,8 @@
 #include <string>
 #include <vector>
 
+#include "simd_lines.h"
+
 namespace pxo {
 
 struct PixieError : std::runtime_error {
@@ -1353,10 +1355,149 @@ static inline RGBX opacity_sse2(RGBX c, float area) {  // applyOpacity(M128, flo
   return rgbx(ch(c.r), ch(c.g), ch(c.b), ch(c.a));
 }
 
+// ---------------------------------------------------------------------------
+// The NEON line kernels (simd/neon.nim:427-700), TIMED CPU BASELINE ONLY (see
+// simd_lines.h): with g_simd_variant = 1 the Normal/Mask/Overwrite lines of
+// fills and of draw run these instead of the scalar loops.  Never set by the
+// parity tests; bench.py times both variants.
+// ---------------------------------------------------------------------------
+int g_simd_variant = 0;
+
+namespace nl {
+using simd::u8x16;
+static inline bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
+static inline u8x16 splat_px(RGBX c) {
+  u8x16 v;
+  for (int k = 0; k < 16; k += 4) {
+    v[k] = c.r;
+    v[k + 1] = c.g;
+    v[k + 2] = c.b;
+    v[k + 3] = c.a;
+  }
+  return v;
+}
+static inline u8x16 cov_bcast(u8x16 cv, int q) {  // coverage of pixels 4q..4q+3, each over its 4 bytes
+  u8x16 v;
+  for (int k = 0; k < 16; k++) v[k] = cv[4 * q + (k >> 2)];
+  return v;
+}
+static inline bool all_bytes(u8x16 v, uint8_t x) {
+  for (int k = 0; k < 16; k++)
+    if (v[k] != x) return false;
+  return true;
+}
+// blendLineNormalNeon(a, b)  :502-527
+static void normal2(RGBX* a, const RGBX* b, int64_t len) {
+  int64_t i = 0;
+  for (; i < len && !aligned16(a + i); i++) a[i] = blendNormal(a[i], b[i]);
+  for (; i < len - 16; i += 16) {
+    u8x16 sv[4];
+    bool opaque = true;
+    for (int q = 0; q < 4; q++) {
+      sv[q] = simd::load16(b + i + 4 * q);
+      opaque = opaque && simd::all_alpha(sv[q], 255);
+    }
+    for (int q = 0; q < 4; q++)
+      simd::store16(a + i + 4 * q, opaque ? sv[q] : simd::normal4(simd::load16(a + i + 4 * q), sv[q]));
+  }
+  for (; i < len; i++) a[i] = blendNormal(a[i], b[i]);
+}
+// blendLineMaskNeon(a, b)  :609-639
+static void mask2(RGBX* a, const RGBX* b, int64_t len) {
+  int64_t i = 0;
+  for (; i < len && !aligned16(a + i); i++) a[i] = blend_px(MaskBlend, a[i], b[i]);
+  for (; i < len - 16; i += 16) {
+    u8x16 sv[4];
+    bool opaque = true;
+    for (int q = 0; q < 4; q++) {
+      sv[q] = simd::load16(b + i + 4 * q);
+      opaque = opaque && simd::all_alpha(sv[q], 255);
+    }
+    if (opaque) continue;
+    for (int q = 0; q < 4; q++)
+      simd::store16(a + i + 4 * q, simd::mul_div255(simd::load16(a + i + 4 * q), simd::alpha_bcast(sv[q])));
+  }
+  for (; i < len; i++) a[i] = blend_px(MaskBlend, a[i], b[i]);
+}
+// blendLineNormalNeon(line, rgbx)  :479-500
+static void normal1(RGBX* a, RGBX c, int64_t len) {
+  int64_t i = 0;
+  for (; i < len && !aligned16(a + i); i++) a[i] = blendNormal(a[i], c);
+  const u8x16 cv = splat_px(c);
+  for (; i < len - 16; i += 16)
+    for (int q = 0; q < 4; q++) simd::store16(a + i + 4 * q, simd::normal4(simd::load16(a + i + 4 * q), cv));
+  for (; i < len; i++) a[i] = blendNormal(a[i], c);
+}
+// blendLineMaskNeon(line, rgbx)  :587-607
+static void mask1(RGBX* a, RGBX c, int64_t len) {
+  int64_t i = 0;
+  for (; i < len && !aligned16(a + i); i++) a[i] = blend_px(MaskBlend, a[i], c);
+  const u8x16 al = u8x16{} + c.a;
+  for (; i < len - 16; i += 16)
+    for (int q = 0; q < 4; q++) simd::store16(a + i + 4 * q, simd::mul_div255(simd::load16(a + i + 4 * q), al));
+  for (; i < len; i++) a[i] = blend_px(MaskBlend, a[i], c);
+}
+// blendLineCoverage{Overwrite,Normal,Mask}Neon  :427-477, :529-585, :641-700
+static void coverage(RGBX* line, const uint8_t* cov, RGBX c, int64_t len, int mode) {
+  auto scalar = [&](int64_t i) {
+    const uint8_t k = cov[i];
+    if (mode == OverwriteBlend) {
+      if (k != 0) line[i] = mul_c(c, k);
+    } else if (mode == NormalBlend) {
+      if (k != 0) line[i] = blendNormal(line[i], mul_c(c, k));
+    } else {
+      if (k == 0) line[i] = RGBX{0, 0, 0, 0};
+      else if (k != 255) line[i] = blend_px(MaskBlend, line[i], mul_c(c, k));
+    }
+  };
+  int64_t i = 0;
+  for (; i < len && !aligned16(line + i); i++) scalar(i);
+  const u8x16 cv = splat_px(c), al = u8x16{} + c.a;
+  for (; i < len - 16; i += 16) {
+    const u8x16 k = simd::load16(cov + i);
+    const bool zero = all_bytes(k, 0), full = all_bytes(k, 255);
+    if (mode == OverwriteBlend) {
+      if (zero) continue;
+      for (int q = 0; q < 4; q++)
+        simd::store16(line + i + 4 * q, full ? cv : simd::mul_div255(cv, cov_bcast(k, q)));
+    } else if (mode == NormalBlend) {
+      if (zero) continue;
+      for (int q = 0; q < 4; q++) {
+        if (full && c.a == 255) {
+          simd::store16(line + i + 4 * q, cv);
+        } else {
+          const u8x16 src = simd::mul_div255(cv, cov_bcast(k, q));
+          simd::store16(line + i + 4 * q, simd::normal4(simd::load16(line + i + 4 * q), src));
+        }
+      }
+    } else {
+      if (zero) {
+        for (int q = 0; q < 4; q++) simd::store16(line + i + 4 * q, u8x16{});
+        continue;
+      }
+      if (full && c.a == 255) continue;
+      for (int q = 0; q < 4; q++) {
+        const u8x16 a = simd::mul_div255(al, cov_bcast(k, q));
+        simd::store16(line + i + 4 * q, simd::mul_div255(simd::load16(line + i + 4 * q), a));
+      }
+    }
+  }
+  for (; i < len; i++) scalar(i);
+}
+}  // namespace nl
+
 static void fillCoverage(Image& img, RGBX c, int64_t startX, int64_t y, const CovRow& cov,
                          int mode) {  // :1479-1526
   int64_t n = (int64_t)cov.c.size();
   RGBX* line = img.data + img.idx(startX, y);
+  if (g_simd_variant && (mode == OverwriteBlend || mode == NormalBlend || mode == MaskBlend)) {
+    nl::coverage(line, cov.c.data(), c, n, mode);
+    if (mode == MaskBlend) {
+      clearUnsafe(img, 0, y, startX, y);
+      clearUnsafe(img, startX + n, y, img.width, y);
+    }
+    return;
+  }
   switch (mode) {
     case OverwriteBlend:  // :1442-1451
       for (int64_t i = 0; i < n; i++)
@@ -1399,6 +1540,8 @@ static void fillHits(Image& img, RGBX c, int64_t startX, int64_t y, const std::v
       forSpans([&](int64_t s, int64_t l) {
         if (c.a == 255) {
           fillUnsafe(img, c, img.idx(s, y), l);
+        } else if (g_simd_variant) {
+          nl::normal1(img.data + img.idx(s, y), c, l);
         } else {
           RGBX* line = img.data + img.idx(s, y);
           for (int64_t i = 0; i < l; i++) line[i] = blendNormal(line[i], c);
@@ -1414,7 +1557,8 @@ static void fillHits(Image& img, RGBX c, int64_t startX, int64_t y, const std::v
         }
         if (c.a != 255) {
           RGBX* line = img.data + img.idx(s, y);
-          for (int64_t i = 0; i < l; i++) line[i] = blend_px(MaskBlend, line[i], c);
+          if (g_simd_variant) nl::mask1(line, c, l);
+          else for (int64_t i = 0; i < l; i++) line[i] = blend_px(MaskBlend, line[i], c);
         }
         filledTo = s + l;
       });
@@ -1709,7 +1853,8 @@ static void blendRect(Image& a, const Image& b, int64_t px, int64_t py, int mode
       if (xStart + px > 0) fillUnsafe(a, RGBX{0, 0, 0, 0}, a.idx(0, y + py), xStart + px);
       RGBX* dl = a.data + a.idx(xStart + px, y + py);
       const RGBX* sl = b.data + b.idx(xStart, y);
-      for (int64_t i = 0; i < xEnd - xStart; i++) dl[i] = blend_px(MaskBlend, dl[i], sl[i]);
+      if (g_simd_variant) nl::mask2(dl, sl, xEnd - xStart);
+      else for (int64_t i = 0; i < xEnd - xStart; i++) dl[i] = blend_px(MaskBlend, dl[i], sl[i]);
       if (xEnd + px < a.width) fillUnsafe(a, RGBX{0, 0, 0, 0}, a.idx(xEnd + px, y + py), a.width - (xEnd + px));
     }
     if (yEnd + py < a.height)
@@ -1719,7 +1864,8 @@ static void blendRect(Image& a, const Image& b, int64_t px, int64_t py, int mode
   for (int64_t y = yStart; y < yEnd; y++) {
     RGBX* dl = a.data + a.idx(xStart + px, y + py);
     const RGBX* sl = b.data + b.idx(xStart, y);
-    for (int64_t i = 0; i < xEnd - xStart; i++) dl[i] = blend_px(mode, dl[i], sl[i]);
+    if (g_simd_variant && mode == NormalBlend) nl::normal2(dl, sl, xEnd - xStart);
+    else for (int64_t i = 0; i < xEnd - xStart; i++) dl[i] = blend_px(mode, dl[i], sl[i]);
   }
 }
 
@@ -2446,6 +2592,9 @@ const char* pxo_last_error(void) { return g_err.c_str(); }
 
 // Golden-pinning mode switch (see g_golden_mode); 0 = scalar oracle.
 void pxo_set_golden_mode(int on) { g_golden_mode = on; }
+
+// 1: the NEON line kernels of the timed CPU baseline (see nl::), 0: scalar.
+void pxo_set_simd_variant(int on) { g_simd_variant = on; }
 
 // This thread's row window for fills and strokes (see g_row_lo).
 void pxo_set_row_window(int64_t lo, int64_t hi) {

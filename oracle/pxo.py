@@ -35,8 +35,8 @@ def build() -> str:
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(_LIB_PATH) or (
-                os.path.getmtime(_LIB_PATH) < os.path.getmtime(os.path.join(_HERE, "pxo.cpp"))):
+        if not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < max(
+                os.path.getmtime(os.path.join(_HERE, f)) for f in ("pxo.cpp", "simd_lines.h")):
             build()
         L = C.CDLL(_LIB_PATH)
         P, I64, F, I = C.c_void_p, C.c_int64, C.c_float, C.c_int
@@ -68,6 +68,7 @@ def lib():
         L.pxo_to_straight.argtypes = [P, I64]
         L.pxo_set_golden_mode.argtypes = [I]
         L.pxo_set_row_window.argtypes = [I64, I64]
+        L.pxo_set_simd_variant.argtypes = [I]
         _lib = L
     return _lib
 
@@ -296,6 +297,13 @@ def set_golden_mode(on: bool):
     """Golden-pinning only: reproduce the build that wrote the reference's
     master PNGs (floored coverage multiply, SSE2 sliver rounding)."""
     lib().pxo_set_golden_mode(1 if on else 0)
+
+
+def set_simd_variant(on: bool):
+    """True: the NEON line kernels of pixie's SIMD build (rounding multiply by
+    alpha) for Normal/Mask/Overwrite lines -- the timed CPU baseline only;
+    False (default): the scalar semantics every parity test uses."""
+    lib().pxo_set_simd_variant(1 if on else 0)
 
 
 def draw_items(img, items, threads: int = 1):

@@ -26,6 +26,7 @@ struct pxg_image {
   uint8_t* data;
   int64_t width, height;
   int owned;
+  bool exported = false;  // pxg_image_device_ptr handed the address out: it must not change
   cudaEvent_t copy_ev = nullptr;  // the last asynchronous upload or download of the image
   bool copy_pending = false;      // ... which no compute on the image has waited for yet
   cudaEvent_t compute_ev = nullptr;  // after the last compute call that named the image
@@ -164,6 +165,8 @@ bool ring_blur_init(size_t* maxSmem);
 bool weights_exact_f16(const uint16_t* hostKern, int r);
 bool launch_blur_ring(uint32_t* img, uint32_t* tmp, long long W, long long H, int r, const uint16_t* kern,
                       bool exactF16, uint32_t oob, int nsm, size_t maxSmem, int* err, cudaStream_t st);
+bool launch_blur_small_fused(const uint32_t* in, uint32_t* out, long long W, long long H, int r,
+                             const uint16_t* kern, uint32_t oob, cudaStream_t st);
 bool launch_blur_small(uint32_t* img, uint32_t* tmp, long long W, long long H, int r, const uint16_t* kern,
                        uint32_t oob, int nsm, cudaStream_t st);
 __global__ void k_blur_x(const uint32_t*, uint32_t*, long long, long long, int, const uint16_t*, uint32_t);
@@ -383,9 +386,17 @@ const uint16_t* weights_for(int64_t r) {
 
 // Both blur passes of an RGBX image (img -> tmp -> img) with the configured
 // kernels; a kernel family that does not take this image or radius hands it
-// to the next one.
-void blur_dispatch(uint32_t* img, uint32_t* tmp, long long W, long long H, int64_t r, uint32_t oob) {
+// to the next one.  With swap_ok the caller owns both buffers and lets the
+// result land in tmp: radii 1..8 then run as one fused launch (img -> tmp)
+// and the function returns true, after which the caller exchanges the two
+// buffers.
+bool blur_dispatch(uint32_t* img, uint32_t* tmp, long long W, long long H, int64_t r, uint32_t oob,
+                   bool swap_ok = false) {
   const uint16_t* kern = weights_for(r);
+  if (swap_ok && g.blur_tensor == 3 && launch_blur_small_fused(img, tmp, W, H, (int)r, kern, oob, g.stream)) {
+    g.last_blur = 5;
+    return true;
+  }
   int used = -1;
   if (g.blur_tensor == 3 && launch_blur_small(img, tmp, W, H, (int)r, kern, oob, g.nsm, g.stream)) used = 4;
   if (used < 0 && g.blur_tensor == 3 && g.ring_ok &&
@@ -403,6 +414,7 @@ void blur_dispatch(uint32_t* img, uint32_t* tmp, long long W, long long H, int64
     used = 0;
   }
   g.last_blur = used;
+  return false;
 }
 
 void* scratch(long long bytes) {
@@ -1211,7 +1223,8 @@ void srv_step(pxg_server* sv) {
     }
     if (j->next >= j->scene->jobs.size()) {
       if (j->blur > 0) {
-        blur_dispatch((uint32_t*)j->canvas.data, (uint32_t*)j->tmp, j->W, j->H, j->blur, 0u);
+        if (blur_dispatch((uint32_t*)j->canvas.data, (uint32_t*)j->tmp, j->W, j->H, j->blur, 0u, true))
+          std::swap(j->canvas.data, j->tmp);  // both the job's own; the old canvas is freed with tmp below
         CU(cudaGetLastError());
       }
       done.push_back(j);
@@ -1489,7 +1502,12 @@ void pxg_image_free(pxg_image* im) {
 
 int64_t pxg_image_width(const pxg_image* im) { return im ? im->width : 0; }
 int64_t pxg_image_height(const pxg_image* im) { return im ? im->height : 0; }
-void* pxg_image_device_ptr(pxg_image* im) { return im ? im->data : nullptr; }
+void* pxg_image_device_ptr(pxg_image* im) {
+  if (!im) return nullptr;
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  im->exported = true;
+  return im->data;
+}
 
 int pxg_image_upload(pxg_image* im, const void* host, int64_t nbytes) {
   std::lock_guard<std::recursive_mutex> lk(g.mu);  // the mode is read and used under the library's lock
@@ -2656,9 +2674,18 @@ int pxg_image_blur(pxg_image* im, float radius, const float* oob) {
     static const float zero[4] = {0, 0, 0, 0};
     uint32_t o = color_to_rgbx(oob ? oob : zero);
     weights_for(r);
-    uint32_t* tmp = (uint32_t*)scratch(im->width * im->height * 4);
+    const long long bytes = im->width * im->height * 4;
+    uint32_t* tmp = (uint32_t*)scratch(bytes);
     Timed t;
-    blur_dispatch((uint32_t*)im->data, tmp, im->width, im->height, r, o);
+    // an image the library allocated, whose address nobody holds, may take
+    // the fused small-radius kernel: the result lands in the scratch buffer
+    // and the two buffers change owners (stream order keeps every earlier
+    // and later use of either buffer in place)
+    const bool swap_ok = im->owned && !im->exported;
+    if (blur_dispatch((uint32_t*)im->data, tmp, im->width, im->height, r, o, swap_ok)) {
+      std::swap(im->data, g.scratch);
+      g.scratch_cap = bytes;
+    }
     CU(cudaGetLastError());
     t.done();
     if (g.blocking) check_device_error();

@@ -122,10 +122,66 @@ __device__ __forceinline__ uint32_t premul8(uint32_t sv) {  // internal.nim:86-9
 // then 256 floats v / 255.0f (the float division, done once on the host).
 constexpr size_t kTblUnitOff = 65536, kTblBytes = 65536 + 1024;
 
-__device__ __forceinline__ Px straight8(const uint8_t* tbl, uint32_t v) {
+__device__ __forceinline__ float small_to_f(uint32_t x) {  // exact for x < 2^23
+  return __uint_as_float(0x4B000000u | x) - 8388608.0f;
+}
+
+// The straight-alpha table entry min(round(c * (255 / a)), 255), evaluated in
+// float64 by the reference, computed without the table.  For a > 0,
+// floor((510 c + a) / (2 a)) is c * 255 / a rounded half up, exactly; the
+// quotient comes from a float reciprocal with one exact remainder correction
+// (every operand is an integer below 2^24).  The float64 product differs from
+// that only at exact ties (c * 255 / a = k + 1/2) for the alphas whose float64
+// 255 / a lies below 255 / a -- 50 58 100 106 116 182 186 200 206 210 212 232
+// 234 242 (kTieAlpha) -- where the product can round below the tie; those few
+// channels take the reference's float64 expression itself.  All 65536
+// (a, c) pairs were checked against the table on the host.
+__device__ __forceinline__ bool tie_alpha(uint32_t a) {
+  const unsigned long long m = a < 128 ? (a < 64 ? 0x0404000000000000ull : 0x0010041000000000ull)
+                                       : (a < 192 ? 0x0440000000000000ull : 0x0004050000144100ull);
+  return (m >> (a & 63)) & 1ull;
+}
+struct AlphaDiv {  // per pixel: 2a as a float and its approximate reciprocal
+  float d, rd;
+  bool tie;
+};
+__device__ __forceinline__ AlphaDiv alpha_div(uint32_t a) {
+  AlphaDiv r;
+  r.d = small_to_f(2u * a);
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r.rd) : "f"(r.d));
+  r.tie = tie_alpha(a);
+  return r;
+}
+__device__ __forceinline__ uint32_t straight_ch(uint32_t c, uint32_t a, const AlphaDiv& ad) {
+  const float n = small_to_f(510u * c + a);
+  const float t = __fmaf_rd(n, ad.rd, 12582912.0f);
+  const float q = t - 12582912.0f;
+  float rem = fmaf(-q, ad.d, n);
+  uint32_t qi = __float_as_uint(t) - 0x4B400000u;
+  if (rem < 0.0f) {
+    qi -= 1u;
+    rem += ad.d;
+  } else if (rem >= ad.d) {
+    qi += 1u;
+    rem -= ad.d;
+  }
+  if (rem == 0.0f && ad.tie) qi = (uint32_t)round((double)c * (255.0 / (double)a));
+  return qi < 255u ? qi : 255u;
+}
+__device__ __forceinline__ Px straight8(const uint8_t* /*tbl*/, uint32_t v) {
   Px p = unpack(v);
-  const uint8_t* row = tbl + p.a * 256;
-  return Px{row[p.r], row[p.g], row[p.b], p.a};
+  if (p.a == 0) return Px{0u, 0u, 0u, 0u};
+  const AlphaDiv ad = alpha_div(p.a);
+  return Px{straight_ch(p.r, p.a, ad), straight_ch(p.g, p.a, ad), straight_ch(p.b, p.a, ad), p.a};
+}
+// v / 255.0f correctly rounded, for integers 0..255: the product with
+// float(1/255) plus one FMA remainder correction (exact for all 256 values).
+__device__ __forceinline__ float unit255(uint32_t v) {
+  const float r = 1.0f / 255.0f;
+  const float x = small_to_f(v);
+  const float q0 = x * r;
+  const float rem = fmaf(-q0, 255.0f, x);
+  return fmaf(rem, r, q0);
 }
 __device__ __forceinline__ uint32_t unit_to_u8(float c) {
   float v = roundf(c * 255.0f);
@@ -167,26 +223,24 @@ __device__ __forceinline__ float sat3(F3 c) {
   return fmaxf(c.r, fmaxf(c.g, c.b)) - fminf(c.r, fminf(c.g, c.b));
 }
 __device__ __forceinline__ F3 setSat(F3 c, float s) {
-  float v[3] = {c.r, c.g, c.b};
+  // the first maximum and the first minimum (strict comparisons in r, g, b
+  // order), selected without an indexed array so nothing goes to local memory
   int imax = 0, imin = 0;
-#pragma unroll
-  for (int i = 1; i < 3; i++) {
-    if (v[i] > v[imax]) imax = i;
-    if (v[i] < v[imin]) imin = i;
-  }
+  float cmax = c.r, cmin = c.r;
+  if (c.g > cmax) { imax = 1; cmax = c.g; }
+  if (c.b > cmax) { imax = 2; cmax = c.b; }
+  if (c.g < cmin) { imin = 1; cmin = c.g; }
+  if (c.b < cmin) { imin = 2; cmin = c.b; }
   if (imax == imin) return F3{0.0f, 0.0f, 0.0f};
-  int imid = 3 - imax - imin;
-  float cmax = v[imax], cmin = v[imin], cmid = v[imid];
-  float out[3];
+  const int imid = 3 - imax - imin;
+  const float cmid = imid == 0 ? c.r : (imid == 1 ? c.g : c.b);
+  float mid = 0.0f, mx = 0.0f;
   if (cmax > cmin) {
-    out[imid] = ((cmid - cmin) * s) / (cmax - cmin);
-    out[imax] = s;
-  } else {
-    out[imid] = 0.0f;
-    out[imax] = 0.0f;
+    mid = ((cmid - cmin) * s) / (cmax - cmin);
+    mx = s;
   }
-  out[imin] = 0.0f;
-  return F3{out[0], out[1], out[2]};
+  return F3{imax == 0 ? mx : (imid == 0 ? mid : 0.0f), imax == 1 ? mx : (imid == 1 ? mid : 0.0f),
+            imax == 2 ? mx : (imid == 2 ? mid : 0.0f)};
 }
 __device__ __forceinline__ float softLight1(float cb, float cs) {
   if (cs <= 0.5f) return cb - ((1.0f - 2.0f * cs) * cb) * (1.0f - cb);
@@ -199,10 +253,9 @@ __device__ __forceinline__ uint32_t blendFloatT(const uint8_t* tbl, uint32_t bp,
 
 static __device__ __noinline__ uint32_t blendFloat(const uint8_t* tbl, uint32_t bp, uint32_t sp, int mode) {
   Px b8 = straight8(tbl, bp), s8 = straight8(tbl, sp);
-  const float* u = reinterpret_cast<const float*>(tbl + kTblUnitOff);  // u[v] = v / 255.0f
-  F3 cb{u[b8.r], u[b8.g], u[b8.b]};
-  F3 cs{u[s8.r], u[s8.g], u[s8.b]};
-  float ab = u[b8.a], as = u[s8.a];
+  F3 cb{unit255(b8.r), unit255(b8.g), unit255(b8.b)};
+  F3 cs{unit255(s8.r), unit255(s8.g), unit255(s8.b)};
+  float ab = unit255(b8.a), as = unit255(s8.a);
   F3 m;
   switch (mode) {
     case kSoftLight:
@@ -229,10 +282,9 @@ template <int MODE>
 __device__ __forceinline__ uint32_t blendFloatT(const uint8_t* tbl, uint32_t bp, uint32_t sp) {
   constexpr int mode = MODE;
   Px b8 = straight8(tbl, bp), s8 = straight8(tbl, sp);
-  const float* u = reinterpret_cast<const float*>(tbl + kTblUnitOff);  // u[v] = v / 255.0f
-  F3 cb{u[b8.r], u[b8.g], u[b8.b]};
-  F3 cs{u[s8.r], u[s8.g], u[s8.b]};
-  float ab = u[b8.a], as = u[s8.a];
+  F3 cb{unit255(b8.r), unit255(b8.g), unit255(b8.b)};
+  F3 cs{unit255(s8.r), unit255(s8.g), unit255(s8.b)};
+  float ab = unit255(b8.a), as = unit255(s8.a);
   F3 m;
   switch (mode) {
     case kSoftLight:
@@ -274,9 +326,6 @@ __device__ __forceinline__ uint32_t fdiv_floor(float n, float d, float rd) {
   qi -= rem < 0.0f ? 1u : 0u;
   qi += rem >= d ? 1u : 0u;
   return qi;
-}
-__device__ __forceinline__ float small_to_f(uint32_t x) {  // exact for x < 2^23
-  return __uint_as_float(0x4B000000u | x) - 8388608.0f;
 }
 // ColorBurn / ColorDodge (blends.nim:111-126, :158-173) with the divisions
 // done as above: the same integers as the reference's integer divisions.

@@ -191,6 +191,124 @@ __global__ void __launch_bounds__(256) k_blur_sy(const uint32_t* __restrict__ in
   }
 }
 
+// Both passes in one launch, out of place (in -> out), for images the caller
+// can swap: a CTA owns a TW x TH output tile; it runs the X pass over the
+// tile's TH + 2R rows (rows outside the image hold the outOfBounds colour, as
+// the Y pass's taps read it there), keeps the quantised bytes in shared
+// memory, then runs the Y pass from shared memory and writes the tile once.
+// DRAM traffic is one read and one write of the image (the halo rows shared
+// by vertical neighbours come from L2).  The arithmetic per output is the
+// two-pass kernels': the same sums, the same floor(S / 65280) between passes.
+constexpr int kFTW = 128, kFTH = 64;  // tile: 128 columns x 64 rows
+template <int R>
+__global__ void __launch_bounds__(256) k_blur_fused(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
+                                                    int W, int H, const uint16_t* __restrict__ kern, uint32_t oob,
+                                                    int vec) {
+  constexpr int NI = kOut + 2 * R;
+  constexpr int D = (4 - (R & 3)) & 3;
+  constexpr int NC = (D + NI + 3) / 4;
+  constexpr int ROWS = kFTH + 2 * R;  // X-pass rows staged
+  __shared__ __align__(16) uint32_t xs[ROWS][kFTW];
+  pdl_trigger();
+  uint64_t w2[2 * R + 1];
+#pragma unroll
+  for (int t = 0; t <= 2 * R; t++) {
+    const float w = (float)kern[t];
+    w2[t] = f2_pack(w, w);
+  }
+  const uint64_t nb = f2_pack(-kBias, -kBias), kq = f2_pack(kQuotC, kQuotC), km = f2_pack(kMagic, kMagic);
+  const int tx0 = blockIdx.x * kFTW, ty0 = blockIdx.y * kFTH;
+  pdl_wait();
+  // X pass: (row, 8-pixel group) tasks over the staged rows
+  constexpr int GPR = kFTW / kOut;  // groups per staged row
+  for (int task = threadIdx.x; task < ROWS * GPR; task += blockDim.x) {
+    const int lr = task / GPR, g = task - lr * GPR;
+    const int y = ty0 - R + lr;
+    const int x0 = tx0 + g * kOut;
+    uint32_t res[kOut];
+    if (y < 0 || y >= H) {
+#pragma unroll
+      for (int o = 0; o < kOut; o++) res[o] = oob;
+    } else {
+      const int xa = x0 - R - D;
+      const uint32_t* row = in + (long long)y * W;
+      uint32_t px[4 * NC];
+      if (vec && xa >= 0 && xa + 4 * NC <= W) {
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+          const uint4 v = __ldg(reinterpret_cast<const uint4*>(row + xa) + c);
+          px[4 * c] = v.x;
+          px[4 * c + 1] = v.y;
+          px[4 * c + 2] = v.z;
+          px[4 * c + 3] = v.w;
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < 4 * NC; i++) {
+          const int x = xa + i;
+          px[i] = (x >= 0 && x < W) ? __ldg(row + x) : oob;
+        }
+      }
+      uint64_t arg[kOut], aba[kOut];
+#pragma unroll
+      for (int o = 0; o < kOut; o++) arg[o] = aba[o] = 0;
+#pragma unroll
+      for (int t = 0; t < NI; t++) {
+        uint64_t rg, ba;
+        px_f2(px[D + t], nb, rg, ba);
+#pragma unroll
+        for (int o = 0; o < kOut; o++) {
+          if (t - o >= 0 && t - o <= 2 * R) {
+            arg[o] = f2_fma(rg, w2[t - o], arg[o]);
+            aba[o] = f2_fma(ba, w2[t - o], aba[o]);
+          }
+        }
+      }
+#pragma unroll
+      for (int o = 0; o < kOut; o++) res[o] = quot_px(arg[o], aba[o], kq, km);
+    }
+    uint4* dst = reinterpret_cast<uint4*>(&xs[lr][g * kOut]);
+    dst[0] = make_uint4(res[0], res[1], res[2], res[3]);
+    dst[1] = make_uint4(res[4], res[5], res[6], res[7]);
+  }
+  __syncthreads();
+  // Y pass: (column, 8-row strip) tasks, consecutive threads on consecutive columns
+  constexpr int STRIPS = kFTH / kOut;
+  for (int task = threadIdx.x; task < STRIPS * kFTW; task += blockDim.x) {
+    const int sidx = task / kFTW, c = task - sidx * kFTW;
+    const int x = tx0 + c, y0 = ty0 + sidx * kOut;
+    if (x >= W || y0 >= H) continue;
+    uint64_t arg[kOut], aba[kOut];
+#pragma unroll
+    for (int o = 0; o < kOut; o++) arg[o] = aba[o] = 0;
+#pragma unroll
+    for (int t = 0; t < NI; t++) {
+      uint64_t rg, ba;
+      px_f2(xs[sidx * kOut + t][c], nb, rg, ba);
+#pragma unroll
+      for (int o = 0; o < kOut; o++) {
+        if (t - o >= 0 && t - o <= 2 * R) {
+          arg[o] = f2_fma(rg, w2[t - o], arg[o]);
+          aba[o] = f2_fma(ba, w2[t - o], aba[o]);
+        }
+      }
+    }
+    uint32_t* q = out + (long long)y0 * W + x;
+#pragma unroll
+    for (int o = 0; o < kOut; o++, q += W)
+      if (y0 + o < H) __stcs(q, quot_px(arg[o], aba[o], kq, km));
+  }
+}
+
+template <int R>
+void launch_fused(const uint32_t* in, uint32_t* out, int W, int H, const uint16_t* kern, uint32_t oob,
+                  cudaStream_t st) {
+  const int vec = (W % 4 == 0) && ((reinterpret_cast<uintptr_t>(in) & 15) == 0);
+  const dim3 grid((unsigned)((W + kFTW - 1) / kFTW), (unsigned)((H + kFTH - 1) / kFTH));
+  launch_pdl(k_blur_fused<R>, grid, dim3(256), 0, st, in, out, W, H, kern, oob, vec);
+  note_launch();
+}
+
 template <int R>
 void launch_small(uint32_t* img, uint32_t* tmp, int W, int H, const uint16_t* kern, uint32_t oob, int nsm,
                   cudaStream_t st) {
@@ -206,6 +324,25 @@ void launch_small(uint32_t* img, uint32_t* tmp, int W, int H, const uint16_t* ke
 }
 
 }  // namespace
+
+// Both passes in one launch, in -> out (out must not overlap in), for radii
+// 1..8; false if r is not for this kernel.
+bool launch_blur_small_fused(const uint32_t* in, uint32_t* out, long long W, long long H, int r,
+                             const uint16_t* kern, uint32_t oob, cudaStream_t st) {
+  if (r < 1 || r > 8 || W < 1 || H < 1 || W > (1 << 26) || H > (1 << 26)) return false;
+  if ((H + kFTH - 1) / kFTH > 65535) return false;
+  switch (r) {
+    case 1: launch_fused<1>(in, out, (int)W, (int)H, kern, oob, st); break;
+    case 2: launch_fused<2>(in, out, (int)W, (int)H, kern, oob, st); break;
+    case 3: launch_fused<3>(in, out, (int)W, (int)H, kern, oob, st); break;
+    case 4: launch_fused<4>(in, out, (int)W, (int)H, kern, oob, st); break;
+    case 5: launch_fused<5>(in, out, (int)W, (int)H, kern, oob, st); break;
+    case 6: launch_fused<6>(in, out, (int)W, (int)H, kern, oob, st); break;
+    case 7: launch_fused<7>(in, out, (int)W, (int)H, kern, oob, st); break;
+    default: launch_fused<8>(in, out, (int)W, (int)H, kern, oob, st); break;
+  }
+  return true;
+}
 
 // Both passes (img -> tmp -> img) for radii 1..kSmallBlurMax; false if r is
 // not for these kernels.

@@ -1,5 +1,8 @@
-"""The default blur kernels -- register-blocked CUDA-core passes for radii
-1..8, tensor-core passes with TMA-fed input rings above: every radius residue
+"""The default blur kernels -- for radii 1..8 the fused one-launch kernel
+(an image the library owns: the result lands in its scratch buffer and the
+buffers swap) or the two register-blocked passes (an image whose device
+address was handed out), tensor-core passes with TMA-fed input rings above:
+every radius residue
 mod 4 (the aligned-load offset), the boundary between byte-split and
 single-MMA weights, images smaller than a tile or a band, ragged sizes,
 segments that end mid-tile, and out-of-bounds colours -- all against the
@@ -23,8 +26,10 @@ def _init():
     px.blur_config(3)
 
 
-def blur_gpu(img, r, oob=(0, 0, 0, 0)):
+def blur_gpu(img, r, oob=(0, 0, 0, 0), exported=False):
     g = px.Image.from_numpy(img)
+    if exported:
+        assert g.device_ptr  # the address is out: the blur must stay in place
     g.blur(r, oob)
     out = g.to_numpy()
     return out, px.last_blur_kernel()
@@ -36,9 +41,10 @@ def blur_ref(img, r, oob=(0, 0, 0, 0)):
     return ref
 
 
-def expected_family(w, h, r):
+def expected_family(w, h, r, exported=False):
     if 1 <= r <= 8:
-        return 4  # the register-blocked small-radius passes take every image
+        # the fused kernel for owned images, the two register-blocked passes in place otherwise
+        return 4 if exported else 5
     # the ring passes: rows of whole 16-byte units in both orientations (TMA), radii 9..128
     if w % 4 == 0 and h % 4 == 0 and w >= 4 and h >= 4 and r <= 128:
         return 3
@@ -47,16 +53,17 @@ def expected_family(w, h, r):
 
 def check(img, r, oob=(0, 0, 0, 0)):
     h, w = img.shape[:2]
-    got, used = blur_gpu(img, r, oob)
-    fam = expected_family(w, h, r)
-    if fam is not None:
-        assert used == fam, f"blur ran on kernel family {used}, expected {fam}"
-    else:
-        assert used in (0, 1), f"blur ran on kernel family {used}"
     ref = blur_ref(img, r, oob)
-    d = np.abs(got.astype(np.int32) - ref.astype(np.int32))
-    assert int(d.max()) == 0, (f"r={r} {img.shape}: max|delta|={int(d.max())} "
-                               f"differing px={int((d.max(axis=2) > 0).sum())}")
+    for exported in ((False, True) if r <= 8 else (False,)):
+        got, used = blur_gpu(img, r, oob, exported)
+        fam = expected_family(w, h, r, exported)
+        if fam is not None:
+            assert used == fam, f"blur ran on kernel family {used}, expected {fam}"
+        else:
+            assert used in (0, 1), f"blur ran on kernel family {used}"
+        d = np.abs(got.astype(np.int32) - ref.astype(np.int32))
+        assert int(d.max()) == 0, (f"r={r} {img.shape} exported={exported}: max|delta|={int(d.max())} "
+                                   f"differing px={int((d.max(axis=2) > 0).sum())}")
 
 
 @pytest.mark.parametrize("r", list(range(1, 13)) + [15, 16, 17, 23, 24, 25, 30, 31, 32, 33, 34, 47, 63, 64, 65,
@@ -128,3 +135,22 @@ def _chain(img, radii):
     for r in radii:
         pxo.blur(ref, r, pxo.color_to_rgbx((0, 0, 0, 0)))
     return ref
+
+
+def test_fused_blur_swaps_buffers_and_keeps_chains_right():
+    """Several fused blurs in a row, with draws and other blurs between them,
+    on two owned images: each swap hands the image the scratch buffer and the
+    scratch the image's old buffer; every result equals the oracle's chain."""
+    a = wl.premultiplied_image(31, 300, 200)
+    b = wl.premultiplied_image(32, 300, 200)
+    A, B = px.Image.from_numpy(a), px.Image.from_numpy(b)
+    ra, rb = a.copy(), b.copy()
+    for step, r in enumerate((1, 4, 8, 20, 2, 3)):
+        A.blur(r)
+        pxo.blur(ra, r, pxo.color_to_rgbx((0, 0, 0, 0)))
+        B.draw(A, (step, -step), 2)
+        pxo.draw(rb, ra, step, -step, 2)
+        B.blur(r + 1)
+        pxo.blur(rb, r + 1, pxo.color_to_rgbx((0, 0, 0, 0)))
+    assert np.array_equal(A.to_numpy(), ra)
+    assert np.array_equal(B.to_numpy(), rb)
