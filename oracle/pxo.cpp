@@ -2593,6 +2593,24 @@ const char* pxo_last_error(void) { return g_err.c_str(); }
 // Golden-pinning mode switch (see g_golden_mode); 0 = scalar oracle.
 void pxo_set_golden_mode(int on) { g_golden_mode = on; }
 
+// The C library's sinf / cosf (what the reference's float32 sin/cos call),
+// element-wise, for the arc-flattening gate test.
+void pxo_libm_sincosf(const float* x, int64_t n, float* s, float* c) {
+  for (int64_t i = 0; i < n; i++) {
+    s[i] = sinf(x[i]);
+    c[i] = cosf(x[i]);
+  }
+}
+
+// The C library's atan2f and the shared float-float arctangent, element-wise
+// (for comparing the stroke joins' decisions under both).
+void pxo_atan2_pairs(const float* y, const float* x, int64_t n, float* libm, float* cr) {
+  for (int64_t i = 0; i < n; i++) {
+    libm[i] = atan2f(y[i], x[i]);
+    cr[i] = atan2_cr(y[i], x[i]);
+  }
+}
+
 // 1: the NEON line kernels of the timed CPU baseline (see nl::), 0: scalar.
 void pxo_set_simd_variant(int on) { g_simd_variant = on; }
 

@@ -69,6 +69,8 @@ def lib():
         L.pxo_set_golden_mode.argtypes = [I]
         L.pxo_set_row_window.argtypes = [I64, I64]
         L.pxo_set_simd_variant.argtypes = [I]
+        L.pxo_libm_sincosf.argtypes = [P, I64, P, P]
+        L.pxo_atan2_pairs.argtypes = [P, P, I64, P, P]
         _lib = L
     return _lib
 
@@ -297,6 +299,23 @@ def set_golden_mode(on: bool):
     """Golden-pinning only: reproduce the build that wrote the reference's
     master PNGs (floored coverage multiply, SSE2 sliver rounding)."""
     lib().pxo_set_golden_mode(1 if on else 0)
+
+
+def libm_sincosf(x):
+    """the C library's sinf and cosf of a float32 array"""
+    x = np.ascontiguousarray(x, np.float32)
+    s, c = np.empty_like(x), np.empty_like(x)
+    lib().pxo_libm_sincosf(_p(x), x.size, _p(s), _p(c))
+    return s, c
+
+
+def atan2_pairs(y, x):
+    """(the C library's atan2f, the shared float-float arctangent) of float32 arrays"""
+    y = np.ascontiguousarray(y, np.float32)
+    x = np.ascontiguousarray(x, np.float32)
+    a, b = np.empty_like(y), np.empty_like(y)
+    lib().pxo_atan2_pairs(_p(y), _p(x), y.size, _p(a), _p(b))
+    return a, b
 
 
 def set_simd_variant(on: bool):

@@ -64,13 +64,24 @@ __device__ __forceinline__ uint32_t nim_u32(float f) { return (uint32_t)(unsigne
 __device__ __forceinline__ float nmin(float x, float y) { return x <= y ? x : y; }
 __device__ __forceinline__ float nmax(float x, float y) { return y <= x ? x : y; }
 
-// `*`(ColorRGBX, uint8)  common.nim:79-90
+// Two channels per 32-bit word: bytes 0 and 2 (r, b) or, after >> 8, bytes 1
+// and 3 (g, a), each in its own 16-bit lane.  floor(x / 255) of both lanes at
+// once is (x + 1 + (x >> 8)) >> 8 -- exact for every 0 <= x <= 65534, checked
+// exhaustively -- and no lane carries into the other (x + 1 + 254 < 2^16).
+__device__ __forceinline__ uint32_t div255_lanes(uint32_t x) {
+  return ((x + 0x00010001u + ((x >> 8) & 0x00FF00FFu)) >> 8) & 0x00FF00FFu;
+}
+// floor(c * k / 255) of all four channels of c (k <= 255)
+__device__ __forceinline__ uint32_t mul_div255_px(uint32_t c, uint32_t k) {
+  return div255_lanes((c & 0x00FF00FFu) * k) | (div255_lanes(((c >> 8) & 0x00FF00FFu) * k) << 8);
+}
+
+// `*`(ColorRGBX, uint8)  common.nim:79-90: (c * k + 127) div 255 per channel
 __device__ __forceinline__ uint32_t mul_c(uint32_t c, uint32_t k) {
   if (k == 0) return 0u;
   if (k == 255) return c;
-  Px p = unpack(c);
-  return pack((p.r * k + 127) / 255, (p.g * k + 127) / 255, (p.b * k + 127) / 255,
-              (p.a * k + 127) / 255);
+  return div255_lanes((c & 0x00FF00FFu) * k + 0x007F007Fu) |
+         (div255_lanes(((c >> 8) & 0x00FF00FFu) * k + 0x007F007Fu) << 8);
 }
 // `*`(ColorRGBX, float32)  common.nim:67-77
 __device__ __forceinline__ uint32_t mul_f(uint32_t c, float opacity) {
@@ -92,19 +103,20 @@ __device__ __forceinline__ uint32_t hardLight1(uint32_t bc, uint32_t ba, uint32_
   return screen1(bc, sc);
 }
 
-__device__ __forceinline__ uint32_t blendNormal(uint32_t bv, uint32_t sv) {  // :60-70
-  uint32_t sa = sv >> 24, ba = bv >> 24;
+// blendNormal  blends.nim:60-70: source + backdrop * (255 - sa) div 255 on
+// every channel (blendAlpha is the same expression on alpha), uint8 wrap-around
+// on the sum; two channels per word (div255_lanes)
+__device__ __forceinline__ uint32_t blendNormal(uint32_t bv, uint32_t sv) {
+  const uint32_t sa = sv >> 24, ba = bv >> 24;
   if (ba == 0 || sa == 255) return sv;
   if (sa == 0) return bv;
-  Px b = unpack(bv), s = unpack(sv);
-  uint32_t k = 255 - sa;
-  return pack(s.r + (b.r * k) / 255, s.g + (b.g * k) / 255, s.b + (b.b * k) / 255,
-              blendAlpha(ba, sa));
+  const uint32_t k = 255 - sa;
+  const uint32_t rb = (div255_lanes((bv & 0x00FF00FFu) * k) + (sv & 0x00FF00FFu)) & 0x00FF00FFu;
+  const uint32_t ga = (div255_lanes(((bv >> 8) & 0x00FF00FFu) * k) + ((sv >> 8) & 0x00FF00FFu)) & 0x00FF00FFu;
+  return rb | (ga << 8);
 }
 __device__ __forceinline__ uint32_t blendMaskPx(uint32_t bv, uint32_t sv) {  // :227-232
-  uint32_t k = sv >> 24;
-  Px b = unpack(bv);
-  return pack((b.r * k) / 255, (b.g * k) / 255, (b.b * k) / 255, (b.a * k) / 255);
+  return mul_div255_px(bv, sv >> 24);
 }
 
 // The straight-alpha table (internal.nim:68-74), uploaded once per device:
@@ -126,62 +138,10 @@ __device__ __forceinline__ float small_to_f(uint32_t x) {  // exact for x < 2^23
   return __uint_as_float(0x4B000000u | x) - 8388608.0f;
 }
 
-// The straight-alpha table entry min(round(c * (255 / a)), 255), evaluated in
-// float64 by the reference, computed without the table.  For a > 0,
-// floor((510 c + a) / (2 a)) is c * 255 / a rounded half up, exactly; the
-// quotient comes from a float reciprocal with one exact remainder correction
-// (every operand is an integer below 2^24).  The float64 product differs from
-// that only at exact ties (c * 255 / a = k + 1/2) for the alphas whose float64
-// 255 / a lies below 255 / a -- 50 58 100 106 116 182 186 200 206 210 212 232
-// 234 242 (kTieAlpha) -- where the product can round below the tie; those few
-// channels take the reference's float64 expression itself.  All 65536
-// (a, c) pairs were checked against the table on the host.
-__device__ __forceinline__ bool tie_alpha(uint32_t a) {
-  const unsigned long long m = a < 128 ? (a < 64 ? 0x0404000000000000ull : 0x0010041000000000ull)
-                                       : (a < 192 ? 0x0440000000000000ull : 0x0004050000144100ull);
-  return (m >> (a & 63)) & 1ull;
-}
-struct AlphaDiv {  // per pixel: 2a as a float and its approximate reciprocal
-  float d, rd;
-  bool tie;
-};
-__device__ __forceinline__ AlphaDiv alpha_div(uint32_t a) {
-  AlphaDiv r;
-  r.d = small_to_f(2u * a);
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r.rd) : "f"(r.d));
-  r.tie = tie_alpha(a);
-  return r;
-}
-__device__ __forceinline__ uint32_t straight_ch(uint32_t c, uint32_t a, const AlphaDiv& ad) {
-  const float n = small_to_f(510u * c + a);
-  const float t = __fmaf_rd(n, ad.rd, 12582912.0f);
-  const float q = t - 12582912.0f;
-  float rem = fmaf(-q, ad.d, n);
-  uint32_t qi = __float_as_uint(t) - 0x4B400000u;
-  if (rem < 0.0f) {
-    qi -= 1u;
-    rem += ad.d;
-  } else if (rem >= ad.d) {
-    qi += 1u;
-    rem -= ad.d;
-  }
-  if (rem == 0.0f && ad.tie) qi = (uint32_t)round((double)c * (255.0 / (double)a));
-  return qi < 255u ? qi : 255u;
-}
-__device__ __forceinline__ Px straight8(const uint8_t* /*tbl*/, uint32_t v) {
+__device__ __forceinline__ Px straight8(const uint8_t* tbl, uint32_t v) {
   Px p = unpack(v);
-  if (p.a == 0) return Px{0u, 0u, 0u, 0u};
-  const AlphaDiv ad = alpha_div(p.a);
-  return Px{straight_ch(p.r, p.a, ad), straight_ch(p.g, p.a, ad), straight_ch(p.b, p.a, ad), p.a};
-}
-// v / 255.0f correctly rounded, for integers 0..255: the product with
-// float(1/255) plus one FMA remainder correction (exact for all 256 values).
-__device__ __forceinline__ float unit255(uint32_t v) {
-  const float r = 1.0f / 255.0f;
-  const float x = small_to_f(v);
-  const float q0 = x * r;
-  const float rem = fmaf(-q0, 255.0f, x);
-  return fmaf(rem, r, q0);
+  const uint8_t* row = tbl + p.a * 256;
+  return Px{row[p.r], row[p.g], row[p.b], p.a};
 }
 __device__ __forceinline__ uint32_t unit_to_u8(float c) {
   float v = roundf(c * 255.0f);
@@ -253,9 +213,10 @@ __device__ __forceinline__ uint32_t blendFloatT(const uint8_t* tbl, uint32_t bp,
 
 static __device__ __noinline__ uint32_t blendFloat(const uint8_t* tbl, uint32_t bp, uint32_t sp, int mode) {
   Px b8 = straight8(tbl, bp), s8 = straight8(tbl, sp);
-  F3 cb{unit255(b8.r), unit255(b8.g), unit255(b8.b)};
-  F3 cs{unit255(s8.r), unit255(s8.g), unit255(s8.b)};
-  float ab = unit255(b8.a), as = unit255(s8.a);
+  const float* u = reinterpret_cast<const float*>(tbl + kTblUnitOff);  // u[v] = v / 255.0f
+  F3 cb{u[b8.r], u[b8.g], u[b8.b]};
+  F3 cs{u[s8.r], u[s8.g], u[s8.b]};
+  float ab = u[b8.a], as = u[s8.a];
   F3 m;
   switch (mode) {
     case kSoftLight:
@@ -282,9 +243,10 @@ template <int MODE>
 __device__ __forceinline__ uint32_t blendFloatT(const uint8_t* tbl, uint32_t bp, uint32_t sp) {
   constexpr int mode = MODE;
   Px b8 = straight8(tbl, bp), s8 = straight8(tbl, sp);
-  F3 cb{unit255(b8.r), unit255(b8.g), unit255(b8.b)};
-  F3 cs{unit255(s8.r), unit255(s8.g), unit255(s8.b)};
-  float ab = unit255(b8.a), as = unit255(s8.a);
+  const float* u = reinterpret_cast<const float*>(tbl + kTblUnitOff);  // u[v] = v / 255.0f
+  F3 cb{u[b8.r], u[b8.g], u[b8.b]};
+  F3 cs{u[s8.r], u[s8.g], u[s8.b]};
+  float ab = u[b8.a], as = u[s8.a];
   F3 m;
   switch (mode) {
     case kSoftLight:
