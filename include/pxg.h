@@ -60,6 +60,9 @@ pxg_image* pxg_image_wrap(void* device_ptr, int64_t width, int64_t height);
 void pxg_image_free(pxg_image* image);
 int64_t pxg_image_width(const pxg_image* image);
 int64_t pxg_image_height(const pxg_image* image);
+/* The image's device address.  Once it has been handed out it stays fixed
+ * for the image's lifetime (a blur of radius 1..8 then runs in place instead
+ * of exchanging the image's buffer with the library's scratch buffer). */
 void* pxg_image_device_ptr(pxg_image* image);
 int pxg_image_upload(pxg_image* image, const void* host_rgbx, int64_t nbytes);
 int pxg_image_download(const pxg_image* image, void* host_rgbx, int64_t nbytes);
@@ -150,6 +153,19 @@ int pxg_image_fill_paint(pxg_image* image, const pxg_paint* paint);
  * (bindings/bindings.nim:133) */
 int pxg_image_blur(pxg_image* image, float radius, const float out_of_bounds[4]);
 
+/* Stroke outlines: 1 (default) builds the outline of a stroke without
+ * dashes on the GPU (strokeShapes, src/pixie/paths.nim:1922-2082: the host
+ * flattens the path into polylines, one kernel thread per polyline point
+ * writes its rectangle, join and caps); 0 builds every outline on the host.
+ * Both give the same bytes: a join whose angle lies within 1e-5 of one of the
+ * join's decision thresholds is rebuilt on the host with the C library's
+ * atan2f, as the reference computes it.  No counterpart in the reference. */
+int pxg_stroke_config(int gpu_outline);
+
+/* Joins the GPU outline found ambiguous and rebuilt on the host, since the
+ * library was loaded.  No counterpart in the reference. */
+int64_t pxg_stroke_fixups(void);
+
 /* Blur kernels: 3 (default) runs radii 1..8 on register-blocked CUDA-core
  * passes and radii 9..128 on the tensor cores with TMA-fed input rings in
  * tensor memory (images whose sides are multiples of 4; others take mode 1's
@@ -160,9 +176,12 @@ int pxg_image_blur(pxg_image* image, float radius, const float out_of_bounds[4])
  * counterpart in the reference. */
 int pxg_blur_config(int use_tensor_cores);
 
-/* The kernel family the last blur ran on: 4 (the small-radius passes of
- * mode 3), 3 (the ring passes), 2, 1 or 0 as above (-1 before any blur).
- * No counterpart in the reference. */
+/* The kernel family the last blur ran on: 5 (the fused one-launch kernel of
+ * mode 3 for radii 1..8, on images the library allocated whose device
+ * address was never handed out: the result lands in the library's scratch
+ * buffer and the two buffers change owners), 4 (the two small-radius passes
+ * of mode 3, in place), 3 (the ring passes), 2, 1 or 0 as above (-1 before
+ * any blur).  No counterpart in the reference. */
 int pxg_last_blur_kernel(void);
 
 /* spread(Image, float32)  src/pixie/images.nim:700-758 (private in the

@@ -154,6 +154,8 @@ def lib():
         L.pxg_server_stats.argtypes = [P, P]
         L.pxg_autotune.argtypes = [I]
         L.pxg_blur_config.argtypes = [I]
+        L.pxg_stroke_config.argtypes = [I]
+        L.pxg_stroke_fixups.restype = I64
         L.pxg_autotune_report.argtypes = [P, I64]
         L.pxg_autotune_report.restype = I64
         _lib = L
@@ -589,6 +591,17 @@ class Server:
 def scene_config(slice_width: int = 256, coverage_bytes: int = -1):
     """Scene drawing configuration (see pxg_scene_config)."""
     _check(lib().pxg_scene_config(int(slice_width), int(coverage_bytes)))
+
+
+def stroke_config(gpu_outline: bool):
+    """True (default): strokes without dashes are outlined on the GPU; False:
+    every outline is built on the host (see pxg_stroke_config)."""
+    _check(lib().pxg_stroke_config(1 if gpu_outline else 0))
+
+
+def stroke_fixups() -> int:
+    """Joins of GPU outlines rebuilt on the host since the library loaded."""
+    return int(lib().pxg_stroke_fixups())
 
 
 def blur_config(mode):

@@ -18,7 +18,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpxg.so")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_UNITS = ["raster.cu", "composite.cu", "filters.cu", "tcblur.cu", "ringblur.cu", "smallblur.cu", "smooth.cu", "paint.cu", "abi.cu", "noalloc.cu"]
+CUDA_UNITS = ["raster.cu", "composite.cu", "filters.cu", "tcblur.cu", "ringblur.cu", "smallblur.cu", "smooth.cu", "paint.cu", "stroke.cu", "abi.cu", "noalloc.cu"]
 HOST_UNITS = ["host_geom.cpp"]
 
 

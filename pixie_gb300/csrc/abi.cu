@@ -58,12 +58,19 @@ struct pxg_masks {
 struct pxg_scene {
   std::vector<pxg::Prim> prims;
   std::vector<pxg::PathJob> jobs;
-  // device copy of prims, uploaded at the first draw after a change
+  // strokes outlined on the GPU: their polylines (jobs with stroke_gpu index
+  // the outline primitives in dstroke)
+  pxg::StrokeGeom sk;
+  // device copy of prims, uploaded at the first draw after a change, and the
+  // outline primitives of sk, built there at the same time
   mutable pxg::Prim* dprims = nullptr;
   mutable long long dcap = 0;
+  mutable pxg::Prim* dstroke = nullptr;
+  mutable long long dscap = 0;
   mutable bool dirty = true;
   ~pxg_scene() {
     if (dprims) cudaFree(dprims);
+    if (dstroke) cudaFree(dstroke);
   }
 };
 
@@ -165,6 +172,8 @@ bool ring_blur_init(size_t* maxSmem);
 bool weights_exact_f16(const uint16_t* hostKern, int r);
 bool launch_blur_ring(uint32_t* img, uint32_t* tmp, long long W, long long H, int r, const uint16_t* kern,
                       bool exactF16, uint32_t oob, int nsm, size_t maxSmem, int* err, cudaStream_t st);
+void launch_stroke_outline(const float2* pts, const StrokeShape* shapes, int nshapes, long long nthreads, Prim* out,
+                           int2* amb, long long amb_cap, unsigned long long* amb_count, int nsm, cudaStream_t st);
 bool launch_blur_small_fused(const uint32_t* in, uint32_t* out, long long W, long long H, int r,
                              const uint16_t* kern, uint32_t oob, cudaStream_t st);
 bool launch_blur_small(uint32_t* img, uint32_t* tmp, long long W, long long H, int r, const uint16_t* kern,
@@ -288,6 +297,17 @@ struct Ctx {
   int rows_ctas_per_sm[2] = {1, 1};  // resident CTAs of each row-kernel variant
   int scene_ctas_per_sm[2] = {1, 1};  // resident CTAs of the scene recording and drawing kernels
   int scene_slice = 256;              // pixels of a row one warp of the drawing pass owns (0: chosen per launch)
+  bool stroke_gpu = true;             // outline strokes without dashes on the GPU (stroke.cu)
+  float2* sk_pts = nullptr;           // outline kernel inputs: polyline points, shapes
+  long long sk_pts_cap = 0;
+  StrokeShape* sk_shapes = nullptr;
+  long long sk_shapes_cap = 0;
+  int2* sk_amb = nullptr;             // joins the outline kernel found ambiguous
+  long long sk_amb_cap = 0;
+  unsigned long long* sk_ambn = nullptr;
+  Prim* sk_prims = nullptr;           // the outline of a single strokePath call
+  long long sk_prims_cap = 0;
+  long long sk_fixups = 0;            // ambiguous joins rebuilt on the host (all calls)
   bool blocking = true;  // image operations wait for their GPU work
   std::map<int64_t, uint16_t*> weights;  // gaussian weights per radius, on the device
   std::map<int64_t, bool> weights_f16;   // every weight of the radius is an exact f16
@@ -622,6 +642,7 @@ struct RunOpts {
   GraphCache* graph = nullptr;    // capture / replay the first launch
   float* rows_ms = nullptr;       // row-kernel time of the first launch (autotuning)
   const Prim* dprims = nullptr;   // primitives already on the device (else staged)
+  long long ndprims = -1;         // how many, when `prims` does not hold them (a GPU outline)
 };
 
 // Runs fill jobs whose primitives are already in `prims` (job.prim_off set).
@@ -634,7 +655,8 @@ void run_jobs(std::vector<PathJob>& jobs, const std::vector<Prim>& prims, std::v
   status.assign((size_t)nj, kOk);
   std::vector<int> todo(nj);
   for (int i = 0; i < nj; i++) todo[i] = i;
-  long long seg_need = std::max<long long>(1 << 16, (long long)prims.size() * 8);
+  const long long nprims = opts.dprims && opts.ndprims >= 0 ? opts.ndprims : (long long)prims.size();
+  long long seg_need = std::max<long long>(1 << 16, nprims * 8);
   long long list_need = seg_need * 4;
   for (int attempt = 0; attempt < 12 && !todo.empty(); attempt++) {
     std::vector<PathJob> run;
@@ -655,7 +677,7 @@ void run_jobs(std::vector<PathJob>& jobs, const std::vector<Prim>& prims, std::v
     }
     const int nr = (int)run.size();
     const int maxBands = setup_max_bands(maxH);
-    ensure_arena(seg_need, list_need, (long long)nr * maxBands, (long long)prims.size(), rows);
+    ensure_arena(seg_need, list_need, (long long)nr * maxBands, nprims, rows);
     const bool graphed = opts.graph && attempt == 0 && g.stream != nullptr;
     std::vector<long long> offs((size_t)nr);
     for (int r = 0; r < nr; r++) offs[(size_t)r] = run[(size_t)r].row_off;
@@ -723,7 +745,7 @@ void run_jobs(std::vector<PathJob>& jobs, const std::vector<Prim>& prims, std::v
     if (timeRows) CU(cudaEventElapsedTime(opts.rows_ms, g.evr0, g.evr1));
     unsigned long long ctr[kNumCounters];
     memcpy(ctr, g.h_up + S.jobsBytes, sizeof ctr);
-    note_stats(nr, (long long)prims.size(), ctr);
+    note_stats(nr, nprims, ctr);
     if (ctr[kCtrOvfRows] > 0 || ctr[kCtrXClears] > 0) {
       if ((long long)ctr[kCtrXClears] > A.xclear_cap) throw ApiError{"Out of workspace memory (cross-row clears)"};
       if (ctr[kCtrOvfRows] > 0) {
@@ -768,7 +790,69 @@ struct HostRun {
   const Prim* dprims;              // the same primitives on the device
   size_t j0, j1;               // paths still to paint
   int status;                  // first failure (kOk when every path was painted)
+  const Prim* dstroke = nullptr;   // GPU-outlined strokes' primitives (jobs with stroke_gpu)
 };
+
+// Lanes per curve of a path with `curves` curve primitives (curve_group).
+int group_for(long long curves) {
+  int gsz = 1;
+  while (gsz < 32 && curves * gsz * 2 <= 256) gsz *= 2;
+  return gsz;
+}
+
+// Builds the outline primitives of sg into dout (stroke.cu): uploads the
+// polylines, runs the outline kernel, then rebuilds on the host, with the C
+// library's atan2f, every join whose decision the kernel found ambiguous and
+// writes those slots over the kernel's.  Waits for the GPU.
+void outline_strokes(const StrokeGeom& sg, Prim* dout) {
+  if (sg.shapes.empty() || sg.nprims == 0) return;
+  const long long npts = (long long)sg.pts.size(), nsh = (long long)sg.shapes.size();
+  dev_grow(g.sk_pts, g.sk_pts_cap, npts);
+  dev_grow(g.sk_shapes, g.sk_shapes_cap, nsh);
+  dev_grow(g.sk_amb, g.sk_amb_cap, npts);
+  if (!g.sk_ambn) CU(cudaMalloc(&g.sk_ambn, sizeof(unsigned long long)));
+  CU(cudaMemcpyAsync(g.sk_pts, sg.pts.data(), sizeof(float2) * (size_t)npts, cudaMemcpyHostToDevice, g.stream));
+  CU(cudaMemcpyAsync(g.sk_shapes, sg.shapes.data(), sizeof(StrokeShape) * (size_t)nsh, cudaMemcpyHostToDevice,
+                     g.stream));
+  CU(cudaMemsetAsync(g.sk_ambn, 0, sizeof(unsigned long long), g.stream));
+  launch_stroke_outline(g.sk_pts, g.sk_shapes, (int)nsh, npts, dout, g.sk_amb, npts, g.sk_ambn, g.nsm, g.stream);
+  CU(cudaGetLastError());
+  unsigned long long namb = 0;
+  CU(cudaMemcpyAsync(&namb, g.sk_ambn, sizeof namb, cudaMemcpyDeviceToHost, g.stream));
+  CU(cudaStreamSynchronize(g.stream));
+  if (namb == 0) return;
+  const long long n = std::min<long long>((long long)namb, npts);
+  std::vector<int2> amb((size_t)n);
+  CU(cudaMemcpy(amb.data(), g.sk_amb, sizeof(int2) * (size_t)n, cudaMemcpyDeviceToHost));
+  std::vector<Prim> fix((size_t)n * 4);
+  for (long long k = 0; k < n; k++) {
+    const StrokeShape& sh = sg.shapes[(size_t)amb[(size_t)k].x];
+    const int i = amb[(size_t)k].y;
+    stroke_join_slot(sg, amb[(size_t)k].x, i, &fix[(size_t)k * 4]);
+    const long long at = sh.prim_off + kStrokeCapSlot + (long long)kStrokeSegSlot * (i - 1) + 4;
+    CU(cudaMemcpyAsync(dout + at, &fix[(size_t)k * 4], sizeof(Prim) * 4, cudaMemcpyHostToDevice, g.stream));
+  }
+  CU(cudaStreamSynchronize(g.stream));
+  g.sk_fixups += n;
+}
+
+// Appends a GPU-outlined stroke to a scene's stroke set: its shapes' point,
+// primitive and thread offsets move past the ones already there.  Returns the
+// stroke's first primitive in the scene's stroke region.
+long long append_stroke(StrokeGeom& dst, const StrokeGeom& src) {
+  const long long p0 = (long long)dst.pts.size(), prim0 = dst.nprims;
+  const long long t0 = dst.shapes.empty() ? 0 : dst.shapes.back().thr_off + dst.shapes.back().npts;
+  dst.pts.insert(dst.pts.end(), src.pts.begin(), src.pts.end());
+  for (StrokeShape sh : src.shapes) {
+    sh.pt_off += p0;
+    sh.prim_off += prim0;
+    sh.thr_off += t0;
+    dst.shapes.push_back(sh);
+  }
+  dst.nprims += src.nprims;
+  dst.ncurves += src.ncurves;
+  return prim0;
+}
 
 // The scene's primitives on the device, uploaded once after each change.
 const Prim* scene_device_prims(const pxg_scene* sc) {
@@ -776,6 +860,10 @@ const Prim* scene_device_prims(const pxg_scene* sc) {
     dev_grow(sc->dprims, sc->dcap, std::max<long long>((long long)sc->prims.size(), 1));
     if (!sc->prims.empty())
       CU(cudaMemcpy(sc->dprims, sc->prims.data(), sizeof(Prim) * sc->prims.size(), cudaMemcpyHostToDevice));
+    if (sc->sk.nprims > 0) {
+      dev_grow(sc->dstroke, sc->dscap, sc->sk.nprims);
+      outline_strokes(sc->sk, sc->dstroke);
+    }
     sc->dirty = false;
   }
   return sc->dprims;
@@ -834,7 +922,7 @@ void run_scene_runs(std::vector<HostRun>& runs) {
       for (size_t j = r.j0; j < r.j1; j++) {
         PathJob pj = (*r.jobs)[j];
         if (pj.group == 0) pj.group = curve_group(*r.prims, pj.prim_off, pj.nprims);
-        pj.prims = r.dprims;
+        pj.prims = pj.stroke_gpu ? r.dstroke : r.dprims;
         pj.pc_off = pc;
         pc += pj.nprims;
         pj.img = r.canvas->data;
@@ -1198,7 +1286,7 @@ void srv_step(pxg_server* sv) {
     if (e == j->next) continue;
     rowBudget -= (long long)(e - j->next) * j->H;
     runs.push_back(HostRun{&j->canvas, const_cast<std::vector<PathJob>*>(&pj), &j->scene->prims,
-                           scene_device_prims(j->scene), j->next, e, kOk});
+                           scene_device_prims(j->scene), j->next, e, kOk, j->scene->dstroke});
     owners.push_back(j);
     budget -= (long long)(e - j->next);
   }
@@ -1586,6 +1674,25 @@ int pxg_image_stroke_path(pxg_image* im, const float* cmds, int64_t n, const flo
     if (!paint_color(color, opacity, blend, rgbx)) return;
     const float* mat = transform ? transform : kIdent;
     float ps = pixel_scale(mat);
+    StrokeGeom sg;
+    if (g.stroke_gpu && build_stroke_geom(cmds, n, ps, width, cap, join, miterLimit, nd, sg) && sg.nprims > 0) {
+      if (sg.nprims > INT32_MAX) throw ApiError{"Path too complex"};
+      Timed t(true);
+      dev_grow(g.sk_prims, g.sk_prims_cap, sg.nprims);
+      outline_strokes(sg, g.sk_prims);
+      std::vector<PathJob> jobs(1, make_job(im, rgbx, blend, mat, ps, 0));
+      jobs[0].prim_off = 0;
+      jobs[0].nprims = (int)sg.nprims;
+      jobs[0].group = group_for(sg.ncurves);
+      RunOpts opts;
+      opts.dprims = g.sk_prims;
+      opts.ndprims = sg.nprims;
+      std::vector<int> st;
+      run_jobs(jobs, std::vector<Prim>(), st, opts);
+      t.done();
+      if (st[0] != kOk) throw ApiError{status_message(st[0])};
+      return;
+    }
     std::vector<Prim> prims;
     build_stroke_prims(cmds, n, ps, width, cap, join, miterLimit, dashes, nd, prims);
     run_single(im, prims, rgbx, blend, mat, ps, 0);
@@ -1666,6 +1773,7 @@ int pxg_scene_clear(pxg_scene* sc) {
   }
   sc->prims.clear();
   sc->jobs.clear();
+  sc->sk = StrokeGeom();
   sc->dirty = true;
   return 0;
 }
@@ -1708,9 +1816,22 @@ int pxg_scene_stroke_path(pxg_scene* sc, const float* cmds, int64_t n, const flo
     if (!paint_color(color, opacity, blend, rgbx)) return;
     const float* mat = transform ? transform : kIdent;
     float ps = pixel_scale(mat);
+    PathJob j = make_job(nullptr, rgbx, blend, mat, ps, 0);
+    thread_local StrokeGeom sg;
+    if (g.stroke_gpu && blend != kMask &&
+        build_stroke_geom(cmds, n, ps, width, cap, join, miterLimit, nd, sg) && sg.nprims > 0) {
+      // the outline is built on the GPU when the scene is next uploaded
+      if (sg.nprims > INT32_MAX) throw ApiError{"Path too complex"};
+      j.stroke_gpu = 1;
+      j.nprims = (int)sg.nprims;
+      j.group = group_for(sg.ncurves);
+      j.prim_off = append_stroke(sc->sk, sg);
+      sc->jobs.push_back(j);
+      sc->dirty = true;
+      return;
+    }
     thread_local std::vector<Prim> prims;  // keeps its capacity between recordings
     build_stroke_prims(cmds, n, ps, width, cap, join, miterLimit, dashes, nd, prims);
-    PathJob j = make_job(nullptr, rgbx, blend, mat, ps, 0);
     j.prim_off = (long long)sc->prims.size();
     j.nprims = (int)prims.size();
     j.group = curve_group(prims, 0, j.nprims);
@@ -1735,10 +1856,12 @@ int pxg_scene_record_batch(pxg_scene* sc, int64_t n, const int32_t* kinds, const
       throw ApiError{"Invalid batch"};
     struct Rec {
       std::vector<Prim> prims;
+      StrokeGeom sg;  // a stroke outlined on the GPU (job.stroke_gpu)
       PathJob job;
       int state = 0;  // 0 nothing to draw, 1 recorded, 2 failed
       std::string err;
     };
+    const bool strokeGpu = g.stroke_gpu;
     std::vector<Rec> rec((size_t)n);
     auto build = [&](int64_t i) {
       Rec& r = rec[(size_t)i];
@@ -1760,6 +1883,16 @@ int pxg_scene_record_batch(pxg_scene* sc, int64_t n, const int32_t* kinds, const
           build_fill_prims(cmds + a, b - a, ps, r.prims);
         } else {
           if (!widths || !caps || !joins || !miters) throw ApiError{"Invalid batch"};
+          if (strokeGpu && blend != kMask &&
+              build_stroke_geom(cmds + a, b - a, ps, widths[i], caps[i], joins[i], miters[i], 0, r.sg) &&
+              r.sg.nprims > 0) {
+            if (r.sg.nprims > INT32_MAX) throw ApiError{"Path too complex"};
+            r.job = make_job(nullptr, rgbx, blend, mat, ps, 0);
+            r.job.stroke_gpu = 1;
+            r.state = 1;
+            return;
+          }
+          r.sg.shapes.clear();
           build_stroke_prims(cmds + a, b - a, ps, widths[i], caps[i], joins[i], miters[i], nullptr, 0, r.prims);
         }
         r.job = make_job(nullptr, rgbx, blend, mat, ps, winding);
@@ -1795,10 +1928,16 @@ int pxg_scene_record_batch(pxg_scene* sc, int64_t n, const int32_t* kinds, const
       if (status) status[i] = r.state == 2 ? 1 : 0;
       if (r.state == 2 && firstErr.empty()) firstErr = r.err;
       if (r.state != 1) continue;
-      r.job.prim_off = (long long)sc->prims.size();
-      r.job.nprims = (int)r.prims.size();
-      r.job.group = curve_group(r.prims, 0, r.job.nprims);
-      sc->prims.insert(sc->prims.end(), r.prims.begin(), r.prims.end());
+      if (r.job.stroke_gpu) {
+        r.job.nprims = (int)r.sg.nprims;
+        r.job.group = group_for(r.sg.ncurves);
+        r.job.prim_off = append_stroke(sc->sk, r.sg);
+      } else {
+        r.job.prim_off = (long long)sc->prims.size();
+        r.job.nprims = (int)r.prims.size();
+        r.job.group = curve_group(r.prims, 0, r.job.nprims);
+        sc->prims.insert(sc->prims.end(), r.prims.begin(), r.prims.end());
+      }
       sc->jobs.push_back(r.job);
       sc->dirty = true;
     }
@@ -1833,7 +1972,7 @@ int pxg_image_draw_scene(pxg_image* im, const pxg_scene* sc) {
       size_t e = i;
       while (e < jobs.size() && jobs[e].mode != kMask) e++;
       std::vector<HostRun> runs(1);
-      runs[0] = HostRun{im, &jobs, &sc->prims, dp, i, e, kOk};
+      runs[0] = HostRun{im, &jobs, &sc->prims, dp, i, e, kOk, sc->dstroke};
       run_scene_runs(runs);
       if (runs[0].status != kOk) throw ApiError{status_message(runs[0].status)};
       i = e;
@@ -2162,6 +2301,18 @@ int pxg_scene_config(int slice_width, int64_t coverage_bytes) {
       g.cov8_cap = coverage_bytes;
     }
   });
+}
+
+int pxg_stroke_config(int gpu_outline) {
+  return guarded([&] {
+    if (gpu_outline != 0 && gpu_outline != 1) throw ApiError{"Invalid stroke configuration"};
+    g.stroke_gpu = gpu_outline != 0;
+  });
+}
+
+int64_t pxg_stroke_fixups(void) {
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  return g.sk_fixups;
 }
 
 int pxg_blur_config(int use_tensor_cores) {

@@ -421,7 +421,135 @@ void build_fill_prims(const float* cmds, int64_t n, float ps, std::vector<Prim>&
   walk_commands(cmds, n, true, error_margin_sq(ps), &out);
 }
 
-// strokeShapes  paths.nim:1922-2082
+// ---- strokeShapes  paths.nim:1922-2082 ----------------------------------
+namespace {
+enum { kButt = 0, kRoundC = 1, kSquare = 2 };
+enum { kMiterJ = 0, kRoundJ = 1, kBevelJ = 2 };
+
+struct StrokeCfg {
+  float hs, miterAngle, minArea;
+  int cap, join;
+};
+// One outline shape in the reference's order: a polygon of at most 5 points,
+// or a circle at c.  Round joins and caps are circles: pixie flattens
+// ellipse(c, hs, hs) (:604-616, :1938-1941) with the same error margin, so
+// they go to the GPU as their four cubics and are flattened there; the other
+// shapes are polygons of lines.
+struct OutShape {
+  P2 p[5];
+  int n;
+  bool circ;
+  P2 c;
+};
+OutShape poly_shape(std::initializer_list<P2> pts) {
+  OutShape o;
+  o.n = 0;
+  for (P2 q : pts) o.p[o.n++] = q;
+  o.circ = false;
+  o.c = P2{0, 0};
+  return o;
+}
+OutShape circle_shape(P2 c) {
+  OutShape o;
+  o.n = 0;
+  o.circ = true;
+  o.c = c;
+  return o;
+}
+// The commands of ellipse(c, hs, hs) are Move + 4 cubics + Close, a closed
+// arc-free subpath: the command walk turns them into exactly these four cubic
+// primitives (the last cubic ends on the start point, so no closing line).
+void circle_prims(P2 c, float hs, Prim* out4) {
+  const double mx = kCircleK * (double)hs, my = kCircleK * (double)hs;
+  const float cx = c.x, cy = c.y;
+  const float q[4][8] = {
+      {cx + hs, cy, cx + hs, (float)(cy + my), (float)(cx + mx), cy + hs, cx, cy + hs},
+      {cx, cy + hs, (float)(cx - mx), cy + hs, cx - hs, (float)(cy + my), cx - hs, cy},
+      {cx - hs, cy, cx - hs, (float)(cy - my), (float)(cx - mx), cy - hs, cx, cy - hs},
+      {cx, cy - hs, (float)(cx + mx), cy - hs, cx + hs, (float)(cy - my), cx + hs, cy}};
+  for (int k = 0; k < 4; k++) {
+    Prim p;
+    memset(&p, 0, sizeof p);
+    p.kind = kPrimCubic;
+    for (int i = 0; i < 4; i++) {
+      p.x[i] = q[k][2 * i];
+      p.y[i] = q[k][2 * i + 1];
+    }
+    out4[k] = p;
+  }
+}
+OutShape rect_shape(P2 a, P2 b, float hs) {  // :1943-1965
+  P2 t = unit(sub(b, a));
+  P2 nrm{t.y, t.x};
+  P2 p0{a.x + nrm.x * hs, a.y - nrm.y * hs}, p1{b.x + nrm.x * hs, b.y - nrm.y * hs};
+  P2 p2{b.x - nrm.x * hs, b.y + nrm.y * hs}, p3{a.x - nrm.x * hs, a.y + nrm.y * hs};
+  return poly_shape({p0, p1, p2, p3, p0});
+}
+float fix_angle(float a) {
+  const float tau = (float)(kPI * 2);
+  while ((double)a > kPI) a -= tau;
+  while ((double)a < -kPI) a += tau;
+  return a;
+}
+// addJoin  :1967-2013; true when a shape was added
+bool join_shape(OutShape& o, P2 prevPos, P2 pos, P2 nextPos, const StrokeCfg& c) {
+  if (c.join == kRoundJ) {
+    float area = (float)kPI * c.hs * c.hs;
+    if (area > c.minArea) {
+      o = circle_shape(pos);
+      return true;
+    }
+    return false;
+  }
+  P2 vn = sub(nextPos, pos), vp = sub(prevPos, pos);
+  float ang = fix_angle(atan2f(vn.y, vn.x) - atan2f(vp.y, vp.x));
+  if (fabs((double)fabsf(ang) - kPI) > (double)kEps) {
+    P2 a = scl(unit(sub(pos, prevPos)), c.hs), b = scl(unit(sub(pos, nextPos)), c.hs);
+    if (ang >= 0) {
+      a = P2{-a.y, a.x};
+      b = P2{b.y, -b.x};
+    } else {
+      a = P2{a.y, -a.x};
+      b = P2{-b.y, b.x};
+    }
+    int lj = c.join;
+    if (lj == kMiterJ && fabsf(ang) < c.miterAngle) lj = kBevelJ;
+    if (lj == kMiterJ) {
+      // line(prevPos + a, pos + a) x line(nextPos + b, pos + b)
+      P2 a0 = add(prevPos, a), a1 = add(pos, a), b0 = add(nextPos, b), b1 = add(pos, b);
+      P2 s1 = sub(a1, a0), s2 = sub(b1, b0);
+      float den = (-s2.x * s1.y + s1.x * s2.y);
+      if (den != 0) {
+        float t = (s2.x * (a0.y - b0.y) - s2.y * (a0.x - b0.x)) / den;
+        P2 at = add(a0, scl(s1, t));
+        float bls = len2(sub(at, pos));
+        float areaSq = 0.25f * (len2(a) * bls + len2(b) * bls);
+        if (areaSq > (c.minArea * c.minArea)) {
+          o = poly_shape({add(pos, a), at, add(pos, b), pos, add(pos, a)});
+          return true;
+        }
+      }
+    } else if (lj == kBevelJ) {
+      float areaSq = 0.25f * len2(a) * len2(b);
+      if (areaSq > (c.minArea * c.minArea)) {
+        o = poly_shape({add(a, pos), add(b, pos), pos, add(a, pos)});
+        return true;
+      }
+    }
+  }
+  return false;
+}
+StrokeCfg stroke_cfg(float ps, float strokeWidth, int lineCap, int lineJoin, float miterLimit) {
+  StrokeCfg c;
+  c.hs = strokeWidth / 2;
+  c.miterAngle = asinf(1 / miterLimit) * 2;
+  c.minArea = kMargin / ps;
+  c.cap = lineCap;
+  c.join = lineJoin;
+  return c;
+}
+}  // namespace
+
 void build_stroke_prims(const float* cmds, int64_t n, float ps, float strokeWidth, int lineCap,
                         int lineJoin, float miterLimit, const float* dashesIn, int64_t nd,
                         std::vector<Prim>& out) {
@@ -430,113 +558,12 @@ void build_stroke_prims(const float* cmds, int64_t n, float ps, float strokeWidt
   const float ems = error_margin_sq(ps);
   std::vector<Poly> shapes = walk_commands(cmds, n, false, ems, nullptr);
   if (strokeWidth <= 0) return;
-  const float hs = strokeWidth / 2;
-  const float miterAngle = asinf(1 / miterLimit) * 2;
-  const float minArea = kMargin / ps;
-  enum { Butt = 0, RoundC = 1, Square = 2 };
-  enum { Miter = 0, RoundJ = 1, Bevel = 2 };
-
-  // Outline shapes in the reference's order.  Round joins and caps are
-  // circles: pixie flattens ellipse(c, hs, hs) (:604-616, :1938-1941) with the
-  // same error margin, so they go to the GPU as their four cubics and are
-  // flattened there; the other shapes are polygons of lines.
-  struct OutShape {  // a polygon of at most 5 points, or a circle at c
-    P2 p[5];
-    int n;
-    bool circ;
-    P2 c;
+  const StrokeCfg cfg = stroke_cfg(ps, strokeWidth, lineCap, lineJoin, miterLimit);
+  const float hs = cfg.hs;
+  auto join = [&](std::vector<OutShape>& o, P2 prevPos, P2 pos, P2 nextPos) {
+    OutShape sh;
+    if (join_shape(sh, prevPos, pos, nextPos, cfg)) o.push_back(sh);
   };
-  auto poly5 = [](std::initializer_list<P2> pts) {
-    OutShape o;
-    o.n = 0;
-    for (P2 q : pts) o.p[o.n++] = q;
-    o.circ = false;
-    o.c = P2{0, 0};
-    return o;
-  };
-  auto circle = [&](P2 c) {
-    OutShape o;
-    o.n = 0;
-    o.circ = true;
-    o.c = c;
-    return o;
-  };
-  // The commands of ellipse(c, hs, hs) are Move + 4 cubics + Close, a closed
-  // arc-free subpath: the command walk turns them into exactly these four
-  // cubic primitives (the last cubic ends on the start point, so no closing
-  // line), built here directly.
-  auto emit_circle = [&](P2 c) {
-    const double mx = kCircleK * (double)hs, my = kCircleK * (double)hs;
-    const float cx = c.x, cy = c.y;
-    const float q[4][8] = {
-        {cx + hs, cy, cx + hs, (float)(cy + my), (float)(cx + mx), cy + hs, cx, cy + hs},
-        {cx, cy + hs, (float)(cx - mx), cy + hs, cx - hs, (float)(cy + my), cx - hs, cy},
-        {cx - hs, cy, cx - hs, (float)(cy - my), (float)(cx - mx), cy - hs, cx, cy - hs},
-        {cx, cy - hs, (float)(cx + mx), cy - hs, cx + hs, (float)(cy - my), cx + hs, cy}};
-    for (int k = 0; k < 4; k++) {
-      Prim p;
-      memset(&p, 0, sizeof p);
-      p.kind = kPrimCubic;
-      for (int i = 0; i < 4; i++) {
-        p.x[i] = q[k][2 * i];
-        p.y[i] = q[k][2 * i + 1];
-      }
-      out.push_back(p);
-    }
-  };
-  auto rect = [&](P2 a, P2 b) {  // :1943-1965
-    P2 t = unit(sub(b, a));
-    P2 nrm{t.y, t.x};
-    P2 p0{a.x + nrm.x * hs, a.y - nrm.y * hs}, p1{b.x + nrm.x * hs, b.y - nrm.y * hs};
-    P2 p2{b.x - nrm.x * hs, b.y + nrm.y * hs}, p3{a.x - nrm.x * hs, a.y + nrm.y * hs};
-    return poly5({p0, p1, p2, p3, p0});
-  };
-  auto fixAngle = [](float a) {
-    const float tau = (float)(kPI * 2);
-    while ((double)a > kPI) a -= tau;
-    while ((double)a < -kPI) a += tau;
-    return a;
-  };
-  auto join = [&](std::vector<OutShape>& o, P2 prevPos, P2 pos, P2 nextPos) {  // :1967-2013
-    if (lineJoin == RoundJ) {
-      float area = (float)kPI * hs * hs;
-      if (area > minArea) o.push_back(circle(pos));
-      return;
-    }
-    P2 vn = sub(nextPos, pos), vp = sub(prevPos, pos);
-    float ang = fixAngle(atan2f(vn.y, vn.x) - atan2f(vp.y, vp.x));
-    if (fabs((double)fabsf(ang) - kPI) > (double)kEps) {
-      P2 a = scl(unit(sub(pos, prevPos)), hs), b = scl(unit(sub(pos, nextPos)), hs);
-      if (ang >= 0) {
-        a = P2{-a.y, a.x};
-        b = P2{b.y, -b.x};
-      } else {
-        a = P2{a.y, -a.x};
-        b = P2{-b.y, b.x};
-      }
-      int lj = lineJoin;
-      if (lj == Miter && fabsf(ang) < miterAngle) lj = Bevel;
-      if (lj == Miter) {
-        // line(prevPos + a, pos + a) x line(nextPos + b, pos + b)
-        P2 a0 = add(prevPos, a), a1 = add(pos, a), b0 = add(nextPos, b), b1 = add(pos, b);
-        P2 s1 = sub(a1, a0), s2 = sub(b1, b0);
-        float den = (-s2.x * s1.y + s1.x * s2.y);
-        if (den != 0) {
-          float t = (s2.x * (a0.y - b0.y) - s2.y * (a0.x - b0.x)) / den;
-          P2 at = add(a0, scl(s1, t));
-          float bls = len2(sub(at, pos));
-          float areaSq = 0.25f * (len2(a) * bls + len2(b) * bls);
-          if (areaSq > (minArea * minArea))
-            o.push_back(poly5({add(pos, a), at, add(pos, b), pos, add(pos, a)}));
-        }
-      } else if (lj == Bevel) {
-        float areaSq = 0.25f * len2(a) * len2(b);
-        if (areaSq > (minArea * minArea))
-          o.push_back(poly5({add(a, pos), add(b, pos), pos, add(a, pos)}));
-      }
-    }
-  };
-
   std::vector<float> dashes(dashesIn, dashesIn + nd);
   if (dashes.size() % 2 != 0) {
     std::vector<float> d2 = dashes;
@@ -552,10 +579,10 @@ void build_stroke_prims(const float* cmds, int64_t n, float ps, float strokeWidt
     std::vector<OutShape>& st = outline;
     const bool open = !eq(s[0], s.back());
     if (open) {
-      if (lineCap == RoundC) st.push_back(circle(s[0]));
-      else if (lineCap == Square) {
+      if (lineCap == kRoundC) st.push_back(circle_shape(s[0]));
+      else if (lineCap == kSquare) {
         P2 t = unit(sub(s[1], s[0]));
-        st.push_back(rect(sub(s[0], scl(t, hs)), s[0]));
+        st.push_back(rect_shape(sub(s[0], scl(t, hs)), s[0], hs));
       }
     }
     for (float d : dashes)
@@ -570,7 +597,7 @@ void build_stroke_prims(const float* cmds, int64_t n, float ps, float strokeWidt
         while (!done) {
           for (size_t j = 0; j < dashes.size(); j++) {
             float d = dashes[j];
-            if (j % 2 == 0) st.push_back(rect(cur, add(cur, scl(dir, fmin_n(dist, d)))));
+            if (j % 2 == 0) st.push_back(rect_shape(cur, add(cur, scl(dir, fmin_n(dist, d))), hs));
             cur = add(cur, scl(dir, d));
             dist -= d;
             if (dist <= 0) {
@@ -580,29 +607,104 @@ void build_stroke_prims(const float* cmds, int64_t n, float ps, float strokeWidt
           }
         }
       } else {
-        st.push_back(rect(prevPos, pos));
+        st.push_back(rect_shape(prevPos, pos, hs));
       }
       if (i < s.size() - 1) join(st, prevPos, pos, s[i + 1]);
     }
     if (!open) {
       join(st, s[s.size() - 2], s.back(), s[1]);
-    } else if (lineCap == RoundC) {
-      st.push_back(circle(s.back()));
-    } else if (lineCap == Square) {
+    } else if (lineCap == kRoundC) {
+      st.push_back(circle_shape(s.back()));
+    } else if (lineCap == kSquare) {
       P2 t = unit(sub(s.back(), s[s.size() - 2]));
-      st.push_back(rect(add(s.back(), scl(t, hs)), s.back()));
+      st.push_back(rect_shape(add(s.back(), scl(t, hs)), s.back(), hs));
     }
   }
   out.reserve(out.size() + outline.size() * 5);
   for (const OutShape& o : outline) {
     if (o.circ) {
-      emit_circle(o.c);
+      Prim c4[4];
+      circle_prims(o.c, hs, c4);
+      out.insert(out.end(), c4, c4 + 4);
     } else if (o.n > 0) {  // emit_polygon_lines on the inline points
       if (!eq(o.p[o.n - 1], o.p[0])) out.push_back(line_prim(o.p[o.n - 1], o.p[0]));
       for (int i = 0; i + 1 < o.n; i++)
         if (!eq(o.p[i], o.p[i + 1])) out.push_back(line_prim(o.p[i], o.p[i + 1]));
     }
   }
+}
+
+// The polylines and per-shape parameters of a stroke for the GPU outline
+// (stroke.cu); false when the stroke needs the host outline (dashes, or a
+// polyline of fewer than two points).
+bool build_stroke_geom(const float* cmds, int64_t n, float ps, float strokeWidth, int lineCap, int lineJoin,
+                       float miterLimit, int64_t nDashes, StrokeGeom& out) {
+  validate_commands(cmds, n);
+  out.pts.clear();
+  out.shapes.clear();
+  out.nprims = 0;
+  out.ncurves = 0;
+  if (nDashes > 0) return false;
+  const float ems = error_margin_sq(ps);
+  std::vector<Poly> shapes = walk_commands(cmds, n, false, ems, nullptr);
+  if (strokeWidth <= 0) return true;  // nothing to draw
+  for (const Poly& s : shapes)
+    if (s.size() < 2) return false;
+  const StrokeCfg cfg = stroke_cfg(ps, strokeWidth, lineCap, lineJoin, miterLimit);
+  const bool roundJoin = lineJoin == kRoundJ && (float)kPI * cfg.hs * cfg.hs > cfg.minArea;
+  long long thr = 0;
+  for (const Poly& s : shapes) {
+    StrokeShape sh;
+    memset(&sh, 0, sizeof sh);
+    sh.pt_off = (long long)out.pts.size();
+    sh.prim_off = out.nprims;
+    sh.thr_off = thr;
+    sh.npts = (int)s.size();
+    sh.closed = eq(s[0], s.back()) ? 1 : 0;
+    sh.hs = cfg.hs;
+    sh.miterAngle = cfg.miterAngle;
+    sh.minArea = cfg.minArea;
+    sh.cap = lineCap;
+    sh.join = lineJoin;
+    sh.roundJoin = roundJoin ? 1 : 0;
+    for (const P2& q : s) out.pts.push_back(float2{q.x, q.y});
+    out.nprims += kStrokeCapSlot + (long long)kStrokeSegSlot * (sh.npts - 1);
+    thr += sh.npts;
+    const long long joins = sh.npts - 2 + (sh.closed ? 1 : 0);
+    const long long caps = sh.closed ? 0 : 2;
+    out.ncurves += 4 * ((roundJoin ? joins : 0) + (lineCap == kRoundC ? caps : 0));
+    out.shapes.push_back(sh);
+  }
+  return true;
+}
+
+// The slot of the join at point i of a GPU-outlined shape (or, after its last
+// segment, the closing join), rebuilt with the C library's atan2f, in the
+// GPU outline's slot form (stroke.cu): a circle's four cubics, a polygon's
+// edges in order (zero-length ones kept) padded with zero-length lines, or
+// four zero-length lines.
+void stroke_join_slot(const StrokeGeom& g, int shape, int i, Prim* out4) {
+  const StrokeShape& sh = g.shapes[(size_t)shape];
+  const float2* q = g.pts.data() + sh.pt_off;
+  auto P = [&](int k) { return P2{q[k].x, q[k].y}; };
+  StrokeCfg cfg;
+  cfg.hs = sh.hs;
+  cfg.miterAngle = sh.miterAngle;
+  cfg.minArea = sh.minArea;
+  cfg.cap = sh.cap;
+  cfg.join = sh.join;
+  const int n = sh.npts;
+  OutShape o;
+  const bool any =
+      i < n - 1 ? join_shape(o, P(i - 1), P(i), P(i + 1), cfg) : join_shape(o, P(n - 2), P(n - 1), P(1), cfg);
+  if (any && o.circ) {
+    circle_prims(o.c, sh.hs, out4);
+    return;
+  }
+  int k = 0;
+  if (any)
+    for (int j = 0; j + 1 < o.n; j++) out4[k++] = line_prim(o.p[j], o.p[j + 1]);
+  for (; k < 4; k++) out4[k] = line_prim(P2{0, 0}, P2{0, 0});
 }
 
 float pixel_scale(const float* m) {  // paths.nim:61-66

@@ -27,6 +27,22 @@ void build_fill_prims(const float* cmds, int64_t n, float pixelScale, std::vecto
 void build_stroke_prims(const float* cmds, int64_t n, float pixelScale, float strokeWidth,
                         int lineCap, int lineJoin, float miterLimit, const float* dashes,
                         int64_t nDashes, std::vector<Prim>& out);
+// A stroke prepared for the GPU outline (stroke.cu): its polylines' points
+// back to back, one StrokeShape per polyline (slot offsets relative to the
+// stroke's first primitive), the primitive count and how many are cubics.
+struct StrokeGeom {
+  std::vector<float2> pts;
+  std::vector<StrokeShape> shapes;
+  long long nprims = 0;
+  long long ncurves = 0;
+};
+// Builds the polylines of strokePath for the GPU outline; false when the stroke
+// needs the host outline (dashes, degenerate polylines).  Throws GeomError.
+bool build_stroke_geom(const float* cmds, int64_t n, float pixelScale, float strokeWidth, int lineCap,
+                       int lineJoin, float miterLimit, int64_t nDashes, StrokeGeom& out);
+// The join slot (4 primitives) of point i of shape `shape`, with the C
+// library's atan2f: the fix-up of a join the GPU found ambiguous.
+void stroke_join_slot(const StrokeGeom& g, int shape, int i, Prim* out4);
 // Validates the command stream (kinds, parameter counts, finiteness).
 void validate_commands(const float* cmds, int64_t n);
 

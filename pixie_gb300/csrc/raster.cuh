@@ -62,12 +62,32 @@ struct PathJob {
   long long row_off;  // prefix of row-kernel work items over the batch
   long long ri_off;     // scenes: row y of the job is Arena::rowidx[ri_off + y * ri_stride]
   long long ri_stride;
+  int stroke_gpu;       // host: the primitives are a GPU-outlined stroke (scene: in its stroke region)
+  int pad_;
   // outputs (setup kernel)
   int status, nseg, nb;
   uint32_t ph;
   long long seg_off, band_off;
   long long startX, startY, pathWidth, pathHeight;
 };
+
+// One polyline of a stroked path outlined on the GPU (strokeShapes,
+// paths.nim:1922-2082, without dashes).  Its outline occupies a fixed slot of
+// primitives: 4 for the start cap, then 8 per segment (its rectangle, then
+// the join at its end point -- or, after the last segment, the closing join
+// or the end cap).  Polygons become their edges in the reference's order;
+// edges of zero length and unused slots are zero-length lines, which the
+// setup kernel drops as horizontal, as shapesToSegments drops them.
+struct StrokeShape {
+  long long pt_off;    // first point of the polyline
+  long long prim_off;  // first primitive of its slot
+  long long thr_off;   // first thread of the outline kernel (exclusive prefix of npts)
+  int npts, closed;    // npts >= 2; closed: first point == last point
+  float hs, miterAngle, minArea;  // strokeWidth / 2, miterLimitToAngle(miterLimit), pixelErrorMargin / pixelScale
+  int cap, join, roundJoin;       // LineCap, LineJoin; roundJoin: pi * hs^2 > minArea (the circle is drawn)
+};
+// Slot offset of point i of a shape: the start cap at 0, segment i at 4 + 8 (i - 1).
+constexpr int kStrokeCapSlot = 4, kStrokeSegSlot = 8;
 
 // Paths [j0, j1) of the job array painted in order onto one canvas (the
 // jobs' img/W/H).  A launch may carry several runs on distinct canvases.

@@ -123,3 +123,16 @@ def test_served_jobs_at_serving_scale():
         if j["blur"]:
             pxo.blur(ref, j["blur"])
         assert_same(out[k], ref, f"served job {k} ({j['side']}^2, {len(j['items'])} paths, blur {j['blur']})")
+
+
+def test_dense_scene_full_size():
+    """The dense-scene workload at its full size: 2000 mixed paths (30 %
+    stroked, outlined on the GPU) painted in order onto 1024x1024."""
+    items = wl.dense_scene(7, n_paths=2000, size=1024.0)
+    sc, failed = _record(items)
+    img = px.Image(1024, 1024)
+    img.draw_scene(sc)
+    ref = pxo.new_image(1024, 1024)
+    skipped = pxo.draw_items(ref, items, THREADS)
+    assert skipped == failed
+    assert_same(img.to_numpy(), ref, "dense scene 1024^2, 2000 paths")
