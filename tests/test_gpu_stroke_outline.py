@@ -79,16 +79,18 @@ def polyline(points, closed=False):
     return np.asarray(c, np.float32)
 
 
-def turn_path(turns, start=(350.0, 350.0), seg=3.0):
-    """a polyline whose consecutive segments turn by the given angles"""
-    pts = [start]
-    heading = 0.0
-    x, y = start
-    for t in [0.0] + list(turns):
-        heading += t
-        x, y = x + seg * math.cos(heading), y + seg * math.sin(heading)
-        pts.append((float(np.float32(x)), float(np.float32(y))))
-    return pts
+def turn_subpaths(turns, side=700, arm=12.0):
+    """one open three-point subpath per turn, on a grid: the segments meet at
+    the grid point and the second turns by the given angle"""
+    cols = int(math.ceil(math.sqrt(len(turns))))
+    step = (side - 4 * arm) / cols
+    c = []
+    for k, t in enumerate(turns):
+        cx, cy = 2 * arm + step * (k % cols), 2 * arm + step * (k // cols)
+        pts = [(cx - arm, cy), (cx, cy), (cx + arm * math.cos(t), cy + arm * math.sin(t))]
+        pts = [(float(np.float32(x)), float(np.float32(y))) for x, y in pts]
+        c += [1.0, pts[0][0], pts[0][1], 2.0, pts[1][0], pts[1][1], 2.0, pts[2][0], pts[2][1]]
+    return np.asarray(c, np.float32)
 
 
 @pytest.mark.parametrize("join", [0, 2])
@@ -101,7 +103,7 @@ def test_joins_at_the_decision_thresholds(join):
     for k in range(-40, 41):
         d = k * 2.5e-7
         turns += [EPS + d, -(EPS + d), PI - miter_angle + d, -(PI - miter_angle + d), PI - 1e-6 + d]
-    cmds = polyline(turn_path(turns))
+    cmds = turn_subpaths(turns)
     before = px.stroke_fixups()
     gpu, host, ref = stroke_both(cmds, 700, 700, [0.2, 0.6, 0.9, 0.8], 2.5, 0, join)
     assert px.stroke_fixups() > before  # the ambiguous joins went through the host
