@@ -168,53 +168,87 @@ __device__ bool put_join(Prim* o, P2 prevPos, P2 pos, P2 nextPos, const StrokeSh
   return amb;
 }
 
-__global__ void __launch_bounds__(256) k_stroke_outline(const float2* __restrict__ pts,
-                                                        const StrokeShape* __restrict__ shapes, int nshapes,
-                                                        long long nthreads, Prim* __restrict__ out, int2* amb,
-                                                        long long amb_cap, unsigned long long* amb_count) {
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < nthreads;
-       t += (long long)gridDim.x * blockDim.x) {
-    int lo = 0, hi = nshapes - 1;  // the last shape whose first thread is <= t
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (shapes[mid].thr_off <= t) lo = mid;
-      else hi = mid - 1;
-    }
-    const StrokeShape S = shapes[lo];
-    const int i = (int)(t - S.thr_off), n = S.npts;
-    const float2* q = pts + S.pt_off;
-    auto P = [&](int k) { return P2{q[k].x, q[k].y}; };
-    if (i == 0) {  // start cap (open polylines)
-      Prim* o = out + S.prim_off;
-      if (!S.closed && S.cap == kRoundCap) {
-        put_circle(o, P(0), S.hs);
-      } else if (!S.closed && S.cap == kSquare) {
-        const P2 tg = unit(sub(P(1), P(0)));
-        put_rect(o, sub(P(0), scl(tg, S.hs)), P(0), S.hs);
-      } else {
-        put_pad(o, 4);
+// Threads run in blocks of kOutlineThreads consecutive points, and their
+// slots are back to back in memory (each shape's slot starts where the one
+// before ends), so a block's output is one contiguous range: every thread
+// builds its slot in shared memory, then the block writes the range with
+// 16-byte stores, consecutive threads on consecutive addresses.
+constexpr int kOutlineThreads = 64;
+constexpr int kSlotMax = kStrokeSegSlot;  // primitives a thread writes at most
+__global__ void __launch_bounds__(kOutlineThreads) k_stroke_outline(const float2* __restrict__ pts,
+                                                                    const StrokeShape* __restrict__ shapes,
+                                                                    int nshapes, long long nthreads,
+                                                                    Prim* __restrict__ out, int2* amb,
+                                                                    long long amb_cap,
+                                                                    unsigned long long* amb_count) {
+  static_assert(sizeof(Prim) == 48, "a primitive is three 16-byte words");
+  __shared__ __align__(16) Prim buf[kOutlineThreads * kSlotMax];  // 24 KB
+  __shared__ long long s_first[kOutlineThreads + 1];
+  for (long long t0 = (long long)blockIdx.x * kOutlineThreads; t0 < nthreads;
+       t0 += (long long)gridDim.x * kOutlineThreads) {
+    const long long t = t0 + threadIdx.x;
+    const bool live = t < nthreads;
+    int lo = 0, i = 0;
+    long long first = 0;  // this thread's first primitive in `out`
+    if (live) {
+      int hi = nshapes - 1;  // the last shape whose first thread is <= t
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (shapes[mid].thr_off <= t) lo = mid;
+        else hi = mid - 1;
       }
-      continue;
+      i = (int)(t - shapes[lo].thr_off);
+      first = shapes[lo].prim_off + (i == 0 ? 0 : kStrokeCapSlot + (long long)kStrokeSegSlot * (i - 1));
+      s_first[threadIdx.x] = first;
+      if (t == nthreads - 1 || threadIdx.x == kOutlineThreads - 1)
+        s_first[threadIdx.x + 1] = first + (i == 0 ? kStrokeCapSlot : kStrokeSegSlot);
     }
-    Prim* o = out + S.prim_off + kStrokeCapSlot + (long long)kStrokeSegSlot * (i - 1);
-    put_rect(o, P(i - 1), P(i), S.hs);
-    bool ambiguous = false;
-    if (i < n - 1) {
-      ambiguous = put_join(o + 4, P(i - 1), P(i), P(i + 1), S);
-    } else if (S.closed) {
-      ambiguous = put_join(o + 4, P(n - 2), P(n - 1), P(1), S);
-    } else if (S.cap == kRoundCap) {
-      put_circle(o + 4, P(n - 1), S.hs);
-    } else if (S.cap == kSquare) {
-      const P2 tg = unit(sub(P(n - 1), P(n - 2)));
-      put_rect(o + 4, add(P(n - 1), scl(tg, S.hs)), P(n - 1), S.hs);
-    } else {
-      put_pad(o + 4, 4);
+    __syncthreads();
+    const long long base = s_first[0];
+    if (live) {
+      const StrokeShape S = shapes[lo];
+      const int n = S.npts;
+      const float2* q = pts + S.pt_off;
+      auto P = [&](int k) { return P2{q[k].x, q[k].y}; };
+      Prim* o = buf + (first - base);
+      if (i == 0) {  // start cap (open polylines)
+        if (!S.closed && S.cap == kRoundCap) {
+          put_circle(o, P(0), S.hs);
+        } else if (!S.closed && S.cap == kSquare) {
+          const P2 tg = unit(sub(P(1), P(0)));
+          put_rect(o, sub(P(0), scl(tg, S.hs)), P(0), S.hs);
+        } else {
+          put_pad(o, 4);
+        }
+      } else {
+        put_rect(o, P(i - 1), P(i), S.hs);
+        bool ambiguous = false;
+        if (i < n - 1) {
+          ambiguous = put_join(o + 4, P(i - 1), P(i), P(i + 1), S);
+        } else if (S.closed) {
+          ambiguous = put_join(o + 4, P(n - 2), P(n - 1), P(1), S);
+        } else if (S.cap == kRoundCap) {
+          put_circle(o + 4, P(n - 1), S.hs);
+        } else if (S.cap == kSquare) {
+          const P2 tg = unit(sub(P(n - 1), P(n - 2)));
+          put_rect(o + 4, add(P(n - 1), scl(tg, S.hs)), P(n - 1), S.hs);
+        } else {
+          put_pad(o + 4, 4);
+        }
+        if (ambiguous) {
+          const unsigned long long k = atomicAdd(amb_count, 1ull);
+          if ((long long)k < amb_cap) amb[k] = make_int2(lo, i);
+        }
+      }
     }
-    if (ambiguous) {
-      const unsigned long long k = atomicAdd(amb_count, 1ull);
-      if ((long long)k < amb_cap) amb[k] = make_int2(lo, i);
-    }
+    __syncthreads();
+    // the block's range [base, end): 16-byte words, consecutive threads on consecutive words
+    const long long nlive = nthreads - t0 < kOutlineThreads ? nthreads - t0 : kOutlineThreads;
+    const long long words = (s_first[nlive] - base) * 3;
+    const uint4* src = reinterpret_cast<const uint4*>(buf);
+    uint4* dst = reinterpret_cast<uint4*>(out + base);
+    for (long long w = threadIdx.x; w < words; w += kOutlineThreads) dst[w] = src[w];
+    __syncthreads();
   }
 }
 
@@ -223,9 +257,10 @@ __global__ void __launch_bounds__(256) k_stroke_outline(const float2* __restrict
 void launch_stroke_outline(const float2* pts, const StrokeShape* shapes, int nshapes, long long nthreads, Prim* out,
                            int2* amb, long long amb_cap, unsigned long long* amb_count, int nsm, cudaStream_t st) {
   if (nthreads <= 0 || nshapes <= 0) return;
-  long long blocks = (nthreads + 255) / 256;
-  if (blocks > (long long)nsm * 16) blocks = (long long)nsm * 16;
-  k_stroke_outline<<<(unsigned)blocks, 256, 0, st>>>(pts, shapes, nshapes, nthreads, out, amb, amb_cap, amb_count);
+  long long blocks = (nthreads + kOutlineThreads - 1) / kOutlineThreads;
+  if (blocks > (long long)nsm * 24) blocks = (long long)nsm * 24;
+  k_stroke_outline<<<(unsigned)blocks, kOutlineThreads, 0, st>>>(pts, shapes, nshapes, nthreads, out, amb, amb_cap,
+                                                                 amb_count);
   note_launch();
 }
 
