@@ -417,6 +417,7 @@ def run_fill_extras(px, wl, args, stream):
     out["paints_2048"] = run_paints(px, wl, stream, cpu=cpu)
     out["glyph_batch"] = run_glyphs(px, wl, args.glyphs)
     out["dense_scene_1024_2000"] = run_scene(px, wl)
+    out["svg_tiger_900"] = run_svg_tiger(px, cpu=cpu)
     if args.serve_jobs > 0:
         rates = tuple(float(r) for r in args.serve_rates.split(",") if r)
         out["serving"] = run_serving(px, wl, args.serve_jobs, args.serve_pool, rates=rates)
@@ -733,6 +734,46 @@ def run_glyphs(px, wl, n, seed=7, page_side=4096, reps=5):
             "autotune": px.autotune_report().strip().splitlines(),
             "note": "batched = one graph launch rendering all masks + one ordered composite; "
                     "plain = blocking fillPath + draw per glyph"}
+
+
+def run_svg_tiger(px, cpu=True, reps=5):
+    """The Ghostscript tiger SVG (the reference's test document) through the SVG
+    front-end: parse + record (host), then one scene draw of its 304 calls
+    onto 900x900 (GPU), beside the oracle making the same calls one by one."""
+    from pixie_gb300 import svg as S
+    with np.load(os.path.join(ROOT, "tests", "golden", "inputs.npz")) as z:
+        text = bytes(z["svg_Ghostscript_Tiger"]).decode("utf-8")
+    t = time.perf_counter()
+    d = S.parse_svg(text)
+    parse_ms = (time.perf_counter() - t) * 1e3
+    t = time.perf_counter()
+    sc, status = S.svg_scene(d)
+    record_ms = (time.perf_counter() - t) * 1e3
+    img = px.Image(d.width, d.height)
+    img.draw_scene(sc)  # first draw: upload and stroke outlines
+    gpu, wall = [], []
+    for _ in range(reps):
+        img.fill([0, 0, 0, 0])
+        t = time.perf_counter()
+        img.draw_scene(sc)
+        wall.append((time.perf_counter() - t) * 1e3)
+        gpu.append(px.last_gpu_ms())
+    out = {"calls": len(sc), "parse_ms_host": round(parse_ms, 1), "record_ms_host": round(record_ms, 1),
+           "gpu_ms_per_draw": round(sorted(gpu)[reps // 2], 3), "draw_call_ms": round(sorted(wall)[reps // 2], 3)}
+    if cpu:
+        from oracle import pxo
+        ref = pxo.new_image(d.width, d.height)
+        t = time.perf_counter()
+        for it in S.svg_items(d):
+            if it["kind"] == "fill":
+                pxo.fill_path(ref, it["cmds"], it["color"], it["opacity"], it["blend"], it["transform"],
+                              it["winding"])
+            else:
+                pxo.stroke_path(ref, it["cmds"], it["color"], it["opacity"], it["blend"], it["transform"],
+                                it["width"], it["cap"], it["join"], it["miter"], it["dashes"])
+        out["cpu_oracle_ms_1core"] = round((time.perf_counter() - t) * 1e3, 1)
+        out["bitexact_vs_oracle"] = bool(np.array_equal(img.to_numpy(), ref))
+    return out
 
 
 def run_scene(px, wl, seed=7, n_paths=2000, size=1024, reps=3):

@@ -623,6 +623,45 @@ def _c(B):
     return B.minify(_load(B, "mandrill"), 1)
 
 
+# ---- tests/test_svg.nim: documents through the SVG front-end ---------------
+# pixie_gb300.svg restates svg.nim's parser; newImage's calls go through the
+# backend one by one.  Of the reference's SVG masters, rect01 is byte for byte
+# what this source draws.  The others were written by another build: dashes
+# matches only with the fills of its horizontal lines skipped (their empty
+# bounds make fillShapes raise here, float -> int of NaN being INT_MIN on x86;
+# a build where it is 0 returns quietly), and those with curves (circle01,
+# ellipse01, quad01, the tiger) differ at curve edges.
+def _svg_case(name):
+    def fn(B):
+        from pixie_gb300 import svg as S
+        doc = S.parse_svg(bytes(_svg_text(name)).decode("utf-8"))
+        img = B.new_image(doc.width, doc.height)
+        for it in S.svg_items(doc):
+            try:
+                if it["kind"] == "fill":
+                    B.fill_path(img, it["cmds"], it["color"], it["opacity"], it["blend"], it["transform"],
+                                it["winding"])
+                else:
+                    B.stroke_path(img, it["cmds"], it["color"], it["opacity"], it["blend"], it["transform"],
+                                  it["width"], it["cap"], it["join"], it["miter"], it["dashes"])
+            except Exception as e:  # a call the reference rejects too
+                if "Invalid line dash value" not in str(e):
+                    raise
+        return img
+    return fn
+
+
+def _svg_text(name):
+    if not _INPUTS:
+        import os
+        with np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "inputs.npz")) as z:
+            _INPUTS.update({k: z[k] for k in z.files})
+    return _INPUTS["svg_" + name]
+
+
+CASES["fileformats/svg/masters/rect01"] = (_svg_case("rect01"), "tests/test_svg.nim:3-22")
+
+
 # ---- tests/test_paints.nim: non-solid paints -------------------------------
 SOLID, IMAGE_PAINT, TILED_PAINT, LINEAR, RADIAL, ANGULAR = range(6)
 _STOPS = [((F.f32(1), 0.0, 0.0, F.f32(1)), 0.0), ((F.f32(1), 0.0, 0.0, F.f32(0.15625)), F.f32(1.0))]

@@ -7,7 +7,8 @@ Each entry is the straight-alpha RGBA uint8 pixel array of one master PNG that
 the reference's own tests write (tests/paths, tests/images, tests/contexts),
 keyed like "paths/pathHeart".  Only the masters used by tests/golden/cases.py
 are stored.  inputs.npz holds the images those tests read (readImage), also
-straight-alpha RGBA.
+straight-alpha RGBA, and a few of the SVG documents tests/test_svg.nim reads
+(as UTF-8 bytes) for the SVG front-end's tests.
 """
 import os
 import sys
@@ -29,6 +30,12 @@ INPUTS = {"turtle": "images/turtle.png", "turtle10x": "images/turtle@10x.png", "
           "minifiedBy2": "images/minifiedBy2.png", "minifiedBy4": "images/minifiedBy4.png"}
 
 
+# SVG documents the reference's tests read (tests/test_svg.nim:3-22), keyed by name.
+SVG_INPUTS = {"svg_Ghostscript_Tiger": "fileformats/svg/Ghostscript_Tiger.svg",
+              "svg_rect01": "fileformats/svg/rect01.svg", "svg_dashes": "fileformats/svg/dashes.svg",
+              "svg_circle01": "fileformats/svg/circle01.svg", "svg_quad01": "fileformats/svg/quad01.svg"}
+
+
 def main(ref_root: str) -> None:
     out = {}
     for name in sorted(CASES):
@@ -37,6 +44,9 @@ def main(ref_root: str) -> None:
     np.savez_compressed(os.path.join(HERE, "goldens.npz"), **out)
     print(f"wrote {len(out)} goldens")
     inputs = {k: read_png(os.path.join(ref_root, "tests", v)) for k, v in INPUTS.items()}
+    for k, v in SVG_INPUTS.items():  # documents for the SVG front-end, as UTF-8 bytes
+        with open(os.path.join(ref_root, "tests", v), "rb") as f:
+            inputs[k] = np.frombuffer(f.read(), np.uint8)
     np.savez_compressed(os.path.join(HERE, "inputs.npz"), **inputs)
     print(f"wrote {len(inputs)} input images")
 
