@@ -66,6 +66,10 @@ int64_t pxg_image_height(const pxg_image* image);
 void* pxg_image_device_ptr(pxg_image* image);
 int pxg_image_upload(pxg_image* image, const void* host_rgbx, int64_t nbytes);
 int pxg_image_download(const pxg_image* image, void* host_rgbx, int64_t nbytes);
+/* applyOpacity(Image, float32)  src/pixie/images.nim:261-277: every channel
+ * times round(255 * opacity), div 255 (0 clears, 255 keeps the image). */
+int pxg_image_apply_opacity(pxg_image* image, float opacity);
+
 /* fill(Image, Color)  src/pixie/images.nim:55-57 */
 int pxg_image_fill(pxg_image* image, const float color[4]);
 

@@ -2611,6 +2611,13 @@ void pxo_atan2_pairs(const float* y, const float* x, int64_t n, float* libm, flo
   }
 }
 
+// applyOpacity  images.nim:261-277
+int pxo_apply_opacity(uint8_t* rgbx_data, int64_t w, int64_t h, float opacity) {
+  Image img{w, h, (RGBX*)rgbx_data};
+  applyOpacity(img, opacity);
+  return 0;
+}
+
 // 1: the NEON line kernels of the timed CPU baseline (see nl::), 0: scalar.
 void pxo_set_simd_variant(int on) { g_simd_variant = on; }
 

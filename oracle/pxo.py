@@ -71,6 +71,7 @@ def lib():
         L.pxo_set_simd_variant.argtypes = [I]
         L.pxo_libm_sincosf.argtypes = [P, I64, P, P]
         L.pxo_atan2_pairs.argtypes = [P, P, I64, P, P]
+        L.pxo_apply_opacity.argtypes = [P, I64, I64, F]
         _lib = L
     return _lib
 
@@ -316,6 +317,10 @@ def atan2_pairs(y, x):
     a, b = np.empty_like(y), np.empty_like(y)
     lib().pxo_atan2_pairs(_p(y), _p(x), y.size, _p(a), _p(b))
     return a, b
+
+
+def apply_opacity(img, opacity):
+    lib().pxo_apply_opacity(_p(img), img.shape[1], img.shape[0], float(opacity))
 
 
 def set_simd_variant(on: bool):

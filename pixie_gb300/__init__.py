@@ -155,6 +155,7 @@ def lib():
         L.pxg_autotune.argtypes = [I]
         L.pxg_blur_config.argtypes = [I]
         L.pxg_stroke_config.argtypes = [I]
+        L.pxg_image_apply_opacity.argtypes = [P, F]
         L.pxg_stroke_fixups.restype = I64
         L.pxg_autotune_report.argtypes = [P, I64]
         L.pxg_autotune_report.restype = I64
@@ -369,6 +370,10 @@ class Image:
 
     def blur(self, radius: float, out_of_bounds=(0, 0, 0, 0)):
         _check(lib().pxg_image_blur(self._h, float(radius), _ptr(_color(out_of_bounds))))
+
+    def apply_opacity(self, opacity: float):
+        """applyOpacity (images.nim:261-277)"""
+        _check(lib().pxg_image_apply_opacity(self._h, float(opacity)))
 
     def spread(self, spread: float):
         _check(lib().pxg_image_spread(self._h, float(spread)))

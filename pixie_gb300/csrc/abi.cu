@@ -2792,6 +2792,17 @@ int pxg_image_stroke_path_paint(pxg_image* im, const float* cmds, int64_t n, con
   });
 }
 
+// applyOpacity  images.nim:261-277
+int pxg_image_apply_opacity(pxg_image* im, float opacity) {
+  return guarded_images({im}, [&] {
+    check_image(im);
+    Timed t;
+    apply_opacity(im, opacity);
+    CU(cudaGetLastError());
+    t.done();
+  });
+}
+
 // fill(image, paint)  pixie.nim:120-131
 int pxg_image_fill_paint(pxg_image* im, const pxg_paint* paint) {
   return guarded([&] {

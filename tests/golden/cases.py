@@ -662,6 +662,440 @@ def _svg_text(name):
 CASES["fileformats/svg/masters/rect01"] = (_svg_case("rect01"), "tests/test_svg.nim:3-22")
 
 
+# ---- tests/test_contexts.nim: the Canvas-2D context front-end ---------------
+# pixie_gb300.context restates contexts.nim; its calls go to the backend.
+class _CtxBackend:
+    """a golden-case backend as the context's drawing surface"""
+
+    def __init__(self, B):
+        self.B = B
+
+    def new_image(self, w, h):
+        return self.B.new_image(w, h)
+
+    def copy(self, img):
+        return self.B.copy(img)
+
+    def size(self, img):
+        return self.B.size(img)
+
+    def fill_path(self, img, cmds, color, opacity, blend, mat, winding):
+        self.B.fill_path(img, cmds, color, opacity, blend, mat, winding)
+
+    def stroke_path(self, img, cmds, color, opacity, blend, mat, width, cap, join, miter, dashes):
+        self.B.stroke_path(img, cmds, color, opacity, blend, mat, width, cap, join, miter, dashes)
+
+    def draw(self, a, b, blend):
+        self.B.draw(a, b, 0, 0, blend)
+
+    def apply_opacity(self, img, opacity):
+        self.B.apply_opacity(img, opacity)
+
+
+def _ctx(B, w=300, h=150):
+    from pixie_gb300.context import Context
+    return Context(B.new_image(w, h), _CtxBackend(B))
+
+
+def _ctx_case(name, lines):
+    def deco(fn):
+        CASES["contexts/" + name] = (lambda B: fn(B).image, f"tests/test_contexts.nim:{lines}")
+        return fn
+    return deco
+
+
+@_ctx_case("clearRect_1", "3-21")
+def _c(B):
+    c = _ctx(B, 300, 160)
+    c.begin_path()
+    c.set_fill_style("#ff6")
+    c.fill_rect(0, 0, 300, 160)
+    c.begin_path()
+    c.set_fill_style("blue")
+    c.move_to(20, 20)
+    c.line_to(180, 20)
+    c.line_to(130, 130)
+    c.close_path()
+    c.fill()
+    c.clear_rect(10, 10, 120, 100)
+    return c
+
+
+@_ctx_case("beginPath_1", "23-38")
+def _c(B):
+    c = _ctx(B)
+    c.begin_path()
+    c.set_stroke_style("blue")
+    c.move_to(20, 20)
+    c.line_to(200, 20)
+    c.stroke()
+    c.begin_path()
+    c.set_stroke_style("green")
+    c.move_to(20, 20)
+    c.line_to(120, 120)
+    c.stroke()
+    return c
+
+
+@_ctx_case("moveTo_1", "40-50")
+def _c(B):
+    c = _ctx(B)
+    c.begin_path()
+    c.move_to(50, 50)
+    c.line_to(200, 50)
+    c.move_to(50, 90)
+    c.line_to(280, 120)
+    c.stroke()
+    return c
+
+
+@_ctx_case("fill_1", "52-67")
+def _c(B):
+    c = _ctx(B)
+    region = Path()
+    for i, (x, y) in enumerate([(30, 90), (110, 20), (240, 130), (60, 130), (190, 20), (270, 90)]):
+        (region.move_to if i == 0 else region.line_to)(x, y)
+    region.close_path()
+    c.set_fill_style("green")
+    c.fill(region, 1)
+    return c
+
+
+@_ctx_case("stroke_1", "69-75")
+def _c(B):
+    c = _ctx(B)
+    c.rect(10, 10, 150, 100)
+    c.stroke()
+    return c
+
+
+@_ctx_case("stroke_2", "77-99")
+def _c(B):
+    c = _ctx(B)
+    for w, col, y, x1 in ((26, "orange", 20, 160), (14, "green", 80, 220), (4, "pink", 140, 280)):
+        c.line_width = F.f32(w)
+        c.set_stroke_style(col)
+        c.move_to(20, y)
+        c.line_to(x1, y)
+        c.stroke()
+    return c
+
+
+@_ctx_case("stroke_3", "101-116")
+def _c(B):
+    c = _ctx(B)
+    c.line_width = 26.0
+    c.set_stroke_style("red")
+    c.begin_path()
+    c.rect(25, 25, 100, 100)
+    c.fill()
+    c.stroke()
+    c.begin_path()
+    c.rect(175, 25, 100, 100)
+    c.stroke()
+    c.fill()
+    return c
+
+
+@_ctx_case("closePath_1", "118-128")
+def _c(B):
+    c = _ctx(B)
+    c.begin_path()
+    c.move_to(20, 140)
+    c.line_to(120, 10)
+    c.line_to(220, 140)
+    c.close_path()
+    c.stroke()
+    return c
+
+
+@_ctx_case("bezierCurveTo_1", "130-143")
+def _c(B):
+    c = _ctx(B)
+    c.begin_path()
+    c.move_to(50, 20)
+    c.bezier_curve_to(230, 30, 150, 80, 250, 100)
+    c.stroke()
+    return c
+
+
+@_ctx_case("bezierCurveTo_2", "145-153")
+def _c(B):
+    c = _ctx(B)
+    c.begin_path()
+    c.move_to(30, 30)
+    c.bezier_curve_to(120, 160, 180, 10, 220, 140)
+    c.stroke()
+    return c
+
+
+@_ctx_case("quadracticCurveTo_1", "155-162")
+def _c(B):
+    c = _ctx(B)
+    c.move_to(50, 20)
+    c.quadratic_curve_to(230, 30, 50, 100)
+    c.stroke()
+    return c
+
+
+@_ctx_case("quadracticCurveTo_2", "164-172")
+def _c(B):
+    c = _ctx(B)
+    c.begin_path()
+    c.move_to(20, 110)
+    c.quadratic_curve_to(230, 150, 250, 20)
+    c.stroke()
+    return c
+
+
+@_ctx_case("ellipse_1", "174-181")
+def _c(B):
+    c = _ctx(B)
+    c.begin_path()
+    c.ellipse(100, 75, 75, 50)
+    c.stroke()
+    return c
+
+
+@_ctx_case("strokeRect_1", "183-188")
+def _c(B):
+    c = _ctx(B)
+    c.set_stroke_style("green")
+    c.stroke_rect(20, 10, 160, 100)
+    return c
+
+
+@_ctx_case("strokeRect_2", "190-198")
+def _c(B):
+    c = _ctx(B)
+    c.line_join = 2
+    c.line_width = 15.0
+    c.set_stroke_style("#38f")
+    c.stroke_rect(30, 30, 160, 90)
+    return c
+
+
+@_ctx_case("setTransform_1", "200-205")
+def _c(B):
+    c = _ctx(B)
+    c.set_transform([1, 0.2, 0, 0.8, 1, 0, 0, 0, 1])
+    c.fill_rect(0, 0, 100, 100)
+    return c
+
+
+@_ctx_case("rotate_simple", "214-219")
+def _c(B):
+    c = _ctx(B)
+    c.rotate(45 * 3.141592653589793 / 180)
+    c.fill_rect(60, 0, 100, 30)
+    return c
+
+
+@_ctx_case("resetTransform_2", "221-233")
+def _c(B):
+    c = _ctx(B)
+    c.transform([1, 0, 0, 1.7, 1, 0, 0, 0, 1])
+    c.set_fill_style("gray")
+    c.fill_rect(40, 40, 50, 20)
+    c.fill_rect(40, 90, 50, 20)
+    c.reset_transform()
+    c.set_fill_style("red")
+    c.fill_rect(40, 40, 50, 20)
+    c.fill_rect(40, 90, 50, 20)
+    return c
+
+
+@_ctx_case("translate_1", "235-246")
+def _c(B):
+    c = _ctx(B)
+    c.translate(110, 30)
+    c.set_fill_style("red")
+    c.fill_rect(0, 0, 80, 80)
+    c.set_transform([1, 0, 0, 0, 1, 0, 0, 0, 1])
+    c.set_fill_style("gray")
+    c.fill_rect(0, 0, 80, 80)
+    return c
+
+
+@_ctx_case("scale_1", "248-259")
+def _c(B):
+    c = _ctx(B)
+    c.scale(9, 3)
+    c.set_fill_style("red")
+    c.fill_rect(10, 10, 8, 20)
+    c.set_transform([1, 0, 0, 0, 1, 0, 0, 0, 1])
+    c.set_fill_style("gray")
+    c.fill_rect(10, 10, 8, 20)
+    return c
+
+
+@_ctx_case("rotate_1", "261-271")
+def _c(B):
+    c = _ctx(B)
+    c.set_fill_style("gray")
+    c.fill_rect(100, 0, 80, 20)
+    c.rotate(45 * 3.141592653589793 / 180)
+    c.set_fill_style("red")
+    c.fill_rect(100, 0, 80, 20)
+    return c
+
+
+@_ctx_case("save_1", "296-309")
+def _c(B):
+    c = _ctx(B)
+    c.save()
+    c.set_fill_style("green")
+    c.fill_rect(10, 10, 100, 100)
+    c.restore()
+    c.fill_rect(150, 40, 100, 100)
+    return c
+
+
+def _clip_circle(c):
+    c.begin_path()
+    c.circle(100, 75, 50)
+    c.clip()
+
+
+@_ctx_case("clip_1", "311-323")
+def _c(B):
+    c = _ctx(B)
+    _clip_circle(c)
+    c.set_fill_style("blue")
+    c.fill_rect(0, 0, 300, 150)
+    c.set_fill_style("orange")
+    c.fill_rect(0, 0, 100, 100)
+    return c
+
+
+@_ctx_case("clip_1b", "325-340")
+def _c(B):
+    c = _ctx(B)
+    c.set_fill_style("blue")
+    c.fill_rect(0, 0, 300, 150)
+    _clip_circle(c)
+    c.set_fill_style("red")
+    c.fill_rect(0, 0, 300, 150)
+    c.set_fill_style("orange")
+    c.fill_rect(0, 0, 100, 100)
+    return c
+
+
+@_ctx_case("clip_1c", "342-360")
+def _c(B):
+    c = _ctx(B)
+    c.save()
+    _clip_circle(c)
+    c.set_fill_style("red")
+    c.fill_rect(0, 0, 300, 150)
+    c.set_fill_style("orange")
+    c.fill_rect(0, 0, 100, 100)
+    c.restore()
+    c.set_fill_style("blue")
+    c.fill_rect(0, 0, 300, 150)
+    return c
+
+
+@_ctx_case("clip_1d", "362-380")
+def _c(B):
+    c = _ctx(B)
+    c.set_fill_style("blue")
+    c.fill_rect(0, 0, 300, 150)
+    _clip_circle(c)
+    c.save_layer()
+    c.set_fill_style("red")
+    c.fill_rect(0, 0, 300, 150)
+    c.set_fill_style("orange")
+    c.fill_rect(0, 0, 100, 100)
+    c.restore()
+    return c
+
+
+@_ctx_case("clip_1e", "382-402")
+def _c(B):
+    c = _ctx(B)
+    c.save()
+    _clip_circle(c)
+    c.save_layer()
+    c.set_fill_style("red")
+    c.fill_rect(0, 0, 300, 150)
+    c.set_fill_style("orange")
+    c.fill_rect(0, 0, 100, 100)
+    c.restore()
+    c.restore()
+    c.set_fill_style("blue")
+    c.fill_rect(0, 0, 300, 150)
+    return c
+
+
+@_ctx_case("clip_1f", "404-423")
+def _c(B):
+    c = _ctx(B)
+    c.save()
+    _clip_circle(c)
+    c.save_layer()
+    c.set_fill_style("red")
+    c.fill_rect(0, 0, 300, 150)
+    c.restore()
+    c.save_layer()
+    c.set_fill_style("orange")
+    c.fill_rect(0, 0, 100, 100)
+    c.restore()
+    return c
+
+
+@_ctx_case("clip_2", "425-435")
+def _c(B):
+    c = _ctx(B)
+    region = Path()
+    region.rect(80, 10, 20, 130)
+    region.rect(40, 50, 100, 50)
+    c.clip(region, 1)
+    c.set_fill_style("blue")
+    c.fill_rect(0, 0, 300, 150)
+    return c
+
+
+@_ctx_case("clip_3", "437-452")
+def _c(B):
+    c = _ctx(B)
+    circle = Path()
+    circle.circle(150, 75, 75)
+    square = Path()
+    square.rect(85, 10, 130, 130)
+    c.clip(circle)
+    c.clip(square)
+    c.set_fill_style("blue")
+    c.fill_rect(0, 0, 300, 150)
+    return c
+
+
+@_ctx_case("setLineDash_1", "494-516")
+def _c(B):
+    c = _ctx(B)
+    y = 15.0
+    for pattern in ([], [1, 1], [10, 10], [20, 5], [15, 3, 3, 3], [20, 3, 3, 3, 3, 3, 3, 3], [12, 3, 3]):
+        c.begin_path()
+        c.set_line_dash(pattern)
+        c.move_to(0, y)
+        c.line_to(300, y)
+        c.stroke()
+        y += 20
+    return c
+
+
+@_ctx_case("globalAlpha_1", "533-547")
+def _c(B):
+    c = _ctx(B)
+    B.fill(c.image, rgba(255, 255, 255, 255))
+    c.global_alpha = 0.5
+    c.set_fill_style("blue")
+    c.fill_rect(10, 10, 100, 100)
+    c.set_fill_style("red")
+    c.fill_rect(50, 50, 100, 100)
+    return c
+
+
 # ---- tests/test_paints.nim: non-solid paints -------------------------------
 SOLID, IMAGE_PAINT, TILED_PAINT, LINEAR, RADIAL, ANGULAR = range(6)
 _STOPS = [((F.f32(1), 0.0, 0.0, F.f32(1)), 0.0), ((F.f32(1), 0.0, 0.0, F.f32(0.15625)), F.f32(1.0))]

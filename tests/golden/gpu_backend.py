@@ -32,6 +32,15 @@ class GpuBackend:
     def minify(self, img, power):
         return img.minify_by2(power)
 
+    def copy(self, img):
+        return img.minify_by2(0)
+
+    def size(self, img):
+        return img.width, img.height
+
+    def apply_opacity(self, img, opacity):
+        img.apply_opacity(opacity)
+
     def magnify(self, img, power):
         return img.magnify_by2(power)
 

@@ -50,3 +50,12 @@ class OracleBackend:
 
     def pixels(self, img):
         return np.asarray(img)
+
+    def copy(self, img):
+        return img.copy()
+
+    def size(self, img):
+        return img.shape[1], img.shape[0]
+
+    def apply_opacity(self, img, opacity):
+        pxo.apply_opacity(img, opacity)

@@ -21,7 +21,9 @@ GOLDENS = np.load(os.path.join(os.path.dirname(__file__), "golden", "goldens.npz
 # cases whose paint has a channel outside {0, 255} at partially covered pixels
 ROUNDING_SENSITIVE = {"paths/arcTo2", "paths/opacityFill", "paths/opacityStroke",
                       "paths/pathBottomArc", "paths/pathCornerArc", "paths/pathHeart",
-                      "paths/pathInvertedCornerArc", "paths/pathRotatedArc"}
+                      "paths/pathInvertedCornerArc", "paths/pathRotatedArc",
+                      "contexts/beginPath_1", "contexts/fill_1", "contexts/resetTransform_2",
+                      "contexts/setTransform_1", "contexts/strokeRect_1", "contexts/strokeRect_2"}
 
 # Masters of tests/test_images_draw.nim that this source's code does not
 # write (the reference's xray only stores them, it never compares):
