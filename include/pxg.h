@@ -188,6 +188,15 @@ int pxg_blur_config(int use_tensor_cores);
  * any blur).  No counterpart in the reference. */
 int pxg_last_blur_kernel(void);
 
+/* Converter trace of the ring blur passes, a profiling aid: enable != 0
+ * switches it on (and clears it) for the passes launched afterwards, 0 off.
+ * If out is not NULL it receives up to n int64 values from the last traced
+ * pass, laid out [converter group 0..1][ring chunk 0..255][event 0..2]: the
+ * clock64 of CTA 0's second converter warp before its barrier waits for the
+ * chunk, after them, and after its tensor-memory stores (0 where nothing was
+ * recorded).  Synchronizes the device.  No counterpart in the reference. */
+int pxg_ring_trace(int enable, int64_t* out, int64_t n);
+
 /* spread(Image, float32)  src/pixie/images.nim:700-758 (private in the
  * reference; shadow's first pass) */
 int pxg_image_spread(pxg_image* image, float spread);

@@ -157,6 +157,7 @@ def lib():
         L.pxg_stroke_config.argtypes = [I]
         L.pxg_image_apply_opacity.argtypes = [P, F]
         L.pxg_stroke_fixups.restype = I64
+        L.pxg_ring_trace.argtypes = [I, P, I64]
         L.pxg_autotune_report.argtypes = [P, I64]
         L.pxg_autotune_report.restype = I64
         _lib = L
@@ -621,6 +622,16 @@ def blur_config(mode):
 def last_blur_kernel() -> int:
     """Kernel family the last blur ran on (3, 2, 1, 0; -1 before any)."""
     return int(lib().pxg_last_blur_kernel())
+
+
+def ring_trace(enable: bool, fetch: bool = False):
+    """The ring blur passes' converter trace (a profiling aid; see
+    pxg_ring_trace in include/pxg.h): switch it on or off; with fetch, the
+    last traced pass's clock64 stamps as an int64 array [group][chunk][event]."""
+    out = np.zeros((2, 256, 3), np.int64) if fetch else None
+    _check(lib().pxg_ring_trace(1 if enable else 0, None if out is None else _ptr(out),
+                                0 if out is None else out.size))
+    return out
 
 
 def autotune(enable: bool):

@@ -170,6 +170,8 @@ bool launch_blur_tcp(uint32_t* img, uint32_t* tmp, long long W, long long H, int
 const void* tcp_blur_kernel(bool x, int n);
 bool ring_blur_init(size_t* maxSmem);
 bool weights_exact_f16(const uint16_t* hostKern, int r);
+long long blur_scratch_bytes(long long W, long long H);
+int ring_trace(int enable, long long* out, long long n);
 bool launch_blur_ring(uint32_t* img, uint32_t* tmp, long long W, long long H, int r, const uint16_t* kern,
                       bool exactF16, uint32_t oob, int nsm, size_t maxSmem, int* err, cudaStream_t st);
 void launch_stroke_outline(const float2* pts, const StrokeShape* shapes, int nshapes, long long nthreads, Prim* out,
@@ -178,6 +180,7 @@ bool launch_blur_small_fused(const uint32_t* in, uint32_t* out, long long W, lon
                              const uint16_t* kern, uint32_t oob, cudaStream_t st);
 bool launch_blur_small(uint32_t* img, uint32_t* tmp, long long W, long long H, int r, const uint16_t* kern,
                        uint32_t oob, int nsm, cudaStream_t st);
+constexpr int kSmallBlurMaxR = 8;  // the largest radius launch_blur_small(_fused) takes
 __global__ void k_blur_x(const uint32_t*, uint32_t*, long long, long long, int, const uint16_t*, uint32_t);
 __global__ void k_blur_y(const uint32_t*, uint32_t*, long long, long long, int, const uint16_t*, uint32_t);
 __global__ void k_blurf_x(const uint32_t*, uint32_t*, long long, long long, int, const uint16_t*, uint32_t);
@@ -410,8 +413,10 @@ const uint16_t* weights_for(int64_t r) {
 // result land in tmp: radii 1..8 then run as one fused launch (img -> tmp)
 // and the function returns true, after which the caller exchanges the two
 // buffers.
-bool blur_dispatch(uint32_t* img, uint32_t* tmp, long long W, long long H, int64_t r, uint32_t oob,
-                   bool swap_ok = false) {
+// tmp holds tmp_bytes: W * H * 4 at least; the tensor-core passes need
+// blur_scratch_bytes(W, H) (a padded intermediate) and are skipped below that.
+bool blur_dispatch(uint32_t* img, uint32_t* tmp, long long tmp_bytes, long long W, long long H, int64_t r,
+                   uint32_t oob, bool swap_ok = false) {
   const uint16_t* kern = weights_for(r);
   if (swap_ok && g.blur_tensor == 3 && launch_blur_small_fused(img, tmp, W, H, (int)r, kern, oob, g.stream)) {
     g.last_blur = 5;
@@ -419,7 +424,7 @@ bool blur_dispatch(uint32_t* img, uint32_t* tmp, long long W, long long H, int64
   }
   int used = -1;
   if (g.blur_tensor == 3 && launch_blur_small(img, tmp, W, H, (int)r, kern, oob, g.nsm, g.stream)) used = 4;
-  if (used < 0 && g.blur_tensor == 3 && g.ring_ok &&
+  if (used < 0 && g.blur_tensor == 3 && g.ring_ok && tmp_bytes >= blur_scratch_bytes(W, H) &&
       launch_blur_ring(img, tmp, W, H, (int)r, kern, g.weights_f16[r], oob, g.nsm, g.ringSmemMax, g.dev_err,
                        g.stream))
     used = 3;
@@ -1214,11 +1219,17 @@ void srv_release(pxg_server* sv, SrvJob* j) {
   j->bytes = 0;
 }
 
+// Device bytes a job holds while admitted: its canvas, and the blur's
+// intermediate buffer when it is blurred.
+long long srv_job_bytes(long long W, long long H, int64_t blur) {
+  return W * H * 4 + (blur > 0 ? blur_scratch_bytes(W, H) : 0);
+}
+
 // Admits queued jobs in arrival order while their canvases fit the budget.
 void srv_admit(pxg_server* sv) {
   while (!sv->queue.empty()) {
     SrvJob* j = sv->queue.front();
-    const long long need = j->W * j->H * 4 * (j->blur > 0 ? 2 : 1);
+    const long long need = srv_job_bytes(j->W, j->H, j->blur);
     if (sv->used + need > sv->budget) break;
     sv->queue.pop_front();
     srv_pool_init();
@@ -1226,7 +1237,7 @@ void srv_admit(pxg_server* sv) {
     j->canvas.width = j->W;
     j->canvas.height = j->H;
     j->canvas.owned = 1;
-    if (j->blur > 0) CU(cudaMallocAsync((void**)&j->tmp, (size_t)(j->W * j->H * 4), g.stream));
+    if (j->blur > 0) CU(cudaMallocAsync((void**)&j->tmp, (size_t)blur_scratch_bytes(j->W, j->H), g.stream));
     CU(cudaMemsetAsync(j->canvas.data, 0, (size_t)(j->W * j->H * 4), g.stream));
     j->bytes = need;
     sv->used += need;
@@ -1311,7 +1322,8 @@ void srv_step(pxg_server* sv) {
     }
     if (j->next >= j->scene->jobs.size()) {
       if (j->blur > 0) {
-        if (blur_dispatch((uint32_t*)j->canvas.data, (uint32_t*)j->tmp, j->W, j->H, j->blur, 0u, true))
+        if (blur_dispatch((uint32_t*)j->canvas.data, (uint32_t*)j->tmp, blur_scratch_bytes(j->W, j->H), j->W, j->H,
+                          j->blur, 0u, true))
           std::swap(j->canvas.data, j->tmp);  // both the job's own; the old canvas is freed with tmp below
         CU(cudaGetLastError());
       }
@@ -2204,7 +2216,7 @@ int64_t pxg_server_submit(pxg_server* sv, const pxg_scene* scene, int64_t width,
     const int64_t r = nim_round_int(blur_radius);
     if (r < 0) throw ApiError{"Cannot apply negative blur"};
     if (r > (1 << 20)) throw ApiError{"Blur radius too large"};
-    const long long need = width * height * 4 * (r > 0 ? 2 : 1);
+    const long long need = srv_job_bytes(width, height, r);
     if (need > sv->budget) throw ApiError{"Job larger than the server's memory budget"};
     SrvJob* j = new SrvJob();
     j->id = sv->next_id++;
@@ -2325,6 +2337,13 @@ int pxg_blur_config(int use_tensor_cores) {
 int pxg_last_blur_kernel(void) {
   std::lock_guard<std::recursive_mutex> lk(g.mu);
   return g.last_blur;
+}
+
+int pxg_ring_trace(int enable, int64_t* out, int64_t n) {
+  return guarded([&] {
+    CU(cudaDeviceSynchronize());
+    if (ring_trace(enable, reinterpret_cast<long long*>(out), n) != 0) throw ApiError{"Ring blur trace unavailable"};
+  });
 }
 
 int pxg_autotune(int enable) {
@@ -2837,14 +2856,17 @@ int pxg_image_blur(pxg_image* im, float radius, const float* oob) {
     uint32_t o = color_to_rgbx(oob ? oob : zero);
     weights_for(r);
     const long long bytes = im->width * im->height * 4;
-    uint32_t* tmp = (uint32_t*)scratch(bytes);
+    // radii the small-radius kernels take need an image-sized buffer; larger
+    // ones the tensor-core passes' padded intermediate
+    const long long tmp_bytes = r <= kSmallBlurMaxR ? bytes : blur_scratch_bytes(im->width, im->height);
+    uint32_t* tmp = (uint32_t*)scratch(tmp_bytes);
     Timed t;
     // an image the library allocated, whose address nobody holds, may take
     // the fused small-radius kernel: the result lands in the scratch buffer
     // and the two buffers change owners (stream order keeps every earlier
     // and later use of either buffer in place)
     const bool swap_ok = im->owned && !im->exported;
-    if (blur_dispatch((uint32_t*)im->data, tmp, im->width, im->height, r, o, swap_ok)) {
+    if (blur_dispatch((uint32_t*)im->data, tmp, tmp_bytes, im->width, im->height, r, o, swap_ok)) {
       std::swap(im->data, g.scratch);
       g.scratch_cap = bytes;
     }

@@ -60,6 +60,18 @@ namespace pxg {
 
 void note_launch();
 
+// Converter trace (a diagnostic, off unless pxg_ring_trace enables it): for
+// CTA 0 and the second warp of each converter group, the clock64 of every
+// ring chunk before its barrier waits, after them, and after its
+// tensor-memory stores -- where a pass's time goes between the roles.
+// (The trace's never-taken branch in the converter loop is also what lets the
+// compiler keep that loop's bookkeeping on the uniform datapath: without it
+// a 4096 x 4096 blur measured 25 % slower, with 5x the branch and 1/50 the
+// uniform-pipe instructions.)
+constexpr int kTraceChunks = 256;
+__device__ int g_ring_trace_on;
+__device__ long long g_ring_trace[2][kTraceChunks][3];
+
 namespace {
 
 using namespace tc;
@@ -83,6 +95,7 @@ constexpr float kMagic = 12582912.0f;          // 1.5 * 2^23
 
 struct RingArgs {
   int alen, clen;  // input row length (pass axis) and number of rows (lines)
+  int opitch;      // pixels between consecutive output rows (>= clen)
   int r;
   int kspan;       // K span of a tile: 64 + 2r rounded up to 16
   int nring;       // ring chunks (ring positions = 64 * nring)
@@ -148,7 +161,10 @@ __device__ __forceinline__ void mma_ts_elect(uint32_t tmem_d, uint32_t tmem_a, u
       "r"(tmem_a), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 
-template <bool SPLIT>
+// DELTA = (first input position of a chunk) mod 4 = (-r) mod 4, the pixel
+// offset of the chunk inside its 16-byte aligned box, fixed per radius: as a
+// template parameter the converters' word selection is straight-line code.
+template <bool SPLIT, int DELTA>
 __global__ void __launch_bounds__(kRingThreads, 1)
     k_blur_ring(const __grid_constant__ CUtensorMap tin, uint32_t* __restrict__ out, const RingArgs a,
                 const uint16_t* __restrict__ kern, int* err) {
@@ -167,6 +183,7 @@ __global__ void __launch_bounds__(kRingThreads, 1)
   uint32_t* taddr_s =
       reinterpret_cast<uint32_t*>(sm + L.bars + (2 * kMaxRaw + 2 * kMaxRing + 2 * kMaxAcc + 1) * 8);
   const int r = a.r;
+  const bool trace = g_ring_trace_on != 0;
   pdl_trigger();  // the next pass may be set up while this one runs
 
   // The Toeplitz weights, once per CTA (K padded with zeros to whole blocks).
@@ -184,15 +201,15 @@ __global__ void __launch_bounds__(kRingThreads, 1)
   if (tid == 0) {
     for (int b = 0; b < kMaxRaw; b++) {
       mbar_init(rawFull + 8 * b, 1);
-      mbar_init(rawEmpty + 8 * b, 16 * kConvWarps);
+      mbar_init(rawEmpty + 8 * b, kConvWarps / 2);  // one lane of each converter warp of a group
     }
     for (int b = 0; b < kMaxRing; b++) {
-      mbar_init(ringFull + 8 * b, 16 * kConvWarps);
+      mbar_init(ringFull + 8 * b, kConvWarps / 2);
       mbar_init(ringEmpty + 8 * b, 1);
     }
     for (int b = 0; b < kMaxAcc; b++) {
       mbar_init(tFull + 8 * b, 1);
-      mbar_init(tEmpty + 8 * b, 128);
+      mbar_init(tEmpty + 8 * b, kEpiWarps / 2);  // one lane of each epilogue warp of a group
     }
     mbar_init(doneBar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
@@ -264,6 +281,7 @@ __global__ void __launch_bounds__(kRingThreads, 1)
         const int cs = s, cseg = seg;
         const uint32_t cphs = phs, cphr = phr;
         const bool reuse = n >= a.nring;
+        const int cn = n;
         n++;
         if (++s == a.nraw) {
           s = 0;
@@ -274,6 +292,8 @@ __global__ void __launch_bounds__(kRingThreads, 1)
           phr ^= 1u;
         }
         if (!mine) continue;
+        const bool tr = trace && blockIdx.x == 0 && lane == 0 && q == 1 && cn < kTraceChunks;
+        if (tr) g_ring_trace[cg][cn][0] = clock64();
         ok = __all_sync(0xffffffffu, mbar_wait(rawFull + 8 * cs, cphs));
         if (ok && reuse) ok = __all_sync(0xffffffffu, mbar_wait(ringEmpty + 8 * cseg, cphr ^ 1u));
         if (!ok) {
@@ -281,6 +301,7 @@ __global__ void __launch_bounds__(kRingThreads, 1)
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        if (tr) g_ring_trace[cg][cn][1] = clock64();
         const uint32_t row = base + L.raw + (uint32_t)(cs * a.rawStride + j * (kRawW * 4));
         const int p0 = s0 - r + kPos * c;
         const bool edge = p0 < 0 || p0 + kPos > a.alen;
@@ -297,19 +318,8 @@ __global__ void __launch_bounds__(kRingThreads, 1)
             qv[4 * v + 3] = d.w;
           }
           uint32_t px[32];
-          if (a.delta == 0) {
 #pragma unroll
-            for (int t = 0; t < 32; t++) px[t] = qv[t];
-          } else if (a.delta == 1) {
-#pragma unroll
-            for (int t = 0; t < 32; t++) px[t] = qv[t + 1];
-          } else if (a.delta == 2) {
-#pragma unroll
-            for (int t = 0; t < 32; t++) px[t] = qv[t + 2];
-          } else {
-#pragma unroll
-            for (int t = 0; t < 32; t++) px[t] = qv[t + 3];
-          }
+          for (int t = 0; t < 32; t++) px[t] = qv[t + DELTA];
           if (edge) {
 #pragma unroll
             for (int t = 0; t < 32; t++) {
@@ -322,10 +332,16 @@ __global__ void __launch_bounds__(kRingThreads, 1)
           for (int t = 0; t < 16; t++) hv[t] = sub_pair(px[2 * t], px[2 * t + 1], sel);
           tmem_st16(tq + (uint32_t)(32 * cseg + 16 * h), hv);
         }
+        // every lane's tensor-memory stores (and shared-memory reads) are
+        // done before the warp's one arrival on each barrier
         asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
+        if (tr) g_ring_trace[cg][cn][2] = clock64();
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-        mbar_arrive(rawEmpty + 8 * cs);
-        mbar_arrive(ringFull + 8 * cseg);
+        __syncwarp();
+        if (lane == 0) {
+          mbar_arrive(rawEmpty + 8 * cs);
+          mbar_arrive(ringFull + 8 * cseg);
+        }
       }
     }
   } else if (warp == kMmaWarp) {
@@ -444,11 +460,12 @@ __global__ void __launch_bounds__(kRingThreads, 1)
             w = __byte_perm(w, __shfl_xor_sync(0xffffffffu, w, 2), selA);
             w = __byte_perm(w, __shfl_xor_sync(0xffffffffu, w, 1), selB);
             const int n = o0 + cc + t + ch;
-            if (n < a.alen && line < a.clen) out[(long long)n * a.clen + line] = w;
+            if (n < a.alen && line < a.clen) out[(long long)n * a.opitch + line] = w;
           }
         }
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-        mbar_arrive(tEmpty + 8 * cacc);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(tEmpty + 8 * cacc);
       }
     }
   }
@@ -462,11 +479,12 @@ __global__ void __launch_bounds__(kRingThreads, 1)
 
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 
-// Row-major image of W x H pixels (u32), boxes of bx x by pixels.
-bool encode_map(CUtensorMap* m, const void* ptr, int W, int H, int bx, int by) {
+// Row-major image of W x H pixels (u32) with rows pitch pixels apart, boxes
+// of bx x by pixels.
+bool encode_map(CUtensorMap* m, const void* ptr, int W, int H, long long pitch, int bx, int by) {
   if (!g_encode) return false;
   cuuint64_t dims[2] = {(cuuint64_t)W, (cuuint64_t)H};
-  cuuint64_t strides[1] = {(cuuint64_t)W * 4};
+  cuuint64_t strides[1] = {(cuuint64_t)pitch * 4};
   cuuint32_t box[2] = {(cuuint32_t)bx, (cuuint32_t)by};
   cuuint32_t estr[2] = {1, 1};
   return g_encode(m, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<void*>(ptr), dims, strides, box, estr,
@@ -478,6 +496,7 @@ bool encode_map(CUtensorMap* m, const void* ptr, int W, int H, int bx, int by) {
 bool plan_pass(RingArgs& a, int alen, int clen, int r, int nsm, size_t maxSmem, bool split, int& grid) {
   a.alen = alen;
   a.clen = clen;
+  a.opitch = clen;
   a.r = r;
   a.kspan = (kPos + 2 * r + 15) / 16 * 16;
   // the ring takes every TMEM column above the accumulators: the converters run
@@ -490,7 +509,12 @@ bool plan_pass(RingArgs& a, int alen, int clen, int r, int nsm, size_t maxSmem, 
   a.nraw = kMaxRaw;
   while (a.nraw > 2 && ring_smem(a, split).total + 1024 > maxSmem) a.nraw--;
   if (ring_smem(a, split).total + 1024 > maxSmem) return false;
-  // segment length: fewest rounds x (outputs + halo) per CTA
+  // segment length: fewest rounds x (outputs + a fixed cost per item) per
+  // CTA.  An item's start (its halo chunks and the hand-offs before its first
+  // tile) costs about one tile of 64 outputs at r = 16 and at r = 64
+  // (measured on 4096 x 4096: segments of 512 outputs over all SMs beat one
+  // whole 4096-pixel row per CTA on 128 SMs by 6 %, and segments of 256 lost
+  // it again)
   const long long nband = (clen + kLines - 1) / kLines;
   double best = 1e300;
   for (int T = 1; T <= 64; T++) {
@@ -499,7 +523,7 @@ bool plan_pass(RingArgs& a, int alen, int clen, int r, int nsm, size_t maxSmem, 
     const long long items = nband * nseg;
     const long long g = std::min<long long>(items, nsm);
     const long long rounds = (items + g - 1) / g;
-    const double cost = (double)rounds * (seglen + a.kspan);
+    const double cost = (double)rounds * (seglen + kPos);
     if (cost < best * 0.999) {
       best = cost;
       a.seglen = seglen;
@@ -517,7 +541,12 @@ void launch_ring_pass(const RingArgs& a, int grid, const CUtensorMap& tin, uint3
                       const uint16_t* kern, int* err, cudaStream_t st) {
   // at least 120 KB, so that no second CTA (and tensor-memory allocation) shares an SM
   const size_t smem = std::max<size_t>(ring_smem(a, SPLIT).total + 1024, 120 * 1024);
-  launch_pdl(k_blur_ring<SPLIT>, dim3(grid), dim3(kRingThreads), smem, st, tin, out, a, kern, err);
+  switch (a.delta) {
+    case 0: launch_pdl(k_blur_ring<SPLIT, 0>, dim3(grid), dim3(kRingThreads), smem, st, tin, out, a, kern, err); break;
+    case 1: launch_pdl(k_blur_ring<SPLIT, 1>, dim3(grid), dim3(kRingThreads), smem, st, tin, out, a, kern, err); break;
+    case 2: launch_pdl(k_blur_ring<SPLIT, 2>, dim3(grid), dim3(kRingThreads), smem, st, tin, out, a, kern, err); break;
+    default: launch_pdl(k_blur_ring<SPLIT, 3>, dim3(grid), dim3(kRingThreads), smem, st, tin, out, a, kern, err); break;
+  }
   note_launch();
 }
 
@@ -551,7 +580,10 @@ bool ring_blur_init(size_t* maxSmem) {
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const void* ks[2] = {(const void*)k_blur_ring<true>, (const void*)k_blur_ring<false>};
+  const void* ks[8] = {(const void*)k_blur_ring<true, 0>,  (const void*)k_blur_ring<true, 1>,
+                       (const void*)k_blur_ring<true, 2>,  (const void*)k_blur_ring<true, 3>,
+                       (const void*)k_blur_ring<false, 0>, (const void*)k_blur_ring<false, 1>,
+                       (const void*)k_blur_ring<false, 2>, (const void*)k_blur_ring<false, 3>};
   for (const void* k : ks)
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {
       cudaGetLastError();
@@ -561,10 +593,22 @@ bool ring_blur_init(size_t* maxSmem) {
   return true;
 }
 
+// Row pitch (pixels) of the transposed intermediate of a blur of an image H
+// pixels high: H, or H + 4 when H * 4 bytes is a multiple of 1 KB.  Pass 1
+// writes four intermediate rows per warp store and its loads and pass 2's
+// read 32 rows per box; at a pitch of a multiple of 1 KB (4096-pixel rows:
+// 16 KB) those rows fall on the same memory channels and a 4096 x 4096 blur
+// ran 25 % slower than a 4096 x 4100 one.  16 more bytes per row spread them.
+long long ring_tmp_pitch(long long H) { return (H * 4) % 1024 == 0 ? H + 4 : H; }
+
+// Bytes of the intermediate buffer a blur of W x H pixels needs.
+long long blur_scratch_bytes(long long W, long long H) { return W * ring_tmp_pitch(H) * 4; }
+
 // Both passes (img -> tmp transposed -> img) on the ring kernels.  Returns
 // false (and launches nothing) when the image or radius is not for this path:
 // width and height must be multiples of 4 (TMA rows of whole 16-byte units
-// in both orientations) and both buffers 16-byte aligned, r in 1..128.
+// in both orientations) and both buffers 16-byte aligned, r in 1..128.  tmp
+// holds blur_scratch_bytes(W, H) bytes (W rows of ring_tmp_pitch(H) pixels).
 bool launch_blur_ring(uint32_t* img, uint32_t* tmp, long long W, long long H, int r, const uint16_t* kern,
                       bool exactF16, uint32_t oob, int nsm, size_t maxSmem, int* err, cudaStream_t st) {
   if (!g_encode || r < 1 || r > 128 || W < 4 || H < 4 || (W & 3) != 0 || (H & 3) != 0 || W > (1 << 24) ||
@@ -610,8 +654,9 @@ bool launch_blur_ring(uint32_t* img, uint32_t* tmp, long long W, long long H, in
         !plan_pass(n.a2, (int)H, (int)W, r, nsm, maxSmem, split, n.g2))
       return false;
     n.a1.oob = n.a2.oob = oob;
-    if (!encode_map(&n.m1, img, (int)W, (int)H, kRawW, kLines) ||
-        !encode_map(&n.m2, tmp, (int)H, (int)W, kRawW, kLines))
+    n.a1.opitch = (int)ring_tmp_pitch(H);  // pass 1 writes the intermediate
+    if (!encode_map(&n.m1, img, (int)W, (int)H, W, kRawW, kLines) ||
+        !encode_map(&n.m2, tmp, (int)H, (int)W, ring_tmp_pitch(H), kRawW, kLines))
       return false;
     cache[next] = n;
     pl = &cache[next];
@@ -626,6 +671,23 @@ bool launch_blur_ring(uint32_t* img, uint32_t* tmp, long long W, long long H, in
     launch_ring_pass<false>(pl->a2, pl->g2, pl->m2, img, kern, err, st);
   }
   return true;
+}
+
+// The converter trace: enable != 0 switches it on for later passes (0 off);
+// out (if not null) receives up to n values of the last traced pass, laid out
+// [group 0..1][chunk 0..255][event 0..2] (0 where nothing was recorded).
+int ring_trace(int enable, long long* out, long long n) {
+  const int on = enable != 0;
+  if (cudaMemcpyToSymbol(g_ring_trace_on, &on, sizeof(int)) != cudaSuccess) return 1;
+  if (on) {
+    static const long long zero[2 * kTraceChunks * 3] = {};
+    if (cudaMemcpyToSymbol(g_ring_trace, zero, sizeof(zero)) != cudaSuccess) return 1;
+  }
+  if (out && n > 0) {
+    const long long cnt = std::min<long long>(n, 2 * kTraceChunks * 3);
+    if (cudaMemcpyFromSymbol(out, g_ring_trace, (size_t)cnt * sizeof(long long)) != cudaSuccess) return 1;
+  }
+  return 0;
 }
 
 }  // namespace pxg

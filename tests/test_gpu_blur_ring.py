@@ -130,6 +130,29 @@ def test_ring_blur_no_device_error_flag():
     assert np.array_equal(g.to_numpy(), _chain(img, (1, 7, 40)))
 
 
+def test_ring_trace_records_the_pipeline_and_changes_nothing():
+    """pxg_ring_trace: with the trace on, the ring passes record CTA 0's
+    converter stamps (non-decreasing per chunk: wait start, wait end, stores
+    done); the bytes are the oracle's either way, and off records nothing."""
+    img = wl.premultiplied_image(12, 2048, 2048)  # CTA 0 converts ~18 chunks per pass
+    want = blur_ref(img, 20)
+    try:
+        px.ring_trace(True)
+        got, used = blur_gpu(img, 20)
+        tr = px.ring_trace(False, fetch=True)
+    finally:
+        px.ring_trace(False)
+    assert used == 3 and np.array_equal(got, want)
+    rec = tr[tr[:, :, 0] > 0]  # (chunk events) recorded by either group
+    assert len(rec) >= 8, tr[:, :24, 0]
+    assert np.all(np.diff(rec, axis=1) >= 0)
+    px.ring_trace(True)
+    px.ring_trace(False)  # enabling clears; a pass with the trace off leaves it clear
+    got2, _ = blur_gpu(img, 20)
+    assert np.array_equal(got2, want)
+    assert not px.ring_trace(False, fetch=True).any()
+
+
 def _chain(img, radii):
     ref = img.copy()
     for r in radii:
