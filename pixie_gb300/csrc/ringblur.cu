@@ -15,8 +15,8 @@
 //
 // Exactness.  A holds each 8-bit channel value v as the f16 subnormal
 // v * 2^-24 (its bit pattern is v itself); B holds integer weights, split into
-// bytes (w = 256 wh + wl, two MMAs) unless every weight of the radius is an
-// exact f16.  Every product is an integer times 2^-24, every sum a multiple
+// bytes (w = 256 wh + wl: one MMA of N = 128 whose B rows 0..63 hold wh and
+// 64..127 hold wl) unless every weight of the radius is an exact f16.  Every product is an integer times 2^-24, every sum a multiple
 // of 2^-24 below 1, exact in the f32 accumulator.  The epilogue forms
 // S * 2^-24 (S the reference's integer sum) and takes
 // floor(S / 65280) = floor(S * C) with C = 1/65280 rounded up to float32,
@@ -111,16 +111,20 @@ struct RingArgs {
 constexpr int kRawBytes = kLines * kRawW * 4;
 
 // Shared-memory layout (offsets from a 1024-aligned base).
+// An epilogue group's output tile staged for its TMA store: 64 positions (box
+// rows) x 32 lines (128 bytes, 128-byte swizzled); two per group.
+constexpr uint32_t kStageBytes = kPos * kLines * 4;
+
 struct RingSmem {
-  uint32_t raw, bhi, blo, bars, total;
+  uint32_t raw, bhi, stage, bars, total;
 };
 __host__ __device__ inline RingSmem ring_smem(const RingArgs& a, bool split) {
   RingSmem s;
   s.raw = 0;
   const uint32_t bBytes = (uint32_t)((a.kspan + 63) / 64) * kBBlockBytes;
-  s.bhi = (uint32_t)a.nraw * a.rawStride;
-  s.blo = s.bhi + bBytes;
-  s.bars = s.blo + (split ? bBytes : 0);
+  s.bhi = (uint32_t)a.nraw * a.rawStride;  // B: 64 rows per K block (128 with byte-split weights)
+  s.stage = s.bhi + (split ? 2 : 1) * bBytes;  // 1024-aligned: every region above is a multiple of 1 KB
+  s.bars = s.stage + 4 * kStageBytes;
   s.total = s.bars + (2 * kMaxRaw + 2 * kMaxRing + 2 * kMaxAcc + 1) * 8 + 16;
   return s;
 }
@@ -166,7 +170,7 @@ __device__ __forceinline__ void mma_ts_elect(uint32_t tmem_d, uint32_t tmem_a, u
 // template parameter the converters' word selection is straight-line code.
 template <bool SPLIT, int DELTA>
 __global__ void __launch_bounds__(kRingThreads, 1)
-    k_blur_ring(const __grid_constant__ CUtensorMap tin, uint32_t* __restrict__ out, const RingArgs a,
+    k_blur_ring(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout, const RingArgs a,
                 const uint16_t* __restrict__ kern, int* err) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~(uintptr_t)1023);
@@ -192,8 +196,11 @@ __global__ void __launch_bounds__(kRingThreads, 1)
     const int n = i / kpad, k = i - n * kpad, t = k - n;
     const uint32_t w = (t >= 0 && t <= 2 * r) ? kern[t] : 0u;
     if (SPLIT) {
-      *reinterpret_cast<uint16_t*>(sm + L.bhi + sw128_off(n, k, kBBlockBytes)) = f16_bits(w >> 8);
-      *reinterpret_cast<uint16_t*>(sm + L.blo + sw128_off(n, k, kBBlockBytes)) = f16_bits(w & 255u);
+      // one 128-row operand per K block: the high weight bytes in rows 0..63,
+      // the low bytes in rows 64..127, so one MMA of N = 128 forms both sums
+      // (accumulator columns [0, 64) and [64, 128))
+      *reinterpret_cast<uint16_t*>(sm + L.bhi + sw128_off(n, k, 2 * kBBlockBytes)) = f16_bits(w >> 8);
+      *reinterpret_cast<uint16_t*>(sm + L.bhi + sw128_off(kPos + n, k, 2 * kBBlockBytes)) = f16_bits(w & 255u);
     } else {
       *reinterpret_cast<uint16_t*>(sm + L.bhi + sw128_off(n, k, kBBlockBytes)) = f16_bits(w);
     }
@@ -214,6 +221,7 @@ __global__ void __launch_bounds__(kRingThreads, 1)
     mbar_init(doneBar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     tmap_prefetch(&tin);
+    tmap_prefetch(&tout);
   }
   if (warp == kMmaWarp) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(taddr_s)),
@@ -346,8 +354,9 @@ __global__ void __launch_bounds__(kRingThreads, 1)
     }
   } else if (warp == kMmaWarp) {
     // ---- MMA issuer ----
-    const uint32_t idesc = instr_desc(128, kPos);
-    const uint64_t bdh = mat_desc_sw128(base + L.bhi, 1024), bdl = mat_desc_sw128(base + L.blo, 1024);
+    const uint32_t idesc = instr_desc(128, SPLIT ? 2 * kPos : kPos);
+    const uint64_t bdh = mat_desc_sw128(base + L.bhi, 1024);
+    constexpr int kBlkShift = SPLIT ? 10 : 9;  // a K block of B is 16 KB (split) or 8 KB, in 16-byte units
     const int kn = a.kspan / 16;                 // K steps of a tile
     const uint32_t ringA = tmem + (uint32_t)kRingCol0;
     int wseg = 0, tseg = 0, acc = 0, tiles = 0;  // next chunk to wait for, the tile's first chunk, accumulator
@@ -378,15 +387,13 @@ __global__ void __launch_bounds__(kRingThreads, 1)
         const uint32_t a0 = ringA + (uint32_t)(32 * tseg);
 #pragma unroll 4
         for (int ks = 0; ks < kw; ks++) {
-          const uint64_t bo = (uint64_t)(((ks >> 2) << 9) + ((ks & 3) << 1));  // (block, 32-byte step) >> 4
+          const uint64_t bo = (uint64_t)(((ks >> 2) << kBlkShift) + ((ks & 3) << 1));  // (block, 32-byte step) >> 4
           mma_ts_elect(d, a0 + 8u * ks, bdh + bo, idesc, ks > 0);
-          if (SPLIT) mma_ts_elect(d + kPos, a0 + 8u * ks, bdl + bo, idesc, ks > 0);
         }
 #pragma unroll 4
         for (int ks = kw; ks < kn; ks++) {
-          const uint64_t bo = (uint64_t)(((ks >> 2) << 9) + ((ks & 3) << 1));
+          const uint64_t bo = (uint64_t)(((ks >> 2) << kBlkShift) + ((ks & 3) << 1));
           mma_ts_elect(d, ringA + 8u * (ks - kw), bdh + bo, idesc, 1);
-          if (SPLIT) mma_ts_elect(d + kPos, ringA + 8u * (ks - kw), bdl + bo, idesc, 1);
         }
         mma_commit_elect(tFull + 8 * acc);
         mma_commit_elect(ringEmpty + 8 * tseg);
@@ -418,11 +425,16 @@ __global__ void __launch_bounds__(kRingThreads, 1)
     const uint64_t k256 = f32x2_splat(256.0f), kq = f32x2_splat(kQuotC24), km = f32x2_splat(kMagic);
     int u = 0, acc = 0;  // tiles seen, their accumulator
     uint32_t aph = 0;
+    int mineCount = 0;  // this group's tiles so far (its staging buffer alternates)
+    // the group's first warp issues its TMA stores
+    const bool issuer = warp == kEpiWarp0 + 4 * e && lane == 0;
+    // this lane's line in the staged tile: 16-byte unit (line >> 2) of a
+    // 128-byte row, swizzled by the row (position) index mod 8
+    const uint32_t unit = (uint32_t)(j >> 2), inUnit = (uint32_t)(j & 3) * 4u;
     bool ok = true;
     for (long long it = blockIdx.x; ok && it < a.nitems; it += gridDim.x) {
       int band, s0, T, nch;
       item_geom(a, it, band, s0, T, nch);
-      const int line = kLines * band + j;
       for (int i = 0; i < T; i++) {
         const bool mine = (u & 1) == e;
         const int cacc = acc;
@@ -435,6 +447,9 @@ __global__ void __launch_bounds__(kRingThreads, 1)
         if (!mine) continue;
         const bool ready = mbar_wait(tFull + 8 * cacc, caph);
         if (!ready && lane == 0) atomicExch(err, 1);
+        // the staging buffer of this tile was last read by the store two of
+        // the group's tiles back
+        if (issuer) bulk_wait_read<1>();
         if (epi_bar_or(e, !ready)) {
           ok = false;
           break;
@@ -442,6 +457,8 @@ __global__ void __launch_bounds__(kRingThreads, 1)
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
         const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(cacc * accCols);
         const int o0 = s0 + kPos * i;
+        const uint32_t stage = base + L.stage + (uint32_t)(2 * e + (mineCount & 1)) * kStageBytes;
+        mineCount++;
 #pragma unroll
         for (int cc = 0; cc < kPos; cc += 32) {
           float hi[32], lo[32];
@@ -459,15 +476,27 @@ __global__ void __launch_bounds__(kRingThreads, 1)
             uint32_t w = __byte_perm(__byte_perm(q0, q1, 0x0040u), __byte_perm(q2, q3, 0x0040u), 0x5410u);
             w = __byte_perm(w, __shfl_xor_sync(0xffffffffu, w, 2), selA);
             w = __byte_perm(w, __shfl_xor_sync(0xffffffffu, w, 1), selB);
-            const int n = o0 + cc + t + ch;
-            if (n < a.alen && line < a.clen) out[(long long)n * a.opitch + line] = w;
+            const uint32_t row = (uint32_t)(cc + t + ch);  // position within the tile
+            asm volatile("st.shared.u32 [%0], %1;\n" ::"r"(stage + row * 128u + (((unit ^ (row & 7u)) << 4) | inUnit)),
+                         "r"(w)
+                         : "memory");
           }
         }
+        // the accumulator is free once its loads are done; the staged tile
+        // goes out as one TMA store (rows past the image and lines past the
+        // band's end are clipped by the tensor map)
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
         __syncwarp();
         if (lane == 0) mbar_arrive(tEmpty + 8 * cacc);
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        epi_bar(e);
+        if (issuer) {
+          tma_store_2d(&tout, kLines * band, o0, stage);
+          bulk_commit();
+        }
       }
     }
+    if (issuer) bulk_wait_all();  // the stores have read shared memory and reached global memory
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
@@ -481,14 +510,16 @@ PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 
 // Row-major image of W x H pixels (u32) with rows pitch pixels apart, boxes
 // of bx x by pixels.
-bool encode_map(CUtensorMap* m, const void* ptr, int W, int H, long long pitch, int bx, int by) {
+bool encode_map(CUtensorMap* m, const void* ptr, int W, int H, long long pitch, int bx, int by,
+                bool swizzle128 = false) {
   if (!g_encode) return false;
   cuuint64_t dims[2] = {(cuuint64_t)W, (cuuint64_t)H};
   cuuint64_t strides[1] = {(cuuint64_t)pitch * 4};
   cuuint32_t box[2] = {(cuuint32_t)bx, (cuuint32_t)by};
   cuuint32_t estr[2] = {1, 1};
   return g_encode(m, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<void*>(ptr), dims, strides, box, estr,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
@@ -537,15 +568,15 @@ bool plan_pass(RingArgs& a, int alen, int clen, int r, int nsm, size_t maxSmem, 
 }
 
 template <bool SPLIT>
-void launch_ring_pass(const RingArgs& a, int grid, const CUtensorMap& tin, uint32_t* out,
+void launch_ring_pass(const RingArgs& a, int grid, const CUtensorMap& tin, const CUtensorMap& tout,
                       const uint16_t* kern, int* err, cudaStream_t st) {
   // at least 120 KB, so that no second CTA (and tensor-memory allocation) shares an SM
   const size_t smem = std::max<size_t>(ring_smem(a, SPLIT).total + 1024, 120 * 1024);
   switch (a.delta) {
-    case 0: launch_pdl(k_blur_ring<SPLIT, 0>, dim3(grid), dim3(kRingThreads), smem, st, tin, out, a, kern, err); break;
-    case 1: launch_pdl(k_blur_ring<SPLIT, 1>, dim3(grid), dim3(kRingThreads), smem, st, tin, out, a, kern, err); break;
-    case 2: launch_pdl(k_blur_ring<SPLIT, 2>, dim3(grid), dim3(kRingThreads), smem, st, tin, out, a, kern, err); break;
-    default: launch_pdl(k_blur_ring<SPLIT, 3>, dim3(grid), dim3(kRingThreads), smem, st, tin, out, a, kern, err); break;
+    case 0: launch_pdl(k_blur_ring<SPLIT, 0>, dim3(grid), dim3(kRingThreads), smem, st, tin, tout, a, kern, err); break;
+    case 1: launch_pdl(k_blur_ring<SPLIT, 1>, dim3(grid), dim3(kRingThreads), smem, st, tin, tout, a, kern, err); break;
+    case 2: launch_pdl(k_blur_ring<SPLIT, 2>, dim3(grid), dim3(kRingThreads), smem, st, tin, tout, a, kern, err); break;
+    default: launch_pdl(k_blur_ring<SPLIT, 3>, dim3(grid), dim3(kRingThreads), smem, st, tin, tout, a, kern, err); break;
   }
   note_launch();
 }
@@ -626,7 +657,8 @@ bool launch_blur_ring(uint32_t* img, uint32_t* tmp, long long W, long long H, in
     bool split;
     RingArgs a1, a2;
     int g1, g2;
-    CUtensorMap m1, m2;
+    CUtensorMap m1, m2;    // pass inputs: image rows, intermediate rows
+    CUtensorMap o1, o2;    // pass outputs: intermediate, image (boxes of 32 lines x 64 positions)
   };
   static Plan cache[8];
   static int ncache = 0, next = 0;
@@ -656,7 +688,9 @@ bool launch_blur_ring(uint32_t* img, uint32_t* tmp, long long W, long long H, in
     n.a1.oob = n.a2.oob = oob;
     n.a1.opitch = (int)ring_tmp_pitch(H);  // pass 1 writes the intermediate
     if (!encode_map(&n.m1, img, (int)W, (int)H, W, kRawW, kLines) ||
-        !encode_map(&n.m2, tmp, (int)H, (int)W, ring_tmp_pitch(H), kRawW, kLines))
+        !encode_map(&n.m2, tmp, (int)H, (int)W, ring_tmp_pitch(H), kRawW, kLines) ||
+        !encode_map(&n.o1, tmp, (int)H, (int)W, ring_tmp_pitch(H), kLines, kPos, true) ||
+        !encode_map(&n.o2, img, (int)W, (int)H, W, kLines, kPos, true))
       return false;
     cache[next] = n;
     pl = &cache[next];
@@ -664,11 +698,11 @@ bool launch_blur_ring(uint32_t* img, uint32_t* tmp, long long W, long long H, in
     if (ncache < 8) ncache++;
   }
   if (split) {
-    launch_ring_pass<true>(pl->a1, pl->g1, pl->m1, tmp, kern, err, st);
-    launch_ring_pass<true>(pl->a2, pl->g2, pl->m2, img, kern, err, st);
+    launch_ring_pass<true>(pl->a1, pl->g1, pl->m1, pl->o1, kern, err, st);
+    launch_ring_pass<true>(pl->a2, pl->g2, pl->m2, pl->o2, kern, err, st);
   } else {
-    launch_ring_pass<false>(pl->a1, pl->g1, pl->m1, tmp, kern, err, st);
-    launch_ring_pass<false>(pl->a2, pl->g2, pl->m2, img, kern, err, st);
+    launch_ring_pass<false>(pl->a1, pl->g1, pl->m1, pl->o1, kern, err, st);
+    launch_ring_pass<false>(pl->a2, pl->g2, pl->m2, pl->o2, kern, err, st);
   }
   return true;
 }
