@@ -27,6 +27,7 @@ struct pxg_image {
   int64_t width, height;
   int owned;
   bool exported = false;  // pxg_image_device_ptr handed the address out: it must not change
+  long long cap = 0;      // bytes allocated at data (owned images)
   cudaEvent_t copy_ev = nullptr;  // the last asynchronous upload or download of the image
   bool copy_pending = false;      // ... which no compute on the image has waited for yet
   cudaEvent_t compute_ev = nullptr;  // after the last compute call that named the image
@@ -1561,7 +1562,10 @@ pxg_image* pxg_new_image(int64_t width, int64_t height) {
   guarded([&] {
     if (width <= 0 || height <= 0) throw ApiError{"Image width and height must be > 0"};
     pxg_image* im = new pxg_image{nullptr, width, height, 1};
-    cudaError_t e = cudaMalloc((void**)&im->data, (size_t)(width * height * 4));
+    // room for a blur's padded intermediate too, so that the buffers a blur
+    // swaps between an image and the scratch buffer keep serving both
+    im->cap = blur_scratch_bytes(width, height);
+    cudaError_t e = cudaMalloc((void**)&im->data, (size_t)im->cap);
     if (e != cudaSuccess) {
       delete im;
       throw ApiError{std::string("CUDA error: ") + cudaGetErrorString(e)};
@@ -2855,10 +2859,9 @@ int pxg_image_blur(pxg_image* im, float radius, const float* oob) {
     static const float zero[4] = {0, 0, 0, 0};
     uint32_t o = color_to_rgbx(oob ? oob : zero);
     weights_for(r);
-    const long long bytes = im->width * im->height * 4;
-    // radii the small-radius kernels take need an image-sized buffer; larger
-    // ones the tensor-core passes' padded intermediate
-    const long long tmp_bytes = r <= kSmallBlurMaxR ? bytes : blur_scratch_bytes(im->width, im->height);
+    // an image-sized buffer for the small-radius kernels, the tensor-core
+    // passes' padded intermediate for the others: one size serves both
+    const long long tmp_bytes = blur_scratch_bytes(im->width, im->height);
     uint32_t* tmp = (uint32_t*)scratch(tmp_bytes);
     Timed t;
     // an image the library allocated, whose address nobody holds, may take
@@ -2868,7 +2871,7 @@ int pxg_image_blur(pxg_image* im, float radius, const float* oob) {
     const bool swap_ok = im->owned && !im->exported;
     if (blur_dispatch((uint32_t*)im->data, tmp, tmp_bytes, im->width, im->height, r, o, swap_ok)) {
       std::swap(im->data, g.scratch);
-      g.scratch_cap = bytes;
+      std::swap(im->cap, g.scratch_cap);
     }
     CU(cudaGetLastError());
     t.done();

@@ -6,14 +6,70 @@
 // vectors (4 pixels) when both row layouts allow it; the blend is a
 // compile-time template per mode so the inner loop carries no dispatch.
 #include <atomic>
+#include <initializer_list>
+#include <vector>
 
 #include "pxg_device.cuh"
 #include "raster.cuh"
 
 namespace pxg {
 
+// Hazards between kernels launched back to back with programmatic dependent
+// launch on one stream.  A kernel launched "late" (its `late` argument set)
+// does its work without waiting for the kernel before it and executes
+// griddepcontrol.wait only before it exits, so its completion still implies
+// the completion of every kernel before it; consecutive independent draws and
+// blurs then overlap each other's ramp and drain.  A kernel may go late only
+// when nothing it writes is read or written, and nothing it reads is written,
+// by a kernel that may still be running: every kernel launched since the last
+// one that waited at its start (tracked below, per stream).  Any launch that
+// does not declare its buffers (note_launch without dep_late) makes the set
+// unknown, so the next kernel waits at its start.  The library's callers hold
+// its lock, which serialises these calls.
+namespace {
+struct InFlight {
+  cudaStream_t st = nullptr;
+  bool unknown = true;
+  std::vector<Span> writes, reads;
+};
+InFlight g_inflight;
+bool g_declared = false;  // the next note_launch is the launch dep_late described
+bool overlap(const Span& a, const Span& b) {
+  const char *pa = static_cast<const char*>(a.p), *pb = static_cast<const char*>(b.p);
+  return a.n && b.n && pa < pb + b.n && pb < pa + a.n;
+}
+bool hits(const Span& x, const std::vector<Span>& set) {
+  for (const Span& y : set)
+    if (overlap(x, y)) return true;
+  return false;
+}
+}  // namespace
+
+bool dep_late(cudaStream_t st, std::initializer_list<Span> writes, std::initializer_list<Span> reads) {
+  InFlight& f = g_inflight;
+  bool late = !f.unknown && f.st == st && f.writes.size() + f.reads.size() < 64;
+  for (const Span& w : writes) late = late && !hits(w, f.writes) && !hits(w, f.reads);
+  for (const Span& r : reads) late = late && !hits(r, f.writes);
+  if (!late) {  // this kernel waits at its start: nothing launched before it still runs after that
+    f.writes.clear();
+    f.reads.clear();
+  }
+  f.st = st;
+  f.unknown = false;
+  f.writes.insert(f.writes.end(), writes.begin(), writes.end());
+  f.reads.insert(f.reads.end(), reads.begin(), reads.end());
+  g_declared = true;
+  return late;
+}
+
 static std::atomic<unsigned long long> g_launches{0};
-void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void note_launch() {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  if (g_declared)
+    g_declared = false;
+  else
+    g_inflight.unknown = true;
+}
 unsigned long long launch_count() { return g_launches.load(); }
 
 template <int MODE>
@@ -34,9 +90,9 @@ template <int MODE>
 __global__ void __launch_bounds__(256) k_draw(uint32_t* __restrict__ a, const uint32_t* __restrict__ b,
                                               long long Wa, long long Wb, long long ax, long long ay,
                                               long long bx, long long by, long long w, long long h,
-                                              const uint8_t* tbl, int vec) {
+                                              const uint8_t* tbl, int vec, int late) {
   pdl_trigger();
-  pdl_wait();
+  if (!late) pdl_wait();
   if (vec) {
     // One 16-byte quad (4 pixels) per thread per iteration: the blend is
     // inlined four times, not sixteen, so the float modes keep their code in
@@ -82,15 +138,16 @@ __global__ void __launch_bounds__(256) k_draw(uint32_t* __restrict__ a, const ui
         *pa = draw_px<MODE>(tbl, *pa, b[(by + r) * Wb + bx + c]);
       }
     }
-    return;
+  } else {
+    const long long n = w * h;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+      long long r = i / w, c = i - r * w;
+      uint32_t* pa = a + (ay + r) * Wa + ax + c;
+      *pa = draw_px<MODE>(tbl, *pa, b[(by + r) * Wb + bx + c]);
+    }
   }
-  const long long n = w * h;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    long long r = i / w, c = i - r * w;
-    uint32_t* pa = a + (ay + r) * Wa + ax + c;
-    *pa = draw_px<MODE>(tbl, *pa, b[(by + r) * Wb + bx + c]);
-  }
+  if (late) pdl_wait();  // completes only after the kernel before it
 }
 
 // MaskBlend zeroes the destination outside the overlap (images.nim:473-520):
@@ -99,9 +156,9 @@ __global__ void __launch_bounds__(256) k_draw(uint32_t* __restrict__ a, const ui
 // visited.
 __global__ void __launch_bounds__(256) k_clear_outside(uint32_t* a, long long Wa, long long Ha,
                                                        long long x0, long long y0, long long x1,
-                                                       long long y1) {
+                                                       long long y1, int late) {
   pdl_trigger();
-  pdl_wait();
+  if (!late) pdl_wait();
   const long long top = y0 * Wa, bottom = (Ha - y1) * Wa, side = x0 + (Wa - x1), mid = (y1 - y0) * side;
   const long long n = top + bottom + mid;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -115,6 +172,7 @@ __global__ void __launch_bounds__(256) k_clear_outside(uint32_t* a, long long Wa
       a[(y0 + r) * Wa + (c < x0 ? c : x1 + (c - x0))] = 0u;
     }
   }
+  if (late) pdl_wait();
 }
 
 // fillUnsafe over the whole image (internal.nim:55-66)
@@ -139,7 +197,7 @@ __global__ void k_blend_pixels(int mode, const uint8_t* tbl, const uint32_t* bd,
 }
 
 typedef void (*DrawKernel)(uint32_t*, const uint32_t*, long long, long long, long long, long long,
-                           long long, long long, long long, long long, const uint8_t*, int);
+                           long long, long long, long long, long long, const uint8_t*, int, int);
 
 template <int M>
 struct DrawTable {
@@ -201,13 +259,16 @@ void launch_draw(uint32_t* a, const uint32_t* b, long long Wa, long long Ha, lon
     if (outside > 0) {
       long long cb = (outside + 255) / 256;
       if (cb > (long long)nsm * 4) cb = (long long)nsm * 4;
-      launch_pdl(k_clear_outside, dim3((unsigned)cb), dim3(256), 0, st, a, Wa, Ha, ax, ay, ax + w, ay + h);
+      const int late = dep_late(st, {Span{a, (size_t)(Wa * Ha * 4)}}, {});
+      launch_pdl(k_clear_outside, dim3((unsigned)cb), dim3(256), 0, st, a, Wa, Ha, ax, ay, ax + w, ay + h, late);
       note_launch();
     }
   }
   if (w > 0 && h > 0) {
+    // the destination is read and written, the source read (the blend tables are constant)
+    const int late = dep_late(st, {Span{a, (size_t)(Wa * Ha * 4)}}, {Span{b, (size_t)(Wb * Hb * 4)}});
     launch_pdl(draw_kernel(mode), dim3((unsigned)blocks), dim3(256), 0, st, a, b, Wa, Wb, ax, ay, xStart, yStart, w,
-               h, tbl, vec);
+               h, tbl, vec, late);
     note_launch();
   }
 }

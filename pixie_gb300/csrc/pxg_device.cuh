@@ -5,6 +5,7 @@
 // operation order and rounding.
 #pragma once
 #include <cstdint>
+#include <initializer_list>
 #include <utility>
 
 #include <cuda_runtime.h>
@@ -34,6 +35,16 @@ __device__ __forceinline__ uint32_t pack(uint32_t r, uint32_t g, uint32_t b, uin
 // an ordinary launch.
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// A device buffer a kernel reads or writes.
+struct Span {
+  const void* p;
+  size_t n;
+};
+// Whether the kernel about to be launched on st may run without waiting for
+// the kernel before it (and wait only before it exits): true when its
+// buffers are disjoint from those of every kernel that may still be running.
+// Records them; the launch's note_launch follows.  Defined in composite.cu.
+bool dep_late(cudaStream_t st, std::initializer_list<Span> writes, std::initializer_list<Span> reads);
 template <class... KArgs, class... Args>
 inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
                               Args&&... args) {
