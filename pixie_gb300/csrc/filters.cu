@@ -473,7 +473,7 @@ void launch_spread(uint32_t* img, uint8_t* a0, uint8_t* a1, long long W, long lo
 constexpr int kShadowTile = 64, kShadowHalo = 32;
 __global__ void __launch_bounds__(1024) k_shadow_tile(const uint32_t* __restrict__ src, uint32_t* __restrict__ out,
                                                      int W, int H, int ox, int oy, int m, int grow, int r,
-                                                     const uint16_t* __restrict__ kern, uint32_t color) {
+                                                     const uint16_t* __restrict__ kern, uint32_t color, int late) {
   extern __shared__ __align__(16) unsigned char sh[];
   const int h = m + r, S = kShadowTile + 2 * h;  // staged side
   unsigned char* b0 = sh;
@@ -482,7 +482,7 @@ __global__ void __launch_bounds__(1024) k_shadow_tile(const uint32_t* __restrict
   const int gx0 = blockIdx.x * kShadowTile - h, gy0 = blockIdx.y * kShadowTile - h;  // staged [0][0]
   const int tid = threadIdx.x, T = blockDim.x;
   pdl_trigger();
-  pdl_wait();
+  if (!late) pdl_wait();
   if (r > 0)  // without a blur there is no weight table
     for (int k = tid; k <= 2 * r; k += T) wk[k] = kern[k];
   const unsigned char neutral = (m > 0 && !grow) ? 255 : 0;
@@ -553,6 +553,7 @@ __global__ void __launch_bounds__(1024) k_shadow_tile(const uint32_t* __restrict
     const uint32_t k = fin[(h + y) * S + h + x];
     out[(long long)gy * W + gx] = pack((c.r * k) / 255, (c.g * k) / 255, (c.b * k) / 255, (c.a * k) / 255);
   }
+  if (late) pdl_wait();
 }
 size_t shadow_tile_smem(int h) {
   const int S = kShadowTile + 2 * h;
@@ -567,8 +568,9 @@ void launch_shadow(const uint32_t* src, uint32_t* out, uint8_t* a0, uint8_t* a1,
   if (m + r <= kShadowHalo && W <= (1 << 24) && H <= (1 << 24) && ox > -(1 << 24) && ox < (1 << 24) &&
       oy > -(1 << 24) && oy < (1 << 24)) {
     const dim3 g((unsigned)((W + kShadowTile - 1) / kShadowTile), (unsigned)((H + kShadowTile - 1) / kShadowTile));
+    const int late = dep_late(st, {Span{out, (size_t)(n * 4)}}, {Span{src, (size_t)(n * 4)}});
     launch_pdl(k_shadow_tile, g, dim3(1024), shadow_tile_smem(m + r), st, src, out, (int)W, (int)H, (int)ox, (int)oy,
-               m, (int)(s > 0), r, kern, color);
+               m, (int)(s > 0), r, kern, color, late);
     note_launch();
     return;
   }

@@ -171,7 +171,7 @@ __device__ __forceinline__ void mma_ts_elect(uint32_t tmem_d, uint32_t tmem_a, u
 template <bool SPLIT, int DELTA>
 __global__ void __launch_bounds__(kRingThreads, 1)
     k_blur_ring(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout, const RingArgs a,
-                const uint16_t* __restrict__ kern, int* err) {
+                const uint16_t* __restrict__ kern, int* err, int late) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~(uintptr_t)1023);
   constexpr int kAcc = SPLIT ? 2 : 4;
@@ -235,7 +235,8 @@ __global__ void __launch_bounds__(kRingThreads, 1)
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   // the weights and barriers above read only constant data; the input
   // (written by the previous kernel) and the output are touched only after it
-  pdl_wait();
+  // -- unless nothing still running touches them (late: wait before exiting)
+  if (!late) pdl_wait();
   const uint32_t tmem = *taddr_s;
 
   if (warp == 0) {
@@ -504,6 +505,7 @@ __global__ void __launch_bounds__(kRingThreads, 1)
   if (warp == kMmaWarp)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemCols)
                  : "memory");
+  if (late) pdl_wait();
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
@@ -569,14 +571,14 @@ bool plan_pass(RingArgs& a, int alen, int clen, int r, int nsm, size_t maxSmem, 
 
 template <bool SPLIT>
 void launch_ring_pass(const RingArgs& a, int grid, const CUtensorMap& tin, const CUtensorMap& tout,
-                      const uint16_t* kern, int* err, cudaStream_t st) {
+                      const uint16_t* kern, int* err, int late, cudaStream_t st) {
   // at least 120 KB, so that no second CTA (and tensor-memory allocation) shares an SM
   const size_t smem = std::max<size_t>(ring_smem(a, SPLIT).total + 1024, 120 * 1024);
   switch (a.delta) {
-    case 0: launch_pdl(k_blur_ring<SPLIT, 0>, dim3(grid), dim3(kRingThreads), smem, st, tin, tout, a, kern, err); break;
-    case 1: launch_pdl(k_blur_ring<SPLIT, 1>, dim3(grid), dim3(kRingThreads), smem, st, tin, tout, a, kern, err); break;
-    case 2: launch_pdl(k_blur_ring<SPLIT, 2>, dim3(grid), dim3(kRingThreads), smem, st, tin, tout, a, kern, err); break;
-    default: launch_pdl(k_blur_ring<SPLIT, 3>, dim3(grid), dim3(kRingThreads), smem, st, tin, tout, a, kern, err); break;
+    case 0: launch_pdl(k_blur_ring<SPLIT, 0>, dim3(grid), dim3(kRingThreads), smem, st, tin, tout, a, kern, err, late); break;
+    case 1: launch_pdl(k_blur_ring<SPLIT, 1>, dim3(grid), dim3(kRingThreads), smem, st, tin, tout, a, kern, err, late); break;
+    case 2: launch_pdl(k_blur_ring<SPLIT, 2>, dim3(grid), dim3(kRingThreads), smem, st, tin, tout, a, kern, err, late); break;
+    default: launch_pdl(k_blur_ring<SPLIT, 3>, dim3(grid), dim3(kRingThreads), smem, st, tin, tout, a, kern, err, late); break;
   }
   note_launch();
 }
@@ -697,13 +699,17 @@ bool launch_blur_ring(uint32_t* img, uint32_t* tmp, long long W, long long H, in
     next = (next + 1) % 8;
     if (ncache < 8) ncache++;
   }
-  if (split) {
-    launch_ring_pass<true>(pl->a1, pl->g1, pl->m1, pl->o1, kern, err, st);
-    launch_ring_pass<true>(pl->a2, pl->g2, pl->m2, pl->o2, kern, err, st);
-  } else {
-    launch_ring_pass<false>(pl->a1, pl->g1, pl->m1, pl->o1, kern, err, st);
-    launch_ring_pass<false>(pl->a2, pl->g2, pl->m2, pl->o2, kern, err, st);
-  }
+  const Span im{img, (size_t)(W * H * 4)}, tm{tmp, (size_t)blur_scratch_bytes(W, H)};
+  const int late1 = dep_late(st, {tm}, {im});  // pass 1: image rows -> intermediate
+  if (split)
+    launch_ring_pass<true>(pl->a1, pl->g1, pl->m1, pl->o1, kern, err, late1, st);
+  else
+    launch_ring_pass<false>(pl->a1, pl->g1, pl->m1, pl->o1, kern, err, late1, st);
+  const int late2 = dep_late(st, {im}, {tm});  // pass 2 (always waits: it reads pass 1's output)
+  if (split)
+    launch_ring_pass<true>(pl->a2, pl->g2, pl->m2, pl->o2, kern, err, late2, st);
+  else
+    launch_ring_pass<false>(pl->a2, pl->g2, pl->m2, pl->o2, kern, err, late2, st);
   return true;
 }
 

@@ -203,7 +203,7 @@ constexpr int kFTW = 128, kFTH = 64;  // tile: 128 columns x 64 rows
 template <int R>
 __global__ void __launch_bounds__(256) k_blur_fused(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
                                                     int W, int H, const uint16_t* __restrict__ kern, uint32_t oob,
-                                                    int vec) {
+                                                    int vec, int late) {
   constexpr int NI = kOut + 2 * R;
   constexpr int D = (4 - (R & 3)) & 3;
   constexpr int NC = (D + NI + 3) / 4;
@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(256) k_blur_fused(const uint32_t* __restrict__
   }
   const uint64_t nb = f2_pack(-kBias, -kBias), kq = f2_pack(kQuotC, kQuotC), km = f2_pack(kMagic, kMagic);
   const int tx0 = blockIdx.x * kFTW, ty0 = blockIdx.y * kFTH;
-  pdl_wait();
+  if (!late) pdl_wait();
   // X pass: (row, 8-pixel group) tasks over the staged rows
   constexpr int GPR = kFTW / kOut;  // groups per staged row
   for (int task = threadIdx.x; task < ROWS * GPR; task += blockDim.x) {
@@ -298,6 +298,7 @@ __global__ void __launch_bounds__(256) k_blur_fused(const uint32_t* __restrict__
     for (int o = 0; o < kOut; o++, q += W)
       if (y0 + o < H) __stcs(q, quot_px(arg[o], aba[o], kq, km));
   }
+  if (late) pdl_wait();
 }
 
 template <int R>
@@ -305,7 +306,9 @@ void launch_fused(const uint32_t* in, uint32_t* out, int W, int H, const uint16_
                   cudaStream_t st) {
   const int vec = (W % 4 == 0) && ((reinterpret_cast<uintptr_t>(in) & 15) == 0);
   const dim3 grid((unsigned)((W + kFTW - 1) / kFTW), (unsigned)((H + kFTH - 1) / kFTH));
-  launch_pdl(k_blur_fused<R>, grid, dim3(256), 0, st, in, out, W, H, kern, oob, vec);
+  const size_t bytes = (size_t)W * (size_t)H * 4;
+  const int late = dep_late(st, {Span{out, bytes}}, {Span{in, bytes}});
+  launch_pdl(k_blur_fused<R>, grid, dim3(256), 0, st, in, out, W, H, kern, oob, vec, late);
   note_launch();
 }
 
