@@ -341,12 +341,16 @@ void init_locked(int device) {
   CU(cudaStreamCreateWithFlags(&g.h2d, cudaStreamNonBlocking));
   CU(cudaStreamCreateWithFlags(&g.d2h, cudaStreamNonBlocking));
   CU(cudaEventCreateWithFlags(&g.compute_ev, cudaEventDisableTiming));
-  // the straight-alpha table (256 x 256 bytes), then v / 255.0f for v = 0..255
+  // the straight-alpha table (256 x 256 bytes), then v / 255.0f for
+  // v = 0..255, then SoftLight's D of that value (W3C: ((16 cb - 12) cb + 4) cb
+  // for cb <= 0.25, else sqrt(cb); float operations in this order, uncontracted)
   std::vector<uint8_t> t(kTblBytes);
   straight_alpha_table(t.data());
   for (int v = 0; v < 256; v++) {
     const float f = (float)v / 255.0f;
     memcpy(t.data() + kTblUnitOff + 4 * v, &f, 4);
+    const float d = f <= 0.25f ? ((16.0f * f - 12.0f) * f + 4.0f) * f : sqrtf(f);
+    memcpy(t.data() + kTblSoftOff + 4 * v, &d, 4);
   }
   CU(cudaMalloc(&g.tbl, kTblBytes));
   CU(cudaMemcpy(g.tbl, t.data(), kTblBytes, cudaMemcpyHostToDevice));

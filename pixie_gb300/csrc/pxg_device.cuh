@@ -142,8 +142,10 @@ __device__ __forceinline__ uint32_t premul8(uint32_t sv) {  // internal.nim:86-9
   return pack((s.r * s.a + 127) / 255, (s.g * s.a + 127) / 255, (s.b * s.a + 127) / 255, s.a);
 }
 // The device table: the straight-alpha table (256 x 256 bytes, row = alpha),
-// then 256 floats v / 255.0f (the float division, done once on the host).
-constexpr size_t kTblUnitOff = 65536, kTblBytes = 65536 + 1024;
+// then 256 floats v / 255.0f (the float division, done once on the host),
+// then SoftLight's D(cb) for cb = v / 255.0f (W3C: a cubic for cb <= 0.25,
+// else sqrt(cb); the same float operations, done once on the host).
+constexpr size_t kTblUnitOff = 65536, kTblSoftOff = 65536 + 1024, kTblBytes = 65536 + 2048;
 
 __device__ __forceinline__ float small_to_f(uint32_t x) {  // exact for x < 2^23
   return __uint_as_float(0x4B000000u | x) - 8388608.0f;
@@ -154,11 +156,29 @@ __device__ __forceinline__ Px straight8(const uint8_t* tbl, uint32_t v) {
   const uint8_t* row = tbl + p.a * 256;
   return Px{row[p.r], row[p.g], row[p.b], p.a};
 }
+// round(c * 255) half away from zero, clamped to 0..255 (0 for NaN), without
+// the conversion unit: for every float w in (0, 255], round(w) equals
+// floor(w + 0.5) with the sum rounded toward zero (checked exhaustively over
+// all 1.13e9 such floats), and adding 1.5 * 2^23 rounding down leaves that
+// floor in the low mantissa bits.
 __device__ __forceinline__ uint32_t unit_to_u8(float c) {
-  float v = roundf(c * 255.0f);
-  if (!(v > 0.0f)) return 0u;
-  if (v > 255.0f) return 255u;
-  return (uint32_t)v;
+  const float w = c * 255.0f;
+  if (!(w > 0.0f)) return 0u;
+  const float t = __fadd_rz(fminf(w, 255.0f), 0.5f);
+  return __float_as_uint(__fadd_rd(t, 12582912.0f)) - 0x4B400000u;
+}
+
+// n / d rounded to nearest from y = RN(1/d): q = RN(n y) is within one ulp of
+// n / d, r = n - q d is exact (one fused multiply-add), and RN(q + r y) is
+// the correctly rounded quotient (Markstein, IBM J. Res. Dev. 34(1), 1990;
+// Muller et al., Handbook of Floating-Point Arithmetic, the correction step of
+// Newton-Raphson division).  One reciprocal serves the three channels'
+// divisions by the same denominator.  For the finite normal operands of the
+// blend formulas; 0 / 0 gives NaN as the IEEE division does.
+__device__ __forceinline__ float div_rcp(float n, float d, float y) {
+  const float q = n * y;
+  const float r = fmaf(-q, d, n);
+  return fmaf(r, y, q);
 }
 
 // chroma float modes (UNPINNED, W3C Compositing Level 1; same operation order
@@ -172,17 +192,17 @@ __device__ __forceinline__ F3 clipColor(F3 c) {
   float n = fminf(c.r, fminf(c.g, c.b));
   float x = fmaxf(c.r, fmaxf(c.g, c.b));
   if (n < 0.0f) {
-    float d = l - n;
-    c.r = l + ((c.r - l) * l) / d;
-    c.g = l + ((c.g - l) * l) / d;
-    c.b = l + ((c.b - l) * l) / d;
+    const float d = l - n, y = __frcp_rn(d);
+    c.r = l + div_rcp((c.r - l) * l, d, y);
+    c.g = l + div_rcp((c.g - l) * l, d, y);
+    c.b = l + div_rcp((c.b - l) * l, d, y);
   }
   if (x > 1.0f) {
-    float d = x - l;
-    float k = 1.0f - l;
-    c.r = l + ((c.r - l) * k) / d;
-    c.g = l + ((c.g - l) * k) / d;
-    c.b = l + ((c.b - l) * k) / d;
+    const float d = x - l, y = __frcp_rn(d);
+    const float k = 1.0f - l;
+    c.r = l + div_rcp((c.r - l) * k, d, y);
+    c.g = l + div_rcp((c.g - l) * k, d, y);
+    c.b = l + div_rcp((c.b - l) * k, d, y);
   }
   return c;
 }
@@ -213,10 +233,11 @@ __device__ __forceinline__ F3 setSat(F3 c, float s) {
   return F3{imax == 0 ? mx : (imid == 0 ? mid : 0.0f), imax == 1 ? mx : (imid == 1 ? mid : 0.0f),
             imax == 2 ? mx : (imid == 2 ? mid : 0.0f)};
 }
-__device__ __forceinline__ float softLight1(float cb, float cs) {
+// W3C SoftLight of one channel; dsl[v] = D(v / 255) (the table above), v the
+// backdrop's straight 8-bit value
+__device__ __forceinline__ float softLight1(float cb, float cs, const float* dsl, uint32_t v) {
   if (cs <= 0.5f) return cb - ((1.0f - 2.0f * cs) * cb) * (1.0f - cb);
-  float d = cb <= 0.25f ? ((16.0f * cb - 12.0f) * cb + 4.0f) * cb : sqrtf(cb);
-  return cb + (2.0f * cs - 1.0f) * (d - cb);
+  return cb + (2.0f * cs - 1.0f) * (dsl[v] - cb);
 }
 // One float mode, inlined where the mode is a compile-time constant (draw).
 template <int MODE>
@@ -225,13 +246,15 @@ __device__ __forceinline__ uint32_t blendFloatT(const uint8_t* tbl, uint32_t bp,
 static __device__ __noinline__ uint32_t blendFloat(const uint8_t* tbl, uint32_t bp, uint32_t sp, int mode) {
   Px b8 = straight8(tbl, bp), s8 = straight8(tbl, sp);
   const float* u = reinterpret_cast<const float*>(tbl + kTblUnitOff);  // u[v] = v / 255.0f
+  const float* dsl = reinterpret_cast<const float*>(tbl + kTblSoftOff);
   F3 cb{u[b8.r], u[b8.g], u[b8.b]};
   F3 cs{u[s8.r], u[s8.g], u[s8.b]};
   float ab = u[b8.a], as = u[s8.a];
   F3 m;
   switch (mode) {
     case kSoftLight:
-      m = F3{softLight1(cb.r, cs.r), softLight1(cb.g, cs.g), softLight1(cb.b, cs.b)};
+      m = F3{softLight1(cb.r, cs.r, dsl, b8.r), softLight1(cb.g, cs.g, dsl, b8.g),
+             softLight1(cb.b, cs.b, dsl, b8.b)};
       break;
     case kHue: m = setLum(setSat(cs, sat3(cb)), lum3(cb)); break;
     case kSaturation: m = setLum(setSat(cb, sat3(cs)), lum3(cb)); break;
@@ -244,9 +267,10 @@ static __device__ __noinline__ uint32_t blendFloat(const uint8_t* tbl, uint32_t 
   float csr = (1.0f - ab) * cs.r + ab * m.r;
   float csg = (1.0f - ab) * cs.g + ab * m.g;
   float csb = (1.0f - ab) * cs.b + ab * m.b;
-  float orr = (as * csr + k * cb.r) / ao;
-  float og = (as * csg + k * cb.g) / ao;
-  float ob = (as * csb + k * cb.b) / ao;
+  const float yo = __frcp_rn(ao);
+  float orr = div_rcp(as * csr + k * cb.r, ao, yo);
+  float og = div_rcp(as * csg + k * cb.g, ao, yo);
+  float ob = div_rcp(as * csb + k * cb.b, ao, yo);
   return premul8(pack(unit_to_u8(orr), unit_to_u8(og), unit_to_u8(ob), unit_to_u8(ao)));
 }
 
@@ -255,13 +279,15 @@ __device__ __forceinline__ uint32_t blendFloatT(const uint8_t* tbl, uint32_t bp,
   constexpr int mode = MODE;
   Px b8 = straight8(tbl, bp), s8 = straight8(tbl, sp);
   const float* u = reinterpret_cast<const float*>(tbl + kTblUnitOff);  // u[v] = v / 255.0f
+  const float* dsl = reinterpret_cast<const float*>(tbl + kTblSoftOff);
   F3 cb{u[b8.r], u[b8.g], u[b8.b]};
   F3 cs{u[s8.r], u[s8.g], u[s8.b]};
   float ab = u[b8.a], as = u[s8.a];
   F3 m;
   switch (mode) {
     case kSoftLight:
-      m = F3{softLight1(cb.r, cs.r), softLight1(cb.g, cs.g), softLight1(cb.b, cs.b)};
+      m = F3{softLight1(cb.r, cs.r, dsl, b8.r), softLight1(cb.g, cs.g, dsl, b8.g),
+             softLight1(cb.b, cs.b, dsl, b8.b)};
       break;
     case kHue: m = setLum(setSat(cs, sat3(cb)), lum3(cb)); break;
     case kSaturation: m = setLum(setSat(cb, sat3(cs)), lum3(cb)); break;
@@ -274,9 +300,10 @@ __device__ __forceinline__ uint32_t blendFloatT(const uint8_t* tbl, uint32_t bp,
   float csr = (1.0f - ab) * cs.r + ab * m.r;
   float csg = (1.0f - ab) * cs.g + ab * m.g;
   float csb = (1.0f - ab) * cs.b + ab * m.b;
-  float orr = (as * csr + k * cb.r) / ao;
-  float og = (as * csg + k * cb.g) / ao;
-  float ob = (as * csb + k * cb.b) / ao;
+  const float yo = __frcp_rn(ao);
+  float orr = div_rcp(as * csr + k * cb.r, ao, yo);
+  float og = div_rcp(as * csg + k * cb.g, ao, yo);
+  float ob = div_rcp(as * csb + k * cb.b, ao, yo);
   return premul8(pack(unit_to_u8(orr), unit_to_u8(og), unit_to_u8(ob), unit_to_u8(ao)));
 }
 
