@@ -827,9 +827,9 @@ def run_scene(px, wl, seed=7, n_paths=2000, size=1024, reps=3):
 # DRAM traffic per operation (dram__bytes_read.sum + dram__bytes_write.sum,
 # summed over the operation's launches) from ncu captures of the same
 # kernels: a blur of 4096x4096 at radius 16 or 64 = the two tensor-core ring
-# passes (python bench.py --case blur16 / blur64).
-TRAFFIC = {"blur:16": 67246336 + 16806656 + 67213312 + 13801984,
-           "blur:64": 67231232 + 17640192 + 67214080 + 17206528}
+# passes (python bench.py --case blur16 / blur64, the first two launches).
+TRAFFIC = {"blur:16": 67226368 + 13997312 + 67230464 + 12313856,
+           "blur:64": 67218432 + 14129920 + 67217664 + 12249088}
 
 
 # -- CPU baseline / reference arm ----------------------------------------------------------
