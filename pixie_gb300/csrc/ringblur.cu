@@ -66,7 +66,7 @@ void note_launch();
 // tensor-memory stores -- where a pass's time goes between the roles.
 // (The trace's never-taken branch in the converter loop is also what lets the
 // compiler keep that loop's bookkeeping on the uniform datapath: without it
-// a 4096 x 4096 blur measured 25 % slower, with 5x the branch and 1/50 the
+// a 4096 x 4096 blur measured 25 % slower, with 3x the branch and 1/50 of the
 // uniform-pipe instructions.)
 constexpr int kTraceChunks = 256;
 __device__ int g_ring_trace_on;
