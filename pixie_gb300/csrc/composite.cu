@@ -91,8 +91,7 @@ __global__ void __launch_bounds__(256) k_draw(uint32_t* __restrict__ a, const ui
                                               long long Wa, long long Wb, long long ax, long long ay,
                                               long long bx, long long by, long long w, long long h,
                                               const uint8_t* tbl, int vec, int late) {
-  pdl_trigger();
-  if (!late) pdl_wait();
+  pdl_late_entry(late);
   if (vec) {
     // One 16-byte quad (4 pixels) per thread per iteration: the blend is
     // inlined four times, not sixteen, so the float modes keep their code in
@@ -147,7 +146,7 @@ __global__ void __launch_bounds__(256) k_draw(uint32_t* __restrict__ a, const ui
       *pa = draw_px<MODE>(tbl, *pa, b[(by + r) * Wb + bx + c]);
     }
   }
-  if (late) pdl_wait();  // completes only after the kernel before it
+  pdl_late_exit(late);  // completes only after the kernel before it
 }
 
 // MaskBlend zeroes the destination outside the overlap (images.nim:473-520):
@@ -157,8 +156,7 @@ __global__ void __launch_bounds__(256) k_draw(uint32_t* __restrict__ a, const ui
 __global__ void __launch_bounds__(256) k_clear_outside(uint32_t* a, long long Wa, long long Ha,
                                                        long long x0, long long y0, long long x1,
                                                        long long y1, int late) {
-  pdl_trigger();
-  if (!late) pdl_wait();
+  pdl_late_entry(late);
   const long long top = y0 * Wa, bottom = (Ha - y1) * Wa, side = x0 + (Wa - x1), mid = (y1 - y0) * side;
   const long long n = top + bottom + mid;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -172,7 +170,7 @@ __global__ void __launch_bounds__(256) k_clear_outside(uint32_t* a, long long Wa
       a[(y0 + r) * Wa + (c < x0 ? c : x1 + (c - x0))] = 0u;
     }
   }
-  if (late) pdl_wait();
+  pdl_late_exit(late);
 }
 
 // fillUnsafe over the whole image (internal.nim:55-66)

@@ -481,8 +481,7 @@ __global__ void __launch_bounds__(1024) k_shadow_tile(const uint32_t* __restrict
   uint32_t* wk = reinterpret_cast<uint32_t*>(sh + ((2 * S * S + 15) & ~15));
   const int gx0 = blockIdx.x * kShadowTile - h, gy0 = blockIdx.y * kShadowTile - h;  // staged [0][0]
   const int tid = threadIdx.x, T = blockDim.x;
-  pdl_trigger();
-  if (!late) pdl_wait();
+  pdl_late_entry(late);
   if (r > 0)  // without a blur there is no weight table
     for (int k = tid; k <= 2 * r; k += T) wk[k] = kern[k];
   const unsigned char neutral = (m > 0 && !grow) ? 255 : 0;
@@ -553,7 +552,7 @@ __global__ void __launch_bounds__(1024) k_shadow_tile(const uint32_t* __restrict
     const uint32_t k = fin[(h + y) * S + h + x];
     out[(long long)gy * W + gx] = pack((c.r * k) / 255, (c.g * k) / 255, (c.b * k) / 255, (c.a * k) / 255);
   }
-  if (late) pdl_wait();
+  pdl_late_exit(late);
 }
 size_t shadow_tile_smem(int h) {
   const int S = kShadowTile + 2 * h;

@@ -35,6 +35,18 @@ __device__ __forceinline__ uint32_t pack(uint32_t r, uint32_t g, uint32_t b, uin
 // an ordinary launch.
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// A kernel that may be launched late waits at its start (late = 0) or just
+// before it exits (late = 1).  It lets the next kernel be set up only once
+// its own start-wait has passed: a kernel launched after one that waits at
+// its start then never overlaps a kernel still running before that one (the
+// in-flight set dep_late checks against restarts there).
+__device__ __forceinline__ void pdl_late_entry(int late) {
+  if (!late) pdl_wait();
+  pdl_trigger();
+}
+__device__ __forceinline__ void pdl_late_exit(int late) {
+  if (late) pdl_wait();
+}
 // A device buffer a kernel reads or writes.
 struct Span {
   const void* p;

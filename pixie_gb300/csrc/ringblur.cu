@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(kRingThreads, 1)
       reinterpret_cast<uint32_t*>(sm + L.bars + (2 * kMaxRaw + 2 * kMaxRing + 2 * kMaxAcc + 1) * 8);
   const int r = a.r;
   const bool trace = g_ring_trace_on != 0;
-  pdl_trigger();  // the next pass may be set up while this one runs
+  if (late) pdl_trigger();  // the next pass may be set up while this one runs (else after the start-wait)
 
   // The Toeplitz weights, once per CTA (K padded with zeros to whole blocks).
   const int kpad = (a.kspan + 63) / 64 * 64;
@@ -236,7 +236,7 @@ __global__ void __launch_bounds__(kRingThreads, 1)
   // the weights and barriers above read only constant data; the input
   // (written by the previous kernel) and the output are touched only after it
   // -- unless nothing still running touches them (late: wait before exiting)
-  if (!late) pdl_wait();
+  if (!late) pdl_late_entry(0);
   const uint32_t tmem = *taddr_s;
 
   if (warp == 0) {
@@ -505,7 +505,7 @@ __global__ void __launch_bounds__(kRingThreads, 1)
   if (warp == kMmaWarp)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemCols)
                  : "memory");
-  if (late) pdl_wait();
+  pdl_late_exit(late);
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;

@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(256) k_blur_fused(const uint32_t* __restrict__
   constexpr int NC = (D + NI + 3) / 4;
   constexpr int ROWS = kFTH + 2 * R;  // X-pass rows staged
   __shared__ __align__(16) uint32_t xs[ROWS][kFTW];
-  pdl_trigger();
+  if (late) pdl_trigger();  // else after the start-wait (pdl_late_entry)
   uint64_t w2[2 * R + 1];
 #pragma unroll
   for (int t = 0; t <= 2 * R; t++) {
@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(256) k_blur_fused(const uint32_t* __restrict__
   }
   const uint64_t nb = f2_pack(-kBias, -kBias), kq = f2_pack(kQuotC, kQuotC), km = f2_pack(kMagic, kMagic);
   const int tx0 = blockIdx.x * kFTW, ty0 = blockIdx.y * kFTH;
-  if (!late) pdl_wait();
+  if (!late) pdl_late_entry(0);
   // X pass: (row, 8-pixel group) tasks over the staged rows
   constexpr int GPR = kFTW / kOut;  // groups per staged row
   for (int task = threadIdx.x; task < ROWS * GPR; task += blockDim.x) {
@@ -298,7 +298,7 @@ __global__ void __launch_bounds__(256) k_blur_fused(const uint32_t* __restrict__
     for (int o = 0; o < kOut; o++, q += W)
       if (y0 + o < H) __stcs(q, quot_px(arg[o], aba[o], kq, km));
   }
-  if (late) pdl_wait();
+  pdl_late_exit(late);
 }
 
 template <int R>
