@@ -217,7 +217,7 @@ DrawKernel draw_kernel(int mode) {
 
 // Grid cap of a draw: whole waves of resident CTAs.  The modes with float
 // formulas or divisions (ColorBurn, ColorDodge, SoftLight, Hue, Saturation,
-// Color, Luminosity) run four waves, the rest one: with consecutive draws
+// Color, Luminosity) run two waves, the rest one: with consecutive draws
 // overlapping (dep_late), a single wave starts every CTA at once and the next
 // draw fills the SMs its slowest CTAs leave idle (2048x2048 Normal alone:
 // 14.3 us with one wave, 15.3 us with two).
@@ -230,7 +230,7 @@ static int draw_grid_cap(int mode, int nsm) {
   }
   const bool heavy = mode == kColorBurn || mode == kColorDodge || mode == kSoftLight || mode == kHue ||
                      mode == kSaturation || mode == kColor || mode == kLuminosity;
-  return nsm * resident[mode] * (heavy ? 4 : 1);
+  return nsm * resident[mode] * (heavy ? 2 : 1);
 }
 
 void launch_draw(uint32_t* a, const uint32_t* b, long long Wa, long long Ha, long long Wb,
