@@ -470,10 +470,14 @@ void launch_spread(uint32_t* img, uint8_t* a0, uint8_t* a1, long long W, long lo
 // (taps outside the image read 0; integer sums and v div 256 div 255 as the
 // blur passes), then colour * alpha / 255 (the MaskBlend draw of the filled
 // result) written once.
+// The blur radius R is a template parameter (0..kShadowHalo): the taps unroll
+// and each thread forms four neighbouring outputs from one window of inputs.
 constexpr int kShadowTile = 64, kShadowHalo = 32;
+template <int R>
 __global__ void __launch_bounds__(1024) k_shadow_tile(const uint32_t* __restrict__ src, uint32_t* __restrict__ out,
-                                                     int W, int H, int ox, int oy, int m, int grow, int r,
+                                                     int W, int H, int ox, int oy, int m, int grow,
                                                      const uint16_t* __restrict__ kern, uint32_t color, int late) {
+  constexpr int r = R;
   extern __shared__ __align__(16) unsigned char sh[];
   const int h = m + r, S = kShadowTile + 2 * h;  // staged side
   unsigned char* b0 = sh;
@@ -525,22 +529,38 @@ __global__ void __launch_bounds__(1024) k_shadow_tile(const uint32_t* __restrict
   }
   const unsigned char* fin = b0;  // final alpha at [h + y][h + x]
   if (r > 0) {
-    // blur along x: rows [m, S - m), the tile's columns, into b1 (0 outside the image)
-    for (int idx = tid; idx < (S - 2 * m) * kShadowTile; idx += T) {
-      const int i = m + idx / kShadowTile, j = h + (idx % kShadowTile);
+    // blur along x: rows [m, S - m), the tile's columns, into b1 (0 outside the
+    // image); a task is four neighbouring outputs of a row
+    constexpr int NT = 2 * R + 4;
+    for (int task = tid; task < (S - 2 * m) * (kShadowTile / 4); task += T) {
+      const int i = m + task / (kShadowTile / 4), j = h + 4 * (task % (kShadowTile / 4));
       const unsigned char* p = b0 + i * S + j - r;
-      uint32_t acc = 0;
-      for (int t = 0; t <= 2 * r; t++) acc += (uint32_t)p[t] * wk[t];
-      b1[i * S + j] = inside(i, j) ? (unsigned char)(acc / 256 / 255) : 0;
+      uint32_t a[4] = {0, 0, 0, 0};
+#pragma unroll
+      for (int t = 0; t < NT; t++) {
+        const uint32_t v = p[t];
+#pragma unroll
+        for (int o = 0; o < 4; o++)
+          if (t - o >= 0 && t - o <= 2 * R) a[o] += v * wk[t - o];
+      }
+#pragma unroll
+      for (int o = 0; o < 4; o++) b1[i * S + j + o] = inside(i, j + o) ? (unsigned char)(a[o] / 256 / 255) : 0;
     }
     __syncthreads();
-    // blur along y: the tile, into b0
-    for (int idx = tid; idx < kShadowTile * kShadowTile; idx += T) {
-      const int i = h + idx / kShadowTile, j = h + (idx % kShadowTile);
+    // blur along y: the tile, into b0; a task is four neighbouring outputs of a column
+    for (int task = tid; task < kShadowTile * (kShadowTile / 4); task += T) {
+      const int j = h + task % kShadowTile, i = h + 4 * (task / kShadowTile);
       const unsigned char* p = b1 + (i - r) * S + j;
-      uint32_t acc = 0;
-      for (int t = 0; t <= 2 * r; t++) acc += (uint32_t)p[t * S] * wk[t];
-      b0[i * S + j] = (unsigned char)(acc / 256 / 255);
+      uint32_t a[4] = {0, 0, 0, 0};
+#pragma unroll
+      for (int t = 0; t < NT; t++) {
+        const uint32_t v = p[t * S];
+#pragma unroll
+        for (int o = 0; o < 4; o++)
+          if (t - o >= 0 && t - o <= 2 * R) a[o] += v * wk[t - o];
+      }
+#pragma unroll
+      for (int o = 0; o < 4; o++) b0[(i + o) * S + j] = (unsigned char)(a[o] / 256 / 255);
     }
     __syncthreads();
   }
@@ -553,6 +573,24 @@ __global__ void __launch_bounds__(1024) k_shadow_tile(const uint32_t* __restrict
     out[(long long)gy * W + gx] = pack((c.r * k) / 255, (c.g * k) / 255, (c.b * k) / 255, (c.a * k) / 255);
   }
   pdl_late_exit(late);
+}
+typedef void (*ShadowTileKernel)(const uint32_t*, uint32_t*, int, int, int, int, int, int, const uint16_t*, uint32_t,
+                                 int);
+template <int R>
+struct ShadowTable {
+  static void fill(ShadowTileKernel* t) {
+    t[R] = k_shadow_tile<R>;
+    ShadowTable<R + 1>::fill(t);
+  }
+};
+template <>
+struct ShadowTable<kShadowHalo + 1> {
+  static void fill(ShadowTileKernel*) {}
+};
+ShadowTileKernel shadow_tile_kernel(int r) {
+  static ShadowTileKernel table[kShadowHalo + 1] = {nullptr};
+  if (!table[0]) ShadowTable<0>::fill(table);
+  return table[r];
 }
 size_t shadow_tile_smem(int h) {
   const int S = kShadowTile + 2 * h;
@@ -568,8 +606,8 @@ void launch_shadow(const uint32_t* src, uint32_t* out, uint8_t* a0, uint8_t* a1,
       oy > -(1 << 24) && oy < (1 << 24)) {
     const dim3 g((unsigned)((W + kShadowTile - 1) / kShadowTile), (unsigned)((H + kShadowTile - 1) / kShadowTile));
     const int late = dep_late(st, {Span{out, (size_t)(n * 4)}}, {Span{src, (size_t)(n * 4)}});
-    launch_pdl(k_shadow_tile, g, dim3(1024), shadow_tile_smem(m + r), st, src, out, (int)W, (int)H, (int)ox, (int)oy,
-               m, (int)(s > 0), r, kern, color, late);
+    launch_pdl(shadow_tile_kernel(r), g, dim3(1024), shadow_tile_smem(m + r), st, src, out, (int)W, (int)H, (int)ox,
+               (int)oy, m, (int)(s > 0), kern, color, late);
     note_launch();
     return;
   }
