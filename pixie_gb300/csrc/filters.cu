@@ -493,38 +493,47 @@ __global__ void __launch_bounds__(1024) k_shadow_tile(const uint32_t* __restrict
     const int gx = gx0 + j, gy = gy0 + i;
     return gx >= 0 && gx < W && gy >= 0 && gy < H;
   };
+  // each warp takes rows, its lanes consecutive columns (no divisions by S)
+  const int nw = T >> 5, wi = tid >> 5, ln = tid & 31;
   // the offset alpha plane (k_alpha_offset), neutral outside the image
-  for (int idx = tid; idx < S * S; idx += T) {
-    const int i = idx / S, j = idx - i * S;
-    const int gx = gx0 + j, gy = gy0 + i;
-    unsigned char v = neutral;
-    if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
-      const int sx = gx - ox, sy = gy - oy;
-      v = (sx >= 0 && sx < W && sy >= 0 && sy < H) ? (unsigned char)(src[(long long)sy * W + sx] >> 24) : 0;
+  for (int i = wi; i < S; i += nw)
+    for (int j = ln; j < S; j += 32) {
+      const int gx = gx0 + j, gy = gy0 + i;
+      unsigned char v = neutral;
+      if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+        const int sx = gx - ox, sy = gy - oy;
+        v = (sx >= 0 && sx < W && sy >= 0 && sy < H) ? (unsigned char)(src[(long long)sy * W + sx] >> 24) : 0;
+      }
+      b0[i * S + j] = v;
     }
-    b0[idx] = v;
-  }
   __syncthreads();
   if (m > 0) {  // spread along x into b1, then along y back into b0 (rows and columns [m, S - m))
-    for (int idx = tid; idx < S * (S - 2 * m); idx += T) {
-      const int i = idx / (S - 2 * m), j = m + (idx - i * (S - 2 * m));
-      const unsigned char* p = b0 + i * S + j - m;
-      uint32_t v = neutral;
-      for (int t = 0; t <= 2 * m; t++) v = grow ? max(v, (uint32_t)p[t]) : min(v, (uint32_t)p[t]);
-      b1[i * S + j] = (unsigned char)v;
-    }
+    for (int i = wi; i < S; i += nw)
+      for (int j = m + ln; j < S - m; j += 32) {
+        const unsigned char* p = b0 + i * S + j - m;
+        uint32_t v = neutral;
+        if (grow)
+          for (int t = 0; t <= 2 * m; t++) v = max(v, (uint32_t)p[t]);
+        else
+          for (int t = 0; t <= 2 * m; t++) v = min(v, (uint32_t)p[t]);
+        b1[i * S + j] = (unsigned char)v;
+      }
     __syncthreads();
-    for (int idx = tid; idx < (S - 2 * m) * (S - 2 * m); idx += T) {
-      const int i = m + idx / (S - 2 * m), j = m + idx % (S - 2 * m);
-      const unsigned char* p = b1 + (i - m) * S + j;
-      uint32_t v = neutral;
-      for (int t = 0; t <= 2 * m; t++) v = grow ? max(v, (uint32_t)p[t * S]) : min(v, (uint32_t)p[t * S]);
-      b0[i * S + j] = inside(i, j) ? (unsigned char)v : 0;  // blur taps outside the image read 0
-    }
+    for (int i = m + wi; i < S - m; i += nw)
+      for (int j = m + ln; j < S - m; j += 32) {
+        const unsigned char* p = b1 + (i - m) * S + j;
+        uint32_t v = neutral;
+        if (grow)
+          for (int t = 0; t <= 2 * m; t++) v = max(v, (uint32_t)p[t * S]);
+        else
+          for (int t = 0; t <= 2 * m; t++) v = min(v, (uint32_t)p[t * S]);
+        b0[i * S + j] = inside(i, j) ? (unsigned char)v : 0;  // blur taps outside the image read 0
+      }
     __syncthreads();
   } else if (neutral != 0) {
-    for (int idx = tid; idx < S * S; idx += T)
-      if (!inside(idx / S, idx % S)) b0[idx] = 0;
+    for (int i = wi; i < S; i += nw)
+      for (int j = ln; j < S; j += 32)
+        if (!inside(i, j)) b0[i * S + j] = 0;
     __syncthreads();
   }
   const unsigned char* fin = b0;  // final alpha at [h + y][h + x]
