@@ -40,13 +40,17 @@
 //               runs the loop with uniform operands; one elected lane issues.
 //   8 warps     epilogue, two groups of four on alternate tiles: TMEM ->
 //               quotient bytes -> a 4 x 4 byte transpose across each quad of
-//               lanes (the four channels of a line) -> whole pixels, stored
-//               transposed: every warp store fills four 32-byte sectors
+//               lanes (the four channels of a line) -> whole pixels, staged
+//               transposed in 128-byte-swizzled shared memory (64 rows of 32
+//               pixels) and written with one TMA store per tile (the group's
+//               first thread issues it after a group barrier)
 // The operand traffic of the MMAs is then the weights only (2 KB per
-// 128 x 64 x 16 step), below the tensor core's math time.  Every mbarrier
-// wait is bounded; a role whose wait runs out sets *err and stops; the others
-// then run out too, in-flight copies and MMAs are waited for (bounded), and
-// the CTA frees its tensor memory.
+// 128 x 64 x 16 step, 4 KB per 128 x 128 x 16 step), below the tensor core's
+// math time.  The intermediate's rows are padded (ring_tmp_pitch) and work
+// items are planned over all SMs (plan_pass).  Every mbarrier wait is
+// bounded; a role whose wait runs out sets *err and stops; the others then
+// run out too, in-flight copies, MMAs and stores are waited for (bounded),
+// and the CTA frees its tensor memory.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
