@@ -180,17 +180,21 @@ __device__ __forceinline__ uint32_t unit_to_u8(float c) {
   return __float_as_uint(__fadd_rd(t, 12582912.0f)) - 0x4B400000u;
 }
 
-// n / d rounded to nearest from y = RN(1/d): q = RN(n y) is within one ulp of
-// n / d, r = n - q d is exact (one fused multiply-add), and RN(q + r y) is
-// the correctly rounded quotient (Markstein, IBM J. Res. Dev. 34(1), 1990;
-// Muller et al., Handbook of Floating-Point Arithmetic, the correction step of
-// Newton-Raphson division).  One reciprocal serves the three channels'
-// divisions by the same denominator.  For the finite normal operands of the
-// blend formulas; 0 / 0 gives NaN as the IEEE division does.
+// n / d rounded to nearest from y = RN(1/d), by the correction step of
+// Newton-Raphson division (Markstein, IBM J. Res. Dev. 34(1), 1990; Muller et
+// al., Handbook of Floating-Point Arithmetic): q0 = RN(n y) may be more than
+// one ulp from n / d, so a first correction q1 = RN(q0 + RN(n - q0 d) y)
+// brings it within one ulp; then r1 = n - q1 d is exact (one fused
+// multiply-add: the remainder of a faithful quotient is representable) and
+// RN(q1 + r1 y) is the correctly rounded quotient (Markstein's theorem: y
+// correctly rounded, q1 within one ulp).  One reciprocal serves the three
+// channels' divisions by the same denominator.  For the finite normal
+// operands of the blend formulas; 0 / 0 gives NaN as the IEEE division does.
 __device__ __forceinline__ float div_rcp(float n, float d, float y) {
-  const float q = n * y;
-  const float r = fmaf(-q, d, n);
-  return fmaf(r, y, q);
+  const float q0 = n * y;
+  const float q1 = fmaf(fmaf(-q0, d, n), y, q0);
+  const float r1 = fmaf(-q1, d, n);
+  return fmaf(r1, y, q1);
 }
 
 // chroma float modes (UNPINNED, W3C Compositing Level 1; same operation order
