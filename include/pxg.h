@@ -393,8 +393,10 @@ float pxg_last_gpu_ms(void);
  * after them (an upload's host buffer must stay unchanged, and a download's
  * holds the image, only after pxg_synchronize), so copies overlap other
  * images' work; pxg_synchronize() waits for everything.  fillPath/strokePath
- * always wait (their errors come from the GPU).  No counterpart in the
- * reference. */
+ * always wait (their errors come from the GPU).  Enqueued calls keep the
+ * order of the calls for every image: a draw, blur or shadow whose images no
+ * kernel still running touches may start before the kernel before it has
+ * finished, and finishes only after it.  No counterpart in the reference. */
 int pxg_set_blocking(int blocking);
 
 /* Number of kernels this library has launched since it was loaded. */
